@@ -1,0 +1,322 @@
+"""Benchmark of the Moebius domain-wall Dslash hot path on GB300.
+
+Workload (default): Moebius DWF, 16^4 x Ls=16, b=1.5, c=0.5, M5=1.8, mf=0.01, gauge
+U = exp(i 0.5 H) (seeded), antiperiodic time, FP32.  One step = DhopEO + DhopOE on
+Gaussian spinors.  The timed loop rotates over 4 independent (in, out) sets
+(4 x 4 half fields x 50 MB + links, larger than the 129 MB L2), so every kernel reads
+inputs that are not L2-resident.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  `value` = algorithmic GB/s of the step (228 B per output 5D site
+per Dhop in FP32: 96 in + 96 out + 8 links x 72 B / Ls), inputs resident in HBM;
+`e2e` = the same metric through the C ABI with pinned host buffers, the host<->device
+copies of each step's input and output inside the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DIMS = (16, 16, 16, 16)
+LS = 16
+MF, M5, B, C, EPS = 0.01, 1.8, 1.5, 0.5, 0.5
+METRIC = "DWF Dhop GB/s vs HBM peak"
+UNIT = "GB/s"
+
+
+def bytes_per_site(prec: int, Ls: int) -> float:
+    spin = 96 if prec == 1 else 192
+    link = 72 if prec == 1 else 144
+    return 2 * spin + 8 * link / Ls
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name: str):
+    """dram bytes per launch from the committed ncu summary (line `traffic_bytes_per_launch: N`)."""
+    f = ROOT / "profiles" / name
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                parts = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(parts) >= 6:
+                    self.samples.append(parts)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist
+
+
+def dist_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------------------
+def cpu_baseline_oracle(U, x_odd, x_even, budget_s=12.0):
+    """The oracle (OpenMP C++ restatement of Grid's site loop) on the host cores, on a
+    bounded sample: as many DhopEO+DhopOE pairs of the full workload as fit in budget_s."""
+    from oracle import oracle as o
+    threads = o.max_threads()
+    op = o.OracleOp(1, 1, DIMS, LS, [MF, M5, B, C], U, np.array([1, 0, 1, 0, 1, 0, -1, 0], float))
+    op.dhop_cb(x_odd, 1)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        op.dhop_cb(x_odd, 1)
+        op.dhop_cb(x_even, 0)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    sites = x_odd.size // 12
+    gbs = 2 * n * sites * bytes_per_site(1, LS) / dt / 1e9
+    return {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} DhopEO+DhopOE pairs of the full 16^4x16 FP32 workload in {dt:.1f} s (oracle, OpenMP)"}
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the oracle's CPU implementation on the same config and metric."""
+    if rank != 0:
+        return
+    import grid_gb300 as g
+    U = g.random_gauge(DIMS, EPS, 1234)
+    nh = int(np.prod(DIMS)) // 2 * LS
+    xo = g.random_gaussian(nh * 12, 1)
+    xe = g.random_gaussian(nh * 12, 2)
+    from oracle import oracle as o
+    threads = o.max_threads()
+    op = o.OracleOp(1, 1, DIMS, LS, [MF, M5, B, C], U, g.antiperiodic_t())
+    for _ in range(max(1, min(args.warmup, 1))):
+        op.dhop_cb(xo, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.dhop_cb(xo, 1)
+        op.dhop_cb(xe, 0)
+    dt = time.perf_counter() - t0
+    gbs = 2 * args.steps * nh * bytes_per_site(1, LS) / dt / 1e9
+    line = {"metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "mobius_dwf_16^4xLs16_dhop_eo_oe_fp32", "dims": list(DIMS), "Ls": LS,
+                       "b": B, "c": C, "M5": M5, "mf": MF, "eps": EPS},
+            "cpu_baseline": {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} DhopEO+DhopOE steps of the full workload (oracle, OpenMP)"},
+            "e2e": {"value": gbs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, ws, rank, local, dist):
+    import grid_gb300 as g
+    g.set_device(local)
+    U = g.random_gauge(DIMS, EPS, 1234)
+    op = g.MobiusFermion(U, DIMS, LS, MF, M5, B, C, precision=g.F32)
+    nh = op.half_sites4 * LS
+    NSET = 4
+    sets = []
+    for k in range(NSET):
+        xo = op.FermionRedBlackField(g.ODD).import_(g.random_gaussian(nh * 12, 10 + k))
+        ye = op.FermionRedBlackField(g.EVEN)
+        xe = op.FermionRedBlackField(g.EVEN).import_(g.random_gaussian(nh * 12, 20 + k))
+        yo = op.FermionRedBlackField(g.ODD)
+        sets.append((xo, ye, xe, yo))
+
+    def step(k):
+        xo, ye, xe, yo = sets[k % NSET]
+        op.DhopEO(xo, ye, 0)
+        op.DhopOE(xe, yo, 0)
+
+    for k in range(max(3, args.warmup)):
+        step(k)
+    op.sync()
+    bpsite = bytes_per_site(1, LS)
+    with ClockSampler(local) as clk:
+        dist_barrier(dist)
+        op.sync()
+        op.event(0)
+        for k in range(args.steps):
+            step(k)
+        op.event(1)
+        op.sync()
+        dt_ms = op.elapsed_ms(0, 1)
+        # per-kernel average launch time of the dominant kernel (DhopEO), same rotation
+        ins = [s[0] for s in sets]
+        outs = [s[1] for s in sets]
+        eo_ms = op.bench_kernel(0, ins, outs, max(20, 4 * args.steps))
+        ins = [s[2] for s in sets]
+        outs = [s[3] for s in sets]
+        oe_ms = op.bench_kernel(1, ins, outs, max(20, 4 * args.steps))
+    dt_ms = dist_max(dist, dt_ms)
+    step_bytes = 2 * nh * bpsite
+    value = dist_sum(dist, step_bytes * args.steps) / (dt_ms / 1e3) / 1e9 if dist else step_bytes * args.steps / (dt_ms / 1e3) / 1e9
+
+    # ---- extra kernels of the config (Mooee, MooeeInv) ----
+    m_ms = op.bench_kernel(2, [s[1] for s in sets], [s[0] for s in sets], 40)
+    mi_ms = op.bench_kernel(3, [s[1] for s in sets], [s[0] for s in sets], 40)
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    host_in = g.PinnedArray(nh * 12)
+    host_out = g.PinnedArray(nh * 12)
+    host_in.array[:] = g.random_gaussian(nh * 12, 99)
+    fin = op.FermionRedBlackField(g.ODD)
+    fout = op.FermionRedBlackField(g.EVEN)
+    import ctypes as Cc
+    pin = host_in.array.ctypes.data_as(Cc.POINTER(Cc.c_double))
+    pout = host_out.array.ctypes.data_as(Cc.POINTER(Cc.c_double))
+    for _ in range(2):
+        g.lib.gb_field_import(fin.h, pin)
+        g.lib.gb_DhopEO(op.h, fin.h, fout.h, 0)
+        g.lib.gb_field_export(fout.h, pout)
+    e2e_steps = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        assert g.lib.gb_field_import(fin.h, pin) == 0
+        assert g.lib.gb_DhopEO(op.h, fin.h, fout.h, 0) == 0
+        assert g.lib.gb_field_export(fout.h, pout) == 0
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    e2e_dt = dist_max(dist, e2e_dt)
+    e2e_value = nh * bpsite / e2e_dt / 1e9 * (ws if dist else 1)
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    achieved = nh * bpsite / (eo_ms / 1e3) / 1e9
+    traffic = profile_traffic("dhop_eo_dwf16_fp32.txt")
+    cpu = cpu_baseline_oracle(U, g.random_gaussian(nh * 12, 10), g.random_gaussian(nh * 12, 20)) if ws == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: seeded exp(i*0.5*H) gauge field, Gaussian spinors",
+        "config": {"workload": "mobius_dwf_16^4xLs16_dhop_eo_oe_fp32", "dims": list(DIMS), "Ls": LS, "b": B, "c": C,
+                   "M5": M5, "mf": MF, "eps": EPS, "boundary": "antiperiodic t",
+                   "l2": "4 rotating input/output sets, 800 MB total (> 129 MB L2)", "parallelism": f"replicas{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "dhop_kernel<float> (DhopEO)", "peak_source": peak_kind,
+                     "bytes_per_site": bpsite, "sites_per_launch": nh},
+        "kernels_ms": {"DhopEO": eo_ms, "DhopOE": oe_ms, "Mooee": m_ms, "MooeeInv": mi_ms},
+        "kernels_gbs": {"DhopEO": achieved, "DhopOE": nh * bpsite / (oe_ms / 1e3) / 1e9,
+                        "Mooee": nh * 192 / (m_ms / 1e3) / 1e9, "MooeeInv": nh * 192 / (mi_ms / 1e3) / 1e9},
+        "gflops_dhop": 1320.0 * nh / (eo_ms / 1e3) / 1e9,
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nh * 12 * 16, "d2h_bytes_per_step": nh * 12 * 16,
+                "path": "gb_field_import (H2D canonical FP64) + gb_DhopEO + gb_field_export (D2H)"},
+        "gpu_launches": 2 * args.steps,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    dist = dist_init(ws)
+    run_gpu(args, ws, rank, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

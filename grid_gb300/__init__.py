@@ -1,0 +1,15 @@
+"""GB300-native Wilson / Moebius domain-wall fermion operators and CG solvers.
+
+The compute path is the in-tree CUDA library ``libgbdwf.so`` (C ABI declared in
+``include/gbdwf.h``); this package is a thin ctypes mirror of Grid's operator, linear
+operator and solver classes over that ABI.  Importing the package loads the library and
+raises if it has not been built: there is no CPU fallback.
+"""
+from .api import (  # noqa: F401
+    GridError, lib, LIB_PATH, F64, F32, F16, EVEN, ODD, FULL, DaggerNo, DaggerYes,
+    FermionField, WilsonFermion, MobiusFermion, MdagMLinearOperator, SchurDiagMooeeOperator,
+    ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
+    CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
+    antiperiodic_t, periodic, set_device, PinnedArray, norm2, innerProduct, axpy, axpby, axpy_norm,
+    pickCheckerboard, setCheckerboard,
+)

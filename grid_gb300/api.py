@@ -1,0 +1,537 @@
+"""ctypes mirror of Grid's fermion-operator / linear-operator / CG interfaces over the
+C ABI of libgbdwf.so.
+
+Names, argument meaning and error behaviour follow Grid:
+  * WilsonFermion(U, dims, mass, ...)                 Grid/qcd/action/fermion/WilsonFermion.h:139-142
+  * MobiusFermion(U, dims, Ls, mf, M5, b, c, ...)     Grid/qcd/action/fermion/MobiusFermion.h:45-67
+  * M, Mdag, Dhop, DhopEO, DhopOE, Meooe, MeooeDag, Mooee, MooeeDag, MooeeInv, MooeeInvDag
+                                                      Grid/qcd/action/fermion/FermionOperator.h:40-192
+  * MdagMLinearOperator, SchurDiagMooeeOperator       Grid/algorithms/LinearOperator.h:74-105,325-349
+  * ConjugateGradient(tol, maxit, err_on_no_conv)     Grid/algorithms/iterative/ConjugateGradient.h:55-59
+  * ConjugateGradientReliableUpdate(tol, maxit, delta, linop_f, linop_d)
+                                                      Grid/algorithms/iterative/ConjugateGradientReliableUpdate.h:58-69
+  * SchurRedBlackDiagMooeeSolve(solver)(op, src, sol) Grid/algorithms/iterative/SchurRedBlack.h:373-436
+Grid asserts where this raises GridError (status code + message); a CG that does not
+converge raises when err_on_no_conv is set, as Grid's ErrorOnNoConverge asserts.
+
+Host arrays are numpy complex128 in the canonical layout of include/gbdwf.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().with_name("libgbdwf.so")
+
+F64, F32, F16 = 0, 1, 2
+EVEN, ODD, FULL = 0, 1, 2
+DaggerNo, DaggerYes = 0, 1
+
+
+class GridError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is not built: run `python grid_gb300/build.py` (the CUDA library is required; "
+            "there is no CPU fallback)")
+    return C.CDLL(str(LIB_PATH))
+
+
+lib = _load()
+
+_vp, _i, _d, _u64, _sz = C.c_void_p, C.c_int, C.c_double, C.c_uint64, C.c_size_t
+_ip, _dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+
+
+class CGParams(C.Structure):
+    _fields_ = [("tolerance", C.c_double), ("max_iterations", C.c_int), ("err_on_no_conv", C.c_int),
+                ("delta", C.c_double), ("relup_every", C.c_int), ("final_cleanup", C.c_int),
+                ("check_every", C.c_int), ("use_graphs", C.c_int)]
+
+
+class CGResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("reliable_updates", C.c_int), ("cleanup_iterations", C.c_int),
+                ("converged", C.c_int), ("true_residual", C.c_double), ("seconds", C.c_double),
+                ("flops", C.c_double)]
+
+
+def _proto(name, args, res=C.c_int):
+    f = getattr(lib, name)
+    f.argtypes = args
+    f.restype = res
+    return f
+
+
+_proto("gb_last_error", [], C.c_char_p)
+_proto("gb_status_string", [_i], C.c_char_p)
+_proto("gb_device_count", [_ip])
+_proto("gb_version", [])
+_proto("gb_wilson_create", [_ip, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
+_proto("gb_mobius_create", [_ip, _i, _d, _d, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
+_proto("gb_op_destroy", [_vp])
+_proto("gb_op_import_gauge", [_vp, _dp])
+_proto("gb_op_import_gauge_device", [_vp, _vp])
+_proto("gb_op_info", [_vp, _ip, _ip, C.POINTER(C.c_int64), _ip])
+_proto("gb_op_set_stream", [_vp, _vp])
+_proto("gb_op_cayley_coeffs", [_vp, _dp])
+_proto("gb_field_create", [_vp, _i, _i, C.POINTER(_vp)])
+_proto("gb_field_destroy", [_vp])
+_proto("gb_field_subset", [_vp, _ip])
+_proto("gb_field_set_subset", [_vp, _i])
+_proto("gb_field_host_len", [_vp, C.POINTER(_sz)])
+_proto("gb_field_import", [_vp, _dp])
+_proto("gb_field_export", [_vp, _dp])
+_proto("gb_field_import_device", [_vp, _vp])
+_proto("gb_field_export_device", [_vp, _vp])
+_proto("gb_field_zero", [_vp])
+_proto("gb_field_copy", [_vp, _vp])
+_proto("gb_field_norm2", [_vp, _dp])
+_proto("gb_field_inner", [_vp, _vp, _dp])
+_proto("gb_field_axpy", [_vp, _d, _vp, _vp])
+_proto("gb_field_axpby", [_vp, _d, _d, _vp, _vp])
+_proto("gb_field_axpy_norm", [_vp, _d, _vp, _vp, _dp])
+_proto("gb_field_pick_checkerboard", [_vp, _vp])
+_proto("gb_field_set_checkerboard", [_vp, _vp])
+for _n in ("gb_M", "gb_Mdag", "gb_MdagM", "gb_Meooe", "gb_MeooeDag", "gb_Mooee", "gb_MooeeDag", "gb_MooeeInv",
+           "gb_MooeeInvDag", "gb_Mpc", "gb_MpcDag", "gb_MpcDagMpc"):
+    _proto(_n, [_vp, _vp, _vp])
+for _n in ("gb_Dhop", "gb_DhopEO", "gb_DhopOE"):
+    _proto(_n, [_vp, _vp, _vp, _i])
+_proto("gb_cg_params_default", [C.POINTER(CGParams)], None)
+_proto("gb_cg_mdagm", [_vp, _vp, _vp, C.POINTER(CGParams), C.POINTER(CGResult)])
+_proto("gb_cg_schur", [_vp, _vp, _vp, C.POINTER(CGParams), C.POINTER(CGResult)])
+_proto("gb_cg_last_per_rhs", [_vp, _ip, _dp])
+_proto("gb_cg_reliable", [_vp, _vp, _i, _vp, _vp, C.POINTER(CGParams), C.POINTER(CGResult)])
+_proto("gb_schur_solve", [_vp, _vp, _vp, _vp, C.POINTER(CGParams), C.POINTER(CGResult), _dp])
+_proto("gb_random_gauge", [_ip, _d, _u64, _dp])
+_proto("gb_random_gaussian", [_sz, _u64, _dp])
+_proto("gb_random_z2", [_sz, _u64, _dp])
+_proto("gb_unit_gauge", [_ip, _dp])
+_proto("gb_bench_kernel", [_vp, _i, C.POINTER(_vp), C.POINTER(_vp), _i, _i, _dp])
+_proto("gb_set_device", [_i])
+_proto("gb_op_sync", [_vp])
+_proto("gb_op_event_record", [_vp, _i])
+_proto("gb_op_event_elapsed", [_vp, _i, _i, _dp])
+_proto("gb_host_alloc", [_sz, C.POINTER(_vp)])
+_proto("gb_host_free", [_vp])
+
+
+def set_device(d: int):
+    _check(lib.gb_set_device(int(d)))
+
+
+class PinnedArray:
+    """Page-locked host buffer viewed as a numpy complex128 array."""
+
+    def __init__(self, n_complex: int):
+        p = _vp()
+        _check(lib.gb_host_alloc(int(n_complex) * 16, C.byref(p)))
+        self.ptr = p
+        buf = (C.c_double * (2 * int(n_complex))).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.complex128)
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            self.array = None
+            lib.gb_host_free(self.ptr)
+            self.ptr = None
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise GridError(rc, (lib.gb_last_error() or b"").decode() or lib.gb_status_string(rc).decode())
+
+
+def _dptr(a: np.ndarray):
+    assert a.dtype in (np.complex128, np.float64) and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+def _dims(dims):
+    d = (C.c_int * 4)(*[int(x) for x in dims])
+    return d
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    lib.gb_device_count(C.byref(n))
+    return n.value
+
+
+def periodic():
+    return np.array([1, 0, 1, 0, 1, 0, 1, 0], dtype=np.float64)
+
+
+def antiperiodic_t():
+    """ImplParams::boundary_phases = {1,1,1,-1} (Test_mobius_bcg_nosplit.cc:51)."""
+    return np.array([1, 0, 1, 0, 1, 0, -1, 0], dtype=np.float64)
+
+
+# ---- seeded inputs ------------------------------------------------------------------
+def random_gauge(dims, eps: float, seed: int) -> np.ndarray:
+    vol = int(np.prod(dims))
+    U = np.empty(vol * 4 * 9, dtype=np.complex128)
+    _check(lib.gb_random_gauge(_dims(dims), float(eps), int(seed), _dptr(U)))
+    return U
+
+
+def unit_gauge(dims) -> np.ndarray:
+    vol = int(np.prod(dims))
+    U = np.empty(vol * 4 * 9, dtype=np.complex128)
+    _check(lib.gb_unit_gauge(_dims(dims), _dptr(U)))
+    return U
+
+
+def random_gaussian(n_complex: int, seed: int) -> np.ndarray:
+    a = np.empty(int(n_complex), dtype=np.complex128)
+    _check(lib.gb_random_gaussian(int(n_complex), int(seed), _dptr(a)))
+    return a
+
+
+def random_z2(n_complex: int, seed: int) -> np.ndarray:
+    a = np.empty(int(n_complex), dtype=np.complex128)
+    _check(lib.gb_random_z2(int(n_complex), int(seed), _dptr(a)))
+    return a
+
+
+# ---- fields ---------------------------------------------------------------------------
+class FermionField:
+    """Lattice<SpinColourVector> on an operator's FermionGrid (FULL) or
+    FermionRedBlackGrid (EVEN/ODD), device resident."""
+
+    def __init__(self, op: "_FermionOperator", subset: int, precision: int | None = None):
+        self.op = op
+        h = _vp()
+        _check(lib.gb_field_create(op.h, subset, op.precision if precision is None else precision, C.byref(h)))
+        self.h = h
+        self.precision = op.precision if precision is None else precision
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib.gb_field_destroy(h)
+            self.h = None
+
+    @property
+    def _as_parameter_(self):
+        return self.h
+
+    @property
+    def checkerboard(self) -> int:
+        s = C.c_int()
+        _check(lib.gb_field_subset(self.h, C.byref(s)))
+        return s.value
+
+    @checkerboard.setter
+    def checkerboard(self, subset: int):
+        _check(lib.gb_field_set_subset(self.h, subset))
+
+    def host_len(self) -> int:
+        n = _sz()
+        _check(lib.gb_field_host_len(self.h, C.byref(n)))
+        return n.value // 2
+
+    def import_(self, a: np.ndarray) -> "FermionField":
+        a = np.ascontiguousarray(a, dtype=np.complex128).reshape(-1)
+        if a.size != self.host_len():
+            raise GridError(1, f"host array has {a.size} complex numbers, field needs {self.host_len()}")
+        _check(lib.gb_field_import(self.h, _dptr(a)))
+        return self
+
+    def export(self) -> np.ndarray:
+        a = np.empty(self.host_len(), dtype=np.complex128)
+        _check(lib.gb_field_export(self.h, _dptr(a)))
+        return a
+
+    def zero(self):
+        _check(lib.gb_field_zero(self.h))
+        return self
+
+    def copy_from(self, other: "FermionField"):
+        _check(lib.gb_field_copy(self.h, other.h))
+        return self
+
+    def norm2(self) -> np.ndarray:
+        out = np.empty(self.op.nrhs, dtype=np.float64)
+        _check(lib.gb_field_norm2(self.h, _dptr(out)))
+        return out
+
+    def inner(self, other: "FermionField") -> np.ndarray:
+        out = np.empty(2 * self.op.nrhs, dtype=np.float64)
+        _check(lib.gb_field_inner(self.h, other.h, _dptr(out)))
+        return out[0::2] + 1j * out[1::2]
+
+
+def norm2(f: FermionField):
+    return f.norm2()
+
+
+def innerProduct(a: FermionField, b: FermionField):
+    return a.inner(b)
+
+
+def axpy(z: FermionField, a: float, x: FermionField, y: FermionField):
+    _check(lib.gb_field_axpy(z.h, float(a), x.h, y.h))
+
+
+def axpby(z: FermionField, a: float, b: float, x: FermionField, y: FermionField):
+    _check(lib.gb_field_axpby(z.h, float(a), float(b), x.h, y.h))
+
+
+def axpy_norm(z: FermionField, a: float, x: FermionField, y: FermionField):
+    out = np.empty(z.op.nrhs, dtype=np.float64)
+    _check(lib.gb_field_axpy_norm(z.h, float(a), x.h, y.h, _dptr(out)))
+    return out
+
+
+def pickCheckerboard(cb: int, half: FermionField, full: FermionField):
+    half.checkerboard = cb
+    _check(lib.gb_field_pick_checkerboard(half.h, full.h))
+
+
+def setCheckerboard(full: FermionField, half: FermionField):
+    _check(lib.gb_field_set_checkerboard(full.h, half.h))
+
+
+# ---- operators ------------------------------------------------------------------------
+class _FermionOperator:
+    h = None
+
+    def _finish(self, h, U, stream):
+        self.h = h
+        Ls, nrhs, half4, prec = C.c_int(), C.c_int(), C.c_int64(), C.c_int()
+        _check(lib.gb_op_info(h, C.byref(Ls), C.byref(nrhs), C.byref(half4), C.byref(prec)))
+        self.Ls, self.nrhs, self.half_sites4, self.precision = Ls.value, nrhs.value, half4.value, prec.value
+        if U is not None:
+            self.ImportGauge(U)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib.gb_op_destroy(self.h)
+            self.h = None
+
+    def ImportGauge(self, U: np.ndarray):
+        U = np.ascontiguousarray(U, dtype=np.complex128).reshape(-1)
+        if U.size != self.vol4 * 36:
+            raise GridError(1, "gauge field has the wrong size")
+        _check(lib.gb_op_import_gauge(self.h, _dptr(U)))
+
+    def set_stream(self, stream_ptr: int):
+        _check(lib.gb_op_set_stream(self.h, _vp(stream_ptr)))
+
+    @property
+    def vol4(self):
+        return int(np.prod(self.dims))
+
+    # grids
+    def FermionField(self, precision=None):
+        return FermionField(self, FULL, precision)
+
+    def FermionRedBlackField(self, cb=ODD, precision=None):
+        return FermionField(self, cb, precision)
+
+    def Mass(self):
+        return self.mass
+
+    # FermionOperator interface
+    def M(self, i, o): _check(lib.gb_M(self.h, i.h, o.h))
+    def Mdag(self, i, o): _check(lib.gb_Mdag(self.h, i.h, o.h))
+    def MdagM(self, i, o): _check(lib.gb_MdagM(self.h, i.h, o.h))
+    def Dhop(self, i, o, dag): _check(lib.gb_Dhop(self.h, i.h, o.h, dag))
+    def DhopEO(self, i, o, dag): _check(lib.gb_DhopEO(self.h, i.h, o.h, dag))
+    def DhopOE(self, i, o, dag): _check(lib.gb_DhopOE(self.h, i.h, o.h, dag))
+    def Meooe(self, i, o): _check(lib.gb_Meooe(self.h, i.h, o.h))
+    def MeooeDag(self, i, o): _check(lib.gb_MeooeDag(self.h, i.h, o.h))
+    def Mooee(self, i, o): _check(lib.gb_Mooee(self.h, i.h, o.h))
+    def MooeeDag(self, i, o): _check(lib.gb_MooeeDag(self.h, i.h, o.h))
+    def MooeeInv(self, i, o): _check(lib.gb_MooeeInv(self.h, i.h, o.h))
+    def MooeeInvDag(self, i, o): _check(lib.gb_MooeeInvDag(self.h, i.h, o.h))
+    def Mpc(self, i, o): _check(lib.gb_Mpc(self.h, i.h, o.h))
+    def MpcDag(self, i, o): _check(lib.gb_MpcDag(self.h, i.h, o.h))
+    def MpcDagMpc(self, i, o): _check(lib.gb_MpcDagMpc(self.h, i.h, o.h))
+
+    def sync(self):
+        _check(lib.gb_op_sync(self.h))
+
+    def event(self, slot: int):
+        _check(lib.gb_op_event_record(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        _check(lib.gb_op_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+    def bench_kernel(self, which: int, ins, outs, reps: int) -> float:
+        n = len(ins)
+        a = (_vp * n)(*[f.h for f in ins])
+        b = (_vp * n)(*[f.h for f in outs])
+        ms = C.c_double()
+        _check(lib.gb_bench_kernel(self.h, which, a, b, n, reps, C.byref(ms)))
+        return ms.value
+
+
+class WilsonFermion(_FermionOperator):
+    """WilsonFermion<WilsonImplD/F>; nrhs > 1 packs right-hand sides that share U."""
+
+    def __init__(self, U, dims, mass, phases=None, precision=F64, nrhs=1, stream=None, flags=0):
+        self.dims = tuple(int(x) for x in dims)
+        self.mass = float(mass)
+        self.kind = 0
+        ph = antiperiodic_t() if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        h = _vp()
+        _check(lib.gb_wilson_create(_dims(dims), float(mass), _dptr(ph), int(precision), int(nrhs),
+                                    _vp(stream or 0), int(flags), C.byref(h)))
+        self._finish(h, U, stream)
+
+
+class MobiusFermion(_FermionOperator):
+    """MobiusFermion<WilsonImplD/F>(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, b, c)."""
+
+    def __init__(self, U, dims, Ls, mf, M5, b, c, phases=None, precision=F64, nrhs=1, stream=None, flags=0):
+        self.dims = tuple(int(x) for x in dims)
+        self.mass = float(mf)
+        self.M5, self.b, self.c = float(M5), float(b), float(c)
+        self.kind = 1
+        ph = antiperiodic_t() if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        h = _vp()
+        _check(lib.gb_mobius_create(_dims(dims), int(Ls), float(mf), float(M5), float(b), float(c), _dptr(ph),
+                                    int(precision), int(nrhs), _vp(stream or 0), int(flags), C.byref(h)))
+        self._finish(h, U, stream)
+
+    def cayley_coeffs(self) -> dict:
+        out = np.empty(9 * self.Ls, dtype=np.float64)
+        _check(lib.gb_op_cayley_coeffs(self.h, _dptr(out)))
+        names = ["bs", "cs", "bee", "cee", "dee", "lee", "leem", "uee", "ueem"]
+        return {n: out[k * self.Ls:(k + 1) * self.Ls].copy() for k, n in enumerate(names)}
+
+
+# ---- linear operators and solvers -----------------------------------------------------
+class MdagMLinearOperator:
+    kind = 0
+
+    def __init__(self, op):
+        self.op = op
+
+    def HermOp(self, i, o):
+        self.op.MdagM(i, o)
+
+    def Op(self, i, o):
+        self.op.M(i, o)
+
+    def AdjOp(self, i, o):
+        self.op.Mdag(i, o)
+
+
+class SchurDiagMooeeOperator:
+    kind = 1
+
+    def __init__(self, op):
+        self.op = op
+
+    def Mpc(self, i, o):
+        self.op.Mpc(i, o)
+
+    def MpcDag(self, i, o):
+        self.op.MpcDag(i, o)
+
+    def HermOp(self, i, o):
+        self.op.MpcDagMpc(i, o)
+
+    Op = Mpc
+    AdjOp = MpcDag
+
+
+def _params(tol, maxit, err, **kw) -> CGParams:
+    p = CGParams()
+    lib.gb_cg_params_default(C.byref(p))
+    p.tolerance = float(tol)
+    p.max_iterations = int(maxit)
+    p.err_on_no_conv = 1 if err else 0
+    for k, v in kw.items():
+        if v is not None:
+            setattr(p, k, v)
+    return p
+
+
+class ConjugateGradient:
+    def __init__(self, tol, maxit, err_on_no_conv=True, check_every=None):
+        self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge = tol, maxit, err_on_no_conv
+        self.check_every = check_every
+        self.IterationsToComplete = 0
+        self.TrueResidual = 0.0
+        self.result = None
+
+    def params(self):
+        return _params(self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge, check_every=self.check_every)
+
+    def __call__(self, linop, src, psi):
+        p, r = self.params(), CGResult()
+        fn = lib.gb_cg_mdagm if linop.kind == 0 else lib.gb_cg_schur
+        _check(fn(linop.op.h, src.h, psi.h, C.byref(p), C.byref(r)))
+        self._store(r, linop.op)
+        return r
+
+    def _store(self, r, op):
+        self.result = r
+        self.IterationsToComplete = r.iterations
+        self.TrueResidual = r.true_residual
+        n = op.nrhs
+        it = (C.c_int * n)()
+        tr = (C.c_double * n)()
+        lib.gb_cg_last_per_rhs(op.h, it, tr)
+        self.per_rhs_iterations = list(it)
+        self.per_rhs_true_residual = list(tr)
+
+
+class ConjugateGradientReliableUpdate(ConjugateGradient):
+    def __init__(self, tol, maxit, delta, linop_f, linop_d, err_on_no_conv=True, relup_every=0,
+                 final_cleanup=True, check_every=None):
+        super().__init__(tol, maxit, err_on_no_conv, check_every)
+        self.Delta, self.linop_f, self.linop_d = delta, linop_f, linop_d
+        self.relup_every, self.DoFinalCleanup = relup_every, final_cleanup
+        self.ReliableUpdatesPerformed = 0
+        self.IterationsToCleanup = 0
+
+    def params(self):
+        return _params(self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge, delta=float(self.Delta),
+                       relup_every=int(self.relup_every), final_cleanup=1 if self.DoFinalCleanup else 0,
+                       check_every=self.check_every)
+
+    def __call__(self, src, psi):
+        p, r = self.params(), CGResult()
+        _check(lib.gb_cg_reliable(self.linop_d.op.h, self.linop_f.op.h, self.linop_d.kind, src.h, psi.h,
+                                  C.byref(p), C.byref(r)))
+        self._store(r, self.linop_d.op)
+        self.ReliableUpdatesPerformed = r.reliable_updates
+        self.IterationsToCleanup = r.cleanup_iterations
+        return r
+
+
+class SchurRedBlackDiagMooeeSolve:
+    """SchurRedBlackDiagMooeeSolve(solver)(op, src, sol).  `solver` is a ConjugateGradient
+    (plain, in op's precision) or a ConjugateGradientReliableUpdate (mixed precision, whose
+    linop_f.op supplies the inner operator)."""
+
+    def __init__(self, solver):
+        self.solver = solver
+        self.unprec_residual = None
+
+    def __call__(self, op, src, sol):
+        s = self.solver
+        lo = s.linop_f.op.h if isinstance(s, ConjugateGradientReliableUpdate) else None
+        p, r = s.params(), CGResult()
+        res = np.zeros(op.nrhs, dtype=np.float64)
+        _check(lib.gb_schur_solve(op.h, lo, src.h, sol.h, C.byref(p), C.byref(r), _dptr(res)))
+        s._store(r, op)
+        if isinstance(s, ConjugateGradientReliableUpdate):
+            s.ReliableUpdatesPerformed = r.reliable_updates
+            s.IterationsToCleanup = r.cleanup_iterations
+        self.unprec_residual = res
+        return r

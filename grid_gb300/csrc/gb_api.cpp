@@ -1,0 +1,777 @@
+// gb_api.cpp -- C ABI: library, operators, fields, field algebra and the operator call
+// sequences of Grid's WilsonFermion / CayleyFermion5D (host side).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "gb_ops.h"
+
+namespace gb {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+size_t Op::link_bytes_per_parity() const { return size_t(half4) * 8 * 18 * (prec == GB_F64 ? 8 : 4); }
+
+size_t Field::half_bytes() const { return n5 * spinor_bytes(prec); }
+void* Field::half_ptr(int parity) const {
+  if (!full()) return data;
+  return static_cast<char*>(data) + (parity ? half_bytes() : 0);
+}
+float* Field::half_norms(int parity) const {
+  if (!norms) return nullptr;
+  if (!full()) return norms;
+  return norms + (parity ? n5 : 0);
+}
+
+static int check_op(const Op* op) {
+  if (!op) { set_error("null operator"); return GB_ERR_BAD_ARG; }
+  if (!op->gauge_loaded) { set_error("operator has no gauge field: call gb_op_import_gauge"); return GB_ERR_BAD_ARG; }
+  return GB_OK;
+}
+static int check_conf(const Field* a, const Field* b) {
+  if (!a || !b) { set_error("null field"); return GB_ERR_BAD_ARG; }
+  if (a->op != b->op || a->n5 != b->n5) { set_error("fields are not conformable"); return GB_ERR_BAD_ARG; }
+  return GB_OK;
+}
+static int check_subset(const Field* f, int subset, const char* what) {
+  if (f->subset != subset) {
+    set_error("%s: field is on the wrong checkerboard (subset %d, expected %d)", what, f->subset, subset);
+    return GB_ERR_BAD_PARITY;
+  }
+  return GB_OK;
+}
+
+int field_alloc(Op* op, int subset, int prec, Field** out) {
+  Field* f = new (std::nothrow) gb_field_s;
+  if (!f) { set_error("host allocation failed"); return GB_ERR_OOM; }
+  f->op = op;
+  f->subset = subset;
+  f->prec = prec;
+  f->n5 = op->n5();
+  const size_t halves = subset == GB_FULL ? 2 : 1;
+  cudaError_t e = cudaMalloc(&f->data, halves * f->half_bytes());
+  if (e != cudaSuccess) {
+    delete static_cast<gb_field_s*>(f);
+    set_error("cudaMalloc of %zu bytes failed: %s", halves * f->n5 * spinor_bytes(prec), cudaGetErrorString(e));
+    return GB_ERR_OOM;
+  }
+  if (prec == GB_F16) {
+    e = cudaMalloc(&f->norms, halves * f->n5 * sizeof(float));
+    if (e != cudaSuccess) {
+      cudaFree(f->data);
+      delete static_cast<gb_field_s*>(f);
+      set_error("cudaMalloc of norms failed: %s", cudaGetErrorString(e));
+      return GB_ERR_OOM;
+    }
+  }
+  *out = f;
+  return GB_OK;
+}
+
+void field_free(Field* f) {
+  if (!f) return;
+  if (f->owned) {
+    cudaFree(f->data);
+    if (f->norms) cudaFree(f->norms);
+  }
+  delete static_cast<gb_field_s*>(f);
+}
+
+// workspace: the slot-th cached field of (full or half, precision); a half workspace
+// field is relabelled to the requested checkerboard
+int ws_get(Op* op, int subset, int prec, int slot, Field** out) {
+  const bool want_full = subset == GB_FULL;
+  int seen = 0;
+  for (Field* f : op->ws) {
+    if (f->full() == want_full && f->prec == prec) {
+      if (seen == slot) {
+        if (!want_full) f->subset = subset;
+        *out = f;
+        return GB_OK;
+      }
+      seen++;
+    }
+  }
+  Field* f = nullptr;
+  for (int k = seen; k <= slot; k++) {
+    GB_TRY(field_alloc(op, subset, prec, &f));
+    op->ws.push_back(f);
+  }
+  *out = f;
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// reductions on whole fields (both halves of a full field), results to host
+// ---------------------------------------------------------------------------------------
+static int parts_per_half(Op* op) {
+  int g, B;
+  red_grid(op, op->n5(), &g, &B);
+  return g;
+}
+
+int field_norm2_dev(Field* f, double* d_out) {
+  Op* op = f->op;
+  const int g = parts_per_half(op);
+  const int halves = f->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_norm2_partial(op, half_view(f, h), f->n5, op->d_partial + size_t(h) * g * op->nrhs));
+  return launch_reduce_final(op, op->d_partial, g * halves, 1, d_out);
+}
+
+int field_inner_dev(Field* a, Field* b, double* d_out) {
+  Op* op = a->op;
+  const int g = parts_per_half(op);
+  const int halves = a->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_inner_partial(op, half_view(a, h), half_view(b, h), a->n5, op->d_partial + size_t(h) * g * op->nrhs * 2));
+  return launch_reduce_final(op, op->d_partial, g * halves, 2, d_out);
+}
+
+static int fetch(Op* op, const double* d_src, double* host, size_t n) {
+  GB_CHECK_CUDA(cudaMemcpyAsync(op->h_result, d_src, n * sizeof(double), cudaMemcpyDeviceToHost, op->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  std::memcpy(host, op->h_result, n * sizeof(double));
+  return GB_OK;
+}
+
+int field_norm2(Field* f, double* out) {
+  GB_TRY(field_norm2_dev(f, f->op->d_result));
+  return fetch(f->op, f->op->d_result, out, f->op->nrhs);
+}
+int field_inner(Field* a, Field* b, double* out) {
+  GB_TRY(field_inner_dev(a, b, a->op->d_result));
+  return fetch(a->op, a->op->d_result, out, size_t(a->op->nrhs) * 2);
+}
+
+int field_axpby(Field* z, double a, double b, Field* x, Field* y) {
+  const int halves = z->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_axpby(z->op, half_view(z, h), a, half_view(x, h), b, half_view(y, h), z->n5));
+  return GB_OK;
+}
+int field_scale(Field* z, double a, Field* x) {
+  const int halves = z->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++) GB_TRY(launch_scale(z->op, half_view(z, h), a, half_view(x, h), z->n5));
+  return GB_OK;
+}
+int field_copy(Field* dst, Field* src) {
+  if (dst == src) return GB_OK;
+  const int halves = dst->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++) GB_TRY(launch_copy(dst->op, half_view(dst, h), half_view(src, h), dst->n5));
+  return GB_OK;
+}
+int field_zero(Field* z) {
+  const int halves = z->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++) GB_TRY(launch_zero(z->op, half_view(z, h), z->n5));
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Operator call sequences
+// ---------------------------------------------------------------------------------------
+// 5D coefficient sets (CayleyFermion5DImplementation.h:155-271)
+void coeffs_meooe5d(const Op* op, int dag, std::vector<double>& l, std::vector<double>& d, std::vector<double>& u) {
+  const int Ls = op->Ls;
+  d = op->bs;
+  u.assign(Ls, 0);
+  l.assign(Ls, 0);
+  if (!dag) {
+    u = op->cs;
+    l = op->cs;
+    u[Ls - 1] = -op->mass * u[Ls - 1];
+    l[0] = -op->mass * l[0];
+  } else {
+    for (int s = 0; s < Ls; s++) {
+      if (s == 0) { u[s] = op->cs[s + 1]; l[s] = -op->mass * op->cs[Ls - 1]; }
+      else if (s == Ls - 1) { u[s] = -op->mass * op->cs[0]; l[s] = op->cs[s - 1]; }
+      else { u[s] = op->cs[s + 1]; l[s] = op->cs[s - 1]; }
+    }
+  }
+}
+void coeffs_mooee(const Op* op, int dag, std::vector<double>& l, std::vector<double>& d, std::vector<double>& u) {
+  const int Ls = op->Ls;
+  d = op->bee;
+  u.assign(Ls, 0);
+  l.assign(Ls, 0);
+  if (!dag) {
+    for (int i = 0; i < Ls; i++) { u[i] = -op->cee[i]; l[i] = -op->cee[i]; }
+    u[Ls - 1] = -op->mass * u[Ls - 1];
+    l[0] = -op->mass * l[0];
+  } else {
+    for (int s = 0; s < Ls; s++) {
+      if (s == 0) { u[s] = -op->cee[s + 1]; l[s] = op->mass * op->cee[Ls - 1]; }
+      else if (s == Ls - 1) { u[s] = op->mass * op->cee[0]; l[s] = -op->cee[s - 1]; }
+      else { u[s] = -op->cee[s + 1]; l[s] = -op->cee[s - 1]; }
+    }
+  }
+}
+// M5D / M5Ddag with unit diagonal used by M and Mdag (CayleyFermion5DImplementation.h:130-231)
+void coeffs_m5d_unit(const Op* op, std::vector<double>& l, std::vector<double>& d, std::vector<double>& u) {
+  const int Ls = op->Ls;
+  d.assign(Ls, 1.0);
+  u.assign(Ls, -1.0);
+  l.assign(Ls, -1.0);
+  u[Ls - 1] = op->mass;
+  l[0] = op->mass;
+}
+
+static int m5d_field(Op* op, Field* psi, Field* phi, Field* chi, const std::vector<double>& l,
+                     const std::vector<double>& d, const std::vector<double>& u, int dag, Field* z, double zc) {
+  const int halves = chi->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++) {
+    HalfView zv = z ? half_view(z, h) : HalfView{nullptr, nullptr, chi->prec};
+    GB_TRY(launch_m5d_z(op, half_view(psi, h), half_view(phi, h), half_view(chi, h), l.data(), d.data(), u.data(), dag,
+                        chi->n5, z ? &zv : nullptr, zc));
+  }
+  return GB_OK;
+}
+
+int op_meooe5d(Op* op, Field* in, Field* out, int dag) {
+  std::vector<double> l, d, u;
+  coeffs_meooe5d(op, dag, l, d, u);
+  return m5d_field(op, in, in, out, l, d, u, dag, nullptr, 0);
+}
+
+int op_dhop_cb(Op* op, Field* in, Field* out, int dag) {
+  // in: half field of parity p ; out: parity 1-p
+  if (in->full() || out->full()) { set_error("DhopEO/OE: half fields expected"); return GB_ERR_BAD_PARITY; }
+  const int p = in->subset;
+  out->subset = 1 - p;
+  return launch_dhop(op, half_view(in, 0), half_view(out, 0), 1 - p, dag);
+}
+
+int op_dhop_full(Op* op, Field* in, Field* out, int dag) {
+  if (!in->full() || !out->full()) { set_error("Dhop: full fields expected"); return GB_ERR_BAD_PARITY; }
+  GB_TRY(launch_dhop(op, half_view(in, 1), half_view(out, 0), 0, dag));
+  return launch_dhop(op, half_view(in, 0), half_view(out, 1), 1, dag);
+}
+
+int op_meooe(Op* op, Field* in, Field* out, int dag) {
+  if (in->full()) { set_error("Meooe: half field expected"); return GB_ERR_BAD_PARITY; }
+  if (op->kind == 0) return op_dhop_cb(op, in, out, dag);
+  Field* t;
+  if (!dag) {  // Meooe = DhopEO/OE (Meooe5D in)
+    GB_TRY(ws_get(op, in->subset, in->prec, WS_MEOOE_A, &t));
+    GB_TRY(op_meooe5d(op, in, t, 0));
+    return op_dhop_cb(op, t, out, 0);
+  }
+  // MeooeDag = MeooeDag5D (DhopEO/OE^dag in)
+  GB_TRY(ws_get(op, 1 - in->subset, in->prec, WS_MEOOE_B, &t));
+  GB_TRY(op_dhop_cb(op, in, t, 1));
+  out->subset = 1 - in->subset;
+  return op_meooe5d(op, t, out, 1);
+}
+
+int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
+  out->subset = in->subset;
+  if (op->kind == 0) {
+    if (z) return field_axpby(out, op->diag_mass, zc, in, z);
+    return field_scale(out, op->diag_mass, in);
+  }
+  std::vector<double> l, d, u;
+  coeffs_mooee(op, dag, l, d, u);
+  return m5d_field(op, in, in, out, l, d, u, dag, z, zc);
+}
+
+int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
+  out->subset = in->subset;
+  if (op->kind == 0) return field_scale(out, 1.0 / op->diag_mass, in);
+  const int halves = in->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_mooee_inv(op, half_view(in, h), half_view(out, h), dag, size_t(op->half4)));
+  return GB_OK;
+}
+
+// SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349)
+int op_mpc(Op* op, Field* in, Field* out, int dag) {
+  if (in->subset != GB_ODD) { set_error("Mpc: odd checkerboard expected"); return GB_ERR_BAD_PARITY; }
+  Field *te1, *te2, *to;
+  GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E1, &te1));
+  GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E2, &te2));
+  GB_TRY(ws_get(op, GB_ODD, in->prec, WS_MPC_O, &to));
+  GB_TRY(op_meooe(op, in, te1, dag));
+  GB_TRY(op_mooee_inv(op, te1, te2, dag));
+  GB_TRY(op_meooe(op, te2, to, dag));
+  return op_mooee(op, in, out, dag, to, -1.0);  // out = Mooee in - tmp
+}
+
+int op_mpcdagmpc(Op* op, Field* in, Field* out) {
+  Field* t;
+  GB_TRY(ws_get(op, GB_ODD, in->prec, WS_MPCDAGMPC, &t));
+  GB_TRY(op_mpc(op, in, t, 0));
+  return op_mpc(op, t, out, 1);
+}
+
+// M / Mdag on full fields (WilsonFermionImplementation.h:113-127,
+// CayleyFermion5DImplementation.h:272-306)
+int op_m(Op* op, Field* in, Field* out, int dag) {
+  if (!in->full() || !out->full()) { set_error("M: full fields expected"); return GB_ERR_BAD_PARITY; }
+  if (op->kind == 0) {
+    GB_TRY(op_dhop_full(op, in, out, dag));
+    return field_axpby(out, 1.0, op->diag_mass, out, in);
+  }
+  Field* Din;
+  GB_TRY(ws_get(op, GB_FULL, in->prec, WS_M_DIN, &Din));
+  Field* t;
+  GB_TRY(ws_get(op, GB_FULL, in->prec, WS_M_T, &t));
+  std::vector<double> l, d, u;
+  coeffs_m5d_unit(op, l, d, u);
+  if (!dag) {
+    GB_TRY(op_meooe5d(op, in, Din, 0));            // Din = Meooe5D psi
+    GB_TRY(op_dhop_full(op, Din, t, 0));           // t = Dhop Din
+    GB_TRY(field_axpby(t, 1.0, 4.0 - op->M5, t, Din));  // t = DW Din
+    return m5d_field(op, in, t, out, l, d, u, 0, in, 1.0);  // out = M5D(psi, t) + psi
+  }
+  GB_TRY(op_dhop_full(op, in, t, 1));
+  GB_TRY(field_axpby(t, 1.0, 4.0 - op->M5, t, in));   // t = DW^dag psi
+  GB_TRY(op_meooe5d(op, t, Din, 1));               // Din = MeooeDag5D t
+  return m5d_field(op, in, Din, out, l, d, u, 1, in, 1.0);  // out = M5Ddag(psi, Din) + psi
+}
+
+int op_mdagm(Op* op, Field* in, Field* out) {
+  Field* t;
+  GB_TRY(ws_get(op, GB_FULL, in->prec, WS_MDAGM, &t));
+  GB_TRY(op_m(op, in, t, 0));
+  return op_m(op, t, out, 1);
+}
+
+// ---------------------------------------------------------------------------------------
+// neighbour tables
+// ---------------------------------------------------------------------------------------
+int build_neighbours(Op* op) {
+  const int* L = op->dims;
+  std::vector<int> tab(size_t(op->half4) * 8);
+  for (int p = 0; p < 2; p++) {
+    for (int64_t site = 0; site < op->vol4; site++) {
+      int x[4];
+      int64_t r = site;
+      for (int k = 0; k < 4; k++) { x[k] = int(r % L[k]); r /= L[k]; }
+      if (((x[0] + x[1] + x[2] + x[3]) & 1) != p) continue;
+      const int64_t xcb = site >> 1;
+      for (int leg = 0; leg < 8; leg++) {
+        const int mu = leg & 3;
+        int y[4] = {x[0], x[1], x[2], x[3]};
+        y[mu] = (y[mu] + (leg < 4 ? 1 : -1) + L[mu]) % L[mu];
+        const int64_t ns = y[0] + int64_t(L[0]) * (y[1] + int64_t(L[1]) * (y[2] + int64_t(L[2]) * y[3]));
+        tab[size_t(xcb) * 8 + leg] = int(ns >> 1);
+      }
+    }
+    GB_CHECK_CUDA(cudaMemcpy(op->nbr[p], tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  return GB_OK;
+}
+
+static void cayley_setup(Op* op) {
+  const int Ls = op->Ls;
+  const double b = op->b, c = op->c, M5 = op->M5, mf = op->mass;
+  op->bs.assign(Ls, 0); op->cs.assign(Ls, 0); op->bee.assign(Ls, 0); op->cee.assign(Ls, 0);
+  op->dee.assign(Ls, 0); op->lee.assign(Ls, 0); op->leem.assign(Ls, 0); op->uee.assign(Ls, 0); op->ueem.assign(Ls, 0);
+  // Moebius tanh: omega_s = 1 (MobiusFermion.h:63-67, Zolotarev.cc:471-473)
+  for (int i = 0; i < Ls; i++) {
+    const double omega = 1.0;
+    op->bs[i] = 0.5 * ((b + c) / omega + (b - c));
+    op->cs[i] = 0.5 * ((b + c) / omega - (b - c));
+    op->bee[i] = op->bs[i] * (4.0 - M5) + 1.0;
+    op->cee[i] = 1.0 - op->cs[i] * (4.0 - M5);
+  }
+  const std::vector<double>& aee = op->cee;
+  for (int i = 0; i < Ls; i++) {
+    op->dee[i] = op->bee[i];
+    if (i < Ls - 1) {
+      op->lee[i] = -op->cee[i + 1] / op->bee[i];
+      op->leem[i] = mf * op->cee[Ls - 1] / op->bee[0];
+      for (int j = 0; j < i; j++) op->leem[i] *= aee[j] / op->bee[j + 1];
+      op->uee[i] = -aee[i] / op->bee[i];
+      op->ueem[i] = mf;
+      for (int j = 1; j <= i; j++) op->ueem[i] *= op->cee[j] / op->bee[j];
+      op->ueem[i] *= aee[0] / op->bee[0];
+    }
+  }
+  double delta_d = mf * op->cee[Ls - 1];
+  for (int j = 0; j < Ls - 1; j++) delta_d *= op->cee[j] / op->bee[j];
+  op->dee[Ls - 1] += delta_d;
+}
+
+static void op_release(Op* op) {
+  for (auto& e : op->events)
+    if (e) cudaEventDestroy(e);
+  for (Field* f : op->ws) field_free(f);
+  op->ws.clear();
+  for (int p = 0; p < 2; p++) {
+    cudaFree(op->links[p]);
+    cudaFree(op->nbr[p]);
+  }
+  cudaFree(op->d_err);
+  cudaFree(op->d_partial);
+  cudaFree(op->d_result);
+  cudaFreeHost(op->h_result);
+  cudaFree(op->d_stage);
+  cudaFree(op->d_cg);
+  cudaFreeHost(op->h_cg);
+  cudaFree(op->d_all_done);
+}
+
+static int op_create(int kind, const int dims[4], int Ls, double mass, double M5, double b, double c,
+                     const double* phases, int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out) {
+  if (!dims || !out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  for (int k = 0; k < 4; k++)
+    if (dims[k] < 2 || (dims[k] & 1)) { set_error("dims[%d] = %d must be even and >= 2", k, dims[k]); return GB_ERR_BAD_ARG; }
+  if (precision < GB_F64 || precision > GB_F16) { set_error("bad precision %d", precision); return GB_ERR_BAD_ARG; }
+  if (nrhs < 1 || Ls < 1) { set_error("nrhs and Ls must be >= 1"); return GB_ERR_BAD_ARG; }
+  if (kind == 1 && (Ls < 2 || Ls > kMaxLs)) { set_error("Ls = %d outside [2, %d]", Ls, kMaxLs); return GB_ERR_BAD_ARG; }
+  if (Ls * nrhs > kMaxL5) { set_error("Ls*nrhs = %d exceeds %d", Ls * nrhs, kMaxL5); return GB_ERR_UNSUPPORTED; }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return GB_ERR_NO_DEVICE; }
+  gb_op_s* op = new (std::nothrow) gb_op_s;
+  if (!op) { set_error("host allocation failed"); return GB_ERR_OOM; }
+  op->kind = kind;
+  op->vol4 = 1;
+  for (int k = 0; k < 4; k++) { op->dims[k] = dims[k]; op->vol4 *= dims[k]; }
+  op->half4 = op->vol4 / 2;
+  if (op->half4 * 8 > int64_t(0x7fffffff)) { delete op; set_error("lattice too large for 32-bit neighbour tables"); return GB_ERR_UNSUPPORTED; }
+  op->Ls = kind == 1 ? Ls : 1;
+  op->nrhs = nrhs;
+  op->L5 = op->Ls * nrhs;
+  op->prec = precision;
+  op->mass = mass;
+  op->M5 = M5;
+  op->b = b;
+  op->c = c;
+  op->diag_mass = 4.0 + mass;
+  op->flags = flags;
+  op->stream = static_cast<cudaStream_t>(stream);
+  cudaGetDevice(&op->device);
+  for (int k = 0; k < 4; k++) {
+    op->phases[k] = phases ? std::complex<double>(phases[2 * k], phases[2 * k + 1]) : std::complex<double>(1, 0);
+    const std::complex<double> z = op->phases[k];
+    if (!(z.imag() == 0 && (z.real() == 1 || z.real() == -1))) op->phases_pm1 = false;
+  }
+  if (kind == 1) cayley_setup(op);
+  int rc = GB_OK;
+  auto alloc = [&](void** p, size_t n) {
+    if (rc != GB_OK) return;
+    if (cudaMalloc(p, n) != cudaSuccess) { set_error("cudaMalloc of %zu bytes failed", n); rc = GB_ERR_OOM; }
+  };
+  for (int p = 0; p < 2; p++) {
+    alloc(&op->links[p], op->link_bytes_per_parity());
+    alloc(reinterpret_cast<void**>(&op->nbr[p]), size_t(op->half4) * 8 * sizeof(int));
+  }
+  alloc(reinterpret_cast<void**>(&op->d_err), sizeof(int));
+  alloc(reinterpret_cast<void**>(&op->d_partial), size_t(2) * kRedBlocks * nrhs * 2 * sizeof(double));
+  alloc(reinterpret_cast<void**>(&op->d_result), size_t(nrhs) * 8 * sizeof(double));
+  alloc(reinterpret_cast<void**>(&op->d_cg), size_t(nrhs) * sizeof(CGScalars));
+  alloc(reinterpret_cast<void**>(&op->d_all_done), 4 * sizeof(int));
+  if (rc == GB_OK && cudaMallocHost(reinterpret_cast<void**>(&op->h_result), size_t(nrhs) * 8 * sizeof(double)) != cudaSuccess) rc = GB_ERR_OOM;
+  if (rc == GB_OK && cudaMallocHost(reinterpret_cast<void**>(&op->h_cg), size_t(nrhs) * sizeof(CGScalars) + 64) != cudaSuccess) rc = GB_ERR_OOM;
+  if (rc == GB_OK && cudaMemset(op->d_err, 0, sizeof(int)) != cudaSuccess) rc = GB_ERR_CUDA;
+  if (rc == GB_OK) rc = build_neighbours(op);
+  if (rc != GB_OK) {
+    op_release(op);
+    delete op;
+    return rc;
+  }
+  op->last_iters.assign(nrhs, 0);
+  op->last_resid.assign(nrhs, 0.0);
+  *out = op;
+  return GB_OK;
+}
+
+int op_import_gauge_dev(Op* op, const double* U_dev) {
+  for (int p = 0; p < 2; p++) GB_TRY(launch_double_store(op, U_dev, p));
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  op->gauge_loaded = true;
+  return GB_OK;
+}
+
+int ensure_stage(Op* op, size_t bytes) {
+  if (op->stage_bytes >= bytes) return GB_OK;
+  cudaFree(op->d_stage);
+  op->d_stage = nullptr;
+  op->stage_bytes = 0;
+  if (cudaMalloc(&op->d_stage, bytes) != cudaSuccess) { set_error("cudaMalloc of %zu staging bytes failed", bytes); return GB_ERR_OOM; }
+  op->stage_bytes = bytes;
+  return GB_OK;
+}
+
+size_t field_host_doubles(const Field* f) {
+  const Op* op = f->op;
+  const size_t n4 = f->full() ? size_t(op->vol4) : size_t(op->half4);
+  return n4 * op->L5 * 24;
+}
+
+int field_import_dev(Field* f, const double* dev) {
+  if (f->full()) {
+    for (int p = 0; p < 2; p++) GB_TRY(launch_import_half(f->op, dev, half_view(f, p), p, 1));
+  } else {
+    GB_TRY(launch_import_half(f->op, dev, half_view(f, 0), f->subset, 0));
+  }
+  return GB_OK;
+}
+int field_export_dev(Field* f, double* dev) {
+  if (f->full()) {
+    for (int p = 0; p < 2; p++) GB_TRY(launch_export_half(f->op, half_view(f, p), dev, p, 1));
+  } else {
+    GB_TRY(launch_export_half(f->op, half_view(f, 0), dev, f->subset, 0));
+  }
+  return GB_OK;
+}
+
+int check_device_error(Op* op) {
+  int h = 0;
+  GB_CHECK_CUDA(cudaMemcpyAsync(&h, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  if (h) {
+    set_error("a bounded device wait timed out");
+    cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream);
+    return GB_ERR_TIMEOUT;
+  }
+  return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+// =======================================================================================
+// C ABI
+// =======================================================================================
+extern "C" {
+
+int gb_version(void) { return 100; }
+const char* gb_last_error(void) { return gb::g_err; }
+const char* gb_status_string(int s) {
+  switch (s) {
+    case GB_OK: return "ok";
+    case GB_ERR_BAD_ARG: return "bad argument";
+    case GB_ERR_BAD_PARITY: return "checkerboard mismatch";
+    case GB_ERR_OOM: return "out of memory";
+    case GB_ERR_CUDA: return "CUDA error";
+    case GB_ERR_NOT_CONVERGED: return "not converged";
+    case GB_ERR_TIMEOUT: return "device wait timed out";
+    case GB_ERR_NO_DEVICE: return "no CUDA device";
+    case GB_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+int gb_device_count(int* n) {
+  int k = 0;
+  if (cudaGetDeviceCount(&k) != cudaSuccess) k = 0;
+  if (n) *n = k;
+  return GB_OK;
+}
+
+int gb_wilson_create(const int dims[4], double mass, const double* phases, int precision, int nrhs, void* stream,
+                     unsigned flags, gb_op_t* out) {
+  return op_create(0, dims, 1, mass, 0, 0, 0, phases, precision, nrhs, stream, flags, out);
+}
+int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,
+                     int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out) {
+  return op_create(1, dims, Ls, mf, M5, b, c, phases, precision, nrhs, stream, flags, out);
+}
+int gb_op_destroy(gb_op_t op) {
+  if (!op) return GB_OK;
+  cudaStreamSynchronize(op->stream);
+  op_release(op);
+  delete op;
+  return GB_OK;
+}
+int gb_op_import_gauge(gb_op_t op, const double* U_host) {
+  if (!op || !U_host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  const size_t bytes = size_t(op->vol4) * 4 * 9 * 16;
+  GB_TRY(ensure_stage(op, bytes));
+  GB_CHECK_CUDA(cudaMemcpyAsync(op->d_stage, U_host, bytes, cudaMemcpyHostToDevice, op->stream));
+  return op_import_gauge_dev(op, op->d_stage);
+}
+int gb_op_import_gauge_device(gb_op_t op, const double* U_device) {
+  if (!op || !U_device) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  return op_import_gauge_dev(op, U_device);
+}
+int gb_op_info(gb_op_t op, int* Ls, int* nrhs, int64_t* half_sites4, int* precision) {
+  if (!op) { set_error("null operator"); return GB_ERR_BAD_ARG; }
+  if (Ls) *Ls = op->Ls;
+  if (nrhs) *nrhs = op->nrhs;
+  if (half_sites4) *half_sites4 = op->half4;
+  if (precision) *precision = op->prec;
+  return GB_OK;
+}
+int gb_op_set_stream(gb_op_t op, void* stream) {
+  if (!op) { set_error("null operator"); return GB_ERR_BAD_ARG; }
+  op->stream = static_cast<cudaStream_t>(stream);
+  return GB_OK;
+}
+int gb_op_cayley_coeffs(gb_op_t op, double* out) {
+  if (!op || !out || op->kind != 1) { set_error("not a Moebius operator"); return GB_ERR_BAD_ARG; }
+  const std::vector<double>* v[9] = {&op->bs, &op->cs, &op->bee, &op->cee, &op->dee, &op->lee, &op->leem, &op->uee, &op->ueem};
+  for (int k = 0; k < 9; k++) std::memcpy(out + k * op->Ls, v[k]->data(), op->Ls * sizeof(double));
+  return GB_OK;
+}
+
+int gb_field_create(gb_op_t op, int subset, int precision, gb_field_t* out) {
+  if (!op || !out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (subset < GB_EVEN || subset > GB_FULL) { set_error("bad subset %d", subset); return GB_ERR_BAD_ARG; }
+  Field* f;
+  GB_TRY(field_alloc(op, subset, precision, &f));
+  *out = static_cast<gb_field_t>(f);
+  return GB_OK;
+}
+int gb_field_destroy(gb_field_t f) {
+  if (f) {
+    cudaStreamSynchronize(f->op->stream);
+    field_free(f);
+  }
+  return GB_OK;
+}
+int gb_field_subset(gb_field_t f, int* subset) {
+  if (!f || !subset) return GB_ERR_BAD_ARG;
+  *subset = f->subset;
+  return GB_OK;
+}
+int gb_field_set_subset(gb_field_t f, int subset) {
+  if (!f || f->full() || subset == GB_FULL || subset < 0) { set_error("only half fields can be relabelled"); return GB_ERR_BAD_ARG; }
+  f->subset = subset;
+  return GB_OK;
+}
+int gb_field_host_len(gb_field_t f, size_t* n) {
+  if (!f || !n) return GB_ERR_BAD_ARG;
+  *n = field_host_doubles(f);
+  return GB_OK;
+}
+int gb_field_import(gb_field_t f, const double* host) {
+  if (!f || !host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  Op* op = f->op;
+  const size_t bytes = field_host_doubles(f) * sizeof(double);
+  GB_TRY(ensure_stage(op, bytes));
+  GB_CHECK_CUDA(cudaMemcpyAsync(op->d_stage, host, bytes, cudaMemcpyHostToDevice, op->stream));
+  GB_TRY(field_import_dev(f, op->d_stage));
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  return GB_OK;
+}
+int gb_field_export(gb_field_t f, double* host) {
+  if (!f || !host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  Op* op = f->op;
+  const size_t bytes = field_host_doubles(f) * sizeof(double);
+  GB_TRY(ensure_stage(op, bytes));
+  GB_TRY(field_export_dev(f, op->d_stage));
+  GB_CHECK_CUDA(cudaMemcpyAsync(host, op->d_stage, bytes, cudaMemcpyDeviceToHost, op->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  return GB_OK;
+}
+int gb_field_import_device(gb_field_t f, const double* dev) {
+  if (!f || !dev) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  return field_import_dev(f, dev);
+}
+int gb_field_export_device(gb_field_t f, double* dev) {
+  if (!f || !dev) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  return field_export_dev(f, dev);
+}
+
+int gb_field_zero(gb_field_t f) {
+  if (!f) return GB_ERR_BAD_ARG;
+  return field_zero(f);
+}
+int gb_field_copy(gb_field_t dst, gb_field_t src) {
+  GB_TRY(check_conf(dst, src));
+  if (dst->full() != src->full()) { set_error("copy: full/half mismatch"); return GB_ERR_BAD_PARITY; }
+  dst->subset = src->subset;
+  return field_copy(dst, src);
+}
+int gb_field_norm2(gb_field_t f, double* out) {
+  if (!f || !out) return GB_ERR_BAD_ARG;
+  return field_norm2(f, out);
+}
+int gb_field_inner(gb_field_t a, gb_field_t b, double* out) {
+  GB_TRY(check_conf(a, b));
+  if (!out) return GB_ERR_BAD_ARG;
+  if (a->subset != b->subset) { set_error("innerProduct: checkerboard mismatch"); return GB_ERR_BAD_PARITY; }
+  return field_inner(a, b, out);
+}
+int gb_field_axpby(gb_field_t z, double a, double b, gb_field_t x, gb_field_t y) {
+  GB_TRY(check_conf(z, x));
+  GB_TRY(check_conf(z, y));
+  if (x->subset != y->subset) { set_error("axpby: checkerboard mismatch"); return GB_ERR_BAD_PARITY; }
+  if (z->full() != x->full()) { set_error("axpby: full/half mismatch"); return GB_ERR_BAD_PARITY; }
+  z->subset = x->subset;
+  return field_axpby(z, a, b, x, y);
+}
+int gb_field_axpy(gb_field_t z, double a, gb_field_t x, gb_field_t y) { return gb_field_axpby(z, a, 1.0, x, y); }
+int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, double* norm_out) {
+  GB_TRY(check_conf(z, x));
+  GB_TRY(check_conf(z, y));
+  if (x->subset != y->subset) { set_error("axpy_norm: checkerboard mismatch"); return GB_ERR_BAD_PARITY; }
+  Op* op = z->op;
+  z->subset = x->subset;
+  int g, B;
+  GB_TRY(red_grid(op, op->n5(), &g, &B));
+  const int halves = z->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_axpy_norm_partial(op, half_view(z, h), a, half_view(x, h), half_view(y, h), z->n5,
+                                    op->d_partial + size_t(h) * g * op->nrhs));
+  GB_TRY(launch_reduce_final(op, op->d_partial, g * halves, 1, op->d_result));
+  return fetch(op, op->d_result, norm_out, op->nrhs);
+}
+int gb_field_pick_checkerboard(gb_field_t half, gb_field_t full) {
+  GB_TRY(check_conf(half, full));
+  if (half->full() || !full->full()) { set_error("pickCheckerboard: (half, full) expected"); return GB_ERR_BAD_PARITY; }
+  Field* f = full;
+  return launch_copy(half->op, half_view(half, 0), half_view(f, half->subset), half->n5);
+}
+int gb_field_set_checkerboard(gb_field_t full, gb_field_t half) {
+  GB_TRY(check_conf(half, full));
+  if (half->full() || !full->full()) { set_error("setCheckerboard: (full, half) expected"); return GB_ERR_BAD_PARITY; }
+  Field* f = full;
+  return launch_copy(half->op, half_view(f, half->subset), half_view(half, 0), half->n5);
+}
+
+// ---- operators ----
+#define GB_OP_PRE(op, in, out)                                                     \
+  GB_TRY(check_op(op));                                                            \
+  GB_TRY(check_conf(in, out));                                                     \
+  if (in->op != op) { set_error("field belongs to another operator"); return GB_ERR_BAD_ARG; } \
+  if (in == out) { set_error("in and out must be distinct fields"); return GB_ERR_BAD_ARG; }
+
+int gb_M(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_m(op, in, out, 0); }
+int gb_Mdag(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_m(op, in, out, 1); }
+int gb_MdagM(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_mdagm(op, in, out); }
+int gb_Dhop(gb_op_t op, gb_field_t in, gb_field_t out, int dag) {
+  GB_OP_PRE(op, in, out);
+  return op_dhop_full(op, in, out, dag);
+}
+int gb_DhopEO(gb_op_t op, gb_field_t in, gb_field_t out, int dag) {
+  GB_OP_PRE(op, in, out);
+  GB_TRY(check_subset(in, GB_ODD, "DhopEO"));
+  return op_dhop_cb(op, in, out, dag);
+}
+int gb_DhopOE(gb_op_t op, gb_field_t in, gb_field_t out, int dag) {
+  GB_OP_PRE(op, in, out);
+  GB_TRY(check_subset(in, GB_EVEN, "DhopOE"));
+  return op_dhop_cb(op, in, out, dag);
+}
+int gb_Meooe(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_meooe(op, in, out, 0); }
+int gb_MeooeDag(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_meooe(op, in, out, 1); }
+int gb_Mooee(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_mooee(op, in, out, 0, nullptr, 0); }
+int gb_MooeeDag(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_mooee(op, in, out, 1, nullptr, 0); }
+int gb_MooeeInv(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_mooee_inv(op, in, out, 0); }
+int gb_MooeeInvDag(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_mooee_inv(op, in, out, 1); }
+int gb_Mpc(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); out->subset = GB_ODD; return op_mpc(op, in, out, 0); }
+int gb_MpcDag(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); out->subset = GB_ODD; return op_mpc(op, in, out, 1); }
+int gb_MpcDagMpc(gb_op_t op, gb_field_t in, gb_field_t out) {
+  GB_OP_PRE(op, in, out);
+  GB_TRY(check_subset(in, GB_ODD, "MpcDagMpc"));
+  out->subset = GB_ODD;
+  return op_mpcdagmpc(op, in, out);
+}
+
+}  // extern "C"

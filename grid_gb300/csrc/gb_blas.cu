@@ -1,0 +1,567 @@
+// gb_blas.cu -- field linear algebra, FP64 reductions, layout conversion, gauge import.
+//
+// Reductions follow Grid's rankInnerProduct / sumD / axpy_norm
+// (Grid/lattice/Lattice_reduction.h:202-372): per-site products in the field's
+// precision, accumulation over sites in FP64, one result per right-hand side.  The
+// partial sums of a fixed grid of CTAs are combined in a fixed order by a second kernel,
+// so a reduction is bit-reproducible from run to run.
+#include <cuda_fp16.h>
+
+#include "gb_device.cuh"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------------------
+// Elementwise: z = a x + b y ; copy with precision change ; zero
+// ---------------------------------------------------------------------------------------
+template <class TZ, class TX, class TY>
+__global__ void __launch_bounds__(256) axpby_kernel(void* z, float* zn, double a, const void* x, const float* xn, double b,
+                                                    const void* y, const float* yn, size_t n5, int use_y) {
+  using R = typename Arith<TZ>::type;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  Spinor<typename Arith<TX>::type> fx;
+  SpinorIO<TX>::load(x, xn, n5, i, fx);
+  Spinor<R> o;
+  if (use_y) {
+    Spinor<typename Arith<TY>::type> fy;
+    SpinorIO<TY>::load(y, yn, n5, i, fy);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      o.re[k] = R(a) * R(fx.re[k]) + R(b) * R(fy.re[k]);
+      o.im[k] = R(a) * R(fx.im[k]) + R(b) * R(fy.im[k]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) { o.re[k] = R(a) * R(fx.re[k]); o.im[k] = R(a) * R(fx.im[k]); }
+  }
+  SpinorIO<TZ>::store(z, zn, n5, i, o);
+}
+
+template <class TZ, class TX>
+__global__ void __launch_bounds__(256) convert_kernel(void* z, float* zn, const void* x, const float* xn, size_t n5) {
+  using R = typename Arith<TZ>::type;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  Spinor<typename Arith<TX>::type> fx;
+  SpinorIO<TX>::load(x, xn, n5, i, fx);
+  Spinor<R> o;
+#pragma unroll
+  for (int k = 0; k < 12; k++) { o.re[k] = R(fx.re[k]); o.im[k] = R(fx.im[k]); }
+  SpinorIO<TZ>::store(z, zn, n5, i, o);
+}
+
+static inline unsigned nblk(size_t n) { return unsigned((n + 255) / 256); }
+
+template <class TZ, class TX, class TY>
+static int axpby_t(Op* op, HalfView z, double a, HalfView x, double b, HalfView y, size_t n5, int use_y) {
+  axpby_kernel<TZ, TX, TY><<<nblk(n5), 256, 0, op->stream>>>(z.data, z.norms, a, x.data, x.norms, b, y.data, y.norms,
+                                                            n5, use_y);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+int launch_axpby(Op* op, HalfView z, double a, HalfView x, double b, HalfView y, size_t n5) {
+  if (x.prec != z.prec || y.prec != z.prec) {
+    set_error("axpby: mixed precisions");
+    return GB_ERR_BAD_ARG;
+  }
+  switch (z.prec) {
+    case GB_F64: return axpby_t<double, double, double>(op, z, a, x, b, y, n5, 1);
+    case GB_F32: return axpby_t<float, float, float>(op, z, a, x, b, y, n5, 1);
+    case GB_F16: return axpby_t<__half, __half, __half>(op, z, a, x, b, y, n5, 1);
+  }
+  return GB_ERR_BAD_ARG;
+}
+
+int launch_scale(Op* op, HalfView z, double a, HalfView x, size_t n5) {
+  if (x.prec != z.prec) {
+    set_error("scale: mixed precisions");
+    return GB_ERR_BAD_ARG;
+  }
+  switch (z.prec) {
+    case GB_F64: return axpby_t<double, double, double>(op, z, a, x, 0, x, n5, 0);
+    case GB_F32: return axpby_t<float, float, float>(op, z, a, x, 0, x, n5, 0);
+    case GB_F16: return axpby_t<__half, __half, __half>(op, z, a, x, 0, x, n5, 0);
+  }
+  return GB_ERR_BAD_ARG;
+}
+
+template <class TZ, class TX> static int convert_t(Op* op, HalfView z, HalfView x, size_t n5) {
+  convert_kernel<TZ, TX><<<nblk(n5), 256, 0, op->stream>>>(z.data, z.norms, x.data, x.norms, n5);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+int launch_copy(Op* op, HalfView dst, HalfView src, size_t n5) {
+  if (dst.prec == src.prec) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(dst.data, src.data, n5 * spinor_bytes(dst.prec), cudaMemcpyDeviceToDevice, op->stream));
+    if (dst.prec == GB_F16)
+      GB_CHECK_CUDA(cudaMemcpyAsync(dst.norms, src.norms, n5 * sizeof(float), cudaMemcpyDeviceToDevice, op->stream));
+    return GB_OK;
+  }
+#define GB_CONV(PD, TD, PS, TS) \
+  if (dst.prec == PD && src.prec == PS) return convert_t<TD, TS>(op, dst, src, n5);
+  GB_CONV(GB_F64, double, GB_F32, float)
+  GB_CONV(GB_F64, double, GB_F16, __half)
+  GB_CONV(GB_F32, float, GB_F64, double)
+  GB_CONV(GB_F32, float, GB_F16, __half)
+  GB_CONV(GB_F16, __half, GB_F64, double)
+  GB_CONV(GB_F16, __half, GB_F32, float)
+#undef GB_CONV
+  return GB_ERR_BAD_ARG;
+}
+
+int launch_zero(Op* op, HalfView z, size_t n5) {
+  GB_CHECK_CUDA(cudaMemsetAsync(z.data, 0, n5 * spinor_bytes(z.prec), op->stream));
+  if (z.prec == GB_F16) GB_CHECK_CUDA(cudaMemsetAsync(z.norms, 0, n5 * sizeof(float), op->stream));
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Reductions
+// ---------------------------------------------------------------------------------------
+struct RedShape {
+  int L5, Ls, nrhs;
+};
+
+struct CGFields {
+  void* psi; float* psin;
+  const void* p; const float* pn;
+};
+
+// kind 0: |x|^2 ; kind 1: <x|y> ; kind 2: z = a x + y (a from host), |z|^2 ;
+// kind 3: r = r - a[rhs] mmp, psi += a[rhs] p (a from the device CG scalars), |r|^2
+template <class T, int KIND>
+__global__ void __launch_bounds__(256) reduce_kernel(const RedShape sh, const void* x, const float* xn, const void* y,
+                                                     const float* yn, void* z, float* zn, double a,
+                                                     const CGScalars* cg, const CGFields cf, size_t n5,
+                                                     double* partial) {
+  using R = typename Arith<T>::type;
+  constexpr int NV = KIND == 1 ? 2 : 1;
+  double v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) v[k] = 0.0;
+  const size_t stride = size_t(gridDim.x) * blockDim.x;  // a multiple of L5
+  size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  R ar = R(a);
+  if (KIND == 3) {
+    const int rhs = int(i % sh.L5) / sh.Ls;
+    ar = -R(cg[rhs].a);
+  }
+  for (; i < n5; i += stride) {
+    Spinor<R> fx;
+    SpinorIO<T>::load(x, xn, n5, i, fx);
+    if (KIND == 0) {
+      R s = 0;
+#pragma unroll
+      for (int k = 0; k < 12; k++) s = fma(fx.re[k], fx.re[k], fma(fx.im[k], fx.im[k], s));
+      v[0] += double(s);
+    } else if (KIND == 1) {
+      Spinor<R> fy;
+      SpinorIO<T>::load(y, yn, n5, i, fy);
+      R sr = 0, si = 0;
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        sr = fma(fx.re[k], fy.re[k], fma(fx.im[k], fy.im[k], sr));
+        si = fma(fx.re[k], fy.im[k], fma(-fx.im[k], fy.re[k], si));
+      }
+      v[0] += double(sr);
+      v[1] += double(si);
+    } else {
+      // KIND 2: z = a*x + y ; KIND 3: z(=y) = y - a*x
+      Spinor<R> fy;
+      SpinorIO<T>::load(y, yn, n5, i, fy);
+      R s = 0;
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        fy.re[k] = fma(ar, fx.re[k], fy.re[k]);
+        fy.im[k] = fma(ar, fx.im[k], fy.im[k]);
+        s = fma(fy.re[k], fy.re[k], fma(fy.im[k], fy.im[k], s));
+      }
+      SpinorIO<T>::store(z, zn, n5, i, fy);
+      v[0] += double(s);
+      if (KIND == 3) {
+        Spinor<R> fp, fs;
+        SpinorIO<T>::load(cf.p, cf.pn, n5, i, fp);
+        SpinorIO<T>::load(cf.psi, cf.psin, n5, i, fs);
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+          fs.re[k] = fma(-ar, fp.re[k], fs.re[k]);
+          fs.im[k] = fma(-ar, fp.im[k], fs.im[k]);
+        }
+        SpinorIO<T>::store(cf.psi, cf.psin, n5, i, fs);
+      }
+    }
+  }
+  block_reduce_rhs<NV>(v, sh.L5, sh.Ls, sh.nrhs, partial);
+}
+
+int red_grid(Op* op, size_t n5, int* blocks, int* threads) {
+  int L5 = op->L5;
+  int m = 1;
+  while (L5 * m * 2 <= 256) m *= 2;
+  int B = op->nrhs == 1 ? 256 : L5 * m;
+  if (B > 1024) {
+    set_error("reduction: L5 = %d too large", L5);
+    return GB_ERR_UNSUPPORTED;
+  }
+  size_t need = (n5 + B - 1) / B;
+  int g = int(need < size_t(kRedBlocks) ? need : size_t(kRedBlocks));
+  if (g < 1) g = 1;
+  *blocks = g;
+  *threads = B;
+  return GB_OK;
+}
+
+template <class T, int KIND>
+static int reduce_t(Op* op, HalfView x, HalfView y, HalfView z, double a, const CGFields& cf, size_t n5,
+                    double* partial) {
+  int g, B;
+  GB_TRY(red_grid(op, n5, &g, &B));
+  RedShape sh{op->L5, op->Ls, op->nrhs};
+  const int NV = KIND == 1 ? 2 : 1;
+  size_t smem = size_t(NV) * (op->nrhs == 1 ? 32 : B) * sizeof(double);
+  reduce_kernel<T, KIND><<<g, B, smem, op->stream>>>(sh, x.data, x.norms, y.data, y.norms, z.data, z.norms, a, op->d_cg,
+                                                    cf, n5, partial);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+template <int KIND>
+static int reduce_p(Op* op, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial,
+                    const CGFields& cf = CGFields{nullptr, nullptr, nullptr, nullptr}) {
+  switch (x.prec) {
+    case GB_F64: return reduce_t<double, KIND>(op, x, y, z, a, cf, n5, partial);
+    case GB_F32: return reduce_t<float, KIND>(op, x, y, z, a, cf, n5, partial);
+    case GB_F16: return reduce_t<__half, KIND>(op, x, y, z, a, cf, n5, partial);
+  }
+  return GB_ERR_BAD_ARG;
+}
+
+int launch_norm2_partial(Op* op, HalfView x, size_t n5, double* partial) {
+  return reduce_p<0>(op, x, x, x, 0.0, n5, partial);
+}
+int launch_inner_partial(Op* op, HalfView a, HalfView b, size_t n5, double* partial) {
+  if (a.prec != b.prec) { set_error("innerProduct: mixed precisions"); return GB_ERR_BAD_ARG; }
+  return reduce_p<1>(op, a, b, a, 0.0, n5, partial);
+}
+// z = a x + y, |z|^2
+int launch_axpy_norm_partial(Op* op, HalfView z, double a, HalfView x, HalfView y, size_t n5, double* partial) {
+  if (x.prec != y.prec || z.prec != x.prec) { set_error("axpy_norm: mixed precisions"); return GB_ERR_BAD_ARG; }
+  return reduce_p<2>(op, x, y, z, a, n5, partial);
+}
+int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, HalfView psi, HalfView p, size_t n5, double* partial) {
+  if (r.prec != mmp.prec || psi.prec != r.prec || p.prec != r.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
+  CGFields cf{psi.data, psi.norms, p.data, p.norms};
+  return reduce_p<3>(op, mmp, r, r, 0.0, n5, partial, cf);
+}
+
+// partial: [nparts][nrhs][nv] -> out[nrhs][nv]; one CTA per rhs, fixed summation order
+__global__ void reduce_final_kernel(const double* partial, int nparts, int nrhs, int nv, double* out) {
+  __shared__ double sm[256][2];
+  const int rhs = blockIdx.x, t = threadIdx.x;
+  double s0 = 0, s1 = 0;
+  for (int b = t; b < nparts; b += blockDim.x) {
+    s0 += partial[(size_t(b) * nrhs + rhs) * nv];
+    if (nv > 1) s1 += partial[(size_t(b) * nrhs + rhs) * nv + 1];
+  }
+  sm[t][0] = s0;
+  sm[t][1] = s1;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (t < st) { sm[t][0] += sm[t + st][0]; sm[t][1] += sm[t + st][1]; }
+    __syncthreads();
+  }
+  if (t == 0) {
+    out[rhs * nv] = sm[0][0];
+    if (nv > 1) out[rhs * nv + 1] = sm[0][1];
+  }
+}
+
+int launch_reduce_final(Op* op, const double* partial, int nparts, int nv, double* out) {
+  reduce_final_kernel<<<op->nrhs, 256, 0, op->stream>>>(partial, nparts, op->nrhs, nv, out);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// CG scalars (ConjugateGradient.h:151-200, ConjugateGradientReliableUpdate.h:163-251),
+// one set per right-hand side.  A right-hand side that has converged keeps a = b = 0,
+// so its solution stays fixed while the others iterate.
+// ---------------------------------------------------------------------------------------
+__global__ void cg_init_kernel(CGScalars* cg, const double* ssq, const double* cp, int nrhs, double tol, double delta,
+                               int* flags) {
+  const int r = threadIdx.x;
+  __shared__ int nd;
+  if (r == 0) nd = 0;
+  __syncthreads();
+  if (r < nrhs) {
+    CGScalars s;
+    s.ssq = ssq[r];
+    s.rsq = tol * tol * ssq[r];
+    s.cp = cp[r];
+    s.c = cp[r];
+    s.cprev = cp[r];
+    s.maxres = cp[r];
+    s.delta = delta;
+    s.a = 0; s.b = 0; s.d = 0;
+    s.done = (cp[r] <= s.rsq) ? 1 : 0;
+    s.iter = 0;
+    s.relup = 0;
+    s.pad = 0;
+    cg[r] = s;
+    if (s.done) atomicAdd(&nd, 1);
+  }
+  __syncthreads();
+  if (r == 0) { flags[0] = (nd == nrhs); flags[1] = 0; }
+}
+
+__global__ void cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs) {
+  const int r = threadIdx.x;
+  if (r >= nrhs) return;
+  double d = 0;
+  for (int b = 0; b < nparts; b++) d += partial[(size_t(b) * nrhs + r) * 2];
+  cg[r].d = d;
+  cg[r].a = cg[r].done ? 0.0 : cg[r].c / d;
+}
+
+__global__ void cg_beta_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs, int* flags) {
+  const int r = threadIdx.x;
+  __shared__ int nd, nr;
+  if (r == 0) { nd = 0; nr = 0; }
+  __syncthreads();
+  if (r < nrhs) {
+    CGScalars s = cg[r];
+    if (!s.done) {
+      double cp = 0;
+      for (int b = 0; b < nparts; b++) cp += partial[size_t(b) * nrhs + r];
+      s.cp = cp;
+      s.b = cp / s.c;
+      s.cprev = s.c;
+      s.c = cp;
+      s.iter += 1;
+      if (cp > s.maxres) s.maxres = cp;
+      if (cp <= s.rsq) s.done = 1;
+      else if (cp < s.delta * s.maxres) s.relup = 1;
+    } else {
+      s.b = 0.0;
+    }
+    cg[r] = s;
+    if (s.done) atomicAdd(&nd, 1);
+    if (s.relup && !s.done) atomicAdd(&nr, 1);
+  }
+  __syncthreads();
+  if (r == 0) { flags[0] = (nd == nrhs); flags[1] = nr; }
+}
+
+__global__ void cg_relup_reset_kernel(CGScalars* cg, const double* cp_true, int nrhs) {
+  const int r = threadIdx.x;
+  if (r >= nrhs) return;
+  CGScalars s = cg[r];
+  if (!s.done) {
+    s.cp = cp_true[r];
+    s.b = cp_true[r] / s.cprev;
+    s.c = cp_true[r];
+    s.maxres = cp_true[r];
+  }
+  s.relup = 0;
+  cg[r] = s;
+}
+
+static inline int rhs_threads(const Op* op) { return 32 * ((op->nrhs + 31) / 32); }
+
+int launch_cg_init(Op* op, const double* d_ssq, const double* d_cp, double tol, double delta) {
+  cg_init_kernel<<<1, rhs_threads(op), 0, op->stream>>>(op->d_cg, d_ssq, d_cp, op->nrhs, tol, delta, op->d_all_done);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+// the per-block partial sums are few (<= 2 * kRedBlocks); the scalar kernels read them
+// directly in a fixed order
+int launch_cg_alpha(Op* op, const double* partial_inner, int nparts) {
+  cg_alpha_kernel<<<1, rhs_threads(op), 0, op->stream>>>(op->d_cg, partial_inner, nparts, op->nrhs);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+int launch_cg_beta(Op* op, const double* partial_norm, int nparts) {
+  cg_beta_kernel<<<1, rhs_threads(op), 0, op->stream>>>(op->d_cg, partial_norm, nparts, op->nrhs, op->d_all_done);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+int launch_cg_relup_reset(Op* op, const double* d_cp_true) {
+  cg_relup_reset_kernel<<<1, rhs_threads(op), 0, op->stream>>>(op->d_cg, d_cp_true, op->nrhs);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// p = b p + r   (the second line of ConjugateGradient.h:175-183)
+template <class T>
+__global__ void __launch_bounds__(256) cg_p_kernel(const RedShape sh, void* p, float* pn, const void* r, const float* rn,
+                                                   const CGScalars* cg, size_t n5) {
+  using R = typename Arith<T>::type;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  const int rhs = int(i % sh.L5) / sh.Ls;
+  const R b = R(cg[rhs].b);
+  Spinor<R> fp, fr;
+  SpinorIO<T>::load(p, pn, n5, i, fp);
+  SpinorIO<T>::load(r, rn, n5, i, fr);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    fp.re[k] = fma(b, fp.re[k], fr.re[k]);
+    fp.im[k] = fma(b, fp.im[k], fr.im[k]);
+  }
+  SpinorIO<T>::store(p, pn, n5, i, fp);
+}
+
+int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5) {
+  RedShape sh{op->L5, op->Ls, op->nrhs};
+  switch (p.prec) {
+    case GB_F64: cg_p_kernel<double><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5); break;
+    case GB_F32: cg_p_kernel<float><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5); break;
+    case GB_F16: cg_p_kernel<__half><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Layout conversion between canonical FP64 and the device planes
+// ---------------------------------------------------------------------------------------
+struct GeoParams {
+  int L[4];
+  int64_t half4, vol4;
+  int L5, Ls, nrhs;
+};
+
+__device__ __forceinline__ int64_t cb_to_site(int64_t xcb, int parity, const GeoParams& g) {
+  const int Lxh = g.L[0] >> 1;
+  const int64_t row = xcb / Lxh;
+  const int xh = int(xcb - row * Lxh);
+  const int y = int(row % g.L[1]);
+  const int64_t zt = row / g.L[1];
+  const int z = int(zt % g.L[2]);
+  const int t = int(zt / g.L[2]);
+  const int x = 2 * xh + ((parity + y + z + t) & 1);
+  return row * g.L[0] + x;
+}
+
+template <class T, bool IMPORT>
+__global__ void __launch_bounds__(256) layout_kernel(const GeoParams g, double* canon, void* dev, float* devn, int parity,
+                                                     int canon_full) {
+  using R = typename Arith<T>::type;
+  const size_t n5 = size_t(g.half4) * g.L5;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  const int64_t xcb = int64_t(i / g.L5);
+  const int s5 = int(i - size_t(xcb) * g.L5);
+  const int rhs = s5 / g.Ls, s = s5 - rhs * g.Ls;
+  const int64_t c4 = canon_full ? cb_to_site(xcb, parity, g) : xcb;
+  const int64_t n4c = canon_full ? g.vol4 : g.half4;
+  double2* c = reinterpret_cast<double2*>(canon) + ((size_t(rhs) * n4c + c4) * g.Ls + s) * 12;
+  Spinor<R> f;
+  if (IMPORT) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const double2 v = c[k];
+      f.re[k] = R(v.x); f.im[k] = R(v.y);
+    }
+    SpinorIO<T>::store(dev, devn, n5, i, f);
+  } else {
+    SpinorIO<T>::load(dev, devn, n5, i, f);
+#pragma unroll
+    for (int k = 0; k < 12; k++) c[k] = make_double2(double(f.re[k]), double(f.im[k]));
+  }
+}
+
+static GeoParams geo(const Op* op) {
+  GeoParams g;
+  for (int k = 0; k < 4; k++) g.L[k] = op->dims[k];
+  g.half4 = op->half4;
+  g.vol4 = op->vol4;
+  g.L5 = op->L5;
+  g.Ls = op->Ls;
+  g.nrhs = op->nrhs;
+  return g;
+}
+
+template <bool IMPORT>
+static int layout_p(Op* op, double* canon, HalfView v, int parity, int canon_full) {
+  GeoParams g = geo(op);
+  const size_t n5 = op->n5();
+  switch (v.prec) {
+    case GB_F64: layout_kernel<double, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
+    case GB_F32: layout_kernel<float, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
+    case GB_F16: layout_kernel<__half, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full) {
+  return layout_p<true>(op, const_cast<double*>(canon), out, parity, canon_is_full);
+}
+int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon_is_full) {
+  return layout_p<false>(op, canon, in, parity, canon_is_full);
+}
+
+// ---------------------------------------------------------------------------------------
+// DoubleStore (Grid/qcd/action/fermion/WilsonImpl.h:127-171) with ImportGauge's -1/2
+// (WilsonFermion5DImplementation.h:149-180), for the links of output parity p.
+// ---------------------------------------------------------------------------------------
+struct PhaseParams {
+  double re[4], im[4];
+};
+
+template <class L>
+__global__ void __launch_bounds__(256) double_store_kernel(const GeoParams g, const PhaseParams ph, const double2* U,
+                                                           L* out, int parity) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= size_t(g.half4) * 8) return;
+  const int64_t xcb = int64_t(t >> 3);
+  const int leg = int(t & 7);
+  const int mu = leg & 3;
+  const int64_t site = cb_to_site(xcb, parity, g);
+  int x[4];
+  {
+    int64_t r = site;
+    for (int k = 0; k < 4; k++) { x[k] = int(r % g.L[k]); r /= g.L[k]; }
+  }
+  double pr = 1, pi = 0;
+  int64_t src = site;
+  if (leg < 4) {
+    if (x[mu] == g.L[mu] - 1) { pr = ph.re[mu]; pi = ph.im[mu]; }
+  } else {
+    if (x[mu] == 0) { pr = ph.re[mu]; pi = -ph.im[mu]; }
+    int xs[4] = {x[0], x[1], x[2], x[3]};
+    xs[mu] = (xs[mu] - 1 + g.L[mu]) % g.L[mu];
+    src = xs[0] + int64_t(g.L[0]) * (xs[1] + int64_t(g.L[1]) * (xs[2] + int64_t(g.L[2]) * xs[3]));
+  }
+  const double2* u = U + (size_t(src) * 4 + mu) * 9;
+  L* o = out + (size_t(xcb) * 8 + leg) * 18;
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) {
+      // forward: U[a][b]; backward: conj(U[b][a])
+      const double2 v = leg < 4 ? u[a * 3 + b] : make_double2(u[b * 3 + a].x, -u[b * 3 + a].y);
+      const double re = -0.5 * (pr * v.x - pi * v.y);
+      const double im = -0.5 * (pr * v.y + pi * v.x);
+      o[(a * 3 + b) * 2] = L(re);
+      o[(a * 3 + b) * 2 + 1] = L(im);
+    }
+}
+
+int launch_double_store(Op* op, const double* U_canon, int parity) {
+  GeoParams g = geo(op);
+  PhaseParams ph;
+  for (int k = 0; k < 4; k++) { ph.re[k] = op->phases[k].real(); ph.im[k] = op->phases[k].imag(); }
+  const size_t n = size_t(op->half4) * 8;
+  const double2* U = reinterpret_cast<const double2*>(U_canon);
+  if (op->prec == GB_F64)
+    double_store_kernel<double><<<nblk(n), 256, 0, op->stream>>>(g, ph, U, static_cast<double*>(op->links[parity]), parity);
+  else
+    double_store_kernel<float><<<nblk(n), 256, 0, op->stream>>>(g, ph, U, static_cast<float*>(op->links[parity]), parity);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+}  // namespace gb

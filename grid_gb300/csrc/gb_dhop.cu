@@ -1,0 +1,236 @@
+// gb_dhop.cu -- the Wilson hopping term on one checkerboard (DhopEO / DhopOE) for
+// 4D Wilson (L5 = nrhs) and 5D domain-wall fields (L5 = Ls * nrhs).
+//
+// Computes, for every output site x of parity p and every fifth-dimension slot s5,
+//   out(x,s5) = sum_mu (1 - g_mu) Ud_mu(x) in(x+mu,s5) + (1 + g_mu) Ud_{mu+4}(x) in(x-mu,s5)
+// (dagger: projector signs swapped), the kernel of Grid's
+// WilsonKernels<Impl>::GenericDhopSite / GenericDhopSiteDag
+// (Grid/qcd/action/fermion/implementation/WilsonKernelsImplementation.h:113-163) with the
+// half-spinor projections of Grid/qcd/spin/TwoSpinor.h:75-330.
+//
+// GB300 structure:
+//  * one CTA covers k4 whole 4D sites x all L5 slots; thread = one 5D output site with
+//    the slot index fastest, so a warp's neighbour reads are contiguous runs of
+//    16-byte vectors in every plane;
+//  * the CTA's 8 doubled links per 4D site arrive in shared memory by one TMA bulk copy
+//    (cp.async.bulk + mbarrier, bounded wait) and serve all L5 slots of the site;
+//  * neighbour indices come from a per-parity table (periodic wrap; the antiperiodic
+//    time boundary is already folded into the stored links, as in Grid's DoubleStore).
+#include <cuda_fp16.h>
+
+#include "gb_device.cuh"
+
+namespace gb {
+
+struct DhopParams {
+  const void* in;
+  const float* in_norms;
+  void* out;
+  float* out_norms;
+  const void* links;
+  const int* nbr;
+  int64_t n4h;
+  size_t n5;
+  int L5;
+  int L5c;  // slots per CTA (L5 split over gridDim.y when above 256)
+  int k4;
+  int* err;
+};
+
+// ---- spin projection (1 + S gamma_MU) f -> two-spinor h, Grid's spProj{X,Y,Z,T}{p,m} ----
+template <int MU, int S, class R>
+__device__ __forceinline__ void project(const Spinor<R>& f, R (&hr)[6], R (&hi)[6]) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const R f0r = f.re[c], f0i = f.im[c], f1r = f.re[3 + c], f1i = f.im[3 + c];
+    const R f2r = f.re[6 + c], f2i = f.im[6 + c], f3r = f.re[9 + c], f3i = f.im[9 + c];
+    if (MU == 0) {  // h0 = f0 + S i f3, h1 = f1 + S i f2
+      hr[c] = f0r - S * f3i; hi[c] = f0i + S * f3r;
+      hr[3 + c] = f1r - S * f2i; hi[3 + c] = f1i + S * f2r;
+    } else if (MU == 1) {  // h0 = f0 - S f3, h1 = f1 + S f2
+      hr[c] = f0r - S * f3r; hi[c] = f0i - S * f3i;
+      hr[3 + c] = f1r + S * f2r; hi[3 + c] = f1i + S * f2i;
+    } else if (MU == 2) {  // h0 = f0 + S i f2, h1 = f1 - S i f3
+      hr[c] = f0r - S * f2i; hi[c] = f0i + S * f2r;
+      hr[3 + c] = f1r + S * f3i; hi[3 + c] = f1i - S * f3r;
+    } else {  // h0 = f0 + S f2, h1 = f1 + S f3
+      hr[c] = f0r + S * f2r; hi[c] = f0i + S * f2i;
+      hr[3 + c] = f1r + S * f3r; hi[3 + c] = f1i + S * f3i;
+    }
+  }
+}
+
+// ---- reconstruction, Grid's accumRecon{X,Y,Z,T}{p,m}; FIRST assigns instead of adding ----
+template <int MU, int S, bool FIRST, class R>
+__device__ __forceinline__ void reconstruct(Spinor<R>& r, const R (&ur)[6], const R (&ui)[6]) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const R u0r = ur[c], u0i = ui[c], u1r = ur[3 + c], u1i = ui[3 + c];
+    R t2r, t2i, t3r, t3i;
+    if (MU == 0) {  // r2 += -S i u1, r3 += -S i u0
+      t2r = S * u1i; t2i = -S * u1r; t3r = S * u0i; t3i = -S * u0r;
+    } else if (MU == 1) {  // r2 += S u1, r3 -= S u0
+      t2r = S * u1r; t2i = S * u1i; t3r = -S * u0r; t3i = -S * u0i;
+    } else if (MU == 2) {  // r2 += -S i u0, r3 += S i u1
+      t2r = S * u0i; t2i = -S * u0r; t3r = -S * u1i; t3i = S * u1r;
+    } else {  // r2 += S u0, r3 += S u1
+      t2r = S * u0r; t2i = S * u0i; t3r = S * u1r; t3i = S * u1i;
+    }
+    if (FIRST) {
+      r.re[c] = u0r; r.im[c] = u0i; r.re[3 + c] = u1r; r.im[3 + c] = u1i;
+      r.re[6 + c] = t2r; r.im[6 + c] = t2i; r.re[9 + c] = t3r; r.im[9 + c] = t3i;
+    } else {
+      r.re[c] += u0r; r.im[c] += u0i; r.re[3 + c] += u1r; r.im[3 + c] += u1i;
+      r.re[6 + c] += t2r; r.im[6 + c] += t2i; r.re[9 + c] += t3r; r.im[9 + c] += t3i;
+    }
+  }
+}
+
+// u = U h for both spins of the two-spinor; U is 9 complex (row-major) in shared memory
+template <class R>
+__device__ __forceinline__ void su3_mul(const R* __restrict__ U, const R (&hr)[6], const R (&hi)[6], R (&ur)[6],
+                                        R (&ui)[6]) {
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const R u0r = U[(a * 3 + 0) * 2], u0i = U[(a * 3 + 0) * 2 + 1];
+    const R u1r = U[(a * 3 + 1) * 2], u1i = U[(a * 3 + 1) * 2 + 1];
+    const R u2r = U[(a * 3 + 2) * 2], u2i = U[(a * 3 + 2) * 2 + 1];
+#pragma unroll
+    for (int sp = 0; sp < 2; sp++) {
+      const int o = sp * 3;
+      R xr = u0r * hr[o];
+      R xi = u0r * hi[o];
+      xr = fma(-u0i, hi[o], xr);
+      xi = fma(u0i, hr[o], xi);
+      xr = fma(u1r, hr[o + 1], xr);
+      xi = fma(u1r, hi[o + 1], xi);
+      xr = fma(-u1i, hi[o + 1], xr);
+      xi = fma(u1i, hr[o + 1], xi);
+      xr = fma(u2r, hr[o + 2], xr);
+      xi = fma(u2r, hi[o + 2], xi);
+      xr = fma(-u2i, hi[o + 2], xr);
+      xi = fma(u2i, hr[o + 2], xi);
+      ur[o + a] = xr;
+      ui[o + a] = xi;
+    }
+  }
+}
+
+template <class T, bool DAG, int LEG>
+__device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8], int s, const typename Arith<T>::type* U,
+                                         Spinor<typename Arith<T>::type>& acc) {
+  using R = typename Arith<T>::type;
+  constexpr int MU = LEG & 3;
+  constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
+  Spinor<R> f;
+  SpinorIO<T>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
+  R hr[6], hi[6], ur[6], ui[6];
+  project<MU, S>(f, hr, hi);
+  su3_mul<R>(U + LEG * 18, hr, hi, ur, ui);
+  reconstruct<MU, S, LEG == 0>(acc, ur, ui);
+}
+
+template <class T, bool DAG>
+__global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p) {
+  using R = typename Arith<T>::type;
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  R* sU = reinterpret_cast<R*>(dyn_smem);
+  __shared__ __align__(8) uint64_t bar;
+
+  const int t = threadIdx.x;
+  const int64_t x0 = int64_t(blockIdx.x) * p.k4;
+  const int nsite = int(min(int64_t(p.k4), p.n4h - x0));
+  if (t == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (t == 0) {
+    const uint32_t bytes = uint32_t(nsite) * 8u * 18u * uint32_t(sizeof(R));
+    mbar_expect_tx(&bar, bytes);
+    bulk_g2s(sU, static_cast<const R*>(p.links) + x0 * 144, bytes, &bar);
+  }
+  const int j = t / p.L5c;
+  const int s = int(blockIdx.y) * p.L5c + (t - j * p.L5c);
+  const bool active = j < nsite && s < p.L5;
+  int nb[8];
+  if (active) {
+    const int4* q = reinterpret_cast<const int4*>(p.nbr + (x0 + j) * 8);
+    const int4 a = __ldg(q), b = __ldg(q + 1);
+    nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
+    nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
+  }
+  if (!mbar_wait_bounded(&bar, 0)) {
+    if (t == 0) atomicExch(p.err, 1);
+    return;
+  }
+  if (!active) return;
+  const R* U = sU + j * 144;
+  Spinor<R> acc;
+  dhop_leg<T, DAG, 0>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 1>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 2>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 3>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 4>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 5>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 6>(p, nb, s, U, acc);
+  dhop_leg<T, DAG, 7>(p, nb, s, U, acc);
+  SpinorIO<T>::store(p.out, p.out_norms, p.n5, size_t(x0 + j) * p.L5 + s, acc);
+}
+
+// 4D sites per CTA: L5 * k4 threads, a multiple of 32 where possible, about 256, and at
+// most 40 KB of staged links
+static int pick_k4(int L5, size_t link_bytes_per_site) {
+  if (L5 >= 128) return 1;
+  int k4 = 256 / L5;
+  while (k4 > 1 && (L5 * k4) % 32 != 0) k4--;
+  if ((L5 * k4) % 32 != 0) k4 = 256 / L5;
+  const int kmax = int((40 * 1024) / link_bytes_per_site);
+  if (k4 > kmax) k4 = kmax;
+  return k4 < 1 ? 1 : k4;
+}
+
+template <class T, bool DAG> static int launch_dhop_t(Op* op, const DhopParams& p) {
+  using R = typename Arith<T>::type;
+  const int threads = p.L5c * p.k4;
+  const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
+  const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
+  const size_t smem = size_t(p.k4) * 144 * sizeof(R);
+  static bool configured = false;
+  if (!configured) {
+    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_kernel<T, DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    configured = true;
+  }
+  dhop_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks), dim3(threads), smem, op->stream>>>(p);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
+  if (in.prec != op->prec || out.prec != op->prec) {
+    set_error("Dhop: field precision differs from the operator's");
+    return GB_ERR_BAD_ARG;
+  }
+  if (op->L5 > kMaxL5) {
+    set_error("Dhop: L5 = %d exceeds %d", op->L5, kMaxL5);
+    return GB_ERR_UNSUPPORTED;
+  }
+  DhopParams p;
+  p.in = in.data;
+  p.in_norms = in.norms;
+  p.out = out.data;
+  p.out_norms = out.norms;
+  p.links = op->links[out_parity];
+  p.nbr = op->nbr[out_parity];
+  p.n4h = op->half4;
+  p.n5 = op->n5();
+  p.L5 = op->L5;
+  p.L5c = op->L5 > 256 ? 256 : op->L5;
+  p.k4 = pick_k4(p.L5c, op->prec == GB_F64 ? 1152 : 576);
+  p.err = op->d_err;
+  switch (op->prec) {
+    case GB_F64: return dag ? launch_dhop_t<double, true>(op, p) : launch_dhop_t<double, false>(op, p);
+    case GB_F32: return dag ? launch_dhop_t<float, true>(op, p) : launch_dhop_t<float, false>(op, p);
+    case GB_F16: return dag ? launch_dhop_t<__half, true>(op, p) : launch_dhop_t<__half, false>(op, p);
+  }
+  return GB_ERR_BAD_ARG;
+}
+
+}  // namespace gb

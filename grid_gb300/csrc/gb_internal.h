@@ -1,0 +1,168 @@
+// gb_internal.h -- private types of the GB300 fermion library (host + device).
+//
+// Device layout of a fermion field (one checkerboard, "half"):
+//   5D site index   i = s5 + L5 * x_cb,  s5 = rhs*Ls + s,  x_cb = site4 >> 1
+//   FP64            12 planes of double2, plane k = complex component spin*3+colour
+//   FP32            6 planes of float4,  plane g = complex components 2g, 2g+1
+//   FP16            3 planes of 16-byte vectors of 8 halves (4 complex components each)
+//                   plus one float norm per 5D site
+//   Each plane holds n5 = half_sites4 * L5 vectors; a full field is the even half
+//   followed by the odd half.  Planes 0..(P/2-1) hold spins 0,1 (the P+ chirality),
+//   the rest spins 2,3 (P-), so the 5D chiral projections read half the planes.
+// Gauge links (per output parity p): [x_cb][leg 0..7][3][3] complex in link precision,
+//   legs 0..3 = Ud_mu(x) (forward), 4..7 = Ud_{mu}(x-mu)^dagger (backward), with the
+//   -1/2 and boundary phases folded in (Grid's DoubleStore).  Neighbour table per parity:
+//   [x_cb][leg] = x_cb of the neighbour in the other parity.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "gbdwf.h"
+
+namespace gb {
+
+constexpr int kMaxLs = 64;      // longest fifth dimension handled by the 5D kernels
+constexpr int kMaxL5 = 1024;    // Ls * nrhs upper bound
+constexpr int kRedBlocks = 1216;  // 8 blocks per SM on 152 SMs for reductions
+
+void set_error(const char* fmt, ...);
+
+#define GB_CHECK_CUDA(call)                                                          \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      ::gb::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      return GB_ERR_CUDA;                                                            \
+    }                                                                                \
+  } while (0)
+
+#define GB_TRY(call)              \
+  do {                            \
+    int rc_ = (call);             \
+    if (rc_ != GB_OK) return rc_; \
+  } while (0)
+
+struct Field;
+
+// Device-side per-right-hand-side scalars of a running CG (all FP64).
+struct CGScalars {
+  double c, d, a, cp, b, rsq, ssq, cprev, maxres, delta;
+  int done, iter, relup, pad;
+};
+
+struct Op {
+  int kind = 0;          // 0 Wilson, 1 Moebius
+  int dims[4] = {0, 0, 0, 0};
+  int64_t vol4 = 0, half4 = 0;
+  int Ls = 1, nrhs = 1, L5 = 1;
+  int prec = GB_F64;     // arithmetic / storage precision of the operator
+  double mass = 0, M5 = 0, b = 0, c = 0, diag_mass = 0;
+  std::complex<double> phases[4];
+  bool phases_pm1 = true;  // every phase is +1 or -1 (12-real reconstruction allowed)
+  unsigned flags = 0;
+  bool recon12 = false;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  bool gauge_loaded = false;
+
+  void* links[2] = {nullptr, nullptr};  // per output parity
+  int* nbr[2] = {nullptr, nullptr};
+  int* d_err = nullptr;                 // device error flag of bounded waits
+
+  // Cayley coefficients (Moebius) -- host copies
+  std::vector<double> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
+
+  // reduction scratch
+  double* d_partial = nullptr;  // kRedBlocks * nrhs * 2
+  double* d_result = nullptr;   // nrhs * 4
+  double* h_result = nullptr;   // pinned, nrhs * 4
+  // canonical FP64 staging buffer for import/export (device)
+  double* d_stage = nullptr;
+  size_t stage_bytes = 0;
+  // CG device scalars
+  CGScalars* d_cg = nullptr;   // nrhs
+  CGScalars* h_cg = nullptr;   // pinned copy
+  int* d_all_done = nullptr;
+  std::vector<int> last_iters;
+  std::vector<double> last_resid;
+
+  // workspace fields keyed by (full|half, precision)
+  std::vector<Field*> ws;
+  cudaEvent_t events[16] = {};
+
+  size_t n5() const { return size_t(half4) * L5; }
+  size_t link_bytes_per_parity() const;
+};
+
+struct Field {
+  Op* op = nullptr;
+  int subset = GB_EVEN;
+  int prec = GB_F64;
+  void* data = nullptr;   // plane 0 of the even (or only) half
+  float* norms = nullptr; // FP16 per-site norms (even half first for full fields)
+  bool owned = true;
+  size_t n5 = 0;          // 5D sites per checkerboard
+  bool full() const { return subset == GB_FULL; }
+  size_t half_bytes() const;   // bytes of one checkerboard's planes
+  void* half_ptr(int parity) const;
+  float* half_norms(int parity) const;
+};
+
+// bytes of one 16-byte vector plane set per 5D site
+inline size_t spinor_bytes(int prec) { return prec == GB_F64 ? 192 : prec == GB_F32 ? 96 : 48; }
+
+// ---- workspace ----
+int ws_get(Op* op, int subset, int prec, int slot, Field** out);
+
+// ---- kernel launchers (gb_dhop.cu, gb_5d.cu, gb_blas.cu) ----
+struct HalfView {
+  void* data;
+  float* norms;
+  int prec;
+};
+inline HalfView half_view(const Field* f, int parity) { return HalfView{f->half_ptr(parity), f->half_norms(parity), f->prec}; }
+
+int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag);
+// chi = diag*phi + upper*P(-/+) psi[s+1] + lower*P(+/-) psi[s-1]   (per rhs block of Ls)
+int launch_m5d(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
+               const double* upper, int dag, size_t n5);
+int launch_mooee_inv(Op* op, HalfView in, HalfView out, int dag, size_t n4);
+// z = a*x + b*y (host scalars); x or y may alias z
+int launch_axpby(Op* op, HalfView z, double a, HalfView x, double b, HalfView y, size_t n5);
+int launch_scale(Op* op, HalfView z, double a, HalfView x, size_t n5);
+int launch_copy(Op* op, HalfView dst, HalfView src, size_t n5);
+int launch_zero(Op* op, HalfView z, size_t n5);
+// reductions: per-rhs results into op->d_result; partial per half
+int launch_norm2_partial(Op* op, HalfView x, size_t n5, double* partial);
+int launch_inner_partial(Op* op, HalfView a, HalfView b, size_t n5, double* partial);
+int launch_axpy_norm_partial(Op* op, HalfView z, double a, HalfView x, HalfView y, size_t n5, double* partial);
+int launch_reduce_final(Op* op, const double* partial, int nparts, int nv, double* out);
+int red_grid(Op* op, size_t n5, int* blocks, int* threads);
+
+// layout conversion between canonical FP64 (device) and the device layout
+int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full);
+int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon_is_full);
+int launch_double_store(Op* op, const double* U_canon, int parity);
+int build_neighbours(Op* op);
+
+// CG kernels (gb_blas.cu)
+// init from device arrays ssq[nrhs] and cp[nrhs]
+int launch_cg_init(Op* op, const double* d_ssq, const double* d_cp, double tol, double delta);
+int launch_cg_alpha(Op* op, const double* partial_inner, int nparts);
+// r -= a mmp ; psi += a p ; partial |r|^2
+int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, HalfView psi, HalfView p, size_t n5, double* partial);
+int launch_cg_beta(Op* op, const double* partial_norm, int nparts);
+// p = b p + r
+int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5);
+// after a reliable update: cp = c = maxres = cp_true ; b = cp_true / cprev
+int launch_cg_relup_reset(Op* op, const double* d_cp_true);
+
+}  // namespace gb
+
+struct gb_op_s : gb::Op {};
+struct gb_field_s : gb::Field {};

@@ -1,0 +1,202 @@
+/* gbdwf.h -- C ABI of the GB300-native Wilson / Moebius domain-wall fermion library.
+ *
+ * The library replaces the device hot path of Grid's fermion operators and their
+ * conjugate-gradient drivers.  Every entry point returns an int status (GB_OK on
+ * success) and never aborts; gb_last_error() returns a thread-local message for the
+ * last failure.  Handles are opaque.  No entry point takes a C++ or torch type.
+ *
+ * Host layout at the boundary ("canonical"), complex<double> interleaved (re, im):
+ *   4D site index  site = x + Lx*(y + Ly*(z + Lz*t))
+ *   gauge field    U[site][mu][a][b], mu = x,y,z,t             (Grid LatticeGaugeField)
+ *   fermion        psi[site][s][spin][colour], s innermost      (Grid sF = s + Ls*sU)
+ *   half field     psi[site>>1][s][spin][colour] over the sites of one parity
+ *   parity         (x+y+z+t) & 1, Even = 0; s takes no part     (WilsonFermion5D.h:37-61)
+ * A multi-RHS operator (nrhs > 1) takes nrhs such fields back to back.
+ *
+ * Device layout is private to the library: structure-of-arrays, 5D site fastest, in
+ * 16-byte vectors (see the design doc in the source tree).
+ */
+#ifndef GBDWF_H
+#define GBDWF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the error convention of Grid's asserts, as return values) ---- */
+enum {
+  GB_OK = 0,
+  GB_ERR_BAD_ARG = 1,       /* conformable()/argument checks                         */
+  GB_ERR_BAD_PARITY = 2,    /* checkerboard mismatch (WilsonFermion5DImplementation.h:426-435) */
+  GB_ERR_OOM = 3,           /* device allocation failed or HBM budget exceeded       */
+  GB_ERR_CUDA = 4,          /* a CUDA runtime error                                  */
+  GB_ERR_NOT_CONVERGED = 5, /* CG hit MaxIterations (ConjugateGradient.h:254)        */
+  GB_ERR_TIMEOUT = 6,       /* a bounded device wait gave up                         */
+  GB_ERR_NO_DEVICE = 7,     /* no CUDA device visible                                */
+  GB_ERR_UNSUPPORTED = 8
+};
+
+/* ---- precisions and subsets ---- */
+enum { GB_F64 = 0, GB_F32 = 1, GB_F16 = 2 };
+enum { GB_EVEN = 0, GB_ODD = 1, GB_FULL = 2 };
+enum { GB_DAG_NO = 0, GB_DAG_YES = 1 };
+
+typedef struct gb_op_s* gb_op_t;       /* a fermion operator on one gauge field       */
+typedef struct gb_field_s* gb_field_t; /* a device fermion field conformable to an op */
+
+/* ---- library ---- */
+int gb_version(void);
+const char* gb_last_error(void);
+const char* gb_status_string(int status);
+int gb_device_count(int* n);
+
+/* ---- operators ----------------------------------------------------------------
+ * gb_wilson_create   ~ WilsonFermion(U, Fgrid, Hgrid, mass, ImplParams)
+ *                      (Grid/qcd/action/fermion/WilsonFermion.h:139-142)
+ * gb_mobius_create   ~ MobiusFermion(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, b, c, ImplParams)
+ *                      (Grid/qcd/action/fermion/MobiusFermion.h:45-67)
+ * dims: Lx, Ly, Lz, Lt (all even).  phases: 4 complex boundary phases (re, im),
+ * ImplParams::boundary_phases (Grid/qcd/action/ActionParams.h:49-66); NULL = periodic.
+ * precision: GB_F64 or GB_F32 (or GB_F16: FP16 spinors with per-site FP32 norms,
+ * FP32 links and arithmetic).  nrhs >= 1 right-hand sides share the gauge field.
+ * stream: a cudaStream_t (NULL = the default stream).
+ * flags: bit 0 = store links as 12 reals and reconstruct the third row.
+ */
+int gb_wilson_create(const int dims[4], double mass, const double* phases, int precision, int nrhs, void* stream,
+                     unsigned flags, gb_op_t* out);
+int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,
+                     int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out);
+int gb_op_destroy(gb_op_t op);
+/* ImportGauge (WilsonFermion5DImplementation.h:149-180): canonical FP64 host field. */
+int gb_op_import_gauge(gb_op_t op, const double* U_host);
+/* the same from a canonical FP64 field already in device memory */
+int gb_op_import_gauge_device(gb_op_t op, const double* U_device);
+/* geometry queries: Ls (1 for Wilson), nrhs, sites in one checkerboard (4D), precision */
+int gb_op_info(gb_op_t op, int* Ls, int* nrhs, int64_t* half_sites4, int* precision);
+int gb_op_set_stream(gb_op_t op, void* stream);
+/* Cayley coefficients as the operator holds them: 9*Ls doubles
+ * bs, cs, bee, cee, dee, lee, leem, uee, ueem (CayleyFermion5DImplementation.h:410-535) */
+int gb_op_cayley_coeffs(gb_op_t op, double* out);
+
+/* ---- fields ---------------------------------------------------------------------
+ * Lattice<vobj>(grid) on the op's FermionGrid (GB_FULL) or FermionRedBlackGrid
+ * (GB_EVEN / GB_ODD).  precision may differ from the op's (for precisionChange).
+ */
+int gb_field_create(gb_op_t op, int subset, int precision, gb_field_t* out);
+int gb_field_destroy(gb_field_t f);
+int gb_field_subset(gb_field_t f, int* subset);
+int gb_field_set_subset(gb_field_t f, int subset); /* relabel a half field's checkerboard */
+/* number of doubles in the canonical host form (all nrhs right-hand sides) */
+int gb_field_host_len(gb_field_t f, size_t* n_doubles);
+int gb_field_import(gb_field_t f, const double* host);
+int gb_field_export(gb_field_t f, double* host);
+int gb_field_import_device(gb_field_t f, const double* dev); /* canonical FP64 in device memory */
+int gb_field_export_device(gb_field_t f, double* dev);
+
+/* ---- field linear algebra (Grid/lattice/Lattice_arith.h, Lattice_reduction.h) ----
+ * Reductions return one value per right-hand side (arrays of length nrhs), in FP64.
+ */
+int gb_field_zero(gb_field_t f);
+int gb_field_copy(gb_field_t dst, gb_field_t src);          /* also precisionChange */
+int gb_field_norm2(gb_field_t f, double* out);              /* norm2               */
+int gb_field_inner(gb_field_t a, gb_field_t b, double* out); /* innerProduct <a|b>: re,im per rhs */
+int gb_field_axpy(gb_field_t z, double a, gb_field_t x, gb_field_t y);               /* z = a x + y   */
+int gb_field_axpby(gb_field_t z, double a, double b, gb_field_t x, gb_field_t y);    /* z = a x + b y */
+int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, double* norm_out);
+int gb_field_pick_checkerboard(gb_field_t half, gb_field_t full); /* half's subset picks */
+int gb_field_set_checkerboard(gb_field_t full, gb_field_t half);
+
+/* ---- operator application (FermionOperator.h:40-192 / CayleyFermion5D) ----------
+ * Full-field ops: M, Mdag, MdagM, Dhop.  Half-field ops pick DhopEO/DhopOE from the
+ * input subset exactly as Grid does (Meooe: Odd in -> Even out).
+ */
+int gb_M(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_Mdag(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MdagM(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_Dhop(gb_op_t op, gb_field_t in, gb_field_t out, int dag);
+int gb_DhopEO(gb_op_t op, gb_field_t in_odd, gb_field_t out_even, int dag);
+int gb_DhopOE(gb_op_t op, gb_field_t in_even, gb_field_t out_odd, int dag);
+int gb_Meooe(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MeooeDag(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_Mooee(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MooeeDag(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MooeeInv(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MooeeInvDag(gb_op_t op, gb_field_t in, gb_field_t out);
+/* SchurDiagMooeeOperator (Grid/algorithms/LinearOperator.h:325-349), odd checkerboard */
+int gb_Mpc(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MpcDag(gb_op_t op, gb_field_t in, gb_field_t out);
+int gb_MpcDagMpc(gb_op_t op, gb_field_t in, gb_field_t out);
+
+/* ---- solvers ------------------------------------------------------------------- */
+typedef struct {
+  double tolerance;      /* ConjugateGradient::Tolerance                                  */
+  int max_iterations;    /* ConjugateGradient::MaxIterations                              */
+  int err_on_no_conv;    /* ErrorOnNoConverge: return GB_ERR_NOT_CONVERGED (never aborts)  */
+  double delta;          /* reliable update when |r|^2 < delta * max|r|^2 since the last  */
+  int relup_every;       /* ... or at least every relup_every inner iterations (0 = off)  */
+  int final_cleanup;     /* ConjugateGradientReliableUpdate::DoFinalCleanup               */
+  int check_every;       /* host convergence poll interval in iterations (0 = default)    */
+  int use_graphs;        /* capture the iteration chunk in a CUDA graph                   */
+} gb_cg_params;
+
+typedef struct {
+  int iterations;         /* IterationsToComplete (max over right-hand sides)            */
+  int reliable_updates;   /* ReliableUpdatesPerformed                                    */
+  int cleanup_iterations; /* IterationsToCleanup                                         */
+  int converged;          /* 1 when every right-hand side converged                      */
+  double true_residual;   /* TrueResidual (max over right-hand sides)                    */
+  double seconds;         /* wall time of the solve                                      */
+  double flops;           /* Grid's flop model for the solve                             */
+} gb_cg_result;
+
+void gb_cg_params_default(gb_cg_params* p);
+
+/* ConjugateGradient<Field>(MdagMLinearOperator) on a full field (Test_wilson_cg_unprec.cc) */
+int gb_cg_mdagm(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* p, gb_cg_result* res);
+/* ConjugateGradient<Field>(SchurDiagMooeeOperator) on an odd half field */
+int gb_cg_schur(gb_op_t op, gb_field_t src_o, gb_field_t psi_o, const gb_cg_params* p, gb_cg_result* res);
+/* per right-hand-side results of the last solve on this op: iterations and true residuals */
+int gb_cg_last_per_rhs(gb_op_t op, int* iterations, double* true_residual);
+/* ConjugateGradientReliableUpdate<FieldD,FieldF>: op_d FP64, op_lo FP32 or FP16 on the
+ * same gauge field; kind 0 = MdagM (full fields), 1 = Schur (odd half fields). */
+int gb_cg_reliable(gb_op_t op_d, gb_op_t op_lo, int kind, gb_field_t src, gb_field_t psi, const gb_cg_params* p,
+                   gb_cg_result* res);
+/* SchurRedBlackDiagMooeeSolve(CG)(M, src, sol) (SchurRedBlack.h:236-291,373-436).
+ * op_lo == NULL: plain CG in op's precision; else mixed precision (reliable update).
+ * unprec_resid (may be NULL): |M sol - src| / |src| per right-hand side. */
+int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, const gb_cg_params* p,
+                   gb_cg_result* res, double* unprec_resid);
+
+/* ---- seeded synthetic inputs (Grid: GridParallelRNG + SU3::HotConfiguration) ----
+ * Counter-based generator keyed by (seed, site, element); independent of thread count.
+ * gb_random_gauge: U = reunitarise(exp(i*eps*H)), H traceless Hermitian with Gaussian
+ * entries, canonical layout.  gb_random_gaussian: n complex numbers with N(0,1) real
+ * and imaginary parts.  gb_random_z2: (+-1 +-i)/sqrt(2) per complex number.
+ */
+int gb_random_gauge(const int dims[4], double eps, uint64_t seed, double* U);
+int gb_random_gaussian(size_t n_complex, uint64_t seed, double* out);
+int gb_random_z2(size_t n_complex, uint64_t seed, double* out);
+int gb_unit_gauge(const int dims[4], double* U);
+
+/* ---- device, stream and host-buffer utilities ------------------------------------ */
+int gb_set_device(int device);                       /* cudaSetDevice for this thread        */
+int gb_op_sync(gb_op_t op);                          /* wait for the op's stream             */
+int gb_op_event_record(gb_op_t op, int slot);        /* slot in [0, 16): event on op stream  */
+int gb_op_event_elapsed(gb_op_t op, int slot0, int slot1, double* ms); /* waits for slot1   */
+int gb_host_alloc(size_t bytes, void** ptr);         /* page-locked host memory              */
+int gb_host_free(void* ptr);
+
+/* ---- timing helpers for benchmarks (CUDA events on the op's stream) --------------- */
+/* Runs `reps` applications of kernel `which` rotating over n_pairs (in,out) field pairs,
+ * returns the average device milliseconds per application.
+ * which: 0 DhopEO, 1 DhopOE, 2 Mooee, 3 MooeeInv, 4 Meooe5D, 5 MpcDagMpc, 6 Dhop(full) */
+int gb_bench_kernel(gb_op_t op, int which, gb_field_t* ins, gb_field_t* outs, int n_pairs, int reps, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBDWF_H */

@@ -1,0 +1,656 @@
+// oracle.hpp -- CPU restatement of Grid's Wilson / Moebius domain-wall fermion hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA library is compared
+// against; the product never links, loads or calls it.  Only tests/, the smoke check and
+// the CPU-baseline leg of bench.py use it.
+//
+// Parity pinning: Grid cannot be compiled in this environment (it needs Eigen, OpenSSL,
+// GMP/MPFR and autotools, none of which are present), and Grid ships no golden data files.
+// The restatement is therefore pinned by the known-answer tests that Grid's own test
+// programs hold for this path (see tests/test_oracle_pins.py):
+//   * DoubleStore + site-loop Dhop equals the naive Cshift formula
+//       (benchmarks/Benchmark_dwf.cc:145-158, 222-232; dagger :235-261)
+//   * DhopEO (+) DhopOE == Dhop                 (benchmarks/Benchmark_dwf.cc:329-356)
+//   * Meo+Moe+Mee+Moo == M, adjointness of Mooee/Meooe, MooeeInv.Mooee == 1,
+//     MpcDagMpc Hermitian                       (tests/core/Test_mobius_even_odd.cc)
+//   * free-field (U = 1) propagator against the momentum-space formula
+//       (tests/core/Test_fft.cc:159,313; WilsonFermionImplementation.h:177-230)
+//   * mixed-precision CG agrees with FP64 CG   (tests/Test_dwf_mixedcg_prec.cc:215)
+//
+// Conventions (all restated from the reference, file:line in the reference checkout):
+//   gamma basis            Grid/qcd/spin/TwoSpinor.h:67-140
+//   leg order / dagger     Grid/qcd/action/fermion/implementation/WilsonKernelsImplementation.h:113-163
+//   DoubleStore + phases   Grid/qcd/action/fermion/WilsonImpl.h:127-171
+//   -1/2 link scaling      Grid/qcd/action/fermion/implementation/WilsonFermionImplementation.h:82-107
+//   diag_mass = 4 + m      Grid/qcd/action/fermion/implementation/WilsonFermionImplementation.h:69-72
+//   5D parity, DW          Grid/qcd/action/fermion/WilsonFermion5D.h:37-61,
+//                          Grid/qcd/action/fermion/implementation/WilsonFermion5DImplementation.h:447-451
+//   Cayley coefficients    Grid/qcd/action/fermion/implementation/CayleyFermion5DImplementation.h:155-271,410-535
+//   M5D / MooeeInv         Grid/qcd/action/fermion/implementation/CayleyFermion5Dcache.h:41-230
+//   Schur operator         Grid/algorithms/LinearOperator.h:286-349
+//   red-black solve        Grid/algorithms/iterative/SchurRedBlack.h:236-291,373-436
+//   CG                     Grid/algorithms/iterative/ConjugateGradient.h:68-257
+//   reliable-update CG     Grid/algorithms/iterative/ConjugateGradientReliableUpdate.h:77-269
+//
+// Canonical host layout (also the library's C-ABI layout):
+//   4D site index  site = x + Lx*(y + Ly*(z + Lz*t))
+//   gauge          U[site][mu][a][b]              complex<double>, mu = x,y,z,t
+//   fermion        psi[site][s][spin][colour]     complex, s = 0..L5-1 innermost of the site
+//   half field     psi[site>>1][s][spin][colour]  over the sites of one parity (Lx even)
+//   parity         (x+y+z+t) & 1, Even = 0; the fifth coordinate takes no part.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace orc {
+
+template <class R> using cplx = std::complex<R>;
+template <class R> using Field = std::vector<cplx<R>>;
+
+constexpr int Ns = 4, Nc = 3, Nsc = 12;
+
+// ---------------------------------------------------------------------------------------
+// Geometry
+// ---------------------------------------------------------------------------------------
+struct Geom {
+  int L[4];
+  int64_t vol;
+  explicit Geom(const int* d) {
+    vol = 1;
+    for (int i = 0; i < 4; i++) { L[i] = d[i]; vol *= d[i]; }
+  }
+  void coords(int64_t site, int x[4]) const {
+    for (int i = 0; i < 4; i++) { x[i] = int(site % L[i]); site /= L[i]; }
+  }
+  int64_t index(const int x[4]) const {
+    return x[0] + int64_t(L[0]) * (x[1] + int64_t(L[1]) * (x[2] + int64_t(L[2]) * x[3]));
+  }
+  int parity(int64_t site) const {
+    int x[4]; coords(site, x);
+    return (x[0] + x[1] + x[2] + x[3]) & 1;
+  }
+  int64_t shift(int64_t site, int mu, int disp) const {
+    int x[4]; coords(site, x);
+    x[mu] = ((x[mu] + disp) % L[mu] + L[mu]) % L[mu];
+    return index(x);
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+// Gamma matrices in Grid's basis (TwoSpinor.h:67-140 comments; spProj*/spRecon* bodies)
+// ---------------------------------------------------------------------------------------
+inline const cplx<double>& gamma_el(int mu, int i, int j) {
+  static const cplx<double> I(0, 1), O(0, 0), P(1, 0), M(-1, 0);
+  static const cplx<double> G[5][4][4] = {
+      {{O, O, O, I}, {O, O, I, O}, {O, -I, O, O}, {-I, O, O, O}},  // gamma_x
+      {{O, O, O, M}, {O, O, P, O}, {O, P, O, O}, {M, O, O, O}},    // gamma_y
+      {{O, O, I, O}, {O, O, O, -I}, {-I, O, O, O}, {O, I, O, O}},  // gamma_z
+      {{O, O, P, O}, {O, O, O, P}, {P, O, O, O}, {O, P, O, O}},    // gamma_t
+      {{P, O, O, O}, {O, P, O, O}, {O, O, M, O}, {O, O, O, M}},    // gamma_5
+  };
+  return G[mu][i][j];
+}
+
+// ---------------------------------------------------------------------------------------
+// Field helpers
+// ---------------------------------------------------------------------------------------
+template <class R> inline double norm2(const Field<R>& a) {
+  double s = 0;
+#pragma omp parallel for reduction(+ : s)
+  for (int64_t i = 0; i < int64_t(a.size()); i++) s += double(std::norm(a[i]));
+  return s;
+}
+template <class R> inline cplx<double> inner(const Field<R>& a, const Field<R>& b) {
+  double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im)
+  for (int64_t i = 0; i < int64_t(a.size()); i++) {
+    cplx<double> z = std::conj(cplx<double>(a[i])) * cplx<double>(b[i]);
+    re += z.real(); im += z.imag();
+  }
+  return {re, im};
+}
+// z = a*x + y
+template <class R> inline void axpy(Field<R>& z, R a, const Field<R>& x, const Field<R>& y) {
+#pragma omp parallel for
+  for (int64_t i = 0; i < int64_t(z.size()); i++) z[i] = a * x[i] + y[i];
+}
+template <class R> inline void pick_cb(const Geom& g, int L5, int parity, const Field<R>& full, Field<R>& half) {
+  half.assign(size_t(g.vol / 2) * L5 * Nsc, cplx<R>(0));
+#pragma omp parallel for
+  for (int64_t site = 0; site < g.vol; site++) {
+    if (g.parity(site) != parity) continue;
+    std::copy_n(&full[size_t(site) * L5 * Nsc], L5 * Nsc, &half[size_t(site >> 1) * L5 * Nsc]);
+  }
+}
+template <class R> inline void set_cb(const Geom& g, int L5, int parity, const Field<R>& half, Field<R>& full) {
+  full.resize(size_t(g.vol) * L5 * Nsc);
+#pragma omp parallel for
+  for (int64_t site = 0; site < g.vol; site++) {
+    if (g.parity(site) != parity) continue;
+    std::copy_n(&half[size_t(site >> 1) * L5 * Nsc], L5 * Nsc, &full[size_t(site) * L5 * Nsc]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// DoubleStore (WilsonImpl.h:127-171) with the -1/2 of ImportGauge folded in
+//   Ud[x][mu]   = -1/2 * U_mu(x) * (phase_mu if x_mu == L_mu-1)
+//   Ud[x][mu+4] = -1/2 * U_mu(x-mu)^dagger * (conj(phase_mu) if x_mu == 0)
+// ---------------------------------------------------------------------------------------
+template <class R>
+void double_store(const Geom& g, const cplx<double>* U, const cplx<double>* phase, std::vector<cplx<R>>& Ud) {
+  Ud.assign(size_t(g.vol) * 8 * 9, cplx<R>(0));
+#pragma omp parallel for
+  for (int64_t site = 0; site < g.vol; site++) {
+    int x[4]; g.coords(site, x);
+    for (int mu = 0; mu < 4; mu++) {
+      cplx<double> pf = (x[mu] == g.L[mu] - 1) ? phase[mu] : cplx<double>(1, 0);
+      cplx<double> pb = (x[mu] == 0) ? std::conj(phase[mu]) : cplx<double>(1, 0);
+      int64_t back = g.shift(site, mu, -1);
+      const cplx<double>* Uf = U + (size_t(site) * 4 + mu) * 9;
+      const cplx<double>* Ub = U + (size_t(back) * 4 + mu) * 9;
+      for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) {
+          Ud[(size_t(site) * 8 + mu) * 9 + a * 3 + b] = cplx<R>(-0.5 * pf * Uf[a * 3 + b]);
+          Ud[(size_t(site) * 8 + mu + 4) * 9 + a * 3 + b] = cplx<R>(-0.5 * pb * std::conj(Ub[b * 3 + a]));
+        }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Site-loop Dhop on full canonical fields (WilsonKernelsImplementation.h:113-163).
+// Non-dagger: out(x) = sum_mu (1 - g_mu) Ud_mu(x) in(x+mu) + (1 + g_mu) Ud_{mu+4}(x) in(x-mu)
+// Dagger swaps the projector signs.  The restatement applies U to all four spins and then
+// the 4x4 projector (1 -/+ gamma_mu); the half-spinor trick is not used here.
+// out_parity >= 0 restricts the output sites (DhopEO/DhopOE); other sites are untouched.
+// ---------------------------------------------------------------------------------------
+template <class R>
+void dhop(const Geom& g, int L5, const std::vector<cplx<R>>& Ud, const Field<R>& in, Field<R>& out, int dag,
+          int out_parity = -1) {
+  out.resize(in.size());
+#pragma omp parallel for schedule(static)
+  for (int64_t site = 0; site < g.vol; site++) {
+    if (out_parity >= 0 && g.parity(site) != out_parity) continue;
+    for (int s = 0; s < L5; s++) {
+      cplx<R> res[Nsc];
+      for (auto& r : res) r = 0;
+      for (int leg = 0; leg < 8; leg++) {
+        int mu = leg & 3;
+        int disp = leg < 4 ? +1 : -1;
+        int64_t nb = g.shift(site, mu, disp);
+        const cplx<R>* U = &Ud[(size_t(site) * 8 + leg) * 9];
+        const cplx<R>* p = &in[(size_t(nb) * L5 + s) * Nsc];
+        cplx<R> phi[Nsc];
+        for (int sp = 0; sp < Ns; sp++)
+          for (int a = 0; a < Nc; a++) {
+            cplx<R> acc = 0;
+            for (int b = 0; b < Nc; b++) acc += U[a * 3 + b] * p[sp * 3 + b];
+            phi[sp * 3 + a] = acc;
+          }
+        // forward leg uses (1 - gamma), backward (1 + gamma); dagger swaps
+        R sign = (disp > 0) ? R(-1) : R(1);
+        if (dag) sign = -sign;
+        for (int sp = 0; sp < Ns; sp++)
+          for (int a = 0; a < Nc; a++) {
+            cplx<R> gp = 0;
+            for (int sq = 0; sq < Ns; sq++) gp += cplx<R>(gamma_el(mu, sp, sq)) * phi[sq * 3 + a];
+            res[sp * 3 + a] += phi[sp * 3 + a] + sign * gp;
+          }
+      }
+      std::copy_n(res, Nsc, &out[(size_t(site) * L5 + s) * Nsc]);
+    }
+  }
+}
+
+// Naive Cshift-form Dhop (benchmarks/Benchmark_dwf.cc:145-158 non-dagger, :235-261 dagger),
+// written from the undoubled links and the boundary phases, as an independent check of
+// DoubleStore + the site loop.
+template <class R>
+void dhop_naive(const Geom& g, int L5, const cplx<double>* U, const cplx<double>* phase, const Field<R>& in,
+                Field<R>& out, int dag) {
+  size_t n = in.size();
+  std::vector<cplx<double>> ref(n, 0), tmp(n), sh(n);
+  auto link = [&](int64_t site, int mu, int a, int b) {
+    int x[4]; g.coords(site, x);
+    cplx<double> ph = (x[mu] == g.L[mu] - 1) ? phase[mu] : cplx<double>(1, 0);
+    return ph * U[(size_t(site) * 4 + mu) * 9 + a * 3 + b];
+  };
+  double sgn = dag ? 1.0 : -1.0;  // non-dag: ref += tmp - G tmp (forward)
+  for (int mu = 0; mu < 4; mu++) {
+    // Cshift(src, mu, +1)(x) = src(x+mu)
+    for (int64_t site = 0; site < g.vol; site++) {
+      int64_t nb = g.shift(site, mu, +1);
+      for (int k = 0; k < L5 * Nsc; k++) sh[size_t(site) * L5 * Nsc + k] = cplx<double>(in[size_t(nb) * L5 * Nsc + k]);
+    }
+    // tmp = U_mu * shifted
+    for (int64_t site = 0; site < g.vol; site++)
+      for (int s = 0; s < L5; s++)
+        for (int sp = 0; sp < Ns; sp++)
+          for (int a = 0; a < Nc; a++) {
+            cplx<double> acc = 0;
+            for (int b = 0; b < Nc; b++) acc += link(site, mu, a, b) * sh[(size_t(site) * L5 + s) * Nsc + sp * 3 + b];
+            tmp[(size_t(site) * L5 + s) * Nsc + sp * 3 + a] = acc;
+          }
+    for (int64_t site = 0; site < g.vol; site++)
+      for (int s = 0; s < L5; s++)
+        for (int sp = 0; sp < Ns; sp++)
+          for (int a = 0; a < Nc; a++) {
+            size_t o = (size_t(site) * L5 + s) * Nsc;
+            cplx<double> gt = 0;
+            for (int sq = 0; sq < Ns; sq++) gt += gamma_el(mu, sp, sq) * tmp[o + sq * 3 + a];
+            ref[o + sp * 3 + a] += tmp[o + sp * 3 + a] + sgn * gt;
+          }
+    // tmp = adj(U_mu) * src ; then Cshift(tmp, mu, -1)(x) = tmp(x-mu)
+    for (int64_t site = 0; site < g.vol; site++)
+      for (int s = 0; s < L5; s++)
+        for (int sp = 0; sp < Ns; sp++)
+          for (int a = 0; a < Nc; a++) {
+            cplx<double> acc = 0;
+            for (int b = 0; b < Nc; b++)
+              acc += std::conj(link(site, mu, b, a)) * cplx<double>(in[(size_t(site) * L5 + s) * Nsc + sp * 3 + b]);
+            tmp[(size_t(site) * L5 + s) * Nsc + sp * 3 + a] = acc;
+          }
+    for (int64_t site = 0; site < g.vol; site++) {
+      int64_t nb = g.shift(site, mu, -1);
+      for (int k = 0; k < L5 * Nsc; k++) sh[size_t(site) * L5 * Nsc + k] = tmp[size_t(nb) * L5 * Nsc + k];
+    }
+    for (int64_t site = 0; site < g.vol; site++)
+      for (int s = 0; s < L5; s++)
+        for (int sp = 0; sp < Ns; sp++)
+          for (int a = 0; a < Nc; a++) {
+            size_t o = (size_t(site) * L5 + s) * Nsc;
+            cplx<double> gt = 0;
+            for (int sq = 0; sq < Ns; sq++) gt += gamma_el(mu, sp, sq) * sh[o + sq * 3 + a];
+            ref[o + sp * 3 + a] += sh[o + sp * 3 + a] - sgn * gt;
+          }
+  }
+  out.resize(n);
+  for (size_t i = 0; i < n; i++) out[i] = cplx<R>(-0.5 * ref[i]);
+}
+
+// ---------------------------------------------------------------------------------------
+// Cayley / Moebius coefficients (CayleyFermion5DImplementation.h:410-535) with the
+// Moebius tanh choice gamma_s = 1 (MobiusFermion.h:63-67; approx/Zolotarev.cc:471-473).
+// ---------------------------------------------------------------------------------------
+struct Cayley {
+  int Ls = 0;
+  double mf = 0, M5 = 0, b = 0, c = 0;
+  std::vector<double> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
+  void setup(int Ls_, double mf_, double M5_, double b_, double c_) {
+    Ls = Ls_; mf = mf_; M5 = M5_; b = b_; c = c_;
+    bs.assign(Ls, 0); cs.assign(Ls, 0); bee.assign(Ls, 0); cee.assign(Ls, 0);
+    dee.assign(Ls, 0); lee.assign(Ls, 0); leem.assign(Ls, 0); uee.assign(Ls, 0); ueem.assign(Ls, 0);
+    for (int i = 0; i < Ls; i++) {
+      double omega = 1.0;
+      bs[i] = 0.5 * ((b + c) / omega + (b - c));
+      cs[i] = 0.5 * ((b + c) / omega - (b - c));
+      bee[i] = bs[i] * (4.0 - M5) + 1.0;
+      cee[i] = 1.0 - cs[i] * (4.0 - M5);
+    }
+    const std::vector<double>& aee = cee;
+    for (int i = 0; i < Ls; i++) {
+      dee[i] = bee[i];
+      if (i < Ls - 1) {
+        lee[i] = -cee[i + 1] / bee[i];
+        leem[i] = mf * cee[Ls - 1] / bee[0];
+        for (int j = 0; j < i; j++) leem[i] *= aee[j] / bee[j + 1];
+        uee[i] = -aee[i] / bee[i];
+        ueem[i] = mf;
+        for (int j = 1; j <= i; j++) ueem[i] *= cee[j] / bee[j];
+        ueem[i] *= aee[0] / bee[0];
+      }
+    }
+    double delta_d = mf * cee[Ls - 1];
+    for (int j = 0; j < Ls - 1; j++) delta_d *= cee[j] / bee[j];
+    dee[Ls - 1] += delta_d;
+  }
+};
+
+// M5D / M5Ddag (CayleyFermion5Dcache.h:41-115) on an n4 x Ls field (full or half):
+//   non-dag: chi[s] = diag[s] phi[s] + upper[s] P- psi[s+1] + lower[s] P+ psi[s-1]
+//   dag    : chi[s] = diag[s] phi[s] + upper[s] P+ psi[s+1] + lower[s] P- psi[s-1]
+// with P+ = spins {0,1}, P- = spins {2,3} (gamma_5 = diag(1,1,-1,-1)).
+template <class R>
+void m5d(int64_t n4, int Ls, const Field<R>& psi, const Field<R>& phi, Field<R>& chi, const std::vector<double>& lower,
+         const std::vector<double>& diag, const std::vector<double>& upper, int dag) {
+  Field<R> res(psi.size());
+#pragma omp parallel for
+  for (int64_t x = 0; x < n4; x++)
+    for (int s = 0; s < Ls; s++) {
+      int sp = (s + 1) % Ls, sm = (s - 1 + Ls) % Ls;
+      size_t o = (size_t(x) * Ls + s) * Nsc, op = (size_t(x) * Ls + sp) * Nsc, om = (size_t(x) * Ls + sm) * Nsc;
+      for (int k = 0; k < Nsc; k++) {
+        bool upper_spin = k < 6;  // spins 0,1
+        cplx<R> v = R(diag[s]) * phi[o + k];
+        if (!dag) v += upper_spin ? R(lower[s]) * psi[om + k] : R(upper[s]) * psi[op + k];
+        else      v += upper_spin ? R(upper[s]) * psi[op + k] : R(lower[s]) * psi[om + k];
+        res[o + k] = v;
+      }
+    }
+  chi.swap(res);
+}
+
+// ---------------------------------------------------------------------------------------
+// Operator interface shared by Wilson and Moebius restatements.  Half fields carry an
+// explicit parity argument (the parity of the input field).
+// ---------------------------------------------------------------------------------------
+template <class R> struct Op {
+  Geom g;
+  int L5;
+  std::vector<cplx<R>> Ud;
+  Op(const int* dims, int L5_) : g(dims), L5(L5_) {}
+  virtual ~Op() {}
+  int64_t half_sites() const { return g.vol / 2; }
+  size_t full_len() const { return size_t(g.vol) * L5 * Nsc; }
+  size_t half_len() const { return size_t(g.vol / 2) * L5 * Nsc; }
+
+  void import_gauge(const cplx<double>* U, const cplx<double>* phase) { double_store<R>(g, U, phase, Ud); }
+  void Dhop(const Field<R>& in, Field<R>& out, int dag) { dhop<R>(g, L5, Ud, in, out, dag); }
+  // in has parity in_parity; out has the other parity
+  void DhopCB(const Field<R>& in, Field<R>& out, int in_parity, int dag) {
+    Field<R> fin(full_len(), cplx<R>(0)), fout(full_len(), cplx<R>(0));
+    set_cb<R>(g, L5, in_parity, in, fin);
+    dhop<R>(g, L5, Ud, fin, fout, dag, 1 - in_parity);
+    pick_cb<R>(g, L5, 1 - in_parity, fout, out);
+  }
+  virtual void M(const Field<R>& in, Field<R>& out) = 0;
+  virtual void Mdag(const Field<R>& in, Field<R>& out) = 0;
+  virtual void Meooe(const Field<R>& in, Field<R>& out, int in_parity) = 0;
+  virtual void MeooeDag(const Field<R>& in, Field<R>& out, int in_parity) = 0;
+  virtual void Mooee(const Field<R>& in, Field<R>& out) = 0;
+  virtual void MooeeDag(const Field<R>& in, Field<R>& out) = 0;
+  virtual void MooeeInv(const Field<R>& in, Field<R>& out) = 0;
+  virtual void MooeeInvDag(const Field<R>& in, Field<R>& out) = 0;
+
+  void MdagM(const Field<R>& in, Field<R>& out) {
+    Field<R> t; M(in, t); Mdag(t, out);
+  }
+  // SchurDiagMooeeOperator (LinearOperator.h:325-349), on the odd checkerboard
+  void Mpc(const Field<R>& in, Field<R>& out) {
+    Field<R> tmp, t2;
+    Meooe(in, tmp, 1);
+    MooeeInv(tmp, t2);
+    Meooe(t2, tmp, 0);
+    Mooee(in, out);
+    axpy<R>(out, R(-1), tmp, out);
+  }
+  void MpcDag(const Field<R>& in, Field<R>& out) {
+    Field<R> tmp, t2;
+    MeooeDag(in, tmp, 1);
+    MooeeInvDag(tmp, t2);
+    MeooeDag(t2, tmp, 0);
+    MooeeDag(in, out);
+    axpy<R>(out, R(-1), tmp, out);
+  }
+  void MpcDagMpc(const Field<R>& in, Field<R>& out) {
+    Field<R> t; Mpc(in, t); MpcDag(t, out);
+  }
+};
+
+// WilsonFermion (WilsonFermionImplementation.h:113-176).  L5 > 1 stacks independent
+// right-hand sides in the fifth slot; the operator is diagonal in it.
+template <class R> struct Wilson : Op<R> {
+  double mass, diag_mass;
+  Wilson(const int* dims, int L5, double m) : Op<R>(dims, L5), mass(m), diag_mass(4.0 + m) {}
+  void M(const Field<R>& in, Field<R>& out) override {
+    this->Dhop(in, out, 0); axpy<R>(out, R(diag_mass), in, out);
+  }
+  void Mdag(const Field<R>& in, Field<R>& out) override {
+    this->Dhop(in, out, 1); axpy<R>(out, R(diag_mass), in, out);
+  }
+  void Meooe(const Field<R>& in, Field<R>& out, int p) override { this->DhopCB(in, out, p, 0); }
+  void MeooeDag(const Field<R>& in, Field<R>& out, int p) override { this->DhopCB(in, out, p, 1); }
+  void Mooee(const Field<R>& in, Field<R>& out) override {
+    out.resize(in.size());
+    for (size_t i = 0; i < in.size(); i++) out[i] = R(diag_mass) * in[i];
+  }
+  void MooeeDag(const Field<R>& in, Field<R>& out) override { Mooee(in, out); }
+  void MooeeInv(const Field<R>& in, Field<R>& out) override {
+    out.resize(in.size());
+    for (size_t i = 0; i < in.size(); i++) out[i] = R(1.0 / diag_mass) * in[i];
+  }
+  void MooeeInvDag(const Field<R>& in, Field<R>& out) override { MooeeInv(in, out); }
+};
+
+// MobiusFermion / CayleyFermion5D (CayleyFermion5DImplementation.h:155-344,
+// CayleyFermion5Dcache.h:117-230).  L5 = Ls.
+template <class R> struct Mobius : Op<R> {
+  Cayley cf;
+  int Ls;
+  Mobius(const int* dims, int Ls_, double mf, double M5, double b, double c) : Op<R>(dims, Ls_), Ls(Ls_) {
+    cf.setup(Ls_, mf, M5, b, c);
+  }
+  int64_t n4(const Field<R>& f) const { return int64_t(f.size() / (size_t(Ls) * Nsc)); }
+
+  void DW(const Field<R>& in, Field<R>& out, int dag) {
+    this->Dhop(in, out, dag); axpy<R>(out, R(4.0 - cf.M5), in, out);
+  }
+  void Meooe5D(const Field<R>& psi, Field<R>& Din) {
+    std::vector<double> diag = cf.bs, upper = cf.cs, lower = cf.cs;
+    upper[Ls - 1] = -cf.mf * upper[Ls - 1];
+    lower[0] = -cf.mf * lower[0];
+    m5d<R>(n4(psi), Ls, psi, psi, Din, lower, diag, upper, 0);
+  }
+  void MeooeDag5D(const Field<R>& psi, Field<R>& Din) {
+    std::vector<double> diag = cf.bs, upper(Ls), lower(Ls);
+    for (int s = 0; s < Ls; s++) {
+      if (s == 0) { upper[s] = cf.cs[s + 1]; lower[s] = -cf.mf * cf.cs[Ls - 1]; }
+      else if (s == Ls - 1) { upper[s] = -cf.mf * cf.cs[0]; lower[s] = cf.cs[s - 1]; }
+      else { upper[s] = cf.cs[s + 1]; lower[s] = cf.cs[s - 1]; }
+    }
+    m5d<R>(n4(psi), Ls, psi, psi, Din, lower, diag, upper, 1);
+  }
+  void Mooee(const Field<R>& psi, Field<R>& chi) override {
+    std::vector<double> diag = cf.bee, upper(Ls), lower(Ls);
+    for (int i = 0; i < Ls; i++) { upper[i] = -cf.cee[i]; lower[i] = -cf.cee[i]; }
+    upper[Ls - 1] = -cf.mf * upper[Ls - 1];
+    lower[0] = -cf.mf * lower[0];
+    m5d<R>(n4(psi), Ls, psi, psi, chi, lower, diag, upper, 0);
+  }
+  void MooeeDag(const Field<R>& psi, Field<R>& chi) override {
+    std::vector<double> diag = cf.bee, upper(Ls), lower(Ls);
+    for (int s = 0; s < Ls; s++) {
+      if (s == 0) { upper[s] = -cf.cee[s + 1]; lower[s] = cf.mf * cf.cee[Ls - 1]; }
+      else if (s == Ls - 1) { upper[s] = cf.mf * cf.cee[0]; lower[s] = -cf.cee[s - 1]; }
+      else { upper[s] = -cf.cee[s + 1]; lower[s] = -cf.cee[s - 1]; }
+    }
+    m5d<R>(n4(psi), Ls, psi, psi, chi, lower, diag, upper, 1);
+  }
+  // LDU solve along s (CayleyFermion5Dcache.h:117-170), component by component.
+  void MooeeInv(const Field<R>& psi, Field<R>& chi) override { mooee_inv(psi, chi, 0); }
+  void MooeeInvDag(const Field<R>& psi, Field<R>& chi) override { mooee_inv(psi, chi, 1); }
+  void mooee_inv(const Field<R>& psi, Field<R>& chi, int dag) {
+    chi.resize(psi.size());
+    const auto& lee = dag ? cf.uee : cf.lee;    // dag: roles of (lee,leem) and (uee,ueem)
+    const auto& leem = dag ? cf.ueem : cf.leem; // swap and the chiralities swap
+    const auto& uee = dag ? cf.lee : cf.uee;
+    const auto& ueem = dag ? cf.leem : cf.ueem;
+    const auto& dee = cf.dee;
+    int64_t n = n4(psi);
+#pragma omp parallel for
+    for (int64_t x = 0; x < n; x++) {
+      for (int k = 0; k < Nsc; k++) {
+        // chirality of the component: "first" = the projector applied in the forward
+        // sweep (P+ non-dag, P- dag), "second" = the other one
+        bool upper_spin = k < 6;
+        bool first = dag ? !upper_spin : upper_spin;
+        auto at = [&](int s) -> size_t { return (size_t(x) * Ls + s) * Nsc + k; };
+        // forward: res_s = psi_s - lee[s-1] P_first res_{s-1};  acc += leem[s] P_second res_s
+        cplx<R> prev = 0, acc = 0;
+        for (int s = 0; s < Ls - 1; s++) {
+          cplx<R> r = psi[at(s)];
+          if (s > 0 && first) r -= R(lee[s - 1]) * prev;
+          if (!first) acc += R(leem[s]) * r;
+          chi[at(s)] = r;
+          prev = r;
+        }
+        cplx<R> r = psi[at(Ls - 1)];
+        if (first) r -= R(lee[Ls - 2]) * prev;
+        else r -= acc;
+        // backward: chi_{Ls-1} = r / dee ; chi_s = chi_s/dee[s] - uee[s] P_second chi_{s+1}
+        //                                               - ueem[s] P_first chi_{Ls-1}
+        r = R(1.0 / dee[Ls - 1]) * r;
+        chi[at(Ls - 1)] = r;
+        cplx<R> last = r, nxt = r;
+        for (int s = Ls - 2; s >= 0; s--) {
+          cplx<R> v = R(1.0 / dee[s]) * chi[at(s)];
+          if (!first) v -= R(uee[s]) * nxt;
+          else v -= R(ueem[s]) * last;
+          chi[at(s)] = v;
+          nxt = v;
+        }
+      }
+    }
+  }
+  void Meooe(const Field<R>& in, Field<R>& out, int p) override {
+    Field<R> t; Meooe5D(in, t); this->DhopCB(t, out, p, 0);
+  }
+  void MeooeDag(const Field<R>& in, Field<R>& out, int p) override {
+    Field<R> t; this->DhopCB(in, t, p, 1); MeooeDag5D(t, out);
+  }
+  void M(const Field<R>& psi, Field<R>& chi) override {
+    Field<R> Din; Meooe5D(psi, Din);
+    DW(Din, chi, 0);
+    axpy<R>(chi, R(1), chi, psi);
+    std::vector<double> diag(Ls, 1.0), upper(Ls, -1.0), lower(Ls, -1.0);
+    upper[Ls - 1] = cf.mf; lower[0] = cf.mf;
+    m5d<R>(n4(psi), Ls, psi, chi, chi, lower, diag, upper, 0);
+  }
+  void Mdag(const Field<R>& psi, Field<R>& chi) override {
+    Field<R> Din; DW(psi, Din, 1);
+    MeooeDag5D(Din, chi);
+    std::vector<double> diag(Ls, 1.0), upper(Ls, -1.0), lower(Ls, -1.0);
+    upper[Ls - 1] = cf.mf; lower[0] = cf.mf;
+    m5d<R>(n4(psi), Ls, psi, chi, chi, lower, diag, upper, 1);
+    axpy<R>(chi, R(1), chi, psi);
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+// ConjugateGradient (ConjugateGradient.h:68-257), same sequence of operations.
+// ---------------------------------------------------------------------------------------
+struct CGResult {
+  int iterations = 0;
+  int reliable_updates = 0;
+  int cleanup_iterations = 0;
+  double true_residual = 0;
+  int converged = 0;
+};
+
+template <class R, class HermOp>
+CGResult cg(HermOp&& A, const Field<R>& src, Field<R>& psi, double tol, int maxit) {
+  CGResult res;
+  size_t n = src.size();
+  psi.resize(n);
+  Field<R> p(n), mmp(n), r(n);
+  double ssq = norm2(src), guess = norm2(psi), a, cp, c, d, b;
+  if (guess == 0.0) { r = src; p = r; a = ssq; }
+  else { A(psi, mmp); for (size_t i = 0; i < n; i++) r[i] = src[i] - mmp[i]; p = r; a = norm2(p); }
+  cp = a;
+  if (ssq == 0.0) { std::fill(psi.begin(), psi.end(), cplx<R>(0)); res.iterations = 1; res.converged = 1; return res; }
+  double rsq = tol * tol * ssq;
+  if (cp <= rsq) { res.true_residual = std::sqrt(a / ssq); res.converged = 1; return res; }
+  for (int k = 1; k <= maxit; k++) {
+    c = cp;
+    A(p, mmp);
+    d = inner(p, mmp).real();
+    a = c / d;
+    // cp = axpy_norm(r, -a, mmp, r)
+    for (size_t i = 0; i < n; i++) r[i] = R(-a) * mmp[i] + r[i];
+    cp = norm2(r);
+    b = cp / c;
+    for (size_t i = 0; i < n; i++) { psi[i] = R(a) * p[i] + psi[i]; p[i] = R(b) * p[i] + r[i]; }
+    if (cp <= rsq) {
+      A(psi, mmp);
+      for (size_t i = 0; i < n; i++) p[i] = mmp[i] - src[i];
+      res.true_residual = std::sqrt(norm2(p)) / std::sqrt(norm2(src));
+      res.iterations = k;
+      res.converged = 1;
+      return res;
+    }
+  }
+  res.iterations = maxit;
+  A(psi, mmp);
+  for (size_t i = 0; i < n; i++) p[i] = mmp[i] - src[i];
+  res.true_residual = std::sqrt(norm2(p) / ssq);
+  return res;
+}
+
+template <class A, class B> inline void precision_change(Field<A>& out, const Field<B>& in) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); i++) out[i] = cplx<A>(in[i]);
+}
+
+// ConjugateGradientReliableUpdate (ConjugateGradientReliableUpdate.h:77-269) with the
+// optional extra rule "reliable update at least every relup_every iterations"
+// (relup_every <= 0 disables it) and the final FP64 cleanup CG.
+template <class HermD, class HermF>
+CGResult cg_reliable(HermD&& Ad, HermF&& Af, const Field<double>& src, Field<double>& psi, double tol, int maxit,
+                     double delta, int relup_every, bool cleanup) {
+  CGResult res;
+  size_t n = src.size();
+  psi.resize(n);
+  Field<double> p(n), mmp(n), r(n);
+  Ad(psi, mmp);
+  for (size_t i = 0; i < n; i++) r[i] = src[i] - mmp[i];
+  p = r;
+  double a = norm2(p), cp = a, ssq = norm2(src), c, d, b;
+  double rsq = tol * tol * ssq;
+  if (cp <= rsq) { res.converged = 1; return res; }
+  Field<float> r_f, psi_f(n, 0), p_f, mmp_f(n);
+  precision_change(r_f, r);
+  p_f = r_f;
+  double maxres = cp;
+  int l = 0, since = 0;
+  for (int k = 1; k <= maxit; k++) {
+    c = cp;
+    Af(p_f, mmp_f);
+    d = inner(p_f, mmp_f).real();
+    a = c / d;
+    for (size_t i = 0; i < n; i++) r_f[i] = float(-a) * mmp_f[i] + r_f[i];
+    cp = norm2(r_f);
+    b = cp / c;
+    for (size_t i = 0; i < n; i++) psi_f[i] = float(a) * p_f[i] + psi_f[i];
+    since++;
+    if (cp > maxres) maxres = cp;
+    if (cp <= rsq) {
+      for (size_t i = 0; i < n; i++) psi[i] += cplx<double>(psi_f[i]);
+      res.iterations = k;
+      res.reliable_updates = l;
+      if (cleanup) {
+        CGResult c2 = cg<double>(Ad, src, psi, tol, maxit);
+        res.cleanup_iterations = c2.iterations;
+        res.true_residual = c2.true_residual;
+        res.converged = c2.converged;
+      } else {
+        Ad(psi, mmp);
+        for (size_t i = 0; i < n; i++) p[i] = mmp[i] - src[i];
+        res.true_residual = std::sqrt(norm2(p) / ssq);
+        res.converged = 1;
+      }
+      return res;
+    } else if (cp < delta * maxres || (relup_every > 0 && since >= relup_every)) {
+      for (size_t i = 0; i < n; i++) psi[i] += cplx<double>(psi_f[i]);
+      Ad(psi, mmp);
+      for (size_t i = 0; i < n; i++) r[i] = src[i] - mmp[i];
+      std::fill(psi_f.begin(), psi_f.end(), cplx<float>(0));
+      precision_change(r_f, r);
+      cp = norm2(r);
+      maxres = cp;
+      b = cp / c;
+      l++;
+      since = 0;
+    }
+    for (size_t i = 0; i < n; i++) p_f[i] = float(b) * p_f[i] + r_f[i];
+  }
+  res.iterations = maxit;
+  res.reliable_updates = l;
+  return res;
+}
+
+}  // namespace orc

@@ -1,0 +1,200 @@
+"""Pins the CPU oracle to the known answers that Grid's own tests hold for this path
+(no golden data files ship with Grid, and Grid cannot be built here):
+
+  * Dhop == naive Cshift formula        benchmarks/Benchmark_dwf.cc:145-158,222-232 (dag :235-261)
+  * DhopEO (+) DhopOE == Dhop           benchmarks/Benchmark_dwf.cc:329-356
+  * even-odd identities                 tests/core/Test_mobius_even_odd.cc, Test_wilson_even_odd.cc
+  * free-field propagator               tests/core/Test_fft.cc:159,313 (WilsonFermionImplementation.h:177-230)
+  * CG true residual / mixed vs FP64    tests/solver/Test_wilson_cg_unprec.cc, tests/Test_dwf_mixedcg_prec.cc:215
+Tolerances: identities at FP64 rounding (1e-12 relative), FP32 restatement 1e-6.
+"""
+import numpy as np
+import pytest
+
+import grid_gb300 as g
+from oracle import oracle as o
+from tests._common import GAMMA, GAMMA5, MOBIUS, fermion, mobius_free_apply, mobius_free_solve, wilson_free_solve
+
+DIMS = (4, 4, 4, 4)
+VOL = 256
+
+
+def _mobius(prec=0, Ls=6, mf=0.1, dims=DIMS, U=None, eps=0.5, seed=11):
+    U = g.random_gauge(dims, eps, seed) if U is None else U
+    return o.OracleOp(1, prec, dims, Ls, [mf, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t()), U
+
+
+def _wilson(prec=0, L5=1, mass=0.1, dims=DIMS, U=None, eps=0.3, seed=7):
+    U = g.random_gauge(dims, eps, seed) if U is None else U
+    return o.OracleOp(0, prec, dims, L5, [mass], U, g.antiperiodic_t()), U
+
+
+def test_gamma_basis_algebra():
+    for mu in range(4):
+        for nu in range(4):
+            ac = GAMMA[mu] @ GAMMA[nu] + GAMMA[nu] @ GAMMA[mu]
+            assert np.allclose(ac, 2 * np.eye(4) * (mu == nu))
+    assert np.allclose(GAMMA[0] @ GAMMA[1] @ GAMMA[2] @ GAMMA[3], GAMMA5)
+
+
+def test_gauge_generator_is_su3_and_seeded():
+    U = g.random_gauge(DIMS, 0.5, 3).reshape(-1, 3, 3)
+    assert np.abs(np.einsum("nij,nkj->nik", U, U.conj()) - np.eye(3)).max() < 1e-14
+    assert np.abs(np.linalg.det(U) - 1).max() < 1e-14
+    assert np.array_equal(U, g.random_gauge(DIMS, 0.5, 3).reshape(-1, 3, 3))
+    assert not np.array_equal(U, g.random_gauge(DIMS, 0.5, 4).reshape(-1, 3, 3))
+    # exp(i eps H): distance from 1 grows with eps
+    d1 = np.abs(g.random_gauge(DIMS, 0.1, 3).reshape(-1, 3, 3) - np.eye(3)).mean()
+    d5 = np.abs(U - np.eye(3)).mean()
+    assert d1 < d5
+    z = g.random_gaussian(200000, 5)
+    assert abs(z.real.std() - 1) < 0.01 and abs(z.imag.mean()) < 0.01
+
+
+@pytest.mark.parametrize("L5", [1, 3])
+@pytest.mark.parametrize("dag", [0, 1])
+@pytest.mark.parametrize("phases", ["antiperiodic", "periodic"])
+def test_dhop_equals_naive_cshift(L5, dag, phases):
+    ph = g.antiperiodic_t() if phases == "antiperiodic" else g.periodic()
+    U = g.random_gauge(DIMS, 0.5, 21)
+    op = o.OracleOp(0, 0, DIMS, L5, [0.1], U, ph)
+    x = fermion(VOL, L5, 22)
+    a = op.apply(o.OP_DHOP_DAG if dag else o.OP_DHOP, x)
+    b = o.dhop_naive(DIMS, L5, U, ph, x, dag)
+    assert o.rel_l2(a, b) < 1e-14
+
+
+def test_dhop_eo_oe_equals_dhop():
+    op, U = _mobius()
+    x = fermion(VOL, 6, 31)
+    full = op.apply(o.OP_DHOP, x)
+    xe, xo = o.pick(DIMS, 6, x, 0), o.pick(DIMS, 6, x, 1)
+    re = op.dhop_cb(xo, 1)  # DhopEO: odd in -> even out
+    ro = op.dhop_cb(xe, 0)  # DhopOE
+    both = o.setcb(DIMS, 6, ro, 1, o.setcb(DIMS, 6, re, 0))
+    assert o.rel_l2(both, full) < 1e-14
+
+
+@pytest.mark.parametrize("kind", ["mobius", "wilson"])
+def test_even_odd_decomposition_identities(kind):
+    op, U = _mobius() if kind == "mobius" else _wilson()
+    L5 = op.L5
+    chi = fermion(VOL, L5, 41)
+    phi = fermion(VOL, L5, 42)
+    ce, co = o.pick(DIMS, L5, chi, 0), o.pick(DIMS, L5, chi, 1)
+    pe, po = o.pick(DIMS, L5, phi, 0), o.pick(DIMS, L5, phi, 1)
+    # Meo + Moe + Mee + Moo == M
+    for dag in (0, 1):
+        oo = op.apply(o.OP_MOOEE_DAG if dag else o.OP_MOOEE, co)
+        ee = op.apply(o.OP_MOOEE_DAG if dag else o.OP_MOOEE, ce)
+        eo = op.apply(o.OP_MEOOE_DAG if dag else o.OP_MEOOE, co, 1)
+        oe = op.apply(o.OP_MEOOE_DAG if dag else o.OP_MEOOE, ce, 0)
+        full = o.setcb(DIMS, L5, oo + oe, 1, o.setcb(DIMS, L5, ee + eo, 0))
+        ref = op.apply(o.OP_MDAG if dag else o.OP_M, chi)
+        assert o.rel_l2(full, ref) < 1e-13
+    ip = lambda a, b: np.vdot(a, b)  # noqa: E731
+    # <phi|Mooee chi>^* == <chi|MooeeDag phi>
+    a = ip(pe, op.apply(o.OP_MOOEE, ce)).conj()
+    b = ip(ce, op.apply(o.OP_MOOEE_DAG, pe))
+    assert abs(a - b) < 1e-12 * abs(a)
+    # <phi|Meooe chi>^* == <chi|MeooeDag phi>   (chi odd -> even)
+    a = ip(pe, op.apply(o.OP_MEOOE, co, 1)).conj()
+    b = ip(co, op.apply(o.OP_MEOOE_DAG, pe, 0))
+    assert abs(a - b) < 1e-12 * abs(a)
+    # MooeeInv Mooee == 1 ; MooeeInvDag MooeeDag == 1
+    assert o.rel_l2(op.apply(o.OP_MOOEE_INV, op.apply(o.OP_MOOEE, ce)), ce) < 1e-13
+    assert o.rel_l2(op.apply(o.OP_MOOEE_INV_DAG, op.apply(o.OP_MOOEE_DAG, ce)), ce) < 1e-13
+    # M adjointness and MpcDagMpc Hermitian, Mpc / MpcDag adjoint
+    a = ip(phi, op.apply(o.OP_M, chi)).conj()
+    b = ip(chi, op.apply(o.OP_MDAG, phi))
+    assert abs(a - b) < 1e-12 * abs(a)
+    a = ip(po, op.apply(o.OP_MPC, co)).conj()
+    b = ip(co, op.apply(o.OP_MPC_DAG, po))
+    assert abs(a - b) < 1e-12 * abs(a)
+    a = ip(po, op.apply(o.OP_MPCDAGMPC, co)).conj()
+    b = ip(co, op.apply(o.OP_MPCDAGMPC, po))
+    assert abs(a - b) < 1e-12 * abs(a)
+    assert abs(ip(co, op.apply(o.OP_MPCDAGMPC, co)).imag) < 1e-12 * abs(ip(co, co))
+
+
+def test_cayley_coefficients_config2():
+    c = o.cayley_coeffs(16, 0.01, 1.8, 1.5, 0.5)
+    assert np.allclose(c["bs"], 1.5) and np.allclose(c["cs"], 0.5)
+    assert np.allclose(c["bee"], 4.3) and np.allclose(c["cee"], -0.1)
+    # LDU of Mooee: d_{Ls-1} carries the mass correction, the rest equals bee
+    assert np.allclose(c["dee"][:-1], 4.3)
+    assert c["lee"][-1] == 0 and c["uee"][-1] == 0
+
+
+def test_free_field_wilson_propagator_momentum_space():
+    """Wilson M^{-1} at U = 1 from the oracle's CG equals the momentum-space formula
+    [-i gamma sin k + W(k)] / [sin^2 k + W(k)^2] (antiperiodic time)."""
+    dims = (4, 4, 4, 6)
+    vol = 384
+    mass = 0.3
+    U = g.unit_gauge(dims)
+    op = o.OracleOp(0, 0, dims, 1, [mass], U, g.antiperiodic_t())
+    eta = fermion(vol, 1, 51)
+    ref = wilson_free_solve(dims, mass, eta)
+    # CG on MdagM psi = Mdag eta
+    b = op.apply(o.OP_MDAG, eta)
+    psi, iters, res = op.cg(0, b, 1e-12, 2000)
+    assert res < 1e-11
+    assert o.rel_l2(psi, ref) < 1e-10
+    # and M applied in momentum space equals the oracle's M
+    assert o.rel_l2(op.apply(o.OP_M, ref), eta) < 1e-12
+
+
+def test_free_field_mobius_momentum_space():
+    dims = (4, 4, 4, 4)
+    Ls, mf = 6, 0.1
+    U = g.unit_gauge(dims)
+    op = o.OracleOp(1, 0, dims, Ls, [mf, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t())
+    x = fermion(VOL, Ls, 61)
+    ref = mobius_free_apply(dims, Ls, mf, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], x)
+    assert o.rel_l2(op.apply(o.OP_M, x), ref) < 1e-12
+    eta = fermion(VOL, Ls, 62)
+    sol = mobius_free_solve(dims, Ls, mf, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], eta)
+    s2, iters, r0, r1 = op.schur_solve(eta, 1e-12, 3000)
+    assert r1 < 1e-10
+    assert o.rel_l2(s2, sol) < 1e-9
+
+
+def test_oracle_cg_wilson_unprec_true_residual():
+    op, U = _wilson()
+    src = fermion(VOL, 1, 71)
+    psi, iters, res = op.cg(0, src, 1e-8, 1000)
+    assert 0 < iters < 1000
+    assert res < 1e-8 * 10
+    r = op.apply(o.OP_MDAGM, psi) - src
+    assert np.linalg.norm(r) / np.linalg.norm(src) < 1e-7
+
+
+def test_oracle_schur_solve_mobius():
+    op, U = _mobius(mf=0.05)
+    src = fermion(VOL, 6, 81)
+    sol, iters, r_cg, r_unprec = op.schur_solve(src, 1e-10, 3000)
+    assert r_unprec < 1e-9
+    assert o.rel_l2(op.apply(o.OP_M, sol), src) < 1e-9
+
+
+def test_oracle_reliable_update_matches_fp64():
+    """tests/Test_dwf_mixedcg_prec.cc:215: mixed and FP64 solutions agree."""
+    U = g.random_gauge(DIMS, 0.5, 91)
+    od, _ = _mobius(0, U=U, mf=0.05)
+    of, _ = _mobius(1, U=U, mf=0.05)
+    src = o.pick(DIMS, 6, fermion(VOL, 6, 92), 1)
+    x64, it64, r64 = od.cg(1, src, 1e-10, 3000)
+    xm, info, rm = o.cg_reliable(od, of, 1, src, 1e-10, 3000, delta=1e-3)
+    assert rm < 1e-10 * 2 and r64 < 1e-10 * 2
+    assert o.rel_l2(xm, x64) < 1e-8
+
+
+def test_oracle_fp32_matches_fp64_dhop():
+    U = g.random_gauge(DIMS, 0.5, 101)
+    od, _ = _mobius(0, U=U)
+    of, _ = _mobius(1, U=U)
+    x = fermion(VOL, 6, 102)
+    xo = o.pick(DIMS, 6, x, 1)
+    assert o.rel_l2(of.dhop_cb(xo, 1), od.dhop_cb(xo, 1)) < 1e-6
+    assert o.rel_l2(of.apply(o.OP_MPCDAGMPC, xo), od.apply(o.OP_MPCDAGMPC, xo)) < 1e-6
