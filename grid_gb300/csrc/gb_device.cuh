@@ -96,10 +96,14 @@ template <> struct SpinorIO<__half> {
       }
     }
   }
+  // planes straddle the chiralities: read the site and keep the requested six components
   static __device__ __forceinline__ void load_half(const void* base, const float* norms, size_t n5, size_t i,
                                                    bool upper, Spinor<float>& f) {
-    load(base, norms, n5, i, f);  // planes straddle the chiralities; read all three
-    (void)upper;
+    Spinor<float> t;
+    load(base, norms, n5, i, t);
+    const int k0 = upper ? 0 : 6;
+#pragma unroll
+    for (int k = 0; k < 6; k++) { f.re[k0 + k] = t.re[k0 + k]; f.im[k0 + k] = t.im[k0 + k]; }
   }
   static __device__ __forceinline__ void store(void* base, float* norms, size_t n5, size_t i, const Spinor<float>& f) {
     float m = 0.f;
