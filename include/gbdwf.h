@@ -109,6 +109,21 @@ int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, doubl
 int gb_field_pick_checkerboard(gb_field_t half, gb_field_t full); /* half's subset picks */
 int gb_field_set_checkerboard(gb_field_t full, gb_field_t half);
 
+/* gb_field_norm2_noalloc: the same per-rhs norm2 as gb_field_norm2, but it allocates
+ * nothing.  It has no counterpart in the reference.  It is for callers that may not call
+ * cudaMalloc/cudaFree while they work: a solve loop running under a fixed HBM budget
+ * (its memory was reserved when the request was admitted and must not grow), or a thread
+ * in a context where allocator calls are forbidden or would stall the device.  The
+ * reduction's partial sums go to one static device array of 64.1 KB that every GPU which
+ * loads the library keeps until the process exits.  Limit: at most 16 right-hand sides
+ * per field (larger fields are rejected with GB_ERR_UNSUPPORTED); any lattice size.
+ * The first call on a device looks up that array's device address (a one-time set-up
+ * per device); make that first call before any stream capture.  All calls share the
+ * array: calls whose work overlaps on the GPU (other streams or threads) race and must
+ * be serialised by the caller.  `out` (nrhs doubles) may be host or device memory; the
+ * call returns when it is written. */
+int gb_field_norm2_noalloc(gb_field_t f, double* out);
+
 /* ---- operator application (FermionOperator.h:40-192 / CayleyFermion5D) ----------
  * Full-field ops: M, Mdag, MdagM, Dhop.  Half-field ops pick DhopEO/DhopOE from the
  * input subset exactly as Grid does (Meooe: Odd in -> Even out).
