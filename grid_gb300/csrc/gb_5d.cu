@@ -253,6 +253,120 @@ __global__ void __launch_bounds__(128) mooee_inv_half_kernel(const InvParams p, 
   }
 }
 
+// FP32 site-pair layout: one thread per (complex component k, 4D site, rhs); the s column
+// of that component is Ls/2 float4 vectors (re_s, re_s+1, im_s, im_s+1), kept in
+// registers for compile-time LS (LS == 0: runtime Ls, column re-read from the output).
+template <bool DAG, int LS>
+__global__ void __launch_bounds__(256) mooee_inv_pair_kernel(const InvParams p, const LduCoef<float> c) {
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= p.nq * 12) return;
+  const int k = int(t / p.nq);
+  const size_t q = t - size_t(k) * p.nq;
+  const int Ls = LS > 0 ? LS : p.Ls;
+  const int nrhs = p.L5 / p.Ls;
+  const size_t x = q / nrhs;
+  const int rhs = int(q - x * nrhs);
+  const size_t np = p.n5 >> 1;
+  const size_t q0 = (x * p.L5 + size_t(rhs) * Ls) >> 1;  // first pair of the column
+  const float4* in = static_cast<const float4*>(p.in) + size_t(k) * np + q0;
+  float4* out = static_cast<float4*>(p.out) + size_t(k) * np + q0;
+  const bool first = DAG ? (k >= 6) : (k < 6);
+  constexpr int NB = LS > 0 ? LS : 2;
+  float cr[NB], ci[NB];
+  float pr = 0.f, pi = 0.f, ar = 0.f, ai = 0.f;
+  // forward sweep, pairs of s
+#pragma unroll
+  for (int m = 0; m < (LS > 0 ? LS / 2 : 1); m++) {
+    if (LS == 0) break;
+    const float4 v = __ldg(in + m);
+    float re[2] = {v.x, v.y}, im[2] = {v.z, v.w};
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+      const int s = 2 * m + l;
+      float r = re[l], i = im[l];
+      if (s < Ls - 1) {
+        if (first) { if (s > 0) { r = fmaf(-c.lee[s - 1], pr, r); i = fmaf(-c.lee[s - 1], pi, i); } }
+        else { ar = fmaf(c.leem[s], r, ar); ai = fmaf(c.leem[s], i, ai); }
+        pr = r; pi = i;
+      } else {
+        if (first) { r = fmaf(-c.lee[Ls - 2], pr, r); i = fmaf(-c.lee[Ls - 2], pi, i); }
+        else { r -= ar; i -= ai; }
+        r *= c.dinv[Ls - 1]; i *= c.dinv[Ls - 1];
+      }
+      cr[s < NB ? s : 0] = r; ci[s < NB ? s : 0] = i;
+    }
+  }
+  if (LS == 0) {  // runtime Ls: same sweep through the output
+    for (int m = 0; m < Ls / 2; m++) {
+      const float4 v = __ldg(in + m);
+      float re[2] = {v.x, v.y}, im[2] = {v.z, v.w};
+      float o[4];
+      for (int l = 0; l < 2; l++) {
+        const int s = 2 * m + l;
+        float r = re[l], i = im[l];
+        if (s < Ls - 1) {
+          if (first) { if (s > 0) { r = fmaf(-c.lee[s - 1], pr, r); i = fmaf(-c.lee[s - 1], pi, i); } }
+          else { ar = fmaf(c.leem[s], r, ar); ai = fmaf(c.leem[s], i, ai); }
+          pr = r; pi = i;
+        } else {
+          if (first) { r = fmaf(-c.lee[Ls - 2], pr, r); i = fmaf(-c.lee[Ls - 2], pi, i); }
+          else { r -= ar; i -= ai; }
+          r *= c.dinv[Ls - 1]; i *= c.dinv[Ls - 1];
+        }
+        o[l] = r; o[2 + l] = i;
+      }
+      out[m] = make_float4(o[0], o[1], o[2], o[3]);
+    }
+  }
+  // backward sweep: chi_s = chi_s / d_s - (uee[s] P_second chi_{s+1} | ueem[s] P_first chi_{Ls-1})
+  float lr, li;
+  if (LS > 0) { lr = cr[NB - 1]; li = ci[NB - 1]; }
+  else { const float4 v = out[Ls / 2 - 1]; lr = v.y; li = v.w; }
+  float nr = lr, ni = li;
+  if (LS > 0) {
+#pragma unroll
+    for (int s = (LS > 0 ? LS : 2) - 2; s >= 0; s--) {
+      float r = cr[s] * c.dinv[s], i = ci[s] * c.dinv[s];
+      if (!first) { r = fmaf(-c.uee[s], nr, r); i = fmaf(-c.uee[s], ni, i); }
+      else { r = fmaf(-c.ueem[s], lr, r); i = fmaf(-c.ueem[s], li, i); }
+      cr[s] = r; ci[s] = i;
+      nr = r; ni = i;
+    }
+#pragma unroll
+    for (int m = 0; m < (LS > 0 ? LS / 2 : 1); m++) out[m] = make_float4(cr[2 * m], cr[2 * m + 1], ci[2 * m], ci[2 * m + 1]);
+  } else {
+    for (int m = Ls / 2 - 1; m >= 0; m--) {
+      float4 v = out[m];
+      float re[2] = {v.x, v.y}, im[2] = {v.z, v.w};
+      for (int l = 1; l >= 0; l--) {
+        const int s = 2 * m + l;
+        if (s == Ls - 1) continue;
+        float r = re[l] * c.dinv[s], i = im[l] * c.dinv[s];
+        if (!first) { r = fmaf(-c.uee[s], nr, r); i = fmaf(-c.uee[s], ni, i); }
+        else { r = fmaf(-c.ueem[s], lr, r); i = fmaf(-c.ueem[s], li, i); }
+        re[l] = r; im[l] = i;
+        nr = r; ni = i;
+      }
+      out[m] = make_float4(re[0], re[1], im[0], im[1]);
+    }
+  }
+}
+
+template <bool DAG> static int launch_inv_pair(Op* op, const InvParams& p, const LduCoef<float>& c) {
+  const size_t n = p.nq * 12;
+  const unsigned blocks = unsigned((n + 255) / 256);
+  switch (op->Ls) {
+#define GB_INVP_CASE(L) \
+  case L: mooee_inv_pair_kernel<DAG, L><<<blocks, 256, 0, op->stream>>>(p, c); break;
+    GB_INVP_CASE(2) GB_INVP_CASE(4) GB_INVP_CASE(6) GB_INVP_CASE(8) GB_INVP_CASE(10) GB_INVP_CASE(12)
+    GB_INVP_CASE(14) GB_INVP_CASE(16) GB_INVP_CASE(20) GB_INVP_CASE(24) GB_INVP_CASE(32)
+#undef GB_INVP_CASE
+    default: mooee_inv_pair_kernel<DAG, 0><<<blocks, 256, 0, op->stream>>>(p, c); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 template <class V, bool DAG>
 static int launch_inv_v(Op* op, const InvParams& p, const LduCoef<typename VecOps<V>::R>& c) {
   const size_t n = p.nq * p.nplanes;
@@ -304,8 +418,8 @@ int launch_mooee_inv(Op* op, HalfView in, HalfView out, int dag, size_t n4) {
   }
   if (in.prec == GB_F32) {
     LduCoef<float> c; fill_ldu(op, dag, c);
-    p.nplanes = 6;
-    return dag ? launch_inv_v<float4, true>(op, p, c) : launch_inv_v<float4, false>(op, p, c);
+    p.nplanes = 12;
+    return dag ? launch_inv_pair<true>(op, p, c) : launch_inv_pair<false>(op, p, c);
   }
   LduCoef<float> c; fill_ldu(op, dag, c);
   p.nplanes = 1;

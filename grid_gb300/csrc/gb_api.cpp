@@ -67,6 +67,7 @@ int field_alloc(Op* op, int subset, int prec, Field** out) {
     set_error("cudaMalloc of %zu bytes failed: %s", halves * f->n5 * spinor_bytes(prec), cudaGetErrorString(e));
     return GB_ERR_OOM;
   }
+  cudaMemset(f->data, 0, halves * f->half_bytes());
   if (prec == GB_F16) {
     e = cudaMalloc(&f->norms, halves * f->n5 * sizeof(float));
     if (e != cudaSuccess) {
@@ -93,22 +94,17 @@ void field_free(Field* f) {
 // field is relabelled to the requested checkerboard
 int ws_get(Op* op, int subset, int prec, int slot, Field** out) {
   const bool want_full = subset == GB_FULL;
-  int seen = 0;
   for (Field* f : op->ws) {
-    if (f->full() == want_full && f->prec == prec) {
-      if (seen == slot) {
-        if (!want_full) f->subset = subset;
-        *out = f;
-        return GB_OK;
-      }
-      seen++;
+    if (f->full() == want_full && f->prec == prec && f->ws_slot == slot) {
+      if (!want_full) f->subset = subset;
+      *out = f;
+      return GB_OK;
     }
   }
   Field* f = nullptr;
-  for (int k = seen; k <= slot; k++) {
-    GB_TRY(field_alloc(op, subset, prec, &f));
-    op->ws.push_back(f);
-  }
+  GB_TRY(field_alloc(op, subset, prec, &f));
+  f->ws_slot = slot;
+  op->ws.push_back(f);
   *out = f;
   return GB_OK;
 }
@@ -432,6 +428,7 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
   if (precision < GB_F64 || precision > GB_F16) { set_error("bad precision %d", precision); return GB_ERR_BAD_ARG; }
   if (nrhs < 1 || Ls < 1) { set_error("nrhs and Ls must be >= 1"); return GB_ERR_BAD_ARG; }
   if (kind == 1 && (Ls < 2 || Ls > kMaxLs)) { set_error("Ls = %d outside [2, %d]", Ls, kMaxLs); return GB_ERR_BAD_ARG; }
+  if (kind == 1 && (Ls & 1)) { set_error("Ls = %d: the fifth dimension must be even", Ls); return GB_ERR_UNSUPPORTED; }
   if (Ls * nrhs > kMaxL5) { set_error("Ls*nrhs = %d exceeds %d", Ls * nrhs, kMaxL5); return GB_ERR_UNSUPPORTED; }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_error("no CUDA device"); return GB_ERR_NO_DEVICE; }
@@ -443,8 +440,10 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
   op->half4 = op->vol4 / 2;
   if (op->half4 * 8 > int64_t(0x7fffffff)) { delete op; set_error("lattice too large for 32-bit neighbour tables"); return GB_ERR_UNSUPPORTED; }
   op->Ls = kind == 1 ? Ls : 1;
-  op->nrhs = nrhs;
-  op->L5 = op->Ls * nrhs;
+  op->nrhs_user = nrhs;
+  op->nrhs = ((op->Ls * nrhs) & 1) ? nrhs + 1 : nrhs;  // keep L5 even (site pairs)
+  op->L5 = op->Ls * op->nrhs;
+  nrhs = op->nrhs;
   op->prec = precision;
   op->mass = mass;
   op->M5 = M5;
@@ -509,7 +508,7 @@ int ensure_stage(Op* op, size_t bytes) {
 size_t field_host_doubles(const Field* f) {
   const Op* op = f->op;
   const size_t n4 = f->full() ? size_t(op->vol4) : size_t(op->half4);
-  return n4 * op->L5 * 24;
+  return n4 * op->Ls * op->nrhs_user * 24;
 }
 
 int field_import_dev(Field* f, const double* dev) {
@@ -602,7 +601,7 @@ int gb_op_import_gauge_device(gb_op_t op, const double* U_device) {
 int gb_op_info(gb_op_t op, int* Ls, int* nrhs, int64_t* half_sites4, int* precision) {
   if (!op) { set_error("null operator"); return GB_ERR_BAD_ARG; }
   if (Ls) *Ls = op->Ls;
-  if (nrhs) *nrhs = op->nrhs;
+  if (nrhs) *nrhs = op->nrhs_user;
   if (half_sites4) *half_sites4 = op->half4;
   if (precision) *precision = op->prec;
   return GB_OK;
@@ -690,13 +689,19 @@ int gb_field_copy(gb_field_t dst, gb_field_t src) {
 }
 int gb_field_norm2(gb_field_t f, double* out) {
   if (!f || !out) return GB_ERR_BAD_ARG;
-  return field_norm2(f, out);
+  std::vector<double> v(f->op->nrhs);
+  GB_TRY(field_norm2(f, v.data()));
+  std::memcpy(out, v.data(), f->op->nrhs_user * sizeof(double));
+  return GB_OK;
 }
 int gb_field_inner(gb_field_t a, gb_field_t b, double* out) {
   GB_TRY(check_conf(a, b));
   if (!out) return GB_ERR_BAD_ARG;
   if (a->subset != b->subset) { set_error("innerProduct: checkerboard mismatch"); return GB_ERR_BAD_PARITY; }
-  return field_inner(a, b, out);
+  std::vector<double> v(2 * a->op->nrhs);
+  GB_TRY(field_inner(a, b, v.data()));
+  std::memcpy(out, v.data(), 2 * a->op->nrhs_user * sizeof(double));
+  return GB_OK;
 }
 int gb_field_axpby(gb_field_t z, double a, double b, gb_field_t x, gb_field_t y) {
   GB_TRY(check_conf(z, x));
@@ -720,7 +725,10 @@ int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, doubl
     GB_TRY(launch_axpy_norm_partial(op, half_view(z, h), a, half_view(x, h), half_view(y, h), z->n5,
                                     op->d_partial + size_t(h) * g * op->nrhs));
   GB_TRY(launch_reduce_final(op, op->d_partial, g * halves, 1, op->d_result));
-  return fetch(op, op->d_result, norm_out, op->nrhs);
+  std::vector<double> v(op->nrhs);
+  GB_TRY(fetch(op, op->d_result, v.data(), op->nrhs));
+  std::memcpy(norm_out, v.data(), op->nrhs_user * sizeof(double));
+  return GB_OK;
 }
 int gb_field_pick_checkerboard(gb_field_t half, gb_field_t full) {
   GB_TRY(check_conf(half, full));

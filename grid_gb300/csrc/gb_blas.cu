@@ -131,8 +131,10 @@ struct CGFields {
 };
 
 // kind 0: |x|^2 ; kind 1: <x|y> ; kind 2: z = a x + y (a from host), |z|^2 ;
-// kind 3: r = r - a[rhs] mmp, psi += a[rhs] p (a from the device CG scalars), |r|^2
-template <class T, int KIND>
+// kind 3: r = r - a[rhs] mmp, psi += a[rhs] p (a from the device CG scalars), |r|^2;
+// TS is the storage of psi (FP32 when r, p, mmp are FP16: an FP16 solution accumulator
+// would round the small increments a*p away)
+template <class T, int KIND, class TS = T>
 __global__ void __launch_bounds__(256) reduce_kernel(const RedShape sh, const void* x, const float* xn, const void* y,
                                                      const float* yn, void* z, float* zn, double a,
                                                      const CGScalars* cg, const CGFields cf, size_t n5,
@@ -182,15 +184,16 @@ __global__ void __launch_bounds__(256) reduce_kernel(const RedShape sh, const vo
       SpinorIO<T>::store(z, zn, n5, i, fy);
       v[0] += double(s);
       if (KIND == 3) {
-        Spinor<R> fp, fs;
+        Spinor<R> fp;
+        Spinor<typename Arith<TS>::type> fs;
         SpinorIO<T>::load(cf.p, cf.pn, n5, i, fp);
-        SpinorIO<T>::load(cf.psi, cf.psin, n5, i, fs);
+        SpinorIO<TS>::load(cf.psi, cf.psin, n5, i, fs);
 #pragma unroll
         for (int k = 0; k < 12; k++) {
           fs.re[k] = fma(-ar, fp.re[k], fs.re[k]);
           fs.im[k] = fma(-ar, fp.im[k], fs.im[k]);
         }
-        SpinorIO<T>::store(cf.psi, cf.psin, n5, i, fs);
+        SpinorIO<TS>::store(cf.psi, cf.psin, n5, i, fs);
       }
     }
   }
@@ -214,7 +217,7 @@ int red_grid(Op* op, size_t n5, int* blocks, int* threads) {
   return GB_OK;
 }
 
-template <class T, int KIND>
+template <class T, int KIND, class TS = T>
 static int reduce_t(Op* op, HalfView x, HalfView y, HalfView z, double a, const CGFields& cf, size_t n5,
                     double* partial) {
   int g, B;
@@ -222,7 +225,7 @@ static int reduce_t(Op* op, HalfView x, HalfView y, HalfView z, double a, const 
   RedShape sh{op->L5, op->Ls, op->nrhs};
   const int NV = KIND == 1 ? 2 : 1;
   size_t smem = size_t(NV) * (op->nrhs == 1 ? 32 : B) * sizeof(double);
-  reduce_kernel<T, KIND><<<g, B, smem, op->stream>>>(sh, x.data, x.norms, y.data, y.norms, z.data, z.norms, a, op->d_cg,
+  reduce_kernel<T, KIND, TS><<<g, B, smem, op->stream>>>(sh, x.data, x.norms, y.data, y.norms, z.data, z.norms, a, op->d_cg,
                                                     cf, n5, partial);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
@@ -252,9 +255,12 @@ int launch_axpy_norm_partial(Op* op, HalfView z, double a, HalfView x, HalfView 
   return reduce_p<2>(op, x, y, z, a, n5, partial);
 }
 int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, HalfView psi, HalfView p, size_t n5, double* partial) {
-  if (r.prec != mmp.prec || psi.prec != r.prec || p.prec != r.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
+  if (r.prec != mmp.prec || p.prec != r.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
   CGFields cf{psi.data, psi.norms, p.data, p.norms};
-  return reduce_p<3>(op, mmp, r, r, 0.0, n5, partial, cf);
+  if (psi.prec == r.prec) return reduce_p<3>(op, mmp, r, r, 0.0, n5, partial, cf);
+  if (r.prec == GB_F16 && psi.prec == GB_F32) return reduce_t<__half, 3, float>(op, mmp, r, r, 0.0, cf, n5, partial);
+  set_error("CG update: solution precision %d with residual precision %d", psi.prec, r.prec);
+  return GB_ERR_BAD_ARG;
 }
 
 // partial: [nparts][nrhs][nv] -> out[nrhs][nv]; one CTA per rhs, fixed summation order
@@ -431,7 +437,7 @@ int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5) {
 struct GeoParams {
   int L[4];
   int64_t half4, vol4;
-  int L5, Ls, nrhs;
+  int L5, Ls, nrhs, nrhs_user;
 };
 
 __device__ __forceinline__ int64_t cb_to_site(int64_t xcb, int parity, const GeoParams& g) {
@@ -456,10 +462,18 @@ __global__ void __launch_bounds__(256) layout_kernel(const GeoParams g, double* 
   const int64_t xcb = int64_t(i / g.L5);
   const int s5 = int(i - size_t(xcb) * g.L5);
   const int rhs = s5 / g.Ls, s = s5 - rhs * g.Ls;
+  Spinor<R> f;
+  if (rhs >= g.nrhs_user) {  // the padding right-hand side: zeros, absent from the host array
+    if (IMPORT) {
+#pragma unroll
+      for (int k = 0; k < 12; k++) { f.re[k] = R(0); f.im[k] = R(0); }
+      SpinorIO<T>::store(dev, devn, n5, i, f);
+    }
+    return;
+  }
   const int64_t c4 = canon_full ? cb_to_site(xcb, parity, g) : xcb;
   const int64_t n4c = canon_full ? g.vol4 : g.half4;
   double2* c = reinterpret_cast<double2*>(canon) + ((size_t(rhs) * n4c + c4) * g.Ls + s) * 12;
-  Spinor<R> f;
   if (IMPORT) {
 #pragma unroll
     for (int k = 0; k < 12; k++) {
@@ -482,6 +496,7 @@ static GeoParams geo(const Op* op) {
   g.L5 = op->L5;
   g.Ls = op->Ls;
   g.nrhs = op->nrhs;
+  g.nrhs_user = op->nrhs_user;
   return g;
 }
 

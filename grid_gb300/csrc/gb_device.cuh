@@ -17,8 +17,8 @@ template <class R> struct Spinor {
 };
 
 // Loads one 5D site's spinor from the plane layout.  T selects the storage:
-//   double -> 12 double2 planes; float -> 6 float4 planes;
-//   __half -> 3 planes of 8 halves scaled by the per-site norm.
+//   double -> 12 double2 planes, one site per vector; float / __half -> the site-pair
+//   layout described below.
 template <class R> struct SpinorIO;
 
 template <> struct SpinorIO<double> {
@@ -48,78 +48,180 @@ template <> struct SpinorIO<double> {
   }
 };
 
+// FP32 and FP16 use the site-pair layout: a 16-byte vector holds data of the two 5D
+// sites (i, i+1), i even, so a thread can compute both with packed f32x2 arithmetic.
+//   FP32: 12 planes (complex component k) of n5/2 float4 = (re_i, re_i+1, im_i, im_i+1)
+//   FP16: 6 planes (components 2q, 2q+1) of n5/2 16-byte vectors of 8 halves
+//         (re_2q@i, re_2q@i+1, im_2q@i, im_2q@i+1, re_2q+1@i, re_2q+1@i+1, im_2q+1@i, im_2q+1@i+1),
+//         each site's values divided by its norm (max |re|,|im| of the site), one float per site.
+// SpinorIO<float/__half> read or write ONE site of that layout (scalar accesses; used by
+// the kernels that are not on the hot path); PairIO below moves whole vectors.
 template <> struct SpinorIO<float> {
   static __device__ __forceinline__ void load(const void* base, const float*, size_t n5, size_t i, Spinor<float>& f) {
-    const float4* p = static_cast<const float4*>(base);
+    const float* p = static_cast<const float*>(base);
+    const size_t np = n5 >> 1, q = i >> 1;
+    const int l = int(i & 1);
 #pragma unroll
-    for (int g = 0; g < 6; g++) {
-      float4 v = __ldg(p + size_t(g) * n5 + i);
-      f.re[2 * g] = v.x; f.im[2 * g] = v.y; f.re[2 * g + 1] = v.z; f.im[2 * g + 1] = v.w;
+    for (int k = 0; k < 12; k++) {
+      const float* v = p + (size_t(k) * np + q) * 4;
+      f.re[k] = __ldg(v + l);
+      f.im[k] = __ldg(v + 2 + l);
     }
   }
   static __device__ __forceinline__ void load_half(const void* base, const float*, size_t n5, size_t i, bool upper,
                                                    Spinor<float>& f) {
-    const float4* p = static_cast<const float4*>(base);
-    const int g0 = upper ? 0 : 3;
+    const float* p = static_cast<const float*>(base);
+    const size_t np = n5 >> 1, q = i >> 1;
+    const int l = int(i & 1), k0 = upper ? 0 : 6;
 #pragma unroll
-    for (int g = 0; g < 3; g++) {
-      float4 v = __ldg(p + size_t(g0 + g) * n5 + i);
-      const int k = 2 * (g0 + g);
-      f.re[k] = v.x; f.im[k] = v.y; f.re[k + 1] = v.z; f.im[k + 1] = v.w;
+    for (int k = k0; k < k0 + 6; k++) {
+      const float* v = p + (size_t(k) * np + q) * 4;
+      f.re[k] = __ldg(v + l);
+      f.im[k] = __ldg(v + 2 + l);
     }
   }
   static __device__ __forceinline__ void store(void* base, float*, size_t n5, size_t i, const Spinor<float>& f) {
-    float4* p = static_cast<float4*>(base);
+    float* p = static_cast<float*>(base);
+    const size_t np = n5 >> 1, q = i >> 1;
+    const int l = int(i & 1);
 #pragma unroll
-    for (int g = 0; g < 6; g++)
-      p[size_t(g) * n5 + i] = make_float4(f.re[2 * g], f.im[2 * g], f.re[2 * g + 1], f.im[2 * g + 1]);
+    for (int k = 0; k < 12; k++) {
+      float* v = p + (size_t(k) * np + q) * 4;
+      v[l] = f.re[k];
+      v[2 + l] = f.im[k];
+    }
   }
 };
-
-// FP16 storage, FP32 arithmetic: plane q (0..2) holds complex components 4q..4q+3 as
-// 8 halves; every component is stored divided by the site's max |re|,|im| (the norm).
-struct Half8 { __half2 h[4]; };
 
 template <> struct SpinorIO<__half> {
   static __device__ __forceinline__ void load(const void* base, const float* norms, size_t n5, size_t i,
                                               Spinor<float>& f) {
-    const uint4* p = static_cast<const uint4*>(base);
+    const __half* p = static_cast<const __half*>(base);
+    const size_t np = n5 >> 1, q = i >> 1;
+    const int l = int(i & 1);
     const float nrm = __ldg(norms + i);
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      uint4 v = __ldg(p + size_t(q) * n5 + i);
-      const __half2* h = reinterpret_cast<const __half2*>(&v);
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        float2 z = __half22float2(h[c]);
-        f.re[4 * q + c] = z.x * nrm; f.im[4 * q + c] = z.y * nrm;
-      }
+    for (int k = 0; k < 12; k++) {
+      const __half* v = p + (size_t(k >> 1) * np + q) * 8 + (k & 1) * 4;
+      f.re[k] = __half2float(v[l]) * nrm;
+      f.im[k] = __half2float(v[2 + l]) * nrm;
     }
   }
-  // planes straddle the chiralities: read the site and keep the requested six components
   static __device__ __forceinline__ void load_half(const void* base, const float* norms, size_t n5, size_t i,
                                                    bool upper, Spinor<float>& f) {
-    Spinor<float> t;
-    load(base, norms, n5, i, t);
-    const int k0 = upper ? 0 : 6;
+    const __half* p = static_cast<const __half*>(base);
+    const size_t np = n5 >> 1, q = i >> 1;
+    const int l = int(i & 1), k0 = upper ? 0 : 6;
+    const float nrm = __ldg(norms + i);
 #pragma unroll
-    for (int k = 0; k < 6; k++) { f.re[k0 + k] = t.re[k0 + k]; f.im[k0 + k] = t.im[k0 + k]; }
+    for (int k = k0; k < k0 + 6; k++) {
+      const __half* v = p + (size_t(k >> 1) * np + q) * 8 + (k & 1) * 4;
+      f.re[k] = __half2float(v[l]) * nrm;
+      f.im[k] = __half2float(v[2 + l]) * nrm;
+    }
   }
   static __device__ __forceinline__ void store(void* base, float* norms, size_t n5, size_t i, const Spinor<float>& f) {
     float m = 0.f;
 #pragma unroll
     for (int k = 0; k < 12; k++) m = fmaxf(m, fmaxf(fabsf(f.re[k]), fabsf(f.im[k])));
     const float inv = m > 0.f ? 1.0f / m : 0.f;
-    uint4* p = static_cast<uint4*>(base);
+    __half* p = static_cast<__half*>(base);
+    const size_t np = n5 >> 1, q = i >> 1;
+    const int l = int(i & 1);
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      uint4 v;
-      __half2* h = reinterpret_cast<__half2*>(&v);
-#pragma unroll
-      for (int c = 0; c < 4; c++) h[c] = __floats2half2_rn(f.re[4 * q + c] * inv, f.im[4 * q + c] * inv);
-      p[size_t(q) * n5 + i] = v;
+    for (int k = 0; k < 12; k++) {
+      __half* v = p + (size_t(k >> 1) * np + q) * 8 + (k & 1) * 4;
+      v[l] = __float2half_rn(f.re[k] * inv);
+      v[2 + l] = __float2half_rn(f.im[k] * inv);
     }
     norms[i] = m;
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+// Site pairs: component k of sites (i, i+1) as packed float2 (lane 0 = site i).
+// ---------------------------------------------------------------------------------------
+struct Pair12 {
+  float2 re[12], im[12];
+};
+
+template <class T> struct PairIO;
+template <> struct PairIO<float> {
+  // q = pair index (= i/2), np = pairs per plane
+  static __device__ __forceinline__ void load(const void* base, const float2*, size_t np, size_t q, Pair12& f) {
+    const float4* p = static_cast<const float4*>(base) + q;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const float4 v = __ldg(p + size_t(k) * np);
+      f.re[k] = make_float2(v.x, v.y);
+      f.im[k] = make_float2(v.z, v.w);
+    }
+  }
+  // components [k0, k0+6): one chirality
+  static __device__ __forceinline__ void load6(const void* base, const float2*, size_t np, size_t q, int k0, Pair12& f) {
+    const float4* p = static_cast<const float4*>(base) + q;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const float4 v = __ldg(p + size_t(k0 + k) * np);
+      f.re[k0 + k] = make_float2(v.x, v.y);
+      f.im[k0 + k] = make_float2(v.z, v.w);
+    }
+  }
+  static __device__ __forceinline__ void store(void* base, float2*, size_t np, size_t q, const Pair12& f) {
+    float4* p = static_cast<float4*>(base) + q;
+#pragma unroll
+    for (int k = 0; k < 12; k++) p[size_t(k) * np] = make_float4(f.re[k].x, f.re[k].y, f.im[k].x, f.im[k].y);
+  }
+};
+
+template <> struct PairIO<__half> {
+  static __device__ __forceinline__ void load(const void* base, const float2* norms, size_t np, size_t q, Pair12& f) {
+    const uint4* p = static_cast<const uint4*>(base) + q;
+    const float2 n = __ldg(norms + q);
+#pragma unroll
+    for (int g = 0; g < 6; g++) {
+      const uint4 v = __ldg(p + size_t(g) * np);
+      const __half2* h = reinterpret_cast<const __half2*>(&v);
+      f.re[2 * g] = __fmul2_rn(__half22float2(h[0]), n);
+      f.im[2 * g] = __fmul2_rn(__half22float2(h[1]), n);
+      f.re[2 * g + 1] = __fmul2_rn(__half22float2(h[2]), n);
+      f.im[2 * g + 1] = __fmul2_rn(__half22float2(h[3]), n);
+    }
+  }
+  static __device__ __forceinline__ void load6(const void* base, const float2* norms, size_t np, size_t q, int k0,
+                                               Pair12& f) {
+    const uint4* p = static_cast<const uint4*>(base) + q;
+    const float2 n = __ldg(norms + q);
+#pragma unroll
+    for (int g = k0 / 2; g < k0 / 2 + 3; g++) {
+      const uint4 v = __ldg(p + size_t(g) * np);
+      const __half2* h = reinterpret_cast<const __half2*>(&v);
+      f.re[2 * g] = __fmul2_rn(__half22float2(h[0]), n);
+      f.im[2 * g] = __fmul2_rn(__half22float2(h[1]), n);
+      f.re[2 * g + 1] = __fmul2_rn(__half22float2(h[2]), n);
+      f.im[2 * g + 1] = __fmul2_rn(__half22float2(h[3]), n);
+    }
+  }
+  static __device__ __forceinline__ void store(void* base, float2* norms, size_t np, size_t q, const Pair12& f) {
+    float m0 = 0.f, m1 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      m0 = fmaxf(m0, fmaxf(fabsf(f.re[k].x), fabsf(f.im[k].x)));
+      m1 = fmaxf(m1, fmaxf(fabsf(f.re[k].y), fabsf(f.im[k].y)));
+    }
+    const float2 inv = make_float2(m0 > 0.f ? 1.0f / m0 : 0.f, m1 > 0.f ? 1.0f / m1 : 0.f);
+    uint4* p = static_cast<uint4*>(base) + q;
+#pragma unroll
+    for (int g = 0; g < 6; g++) {
+      uint4 v;
+      __half2* h = reinterpret_cast<__half2*>(&v);
+      h[0] = __float22half2_rn(__fmul2_rn(f.re[2 * g], inv));
+      h[1] = __float22half2_rn(__fmul2_rn(f.im[2 * g], inv));
+      h[2] = __float22half2_rn(__fmul2_rn(f.re[2 * g + 1], inv));
+      h[3] = __float22half2_rn(__fmul2_rn(f.im[2 * g + 1], inv));
+      p[size_t(g) * np] = v;
+    }
+    norms[q] = make_float2(m0, m1);
   }
 };
 

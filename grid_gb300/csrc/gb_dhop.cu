@@ -203,6 +203,211 @@ template <class T, bool DAG> static int launch_dhop_t(Op* op, const DhopParams& 
   return GB_OK;
 }
 
+// =======================================================================================
+// FP32 / FP16 storage: two 5D sites (s5, s5+1) per thread in packed f32x2 arithmetic.
+// Every operation acts identically on both lanes, so the site-pair layout needs no lane
+// shuffles; the links are expanded in shared memory to (re, re, im, im) so one 16-byte
+// shared load gives both broadcast pairs.
+// =======================================================================================
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+// a + S*b
+template <int S> __device__ __forceinline__ float2 adds2(float2 a, float2 b) { return S > 0 ? add2(a, b) : sub2(a, b); }
+
+template <int MU, int S>
+__device__ __forceinline__ void project2(const Pair12& f, float2 (&hr)[6], float2 (&hi)[6]) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float2 f0r = f.re[c], f0i = f.im[c], f1r = f.re[3 + c], f1i = f.im[3 + c];
+    const float2 f2r = f.re[6 + c], f2i = f.im[6 + c], f3r = f.re[9 + c], f3i = f.im[9 + c];
+    if (MU == 0) {  // h0 = f0 + S i f3, h1 = f1 + S i f2
+      hr[c] = adds2<-S>(f0r, f3i); hi[c] = adds2<S>(f0i, f3r);
+      hr[3 + c] = adds2<-S>(f1r, f2i); hi[3 + c] = adds2<S>(f1i, f2r);
+    } else if (MU == 1) {  // h0 = f0 - S f3, h1 = f1 + S f2
+      hr[c] = adds2<-S>(f0r, f3r); hi[c] = adds2<-S>(f0i, f3i);
+      hr[3 + c] = adds2<S>(f1r, f2r); hi[3 + c] = adds2<S>(f1i, f2i);
+    } else if (MU == 2) {  // h0 = f0 + S i f2, h1 = f1 - S i f3
+      hr[c] = adds2<-S>(f0r, f2i); hi[c] = adds2<S>(f0i, f2r);
+      hr[3 + c] = adds2<S>(f1r, f3i); hi[3 + c] = adds2<-S>(f1i, f3r);
+    } else {  // h0 = f0 + S f2, h1 = f1 + S f3
+      hr[c] = adds2<S>(f0r, f2r); hi[c] = adds2<S>(f0i, f2i);
+      hr[3 + c] = adds2<S>(f1r, f3r); hi[3 + c] = adds2<S>(f1i, f3i);
+    }
+  }
+}
+
+// acc (+)= reconstruction of u; FIRST assigns
+template <int MU, int S, bool FIRST>
+__device__ __forceinline__ void reconstruct2(Pair12& r, const float2 (&ur)[6], const float2 (&ui)[6]) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float2 u0r = ur[c], u0i = ui[c], u1r = ur[3 + c], u1i = ui[3 + c];
+    if (FIRST) {
+      r.re[c] = u0r; r.im[c] = u0i; r.re[3 + c] = u1r; r.im[3 + c] = u1i;
+      const float2 zero = f2(0.f);
+      if (MU == 0) {  // r2 = -S i u1, r3 = -S i u0
+        r.re[6 + c] = adds2<S>(zero, u1i); r.im[6 + c] = adds2<-S>(zero, u1r);
+        r.re[9 + c] = adds2<S>(zero, u0i); r.im[9 + c] = adds2<-S>(zero, u0r);
+      } else if (MU == 1) {  // r2 = S u1, r3 = -S u0
+        r.re[6 + c] = adds2<S>(zero, u1r); r.im[6 + c] = adds2<S>(zero, u1i);
+        r.re[9 + c] = adds2<-S>(zero, u0r); r.im[9 + c] = adds2<-S>(zero, u0i);
+      } else if (MU == 2) {  // r2 = -S i u0, r3 = S i u1
+        r.re[6 + c] = adds2<S>(zero, u0i); r.im[6 + c] = adds2<-S>(zero, u0r);
+        r.re[9 + c] = adds2<-S>(zero, u1i); r.im[9 + c] = adds2<S>(zero, u1r);
+      } else {  // r2 = S u0, r3 = S u1
+        r.re[6 + c] = adds2<S>(zero, u0r); r.im[6 + c] = adds2<S>(zero, u0i);
+        r.re[9 + c] = adds2<S>(zero, u1r); r.im[9 + c] = adds2<S>(zero, u1i);
+      }
+    } else {
+      r.re[c] = add2(r.re[c], u0r); r.im[c] = add2(r.im[c], u0i);
+      r.re[3 + c] = add2(r.re[3 + c], u1r); r.im[3 + c] = add2(r.im[3 + c], u1i);
+      if (MU == 0) {
+        r.re[6 + c] = adds2<S>(r.re[6 + c], u1i); r.im[6 + c] = adds2<-S>(r.im[6 + c], u1r);
+        r.re[9 + c] = adds2<S>(r.re[9 + c], u0i); r.im[9 + c] = adds2<-S>(r.im[9 + c], u0r);
+      } else if (MU == 1) {
+        r.re[6 + c] = adds2<S>(r.re[6 + c], u1r); r.im[6 + c] = adds2<S>(r.im[6 + c], u1i);
+        r.re[9 + c] = adds2<-S>(r.re[9 + c], u0r); r.im[9 + c] = adds2<-S>(r.im[9 + c], u0i);
+      } else if (MU == 2) {
+        r.re[6 + c] = adds2<S>(r.re[6 + c], u0i); r.im[6 + c] = adds2<-S>(r.im[6 + c], u0r);
+        r.re[9 + c] = adds2<-S>(r.re[9 + c], u1i); r.im[9 + c] = adds2<S>(r.im[9 + c], u1r);
+      } else {
+        r.re[6 + c] = adds2<S>(r.re[6 + c], u0r); r.im[6 + c] = adds2<S>(r.im[6 + c], u0i);
+        r.re[9 + c] = adds2<S>(r.re[9 + c], u1r); r.im[9 + c] = adds2<S>(r.im[9 + c], u1i);
+      }
+    }
+  }
+}
+
+// u = U h on both spins; Ux: 9 float4 (re, re, im, im) in shared memory
+__device__ __forceinline__ void su3_mul2(const float4* __restrict__ Ux, const float2 (&hr)[6], const float2 (&hi)[6],
+                                         float2 (&ur)[6], float2 (&ui)[6]) {
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float4 w0 = Ux[a * 3 + 0], w1 = Ux[a * 3 + 1], w2 = Ux[a * 3 + 2];
+    const float2 r0 = make_float2(w0.x, w0.y), i0 = make_float2(w0.z, w0.w);
+    const float2 r1 = make_float2(w1.x, w1.y), i1 = make_float2(w1.z, w1.w);
+    const float2 r2 = make_float2(w2.x, w2.y), i2 = make_float2(w2.z, w2.w);
+#pragma unroll
+    for (int sp = 0; sp < 2; sp++) {
+      const int o = sp * 3;
+      float2 p = __fmul2_rn(r0, hr[o]);
+      float2 q = __fmul2_rn(i0, hi[o]);
+      float2 xi = __fmul2_rn(r0, hi[o]);
+      xi = __ffma2_rn(i0, hr[o], xi);
+      p = __ffma2_rn(r1, hr[o + 1], p);
+      q = __ffma2_rn(i1, hi[o + 1], q);
+      xi = __ffma2_rn(r1, hi[o + 1], xi);
+      xi = __ffma2_rn(i1, hr[o + 1], xi);
+      p = __ffma2_rn(r2, hr[o + 2], p);
+      q = __ffma2_rn(i2, hi[o + 2], q);
+      xi = __ffma2_rn(r2, hi[o + 2], xi);
+      xi = __ffma2_rn(i2, hr[o + 2], xi);
+      ur[o + a] = sub2(p, q);
+      ui[o + a] = xi;
+    }
+  }
+}
+
+template <class T, bool DAG, int LEG>
+__device__ __forceinline__ void dhop_pair_leg(const DhopParams& p, const int (&nb)[8], int sp, size_t np, int hl,
+                                              const float4* Ux, Pair12& acc) {
+  constexpr int MU = LEG & 3;
+  constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
+  Pair12 f;
+  PairIO<T>::load(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[LEG]) * hl + sp, f);
+  float2 hr[6], hi[6], ur[6], ui[6];
+  project2<MU, S>(f, hr, hi);
+  su3_mul2(Ux + LEG * 9, hr, hi, ur, ui);
+  reconstruct2<MU, S, LEG == 0>(acc, ur, ui);
+}
+
+// shared-memory stride of one 4D site's expanded links, in float4: 72 + 1 so that the
+// sites of one warp fall on different banks
+constexpr int kUxStride = 73;
+
+template <class T, bool DAG>
+__global__ void __launch_bounds__(128) dhop_pair_kernel(const DhopParams p) {
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  float* sraw = reinterpret_cast<float*>(dyn_smem);                                  // k4 * 144 floats
+  float4* sUx = reinterpret_cast<float4*>(dyn_smem + size_t(p.k4) * 144 * sizeof(float));  // k4 * kUxStride
+  __shared__ __align__(8) uint64_t bar;
+
+  const int t = threadIdx.x;
+  const int hl = p.L5 >> 1;            // pairs per 4D site
+  const int hc = p.L5c >> 1;           // pairs per 4D site in this CTA
+  const int64_t x0 = int64_t(blockIdx.x) * p.k4;
+  const int nsite = int(min(int64_t(p.k4), p.n4h - x0));
+  if (t == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (t == 0) {
+    const uint32_t bytes = uint32_t(nsite) * 144u * uint32_t(sizeof(float));
+    mbar_expect_tx(&bar, bytes);
+    bulk_g2s(sraw, static_cast<const float*>(p.links) + x0 * 144, bytes, &bar);
+  }
+  const int j = t / hc;
+  const int sp = int(blockIdx.y) * hc + (t - j * hc);
+  const bool active = j < nsite && sp < hl;
+  int nb[8];
+  if (active) {
+    const int4* q = reinterpret_cast<const int4*>(p.nbr + (x0 + j) * 8);
+    const int4 a = __ldg(q), b = __ldg(q + 1);
+    nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
+    nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
+  }
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (!ok && t == 0) atomicExch(p.err, 1);
+  // expand (re, im) -> (re, re, im, im); every thread takes part in the barrier
+  if (ok) {
+    for (int e = t; e < nsite * 72; e += blockDim.x) {
+      const int site = e / 72, el = e - site * 72;
+      const float re = sraw[2 * e], im = sraw[2 * e + 1];
+      sUx[site * kUxStride + el] = make_float4(re, re, im, im);
+    }
+  }
+  __syncthreads();
+  if (!ok || !active) return;
+  const size_t np = p.n5 >> 1;
+  const float4* Ux = sUx + j * kUxStride;
+  Pair12 acc;
+  dhop_pair_leg<T, DAG, 0>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 1>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 2>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 3>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 4>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 5>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 6>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 7>(p, nb, sp, np, hl, Ux, acc);
+  PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
+}
+
+// CTA = k4 4D sites x (L5c/2) pair threads, about 128 threads
+static int pick_k4_pair(int hc) {
+  if (hc >= 64) return 1;
+  int k4 = 128 / hc;
+  while (k4 > 1 && (hc * k4) % 32 != 0) k4--;
+  if ((hc * k4) % 32 != 0) k4 = 128 / hc;
+  if (k4 > 48) k4 = 48;  // shared memory: 48 x (576 + 1168) B
+  return k4 < 1 ? 1 : k4;
+}
+
+template <class T, bool DAG> static int launch_dhop_pair_t(Op* op, DhopParams p) {
+  p.L5c = p.L5 > 256 ? 256 : p.L5;  // even
+  p.k4 = pick_k4_pair(p.L5c / 2);
+  const int threads = (p.L5c / 2) * p.k4;
+  const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
+  const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
+  const size_t smem = size_t(p.k4) * (144 * sizeof(float) + kUxStride * sizeof(float4));
+  static bool configured = false;
+  if (!configured) {
+    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_pair_kernel<T, DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    configured = true;
+  }
+  dhop_pair_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks), dim3(threads), smem, op->stream>>>(p);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
   if (in.prec != op->prec || out.prec != op->prec) {
     set_error("Dhop: field precision differs from the operator's");
@@ -227,8 +432,8 @@ int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
   p.err = op->d_err;
   switch (op->prec) {
     case GB_F64: return dag ? launch_dhop_t<double, true>(op, p) : launch_dhop_t<double, false>(op, p);
-    case GB_F32: return dag ? launch_dhop_t<float, true>(op, p) : launch_dhop_t<float, false>(op, p);
-    case GB_F16: return dag ? launch_dhop_t<__half, true>(op, p) : launch_dhop_t<__half, false>(op, p);
+    case GB_F32: return dag ? launch_dhop_pair_t<float, true>(op, p) : launch_dhop_pair_t<float, false>(op, p);
+    case GB_F16: return dag ? launch_dhop_pair_t<__half, true>(op, p) : launch_dhop_pair_t<__half, false>(op, p);
   }
   return GB_ERR_BAD_ARG;
 }

@@ -59,7 +59,11 @@ struct Op {
   int kind = 0;          // 0 Wilson, 1 Moebius
   int dims[4] = {0, 0, 0, 0};
   int64_t vol4 = 0, half4 = 0;
-  int Ls = 1, nrhs = 1, L5 = 1;
+  // nrhs_user right-hand sides are visible at the ABI; internally nrhs is rounded up so
+  // that L5 = Ls * nrhs is even (site pairs never straddle a 4D site).  The extra
+  // right-hand side, when there is one, holds zeros: it converges at CG set-up and no
+  // reduction result of it is returned.
+  int Ls = 1, nrhs = 1, nrhs_user = 1, L5 = 1;
   int prec = GB_F64;     // arithmetic / storage precision of the operator
   double mass = 0, M5 = 0, b = 0, c = 0, diag_mass = 0;
   std::complex<double> phases[4];
@@ -106,6 +110,7 @@ struct Field {
   void* data = nullptr;   // plane 0 of the even (or only) half
   float* norms = nullptr; // FP16 per-site norms (even half first for full fields)
   bool owned = true;
+  int ws_slot = -1;       // workspace slot of the owning operator (-1: a user field)
   size_t n5 = 0;          // 5D sites per checkerboard
   bool full() const { return subset == GB_FULL; }
   size_t half_bytes() const;   // bytes of one checkerboard's planes

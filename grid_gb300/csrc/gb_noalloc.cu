@@ -97,7 +97,7 @@ extern "C" int gb_field_norm2_noalloc(gb_field_t f, double* out) {
   if (!f || !out) { set_error("norm2 (no allocation): null argument"); return GB_ERR_BAD_ARG; }
   Op* op = f->op;
   if (op->nrhs > kNaMaxRhs) {
-    set_error("norm2 (no allocation): %d right-hand sides exceed the static scratch limit of %d", op->nrhs, kNaMaxRhs);
+    set_error("norm2 (no allocation): %d right-hand sides exceed the static scratch limit of %d", op->nrhs_user, kNaMaxRhs);
     return GB_ERR_UNSUPPORTED;
   }
   double* scratch = nullptr;
@@ -125,7 +125,7 @@ extern "C" int gb_field_norm2_noalloc(gb_field_t f, double* out) {
   double* result = scratch + size_t(2) * kNaMaxBlocks * kNaMaxRhs;
   norm2_static_final<<<1, 32 * ((op->nrhs + 31) / 32), 0, op->stream>>>(scratch, g * halves, op->nrhs, result);
   GB_CHECK_CUDA(cudaGetLastError());
-  GB_CHECK_CUDA(cudaMemcpyAsync(out, result, size_t(op->nrhs) * sizeof(double), cudaMemcpyDefault, op->stream));
+  GB_CHECK_CUDA(cudaMemcpyAsync(out, result, size_t(op->nrhs_user) * sizeof(double), cudaMemcpyDefault, op->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
   return GB_OK;
 }

@@ -150,6 +150,7 @@ int cg_solve(Op* op, int kind, Field* src, Field* psi, const gb_cg_params* P, gb
   for (int i = 0; i < n; i++) {
     op->last_iters[i] = op->h_cg[i].iter;
     op->last_resid[i] = res[i];
+    if (i >= op->nrhs_user) continue;  // padding right-hand side
     R->iterations = std::max(R->iterations, op->h_cg[i].iter);
     R->true_residual = std::max(R->true_residual, res[i]);
   }
@@ -182,7 +183,8 @@ int cg_reliable(Op* od, Op* of, int kind, Field* src, Field* psi, const gb_cg_pa
   GB_TRY(field_for(of, kind, GB_ODD, lp, WS_RU_PF, WS_FRU_PF, &p_f));
   GB_TRY(field_for(of, kind, GB_ODD, lp, WS_RU_MMPF, WS_FRU_MMPF, &mmp_f));
   GB_TRY(field_for(of, kind, GB_ODD, lp, WS_RU_RF, WS_FRU_RF, &r_f));
-  GB_TRY(field_for(of, kind, GB_ODD, lp, WS_RU_XF, WS_FRU_XF, &x_f));
+  // the inner solution accumulates in FP32 even when r, p, mmp are FP16-stored
+  GB_TRY(field_for(of, kind, GB_ODD, lp == GB_F16 ? GB_F32 : lp, WS_RU_XF, WS_FRU_XF, &x_f));
   if (!src->full()) {
     mmp_d->subset = r_d->subset = t_d->subset = src->subset;
     p_f->subset = mmp_f->subset = r_f->subset = x_f->subset = src->subset;
@@ -309,7 +311,7 @@ int schur_solve(Op* op, Op* olo, Field* src, Field* sol, const gb_cg_params* P, 
     std::vector<double> nr(n), ns(n);
     GB_TRY(field_norm2(res, nr.data()));
     GB_TRY(field_norm2(src, ns.data()));
-    for (int i = 0; i < n; i++) unprec[i] = ns[i] > 0 ? std::sqrt(nr[i] / ns[i]) : 0.0;
+    for (int i = 0; i < op->nrhs_user; i++) unprec[i] = ns[i] > 0 ? std::sqrt(nr[i] / ns[i]) : 0.0;
   }
   return rc;
 }
@@ -362,7 +364,7 @@ int gb_cg_schur(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* 
 
 int gb_cg_last_per_rhs(gb_op_t op, int* iterations, double* true_residual) {
   if (!op) return GB_ERR_BAD_ARG;
-  for (int i = 0; i < op->nrhs; i++) {
+  for (int i = 0; i < op->nrhs_user; i++) {
     if (iterations) iterations[i] = op->last_iters[i];
     if (true_residual) true_residual[i] = op->last_resid[i];
   }

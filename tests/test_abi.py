@@ -48,3 +48,5 @@ def test_bad_arguments_are_rejected_before_any_device_call():
     dims = (C.c_int * 4)(4, 4, 4, 4)
     assert g.lib.gb_mobius_create(dims, 1, 0.1, 1.8, 1.5, 0.5, None, 0, 1, None, 0, C.byref(h)) == 1  # Ls < 2
     assert g.lib.gb_mobius_create(dims, 16, 0.1, 1.8, 1.5, 0.5, None, 0, 100, None, 0, C.byref(h)) == 8  # L5 too big
+    # the fifth dimension must be even (site pairs of the FP32/FP16 layout)
+    assert g.lib.gb_mobius_create(dims, 5, 0.1, 1.8, 1.5, 0.5, None, 0, 1, None, 0, C.byref(h)) == 8

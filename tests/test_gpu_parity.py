@@ -72,7 +72,7 @@ def test_full_dhop_and_M(gpu_available, prec):
 
 
 @pytest.mark.parametrize("prec", [g.F64, g.F32])
-@pytest.mark.parametrize("Ls", [4, 8, 12, 16, 5])
+@pytest.mark.parametrize("Ls", [4, 6, 8, 12, 16, 18])
 def test_mobius_half_ops(gpu_available, prec, Ls):
     dims = (4, 4, 4, 4)
     op, ref, U = mobius_pair(dims, Ls, 0.01, prec, seed=Ls)
