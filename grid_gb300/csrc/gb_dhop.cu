@@ -326,8 +326,13 @@ __device__ __forceinline__ void dhop_pair_leg(const DhopParams& p, const int (&n
 // sites of one warp fall on different banks
 constexpr int kUxStride = 73;
 
+// resident CTAs of 128 threads per SM the register allocation targets
+#ifndef GB_DHOP_MINB
+#define GB_DHOP_MINB 4
+#endif
+
 template <class T, bool DAG>
-__global__ void __launch_bounds__(128) dhop_pair_kernel(const DhopParams p) {
+__global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p) {
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   float* sraw = reinterpret_cast<float*>(dyn_smem);                                  // k4 * 144 floats
   float4* sUx = reinterpret_cast<float4*>(dyn_smem + size_t(p.k4) * 144 * sizeof(float));  // k4 * kUxStride
