@@ -11,5 +11,5 @@ from .api import (  # noqa: F401
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
     antiperiodic_t, periodic, set_device, PinnedArray, norm2, innerProduct, axpy, axpby, axpy_norm,
-    pickCheckerboard, setCheckerboard,
+    pickCheckerboard, setCheckerboard, Server, Request, make_request, request_bytes,
 )

@@ -461,15 +461,17 @@ def _params(tol, maxit, err, **kw) -> CGParams:
 
 
 class ConjugateGradient:
-    def __init__(self, tol, maxit, err_on_no_conv=True, check_every=None):
+    def __init__(self, tol, maxit, err_on_no_conv=True, check_every=None, use_graphs=0):
         self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge = tol, maxit, err_on_no_conv
         self.check_every = check_every
+        self.use_graphs = int(use_graphs)
         self.IterationsToComplete = 0
         self.TrueResidual = 0.0
         self.result = None
 
     def params(self):
-        return _params(self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge, check_every=self.check_every)
+        return _params(self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge, check_every=self.check_every,
+                       use_graphs=self.use_graphs)
 
     def __call__(self, linop, src, psi):
         p, r = self.params(), CGResult()
@@ -492,8 +494,8 @@ class ConjugateGradient:
 
 class ConjugateGradientReliableUpdate(ConjugateGradient):
     def __init__(self, tol, maxit, delta, linop_f, linop_d, err_on_no_conv=True, relup_every=0,
-                 final_cleanup=True, check_every=None):
-        super().__init__(tol, maxit, err_on_no_conv, check_every)
+                 final_cleanup=True, check_every=None, use_graphs=0):
+        super().__init__(tol, maxit, err_on_no_conv, check_every, use_graphs)
         self.Delta, self.linop_f, self.linop_d = delta, linop_f, linop_d
         self.relup_every, self.DoFinalCleanup = relup_every, final_cleanup
         self.ReliableUpdatesPerformed = 0
@@ -502,7 +504,7 @@ class ConjugateGradientReliableUpdate(ConjugateGradient):
     def params(self):
         return _params(self.Tolerance, self.MaxIterations, self.ErrorOnNoConverge, delta=float(self.Delta),
                        relup_every=int(self.relup_every), final_cleanup=1 if self.DoFinalCleanup else 0,
-                       check_every=self.check_every)
+                       check_every=self.check_every, use_graphs=self.use_graphs)
 
     def __call__(self, src, psi):
         p, r = self.params(), CGResult()
@@ -535,3 +537,92 @@ class SchurRedBlackDiagMooeeSolve:
             s.IterationsToCleanup = r.cleanup_iterations
         self.unprec_residual = res
         return r
+
+
+# ---- propagator-solve service ---------------------------------------------------------
+class Request(C.Structure):
+    _fields_ = [("dims", C.c_int * 4), ("Ls", C.c_int), ("mf", C.c_double), ("M5", C.c_double), ("b", C.c_double),
+                ("c", C.c_double), ("eps", C.c_double), ("gauge_seed", C.c_uint64), ("nsrc", C.c_int),
+                ("src_seed", C.c_uint64), ("tolerance", C.c_double), ("max_iterations", C.c_int),
+                ("inner_precision", C.c_int), ("dry_seconds", C.c_double), ("t_submit", C.c_double),
+                ("solution", C.POINTER(C.c_double))]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int), ("nsrc", C.c_int), ("chunk", C.c_int),
+                ("iterations", C.c_int), ("reliable_updates", C.c_int), ("cleanup_iterations", C.c_int),
+                ("true_residual", C.c_double), ("solution_norm2", C.c_double), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_end", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("budget_bytes", C.c_size_t), ("used_bytes", C.c_size_t), ("peak_used_bytes", C.c_size_t),
+                ("running", C.c_int), ("max_running", C.c_int), ("queued", C.c_int), ("submitted", C.c_int64),
+                ("finished", C.c_int64), ("now", C.c_double)]
+
+
+_proto("gb_server_create", [C.c_size_t, _i, C.c_uint, C.POINTER(_vp)])
+_proto("gb_server_submit", [_vp, C.POINTER(Request), C.POINTER(C.c_int64)])
+_proto("gb_server_wait", [_vp, C.c_int64, _d])
+_proto("gb_server_results", [_vp, C.POINTER(RequestResult), _i, _ip])
+_proto("gb_server_stats", [_vp, C.POINTER(ServerStats)])
+_proto("gb_server_destroy", [_vp])
+_proto("gb_request_bytes", [C.POINTER(Request), C.POINTER(C.c_size_t)])
+
+
+def make_request(dims, Ls, mf, eps, gauge_seed, nsrc, src_seed, M5=1.8, b=1.5, c=0.5, tol=1e-10, maxit=20000,
+                 inner=F32, dry_seconds=0.0, solution: np.ndarray | None = None) -> Request:
+    r = Request()
+    r.dims = (C.c_int * 4)(*[int(x) for x in dims])
+    r.Ls, r.mf, r.M5, r.b, r.c, r.eps = int(Ls), float(mf), float(M5), float(b), float(c), float(eps)
+    r.gauge_seed, r.nsrc, r.src_seed = int(gauge_seed), int(nsrc), int(src_seed)
+    r.tolerance, r.max_iterations, r.inner_precision, r.dry_seconds = float(tol), int(maxit), int(inner), float(dry_seconds)
+    r.solution = solution.ctypes.data_as(_dp) if solution is not None else C.POINTER(C.c_double)()
+    r._keep = solution
+    return r
+
+
+def request_bytes(r: Request) -> int:
+    n = C.c_size_t()
+    _check(lib.gb_request_bytes(C.byref(r), C.byref(n)))
+    return n.value
+
+
+class Server:
+    """Continuous-batching propagator-solve service (gb_server_*)."""
+
+    DRY_RUN, GRAPHS = 1, 2
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 4, flags: int = 0):
+        h = _vp()
+        _check(lib.gb_server_create(int(hbm_budget_bytes), int(slots), int(flags), C.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def submit(self, r: Request) -> int:
+        i = C.c_int64()
+        self._keep.append(r)
+        _check(lib.gb_server_submit(self.h, C.byref(r), C.byref(i)))
+        return i.value
+
+    def wait(self, count: int, timeout: float = 600.0) -> bool:
+        return lib.gb_server_wait(self.h, int(count), float(timeout)) == 0
+
+    def results(self, max_n: int = 4096):
+        buf = (RequestResult * max_n)()
+        n = C.c_int()
+        _check(lib.gb_server_results(self.h, buf, max_n, C.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        _check(lib.gb_server_stats(self.h, C.byref(s)))
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib.gb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -109,12 +109,9 @@ int launch_m5d_z(Op* op, HalfView psi, HalfView phi, HalfView chi, const double*
   p.n5 = n5;
   p.L5 = op->L5;
   p.Ls = op->Ls;
-  switch (psi.prec) {
-    case GB_F64: return launch_m5d_p<double>(op, p, lower, diag, upper, dag);
-    case GB_F32: return launch_m5d_p<float>(op, p, lower, diag, upper, dag);
-    case GB_F16: return launch_m5d_p<__half>(op, p, lower, diag, upper, dag);
-  }
-  return GB_ERR_BAD_ARG;
+  // FP32 / FP16 (site-pair layout, Ls even): one thread per pair of s slots
+  if (psi.prec != GB_F64) return launch_m5d_pair(op, psi, phi, chi, lower, diag, upper, dag, n5, z, zc);
+  return launch_m5d_p<double>(op, p, lower, diag, upper, dag);
 }
 
 int launch_m5d(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,

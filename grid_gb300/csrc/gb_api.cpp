@@ -112,15 +112,9 @@ int ws_get(Op* op, int subset, int prec, int slot, Field** out) {
 // ---------------------------------------------------------------------------------------
 // reductions on whole fields (both halves of a full field), results to host
 // ---------------------------------------------------------------------------------------
-static int parts_per_half(Op* op) {
-  int g, B;
-  red_grid(op, op->n5(), &g, &B);
-  return g;
-}
-
 int field_norm2_dev(Field* f, double* d_out) {
   Op* op = f->op;
-  const int g = parts_per_half(op);
+  const int g = red_parts(op, f->prec);
   const int halves = f->full() ? 2 : 1;
   for (int h = 0; h < halves; h++)
     GB_TRY(launch_norm2_partial(op, half_view(f, h), f->n5, op->d_partial + size_t(h) * g * op->nrhs));
@@ -129,7 +123,7 @@ int field_norm2_dev(Field* f, double* d_out) {
 
 int field_inner_dev(Field* a, Field* b, double* d_out) {
   Op* op = a->op;
-  const int g = parts_per_half(op);
+  const int g = red_parts(op, a->prec);
   const int halves = a->full() ? 2 : 1;
   for (int h = 0; h < halves; h++)
     GB_TRY(launch_inner_partial(op, half_view(a, h), half_view(b, h), a->n5, op->d_partial + size_t(h) * g * op->nrhs * 2));
@@ -718,8 +712,7 @@ int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, doubl
   if (x->subset != y->subset) { set_error("axpy_norm: checkerboard mismatch"); return GB_ERR_BAD_PARITY; }
   Op* op = z->op;
   z->subset = x->subset;
-  int g, B;
-  GB_TRY(red_grid(op, op->n5(), &g, &B));
+  const int g = red_parts(op, z->prec);
   const int halves = z->full() ? 2 : 1;
   for (int h = 0; h < halves; h++)
     GB_TRY(launch_axpy_norm_partial(op, half_view(z, h), a, half_view(x, h), half_view(y, h), z->n5,

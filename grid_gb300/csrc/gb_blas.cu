@@ -66,12 +66,8 @@ int launch_axpby(Op* op, HalfView z, double a, HalfView x, double b, HalfView y,
     set_error("axpby: mixed precisions");
     return GB_ERR_BAD_ARG;
   }
-  switch (z.prec) {
-    case GB_F64: return axpby_t<double, double, double>(op, z, a, x, b, y, n5, 1);
-    case GB_F32: return axpby_t<float, float, float>(op, z, a, x, b, y, n5, 1);
-    case GB_F16: return axpby_t<__half, __half, __half>(op, z, a, x, b, y, n5, 1);
-  }
-  return GB_ERR_BAD_ARG;
+  if (z.prec != GB_F64) return launch_axpby_pair(op, z, a, x, b, y, n5, 1);
+  return axpby_t<double, double, double>(op, z, a, x, b, y, n5, 1);
 }
 
 int launch_scale(Op* op, HalfView z, double a, HalfView x, size_t n5) {
@@ -79,12 +75,8 @@ int launch_scale(Op* op, HalfView z, double a, HalfView x, size_t n5) {
     set_error("scale: mixed precisions");
     return GB_ERR_BAD_ARG;
   }
-  switch (z.prec) {
-    case GB_F64: return axpby_t<double, double, double>(op, z, a, x, 0, x, n5, 0);
-    case GB_F32: return axpby_t<float, float, float>(op, z, a, x, 0, x, n5, 0);
-    case GB_F16: return axpby_t<__half, __half, __half>(op, z, a, x, 0, x, n5, 0);
-  }
-  return GB_ERR_BAD_ARG;
+  if (z.prec != GB_F64) return launch_axpby_pair(op, z, a, x, 0.0, x, n5, 0);
+  return axpby_t<double, double, double>(op, z, a, x, 0, x, n5, 0);
 }
 
 template <class TZ, class TX> static int convert_t(Op* op, HalfView z, HalfView x, size_t n5) {
@@ -242,20 +234,32 @@ static int reduce_p(Op* op, HalfView x, HalfView y, HalfView z, double a, size_t
   return GB_ERR_BAD_ARG;
 }
 
+// FP32 / FP16 fields reduce through the pair kernels (gb_pair.cu), whose partial count
+// red_parts() reports; FP64 through reduce_kernel
 int launch_norm2_partial(Op* op, HalfView x, size_t n5, double* partial) {
+  if (x.prec != GB_F64) return launch_reduce_pair(op, 0, x, x, x, 0.0, n5, partial, nullptr, nullptr);
   return reduce_p<0>(op, x, x, x, 0.0, n5, partial);
 }
 int launch_inner_partial(Op* op, HalfView a, HalfView b, size_t n5, double* partial) {
   if (a.prec != b.prec) { set_error("innerProduct: mixed precisions"); return GB_ERR_BAD_ARG; }
+  if (a.prec != GB_F64) return launch_reduce_pair(op, 1, a, b, a, 0.0, n5, partial, nullptr, nullptr);
   return reduce_p<1>(op, a, b, a, 0.0, n5, partial);
 }
 // z = a x + y, |z|^2
 int launch_axpy_norm_partial(Op* op, HalfView z, double a, HalfView x, HalfView y, size_t n5, double* partial) {
   if (x.prec != y.prec || z.prec != x.prec) { set_error("axpy_norm: mixed precisions"); return GB_ERR_BAD_ARG; }
+  if (x.prec != GB_F64) return launch_reduce_pair(op, 2, x, y, z, a, n5, partial, nullptr, nullptr);
   return reduce_p<2>(op, x, y, z, a, n5, partial);
 }
 int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, HalfView psi, HalfView p, size_t n5, double* partial) {
   if (r.prec != mmp.prec || p.prec != r.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
+  if (r.prec != GB_F64) {
+    if (!(psi.prec == r.prec || (r.prec == GB_F16 && psi.prec == GB_F32))) {
+      set_error("CG update: solution precision %d with residual precision %d", psi.prec, r.prec);
+      return GB_ERR_BAD_ARG;
+    }
+    return launch_reduce_pair(op, 3, mmp, r, r, 0.0, n5, partial, &psi, &p);
+  }
   CGFields cf{psi.data, psi.norms, p.data, p.norms};
   if (psi.prec == r.prec) return reduce_p<3>(op, mmp, r, r, 0.0, n5, partial, cf);
   if (r.prec == GB_F16 && psi.prec == GB_F32) return reduce_t<__half, 3, float>(op, mmp, r, r, 0.0, cf, n5, partial);
@@ -421,12 +425,9 @@ __global__ void __launch_bounds__(256) cg_p_kernel(const RedShape sh, void* p, f
 }
 
 int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5) {
+  if (p.prec != GB_F64) return launch_cg_p_pair(op, p, r, n5);
   RedShape sh{op->L5, op->Ls, op->nrhs};
-  switch (p.prec) {
-    case GB_F64: cg_p_kernel<double><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5); break;
-    case GB_F32: cg_p_kernel<float><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5); break;
-    case GB_F16: cg_p_kernel<__half><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5); break;
-  }
+  cg_p_kernel<double><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }

@@ -309,7 +309,7 @@ __device__ __forceinline__ void su3_mul2(const float4* __restrict__ Ux, const fl
   }
 }
 
-template <class T, bool DAG, int LEG>
+template <class T, bool DAG, int LEG, bool FIRST>
 __device__ __forceinline__ void dhop_pair_leg(const DhopParams& p, const int (&nb)[8], int sp, size_t np, int hl,
                                               const float4* Ux, Pair12& acc) {
   constexpr int MU = LEG & 3;
@@ -319,8 +319,14 @@ __device__ __forceinline__ void dhop_pair_leg(const DhopParams& p, const int (&n
   float2 hr[6], hi[6], ur[6], ui[6];
   project2<MU, S>(f, hr, hi);
   su3_mul2(Ux + LEG * 9, hr, hi, ur, ui);
-  reconstruct2<MU, S, LEG == 0>(acc, ur, ui);
+  reconstruct2<MU, S, FIRST>(acc, ur, ui);
 }
+
+// leg order: GB_DHOP_ORDER 1 visits +mu and -mu back to back (x, y first): the +-x and
+// +-y neighbour rows of a CTA's two x-rows overlap, so the second visit can hit in L1
+#ifndef GB_DHOP_ORDER
+#define GB_DHOP_ORDER 1
+#endif
 
 // shared-memory stride of one 4D site's expanded links, in float4: 72 + 1 so that the
 // sites of one warp fall on different banks
@@ -375,15 +381,150 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
   const size_t np = p.n5 >> 1;
   const float4* Ux = sUx + j * kUxStride;
   Pair12 acc;
-  dhop_pair_leg<T, DAG, 0>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 1>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 2>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 3>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 4>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 5>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 6>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 7>(p, nb, sp, np, hl, Ux, acc);
+#if GB_DHOP_ORDER == 1
+  dhop_pair_leg<T, DAG, 0, true>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 4, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 1, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 5, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 2, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 6, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 3, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 7, false>(p, nb, sp, np, hl, Ux, acc);
+#else
+  dhop_pair_leg<T, DAG, 0, true>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 1, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 2, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 3, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 4, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 5, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 6, false>(p, nb, sp, np, hl, Ux, acc);
+  dhop_pair_leg<T, DAG, 7, false>(p, nb, sp, np, hl, Ux, acc);
+#endif
   PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// FP32 with the neighbour spinors of the next legs in flight without holding registers:
+// each thread copies its own neighbour pair (12 x 16 B) of leg l+DEPTH into its own
+// shared-memory slots with cp.async (L2-only, 16 B per copy) while it computes leg l.
+// A thread only reads slots it wrote, so the pipeline needs no CTA barrier.  Slots are
+// laid out [stage][component][thread] so consecutive threads hit consecutive banks.
+// The links arrive by one TMA bulk copy per CTA as in the other kernels.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+constexpr int kCpaDepth = 3;
+static int pick_k4_pair(int hc);
+
+template <bool DAG, int LEG>
+__device__ __forceinline__ void dhop_slot_leg(const float4* __restrict__ slot, int nthr, const float4* Ux, Pair12& acc) {
+  constexpr int MU = LEG & 3;
+  constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
+  Pair12 f;
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const float4 v = slot[k * nthr];
+    f.re[k] = make_float2(v.x, v.y);
+    f.im[k] = make_float2(v.z, v.w);
+  }
+  float2 hr[6], hi[6], ur[6], ui[6];
+  project2<MU, S>(f, hr, hi);
+  su3_mul2(Ux + LEG * 9, hr, hi, ur, ui);
+  reconstruct2<MU, S, LEG == 0>(acc, ur, ui);
+}
+
+template <bool DAG>
+__global__ void __launch_bounds__(128, 2) dhop_cpa_kernel(const DhopParams p) {
+  extern __shared__ __align__(128) unsigned char dyn_smem[];
+  const int k4 = p.k4;
+  const int hl = p.L5 >> 1, hc = p.L5c >> 1;
+  const int nthr = blockDim.x;
+  float* sraw = reinterpret_cast<float*>(dyn_smem);                     // k4*144 floats
+  float4* sUx = reinterpret_cast<float4*>(dyn_smem + size_t(k4) * 576);  // k4*kUxStride
+  float4* slots = sUx + size_t(k4) * kUxStride;                         // [kCpaDepth][12][nthr]
+  __shared__ __align__(8) uint64_t bar;
+
+  const int t = threadIdx.x;
+  const int64_t x0 = int64_t(blockIdx.x) * k4;
+  const int nsite = int(min(int64_t(k4), p.n4h - x0));
+  if (t == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (t == 0) {
+    const uint32_t bytes = uint32_t(nsite) * 576u;
+    mbar_expect_tx(&bar, bytes);
+    bulk_g2s(sraw, static_cast<const float*>(p.links) + x0 * 144, bytes, &bar);
+  }
+  const int j = t / hc;
+  const int sp = int(blockIdx.y) * hc + (t - j * hc);
+  const bool active = j < nsite && sp < hl;
+  const size_t np = p.n5 >> 1;
+  const float4* gin = static_cast<const float4*>(p.in);
+  int nb[8];
+  if (active) {
+    const int4* q = reinterpret_cast<const int4*>(p.nbr + (x0 + j) * 8);
+    const int4 a = __ldg(q), b = __ldg(q + 1);
+    nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
+    nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
+  }
+  auto issue = [&](int leg, int stage) {
+    if (active) {
+      const float4* src = gin + size_t(nb[leg]) * hl + sp;
+      float4* dst = slots + size_t(stage) * 12 * nthr + t;
+#pragma unroll
+      for (int k = 0; k < 12; k++) cp_async16(dst + size_t(k) * nthr, src + size_t(k) * np);
+    }
+    cp_async_commit();  // empty groups keep the per-thread group count uniform
+  };
+  issue(0, 0);
+  issue(1, 1);
+  issue(2, 2);
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (!ok && t == 0) atomicExch(p.err, 1);
+  if (ok) {
+    for (int e = t; e < nsite * 72; e += nthr) {
+      const int site = e / 72, el = e - site * 72;
+      const float re = sraw[2 * e], im = sraw[2 * e + 1];
+      sUx[site * kUxStride + el] = make_float4(re, re, im, im);
+    }
+  }
+  __syncthreads();
+  const float4* Ux = sUx + j * kUxStride;
+  Pair12 acc;
+#define GB_CPA_LEG(L, WAITN)                                                       \
+  {                                                                                \
+    cp_async_wait<WAITN>();                                                        \
+    if (ok && active) dhop_slot_leg<DAG, L>(slots + size_t((L) % kCpaDepth) * 12 * nthr + t, nthr, Ux, acc); \
+    if ((L) + kCpaDepth < 8) issue((L) + kCpaDepth, (L) % kCpaDepth);              \
+  }
+  // groups in flight after leg L's issue: 3 until the last issues, then 2, 1, 0
+  GB_CPA_LEG(0, 2) GB_CPA_LEG(1, 2) GB_CPA_LEG(2, 2) GB_CPA_LEG(3, 2) GB_CPA_LEG(4, 2)
+  GB_CPA_LEG(5, 2) GB_CPA_LEG(6, 1) GB_CPA_LEG(7, 0)
+#undef GB_CPA_LEG
+  if (ok && active) PairIO<float>::store(p.out, nullptr, np, size_t(x0 + j) * hl + sp, acc);
+}
+
+template <bool DAG> static int launch_dhop_cpa(Op* op, DhopParams p) {
+  p.L5c = p.L5 > 256 ? 256 : p.L5;
+  const int hc = p.L5c / 2;
+  p.k4 = pick_k4_pair(hc);
+  const int threads = hc * p.k4;
+  const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
+  const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
+  const size_t smem = size_t(p.k4) * (576 + kUxStride * 16) + size_t(kCpaDepth) * 12 * threads * 16;
+  static bool configured = false;
+  if (!configured) {
+    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_cpa_kernel<DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    configured = true;
+  }
+  dhop_cpa_kernel<DAG><<<dim3(unsigned(blocks), ychunks), dim3(threads), smem, op->stream>>>(p);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
 }
 
 // CTA = k4 4D sites x (L5c/2) pair threads, about 128 threads
@@ -437,7 +578,11 @@ int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
   p.err = op->d_err;
   switch (op->prec) {
     case GB_F64: return dag ? launch_dhop_t<double, true>(op, p) : launch_dhop_t<double, false>(op, p);
+#ifdef GB_DHOP_CPA
+    case GB_F32: return dag ? launch_dhop_cpa<true>(op, p) : launch_dhop_cpa<false>(op, p);
+#else
     case GB_F32: return dag ? launch_dhop_pair_t<float, true>(op, p) : launch_dhop_pair_t<float, false>(op, p);
+#endif
     case GB_F16: return dag ? launch_dhop_pair_t<__half, true>(op, p) : launch_dhop_pair_t<__half, false>(op, p);
   }
   return GB_ERR_BAD_ARG;

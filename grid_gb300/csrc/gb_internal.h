@@ -148,6 +148,21 @@ int launch_inner_partial(Op* op, HalfView a, HalfView b, size_t n5, double* part
 int launch_axpy_norm_partial(Op* op, HalfView z, double a, HalfView x, HalfView y, size_t n5, double* partial);
 int launch_reduce_final(Op* op, const double* partial, int nparts, int nv, double* out);
 int red_grid(Op* op, size_t n5, int* blocks, int* threads);
+// pair-layout (FP32 / FP16) kernels, gb_pair.cu
+int red_grid_pair(Op* op, size_t np, int* blocks, int* threads);
+int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
+                    const double* upper, int dag, size_t n5, const HalfView* z, double zc);
+int launch_reduce_pair(Op* op, int kind, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial,
+                       HalfView* psi, HalfView* p);
+int launch_cg_p_pair(Op* op, HalfView p, HalfView r, size_t n5);
+int launch_axpby_pair(Op* op, HalfView z, double a, HalfView x, double b, HalfView y, size_t n5, int use_y);
+// partial sums per checkerboard half that a reduction over a field of precision prec writes
+inline int red_parts(Op* op, int prec) {
+  int g = 1, B = 256;
+  if (prec == GB_F64) red_grid(op, op->n5(), &g, &B);
+  else red_grid_pair(op, op->n5() >> 1, &g, &B);
+  return g;
+}
 
 // layout conversion between canonical FP64 (device) and the device layout
 int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full);

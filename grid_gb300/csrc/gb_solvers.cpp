@@ -34,9 +34,7 @@ struct Parts {
   int halves;
 };
 Parts parts_of(Op* op, const Field* f) {
-  int g, B;
-  red_grid(op, op->n5(), &g, &B);
-  return Parts{g, f->full() ? 2 : 1};
+  return Parts{red_parts(op, f->prec), f->full() ? 2 : 1};
 }
 
 // d = <p|mmp> -> a
@@ -97,6 +95,71 @@ int field_for(Op* op, int kind, int subset_half, int prec, int slot_half, int sl
   return ws_get(op, subset_half, prec, slot_half, out);
 }
 
+// m CG iterations on op's stream, every one identical (the p update of the first one is
+// p = 0*p + r = r), so a chunk of `chunk` iterations can be captured once as a CUDA graph
+// and replayed: the first chunk runs as direct launches (it allocates the workspace), the
+// following full chunks replay the graph.
+struct ChunkRunner {
+  Op* op;
+  int kind;
+  Field *p, *mmp, *r, *psi;
+  int chunk;
+  bool graphs;
+  int runs = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~ChunkRunner() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+  int launch(int m) {
+    for (int j = 0; j < m; j++) {
+      GB_TRY(cg_p_update(op, p, r));
+      GB_TRY(op_hermop(op, kind, p, mmp));
+      GB_TRY(cg_alpha(op, p, mmp));
+      GB_TRY(cg_update(op, r, mmp, psi, p));
+    }
+    return GB_OK;
+  }
+  int iterate(int m) {
+    const bool use = graphs && m == chunk && runs > 0 && op->stream != nullptr;
+    runs++;
+    if (!use) return launch(m);
+    if (!exec) {
+      GB_CHECK_CUDA(cudaStreamBeginCapture(op->stream, cudaStreamCaptureModeThreadLocal));
+      const int rc = launch(m);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(op->stream, &g);
+      if (rc != GB_OK) { if (g) cudaGraphDestroy(g); return rc; }
+      if (e != cudaSuccess) { set_error("CG graph capture: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
+      graph = g;
+      GB_CHECK_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    }
+    GB_CHECK_CUDA(cudaGraphLaunch(exec, op->stream));
+    return GB_OK;
+  }
+};
+
+// a private stream for a graph-captured solve on an operator bound to the legacy
+// default stream (which cannot be captured); restored and released on scope exit
+struct SolveStream {
+  Op* ops[2];
+  cudaStream_t saved[2];
+  cudaStream_t own = nullptr;
+  SolveStream(Op* a, Op* b, bool want) : ops{a, b}, saved{a ? a->stream : nullptr, b ? b->stream : nullptr} {
+    if (!want || (a && a->stream)) return;
+    cudaDeviceSynchronize();
+    if (cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking) != cudaSuccess) { own = nullptr; return; }
+    for (Op* o : ops) if (o) o->stream = own;
+  }
+  ~SolveStream() {
+    if (!own) return;
+    cudaStreamSynchronize(own);
+    for (int i = 0; i < 2; i++) if (ops[i]) ops[i]->stream = saved[i];
+    cudaStreamDestroy(own);
+  }
+};
+
 }  // namespace
 
 // Plain CG in op's precision.  psi holds the initial guess on entry.
@@ -131,14 +194,11 @@ int cg_solve(Op* op, int kind, Field* src, Field* psi, const gb_cg_params* P, gb
   int flags[2] = {0, 0};
   GB_TRY(fetch_scalars(op, flags));
   int k = 0;
+  ChunkRunner runner{op, kind, p, mmp, r, psi, chunk, P->use_graphs != 0};
   while (!flags[0] && k < P->max_iterations) {
     const int m = std::min(chunk, P->max_iterations - k);
-    for (int j = 0; j < m; j++, k++) {
-      if (k > 0) GB_TRY(cg_p_update(op, p, r));
-      GB_TRY(op_hermop(op, kind, p, mmp));
-      GB_TRY(cg_alpha(op, p, mmp));
-      GB_TRY(cg_update(op, r, mmp, psi, p));
-    }
+    GB_TRY(runner.iterate(m));
+    k += m;
     GB_TRY(fetch_scalars(op, flags));
     GB_TRY(check_device_error(op));
   }
@@ -212,14 +272,11 @@ int cg_reliable(Op* od, Op* of, int kind, Field* src, Field* psi, const gb_cg_pa
     GB_TRY(field_copy(mmp_d, x_f));
     return field_axpby(psi, 1.0, 1.0, psi, mmp_d);
   };
+  ChunkRunner runner{of, kind, p_f, mmp_f, r_f, x_f, chunk, P->use_graphs != 0};
   while (!flags[0] && k < P->max_iterations) {
     const int m = std::min(chunk, P->max_iterations - k);
-    for (int j = 0; j < m; j++, k++) {
-      if (k > 0) GB_TRY(cg_p_update(of, p_f, r_f));
-      GB_TRY(op_hermop(of, kind, p_f, mmp_f));
-      GB_TRY(cg_alpha(of, p_f, mmp_f));
-      GB_TRY(cg_update(of, r_f, mmp_f, x_f, p_f));
-    }
+    GB_TRY(runner.iterate(m));
+    k += m;
     since += m;
     GB_TRY(fetch_scalars(of, flags));
     GB_TRY(check_device_error(of));
@@ -352,6 +409,7 @@ static int finish(int rc, const gb_cg_params* p) {
 int gb_cg_mdagm(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* p, gb_cg_result* res) {
   GB_TRY(solve_checks(op, src, psi, p, res));
   if (!src->full() || !psi->full()) { set_error("MdagM CG: full fields expected"); return GB_ERR_BAD_PARITY; }
+  SolveStream ss(op, nullptr, p->use_graphs != 0);
   return finish(cg_solve(op, 0, src, psi, p, res), p);
 }
 
@@ -359,6 +417,7 @@ int gb_cg_schur(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* 
   GB_TRY(solve_checks(op, src, psi, p, res));
   if (src->subset != GB_ODD) { set_error("Schur CG: odd source expected"); return GB_ERR_BAD_PARITY; }
   psi->subset = GB_ODD;
+  SolveStream ss(op, nullptr, p->use_graphs != 0);
   return finish(cg_solve(op, 1, src, psi, p, res), p);
 }
 
@@ -379,6 +438,7 @@ int gb_cg_reliable(gb_op_t op_d, gb_op_t op_lo, int kind, gb_field_t src, gb_fie
   if (kind == 0 && (!src->full() || !psi->full())) { set_error("reliable CG: full fields expected"); return GB_ERR_BAD_PARITY; }
   if (kind == 1 && src->subset != GB_ODD) { set_error("reliable CG: odd source expected"); return GB_ERR_BAD_PARITY; }
   if (kind == 1) psi->subset = GB_ODD;
+  SolveStream ss(op_d, op_lo, p->use_graphs != 0);
   return finish(cg_reliable(op_d, op_lo, kind, src, psi, p, res), p);
 }
 
@@ -387,6 +447,7 @@ int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, co
   GB_TRY(solve_checks(op, src, sol, p, res));
   if (!src->full() || !sol->full()) { set_error("Schur solve: full fields expected"); return GB_ERR_BAD_PARITY; }
   if (op_lo && (op->prec != GB_F64 || op_lo->prec == GB_F64)) { set_error("Schur solve: mixed needs FP64 op and FP32/FP16 op_lo"); return GB_ERR_BAD_ARG; }
+  SolveStream ss(op, op_lo, p->use_graphs != 0);
   return finish(schur_solve(op, op_lo, src, sol, p, res, unprec_resid), p);
 }
 

@@ -196,6 +196,56 @@ int gb_random_gaussian(size_t n_complex, uint64_t seed, double* out);
 int gb_random_z2(size_t n_complex, uint64_t seed, double* out);
 int gb_unit_gauge(const int dims[4], double* U);
 
+/* ---- propagator-solve service (continuous batching under an HBM budget) -----------
+ * No single Grid interface corresponds: a service loop in front of
+ * SchurRedBlackDiagMooeeSolve(ConjugateGradientReliableUpdate) on MobiusFermion.
+ * A request solves M x = b for nsrc Gaussian 5D sources on a seeded gauge field; its
+ * sources share one multi-RHS operator.  Workers (slots) admit the queue head when its
+ * memory estimate fits the budget; solves of different requests overlap on the device.
+ * flags: bit 0 = dry run (no device work: each request sleeps dry_seconds),
+ *        bit 1 = capture the CG iteration chunks in CUDA graphs. */
+typedef struct {
+  int dims[4];
+  int Ls;
+  double mf, M5, b, c;
+  double eps;           /* gauge field U = exp(i eps H), seeded by gauge_seed */
+  uint64_t gauge_seed;
+  int nsrc;             /* 1..: Gaussian sources seeded by src_seed */
+  uint64_t src_seed;
+  double tolerance;     /* CG tolerance (default 1e-10) */
+  int max_iterations;
+  int inner_precision;  /* GB_F32 or GB_F16 */
+  double dry_seconds;   /* dry-run duration */
+  double t_submit;      /* set by the server */
+  double* solution;     /* optional host buffer: nsrc canonical full 5D fields */
+} gb_request;
+
+typedef struct {
+  int64_t id;
+  int status;           /* GB_OK, GB_ERR_OOM (does not fit the budget), solver status */
+  int nsrc, chunk;      /* sources, and sources per multi-RHS solve */
+  int iterations, reliable_updates, cleanup_iterations;
+  double true_residual; /* max over sources of |M x - b| / |b| */
+  double solution_norm2;
+  double t_submit, t_start, t_end; /* seconds since the server was created */
+} gb_request_result;
+
+typedef struct {
+  size_t budget_bytes, used_bytes, peak_used_bytes;
+  int running, max_running, queued;
+  int64_t submitted, finished;
+  double now;
+} gb_server_stats_t;
+
+typedef struct gb_server_s* gb_server_t;
+int gb_server_create(size_t hbm_budget_bytes, int slots, unsigned flags, gb_server_t* out);
+int gb_server_submit(gb_server_t s, const gb_request* r, int64_t* id);
+int gb_server_wait(gb_server_t s, int64_t finished_count, double timeout_s);
+int gb_server_results(gb_server_t s, gb_request_result* out, int max, int* n);
+int gb_server_stats(gb_server_t s, gb_server_stats_t* st);
+int gb_server_destroy(gb_server_t s);
+int gb_request_bytes(const gb_request* r, size_t* bytes); /* the admission estimate */
+
 /* ---- device, stream and host-buffer utilities ------------------------------------ */
 int gb_set_device(int device);                       /* cudaSetDevice for this thread        */
 int gb_op_sync(gb_op_t op);                          /* wait for the op's stream             */
