@@ -298,7 +298,163 @@ def run_gpu(args, ws, rank, local, dist):
         "gpu_launches": 2 * args.steps,
         "cpu_baseline": cpu,
     }
+    if ws == 1 and not args.no_extras:
+        extras = {}
+        for name, fn in (("cg_schur_24^4xLs12", lambda: extra_cg_schur(g)),
+                         ("multi_rhs_wilson_32^3x64", lambda: extra_multi_rhs(g)),
+                         ("serving", lambda: extra_serving(g, max_requests=args.serve_requests,
+                                                           seconds=args.serve_seconds))):
+            t0 = time.perf_counter()
+            try:
+                extras[name] = fn()
+            except Exception as e:  # a failed extra is reported, the headline line still prints
+                extras[name] = {"error": f"{type(e).__name__}: {e}"}
+            extras[name]["bench_wall_s"] = time.perf_counter() - t0
+        line["extra"] = extras
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
+# the other workloads of the path, reported beside the headline (N = 1 only)
+# ---------------------------------------------------------------------------------------
+def extra_cg_schur(g, fp64_maxit=20000):
+    """Mixed-precision SchurRedBlack CG on Moebius DWF 24^4 x Ls=12, mf=0.005, gauge eps=0.6,
+    to a true residual of 1e-10: FP32 inner, FP16-stored inner (FP32 norms/arithmetic), a
+    4-RHS batched mixed solve, and the plain FP64 CG.  Reliable updates every 100
+    iterations or when |r|^2 drops by 1e-6 (|r| by 1e-3)."""
+    dims, Ls, mf = (24, 24, 24, 24), 12, 0.005
+    U = g.random_gauge(dims, 0.6, 3003)
+    vol = int(np.prod(dims))
+    out = {"workload": "mobius_dwf_24^4xLs12_mf0.005_schur_cg_1e-10"}
+
+    def solve(inner, nrhs, seed):
+        od = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=g.F64, nrhs=nrhs)
+        src = g.random_gaussian(vol * Ls * 12 * nrhs, seed)
+        fs = od.FermionField().import_(src)
+        fx = od.FermionField().zero()
+        if inner is None:
+            cg = g.ConjugateGradient(1e-10, fp64_maxit, err_on_no_conv=False, check_every=20)
+            solver = g.SchurRedBlackDiagMooeeSolve(cg)
+            keep = None
+        else:
+            of = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=inner, nrhs=nrhs)
+            cg = g.ConjugateGradientReliableUpdate(1e-10, 30000, 1e-6, g.SchurDiagMooeeOperator(of),
+                                                   g.SchurDiagMooeeOperator(od), relup_every=100,
+                                                   err_on_no_conv=False, check_every=20)
+            solver = g.SchurRedBlackDiagMooeeSolve(cg)
+            keep = of
+        od.sync()
+        t0 = time.perf_counter()
+        r = solver(od, fs, fx)
+        od.sync()
+        dt = time.perf_counter() - t0
+        x = fx.export()
+        del keep
+        return {"seconds": dt, "solves_per_s": nrhs / dt, "iterations": int(r.iterations),
+                "reliable_updates": int(r.reliable_updates), "cleanup_iterations": int(r.cleanup_iterations),
+                "true_residual": float(r.true_residual), "unprec_residual": float(max(solver.unprec_residual)),
+                "converged": int(r.converged), "nrhs": nrhs}, x
+
+    m32, x32 = solve(g.F32, 1, 77)
+    m16, x16 = solve(g.F16, 1, 77)
+    mb, _ = solve(g.F32, 4, 78)
+    f64, x64 = solve(None, 1, 77)
+    from oracle import oracle as o
+    m32["solution_rel_err_vs_fp64"] = o.rel_l2(x32, x64)
+    m16["solution_rel_err_vs_fp64"] = o.rel_l2(x16, x64)
+    out.update({"mixed_fp32": m32, "mixed_fp16": m16, "mixed_fp32_batched4": mb, "fp64": f64,
+                "speedup_mixed_vs_fp64": m32["solves_per_s"] / f64["solves_per_s"],
+                "speedup_mixed_batched_vs_fp64": mb["solves_per_s"] / f64["solves_per_s"]})
+    return out
+
+
+def extra_multi_rhs(g):
+    """Wilson 32^3 x 64, m = 0.02, gauge eps = 0.5, 12 point sources (spin x colour at the
+    origin) + 4 Z2-noise sources: the FP32 16-RHS DhopEO (links read once for all 16) and
+    the batched Schur CG to 1e-10 with FP64 reliable updates."""
+    dims, nrhs, mass = (32, 32, 32, 64), 16, 0.02
+    vol = int(np.prod(dims))
+    U = g.random_gauge(dims, 0.5, 4004)
+    srcs = []
+    for sc in range(12):  # point sources psi[site 0][spin][colour]
+        a = np.zeros(vol * 12, dtype=np.complex128)
+        a[sc] = 1.0
+        srcs.append(a)
+    for k in range(4):
+        srcs.append(g.random_z2(vol * 12, 500 + k))
+    src = np.concatenate(srcs)
+    out = {"workload": "wilson_32^3x64_m0.02_16rhs"}
+    of = g.WilsonFermion(U, dims, mass, precision=g.F32, nrhs=nrhs)
+    ins = [of.FermionRedBlackField(g.ODD).import_(g.random_gaussian(of.half_sites4 * 12 * nrhs, 90 + k)) for k in range(2)]
+    outs = [of.FermionRedBlackField(g.EVEN) for _ in range(2)]
+    ms = of.bench_kernel(0, ins, outs, 20)
+    sites = of.half_sites4 * nrhs
+    out["dhop_eo_16rhs_ms"] = ms
+    out["dhop_eo_16rhs_gbs"] = sites * (192 + 576 / nrhs) / (ms / 1e3) / 1e9
+    out["dhop_eo_16rhs_bytes_per_site_rhs"] = 192 + 576 / nrhs
+    del ins, outs
+    od = g.WilsonFermion(U, dims, mass, precision=g.F64, nrhs=nrhs)
+    fs = od.FermionField().import_(src)
+    fx = od.FermionField().zero()
+    cg = g.ConjugateGradientReliableUpdate(1e-10, 20000, 1e-6, g.SchurDiagMooeeOperator(of),
+                                           g.SchurDiagMooeeOperator(od), relup_every=100, err_on_no_conv=False)
+    solver = g.SchurRedBlackDiagMooeeSolve(cg)
+    od.sync()
+    t0 = time.perf_counter()
+    r = solver(od, fs, fx)
+    od.sync()
+    dt = time.perf_counter() - t0
+    out.update({"batched_solve_seconds": dt, "solves_per_s": nrhs / dt, "iterations": int(r.iterations),
+                "reliable_updates": int(r.reliable_updates), "true_residual": float(r.true_residual),
+                "unprec_residual": float(max(solver.unprec_residual)), "converged": int(r.converged)})
+    return out
+
+
+def serving_stream(seconds, rate=20.0, seed=5005):
+    """The seeded request stream: Poisson arrivals, Moebius DWF volume from {8^4, 12^4,
+    16^4, 24^4, 16^3x32}, Ls from {8, 12, 16}, mf log-uniform in [1e-3, 1e-1], gauge eps
+    uniform in [0.3, 0.7], 1-12 Gaussian sources."""
+    rng = np.random.default_rng(seed)
+    vols = [(8, 8, 8, 8), (12, 12, 12, 12), (16, 16, 16, 16), (24, 24, 24, 24), (16, 16, 16, 32)]
+    t, reqs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        reqs.append(dict(t=t, dims=vols[rng.integers(len(vols))], Ls=int(rng.choice([8, 12, 16])),
+                         mf=float(np.exp(rng.uniform(np.log(1e-3), np.log(1e-1)))), eps=float(rng.uniform(0.3, 0.7)),
+                         gauge_seed=int(rng.integers(1 << 62)), nsrc=int(rng.integers(1, 13)),
+                         src_seed=int(rng.integers(1 << 62))))
+    return reqs
+
+
+def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0):
+    """Replays the first `max_requests` requests of the seeded stream at their arrival
+    times into the service (HBM budget 150 GB, mixed-precision CG to 1e-10)."""
+    reqs = serving_stream(seconds)[:max_requests]
+    srv = g.Server(int(budget_gb * (1 << 30)), slots=slots, flags=g.Server.GRAPHS)
+    t0 = time.perf_counter()
+    for q in reqs:
+        delay = q["t"] - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        srv.submit(g.make_request(q["dims"], q["Ls"], q["mf"], q["eps"], q["gauge_seed"], q["nsrc"], q["src_seed"]))
+    ok = srv.wait(len(reqs), 1800)
+    wall = time.perf_counter() - t0
+    res = srv.results(len(reqs) + 8)
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r.t_end - r.t_submit for r in res])
+    good = [r for r in res if r.status == 0]
+    nsol = sum(r.nsrc for r in good)
+    return {"workload": f"serving: first {len(reqs)} requests of the seeded Poisson(20/s) stream",
+            "completed": len(good), "failed": len(res) - len(good), "all_done": bool(ok), "wall_s": wall,
+            "solves_per_s": nsol / wall, "requests_per_s": len(good) / wall,
+            "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "max_true_residual": float(max((r.true_residual for r in good), default=0.0)),
+            "max_running": int(st.max_running), "peak_hbm_gb": st.peak_used_bytes / (1 << 30), "slots": slots,
+            "budget_gb": budget_gb}
 
 
 def main():
@@ -307,6 +463,9 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="only the headline DhopEO/DhopOE measurement")
+    ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving stream to replay")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the seeded arrival stream")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

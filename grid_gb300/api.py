@@ -551,7 +551,8 @@ class Request(C.Structure):
 class RequestResult(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int), ("nsrc", C.c_int), ("chunk", C.c_int),
                 ("iterations", C.c_int), ("reliable_updates", C.c_int), ("cleanup_iterations", C.c_int),
-                ("true_residual", C.c_double), ("solution_norm2", C.c_double), ("t_submit", C.c_double),
+                ("true_residual", C.c_double), ("unprec_residual", C.c_double), ("solution_norm2", C.c_double),
+                ("t_submit", C.c_double),
                 ("t_start", C.c_double), ("t_end", C.c_double)]
 
 

@@ -213,7 +213,8 @@ int solve_request(gb_server_s* S, const gb_request& rq, int nsrc, uint64_t src_s
     out->iterations = std::max(out->iterations, R.iterations);
     out->reliable_updates += R.reliable_updates;
     out->cleanup_iterations = std::max(out->cleanup_iterations, R.cleanup_iterations);
-    for (double u : unprec) out->true_residual = std::max(out->true_residual, u);
+    out->true_residual = std::max(out->true_residual, R.true_residual);
+    for (double u : unprec) out->unprec_residual = std::max(out->unprec_residual, u);
     if (rc) break;
     std::vector<double> n2(nsrc);
     if ((rc = gb_field_norm2(sol, n2.data()))) break;

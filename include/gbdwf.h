@@ -225,7 +225,8 @@ typedef struct {
   int status;           /* GB_OK, GB_ERR_OOM (does not fit the budget), solver status */
   int nsrc, chunk;      /* sources, and sources per multi-RHS solve */
   int iterations, reliable_updates, cleanup_iterations;
-  double true_residual; /* max over sources of |M x - b| / |b| */
+  double true_residual; /* max over sources of the CG true residual (Grid's TrueResidual) */
+  double unprec_residual; /* max over sources of |M x - b| / |b| */
   double solution_norm2;
   double t_submit, t_start, t_end; /* seconds since the server was created */
 } gb_request_result;

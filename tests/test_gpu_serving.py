@@ -30,7 +30,7 @@ def test_same_alone_and_in_the_mix(gpu_available):
     s = g.Server(40 * GB, slots=1)
     (r0,) = run(s, [g.make_request(dims, Ls, 0.05, 0.5, 11, 2, 12, solution=alone)])
     s.close()
-    assert r0.status == 0 and r0.true_residual < 1e-10
+    assert r0.status == 0 and r0.true_residual < 1e-10 and r0.unprec_residual < 1e-9
     mixed = sol_buffer(dims, Ls, 2)
     s = g.Server(40 * GB, slots=4)
     others = [g.make_request((8, 8, 8, 16), 12, 0.02, 0.4, 21, 3, 22),
@@ -40,7 +40,7 @@ def test_same_alone_and_in_the_mix(gpu_available):
     st = s.stats()
     s.close()
     assert all(x.status == 0 for x in res)
-    assert all(x.true_residual < 1e-10 for x in res)
+    assert all(x.true_residual < 1e-10 and x.unprec_residual < 1e-9 for x in res)
     assert st.max_running >= 2  # the solves overlapped on the device
     assert o.rel_l2(mixed, alone) < 1e-12
     assert res[2].iterations == r0.iterations
@@ -52,7 +52,7 @@ def test_service_solution_matches_oracle(gpu_available):
     s = g.Server(40 * GB, slots=2)
     (r,) = run(s, [g.make_request(dims, Ls, mf, 0.5, 7, 1, 8, solution=sol)])
     s.close()
-    assert r.status == 0 and r.true_residual < 1e-10
+    assert r.status == 0 and r.true_residual < 1e-10 and r.unprec_residual < 1e-9
     U = g.random_gauge(dims, 0.5, 7)
     src = g.random_gaussian(int(np.prod(dims)) * Ls * 12, 8)
     ref = o.OracleOp(1, 0, dims, Ls, [mf, 1.8, 1.5, 0.5], U, g.antiperiodic_t())
