@@ -67,7 +67,10 @@ int field_alloc(Op* op, int subset, int prec, Field** out) {
     set_error("cudaMalloc of %zu bytes failed: %s", halves * f->n5 * spinor_bytes(prec), cudaGetErrorString(e));
     return GB_ERR_OOM;
   }
-  cudaMemset(f->data, 0, halves * f->half_bytes());
+  // zero on the operator's stream: a non-blocking stream does not wait for work on the
+  // legacy default stream, so a plain cudaMemset could land after this stream's kernels
+  // have written the (lazily allocated) field
+  cudaMemsetAsync(f->data, 0, halves * f->half_bytes(), op->stream);
   if (prec == GB_F16) {
     e = cudaMalloc(&f->norms, halves * f->n5 * sizeof(float));
     if (e != cudaSuccess) {
@@ -76,6 +79,7 @@ int field_alloc(Op* op, int subset, int prec, Field** out) {
       set_error("cudaMalloc of norms failed: %s", cudaGetErrorString(e));
       return GB_ERR_OOM;
     }
+    cudaMemsetAsync(f->norms, 0, halves * f->n5 * sizeof(float), op->stream);
   }
   *out = f;
   return GB_OK;
@@ -359,7 +363,8 @@ int build_neighbours(Op* op) {
         tab[size_t(xcb) * 8 + leg] = int(ns >> 1);
       }
     }
-    GB_CHECK_CUDA(cudaMemcpy(op->nbr[p], tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+    GB_CHECK_CUDA(cudaMemcpyAsync(op->nbr[p], tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, op->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));  // tab is reused for the next parity
   }
   return GB_OK;
 }
@@ -469,7 +474,7 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
   alloc(reinterpret_cast<void**>(&op->d_all_done), 4 * sizeof(int));
   if (rc == GB_OK && cudaMallocHost(reinterpret_cast<void**>(&op->h_result), size_t(nrhs) * 8 * sizeof(double)) != cudaSuccess) rc = GB_ERR_OOM;
   if (rc == GB_OK && cudaMallocHost(reinterpret_cast<void**>(&op->h_cg), size_t(nrhs) * sizeof(CGScalars) + 64) != cudaSuccess) rc = GB_ERR_OOM;
-  if (rc == GB_OK && cudaMemset(op->d_err, 0, sizeof(int)) != cudaSuccess) rc = GB_ERR_CUDA;
+  if (rc == GB_OK && cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream) != cudaSuccess) rc = GB_ERR_CUDA;
   if (rc == GB_OK) rc = build_neighbours(op);
   if (rc != GB_OK) {
     op_release(op);

@@ -312,6 +312,25 @@ void worker(gb_server_s* S) {
 
 extern "C" {
 
+int gb_random_gauge_device(const int dims[4], double eps, uint64_t seed, double* U_dev, void* stream) {
+  if (!dims || !U_dev) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  int64_t vol = 1;
+  for (int k = 0; k < 4; k++) vol *= dims[k];
+  const int64_t nl = vol * 4;
+  random_gauge_kernel<<<unsigned((nl + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+      nl, eps, seed, reinterpret_cast<double2*>(U_dev));
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+int gb_random_gaussian_device(size_t n_complex, uint64_t seed, double* out_dev, void* stream) {
+  if (!out_dev) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  random_gaussian_kernel<<<unsigned((n_complex + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      n_complex, seed, reinterpret_cast<double2*>(out_dev));
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 int gb_server_create(size_t hbm_budget_bytes, int slots, unsigned flags, gb_server_t* out) {
   if (!out || slots < 1 || hbm_budget_bytes == 0) { set_error("server: bad arguments"); return GB_ERR_BAD_ARG; }
   gb_server_s* S = new gb_server_s;

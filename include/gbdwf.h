@@ -192,6 +192,9 @@ int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, co
  * and imaginary parts.  gb_random_z2: (+-1 +-i)/sqrt(2) per complex number.
  */
 int gb_random_gauge(const int dims[4], double eps, uint64_t seed, double* U);
+/* the same constructions evaluated on the device into device memory (stream may be NULL) */
+int gb_random_gauge_device(const int dims[4], double eps, uint64_t seed, double* U_dev, void* stream);
+int gb_random_gaussian_device(size_t n_complex, uint64_t seed, double* out_dev, void* stream);
 int gb_random_gaussian(size_t n_complex, uint64_t seed, double* out);
 int gb_random_z2(size_t n_complex, uint64_t seed, double* out);
 int gb_unit_gauge(const int dims[4], double* U);
