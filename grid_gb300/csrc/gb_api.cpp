@@ -249,8 +249,8 @@ int op_dhop_cb(Op* op, Field* in, Field* out, int dag) {
 
 int op_dhop_full(Op* op, Field* in, Field* out, int dag) {
   if (!in->full() || !out->full()) { set_error("Dhop: full fields expected"); return GB_ERR_BAD_PARITY; }
-  GB_TRY(launch_dhop(op, half_view(in, 1), half_view(out, 0), 0, dag));
-  return launch_dhop(op, half_view(in, 0), half_view(out, 1), 1, dag);
+  // both checkerboards in one launch: blockIdx.z selects the output parity
+  return launch_dhop_full(op, half_view(in, 1), half_view(out, 0), half_view(in, 0), half_view(out, 1), dag);
 }
 
 int op_meooe(Op* op, Field* in, Field* out, int dag) {

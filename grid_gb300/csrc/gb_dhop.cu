@@ -35,7 +35,24 @@ struct DhopParams {
   int L5c;  // slots per CTA (L5 split over gridDim.y when above 256)
   int k4;
   int* err;
+  // second checkerboard of a full-lattice Dhop, taken by the CTAs with blockIdx.z == 1
+  const void* in2;
+  const float* in2_norms;
+  void* out2;
+  float* out2_norms;
+  const void* links2;
+  const int* nbr2;
 };
+
+// the parameters of this CTA's checkerboard (both parities of a full Dhop run in one grid)
+__device__ __forceinline__ DhopParams dhop_side(const DhopParams& p) {
+  DhopParams q = p;
+  if (blockIdx.z) {
+    q.in = p.in2; q.in_norms = p.in2_norms; q.out = p.out2; q.out_norms = p.out2_norms;
+    q.links = p.links2; q.nbr = p.nbr2;
+  }
+  return q;
+}
 
 // ---- spin projection (1 + S gamma_MU) f -> two-spinor h, Grid's spProj{X,Y,Z,T}{p,m} ----
 template <int MU, int S, class R>
@@ -131,7 +148,8 @@ __device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8]
 }
 
 template <class T, bool DAG>
-__global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p) {
+__global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
+  const DhopParams p = dhop_side(p0);
   using R = typename Arith<T>::type;
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   R* sU = reinterpret_cast<R*>(dyn_smem);
@@ -198,7 +216,7 @@ template <class T, bool DAG> static int launch_dhop_t(Op* op, const DhopParams& 
     GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_kernel<T, DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     configured = true;
   }
-  dhop_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks), dim3(threads), smem, op->stream>>>(p);
+  dhop_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -338,7 +356,8 @@ constexpr int kUxStride = 73;
 #endif
 
 template <class T, bool DAG>
-__global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p) {
+__global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p0) {
+  const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   float* sraw = reinterpret_cast<float*>(dyn_smem);                                  // k4 * 144 floats
   float4* sUx = reinterpret_cast<float4*>(dyn_smem + size_t(p.k4) * 144 * sizeof(float));  // k4 * kUxStride
@@ -440,7 +459,8 @@ __device__ __forceinline__ void dhop_slot_leg(const float4* __restrict__ slot, i
 }
 
 template <bool DAG>
-__global__ void __launch_bounds__(128, 2) dhop_cpa_kernel(const DhopParams p) {
+__global__ void __launch_bounds__(128, 2) dhop_cpa_kernel(const DhopParams p0) {
+  const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   const int k4 = p.k4;
   const int hl = p.L5 >> 1, hc = p.L5c >> 1;
@@ -522,7 +542,7 @@ template <bool DAG> static int launch_dhop_cpa(Op* op, DhopParams p) {
     GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_cpa_kernel<DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     configured = true;
   }
-  dhop_cpa_kernel<DAG><<<dim3(unsigned(blocks), ychunks), dim3(threads), smem, op->stream>>>(p);
+  dhop_cpa_kernel<DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -549,13 +569,14 @@ template <class T, bool DAG> static int launch_dhop_pair_t(Op* op, DhopParams p)
     GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_pair_kernel<T, DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     configured = true;
   }
-  dhop_pair_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks), dim3(threads), smem, op->stream>>>(p);
+  dhop_pair_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
 
-int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
-  if (in.prec != op->prec || out.prec != op->prec) {
+static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, const HalfView* in2,
+                             const HalfView* out2, int dag) {
+  if (in.prec != op->prec || out.prec != op->prec || (in2 && (in2->prec != op->prec || out2->prec != op->prec))) {
     set_error("Dhop: field precision differs from the operator's");
     return GB_ERR_BAD_ARG;
   }
@@ -570,6 +591,12 @@ int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
   p.out_norms = out.norms;
   p.links = op->links[out_parity];
   p.nbr = op->nbr[out_parity];
+  p.in2 = in2 ? in2->data : nullptr;
+  p.in2_norms = in2 ? in2->norms : nullptr;
+  p.out2 = out2 ? out2->data : nullptr;
+  p.out2_norms = out2 ? out2->norms : nullptr;
+  p.links2 = in2 ? op->links[1 - out_parity] : nullptr;
+  p.nbr2 = in2 ? op->nbr[1 - out_parity] : nullptr;
   p.n4h = op->half4;
   p.n5 = op->n5();
   p.L5 = op->L5;
@@ -586,6 +613,14 @@ int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
     case GB_F16: return dag ? launch_dhop_pair_t<__half, true>(op, p) : launch_dhop_pair_t<__half, false>(op, p);
   }
   return GB_ERR_BAD_ARG;
+}
+
+int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
+  return launch_dhop_sides(op, in, out, out_parity, nullptr, nullptr, dag);
+}
+
+int launch_dhop_full(Op* op, HalfView in_odd, HalfView out_even, HalfView in_even, HalfView out_odd, int dag) {
+  return launch_dhop_sides(op, in_odd, out_even, 0, &in_even, &out_odd, dag);
 }
 
 }  // namespace gb

@@ -133,6 +133,7 @@ struct HalfView {
 inline HalfView half_view(const Field* f, int parity) { return HalfView{f->half_ptr(parity), f->half_norms(parity), f->prec}; }
 
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag);
+int launch_dhop_full(Op* op, HalfView in_odd, HalfView out_even, HalfView in_even, HalfView out_odd, int dag);
 // chi = diag*phi + upper*P(-/+) psi[s+1] + lower*P(+/-) psi[s-1]   (per rhs block of Ls)
 int launch_m5d(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
                const double* upper, int dag, size_t n5);
