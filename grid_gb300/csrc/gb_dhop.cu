@@ -297,15 +297,21 @@ __device__ __forceinline__ void reconstruct2(Pair12& r, const float2 (&ur)[6], c
   }
 }
 
-// u = U h on both spins; Ux: 9 float4 (re, re, im, im) in shared memory
-__device__ __forceinline__ void su3_mul2(const float4* __restrict__ Ux, const float2 (&hr)[6], const float2 (&hi)[6],
+// Links in shared memory: per 4D site 8 legs x 9 complex as (re, im) float pairs, one
+// 4D site every kLinkStride floats.  The stride (592 B) keeps each site's TMA destination
+// 16-byte aligned and puts the (up to 8) sites one warp touches on distinct bank pairs,
+// so a warp's 64-bit link load is one conflict-free broadcast wavefront.
+constexpr int kLinkStride = 148;
+
+// u = U h on both spins; U: 9 (re, im) in shared memory, broadcast to both lanes
+__device__ __forceinline__ void su3_mul2(const float2* __restrict__ U, const float2 (&hr)[6], const float2 (&hi)[6],
                                          float2 (&ur)[6], float2 (&ui)[6]) {
 #pragma unroll
   for (int a = 0; a < 3; a++) {
-    const float4 w0 = Ux[a * 3 + 0], w1 = Ux[a * 3 + 1], w2 = Ux[a * 3 + 2];
-    const float2 r0 = make_float2(w0.x, w0.y), i0 = make_float2(w0.z, w0.w);
-    const float2 r1 = make_float2(w1.x, w1.y), i1 = make_float2(w1.z, w1.w);
-    const float2 r2 = make_float2(w2.x, w2.y), i2 = make_float2(w2.z, w2.w);
+    const float2 w0 = U[a * 3 + 0], w1 = U[a * 3 + 1], w2 = U[a * 3 + 2];
+    const float2 r0 = f2(w0.x), i0 = f2(w0.y);
+    const float2 r1 = f2(w1.x), i1 = f2(w1.y);
+    const float2 r2 = f2(w2.x), i2 = f2(w2.y);
 #pragma unroll
     for (int sp = 0; sp < 2; sp++) {
       const int o = sp * 3;
@@ -329,38 +335,29 @@ __device__ __forceinline__ void su3_mul2(const float4* __restrict__ Ux, const fl
 
 template <class T, bool DAG, int LEG, bool FIRST>
 __device__ __forceinline__ void dhop_pair_leg(const DhopParams& p, const int (&nb)[8], int sp, size_t np, int hl,
-                                              const float4* Ux, Pair12& acc) {
+                                              const float2* U, Pair12& acc) {
   constexpr int MU = LEG & 3;
   constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
   Pair12 f;
   PairIO<T>::load(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[LEG]) * hl + sp, f);
   float2 hr[6], hi[6], ur[6], ui[6];
   project2<MU, S>(f, hr, hi);
-  su3_mul2(Ux + LEG * 9, hr, hi, ur, ui);
+  su3_mul2(U + LEG * 9, hr, hi, ur, ui);
   reconstruct2<MU, S, FIRST>(acc, ur, ui);
 }
-
-// leg order: GB_DHOP_ORDER 1 visits +mu and -mu back to back (x, y first): the +-x and
-// +-y neighbour rows of a CTA's two x-rows overlap, so the second visit can hit in L1
-#ifndef GB_DHOP_ORDER
-#define GB_DHOP_ORDER 1
-#endif
-
-// shared-memory stride of one 4D site's expanded links, in float4: 72 + 1 so that the
-// sites of one warp fall on different banks
-constexpr int kUxStride = 73;
 
 // resident CTAs of 128 threads per SM the register allocation targets
 #ifndef GB_DHOP_MINB
 #define GB_DHOP_MINB 4
 #endif
 
+// CTA = k4 4D sites x hc pair threads.  Thread (j, sp) computes the 5D sites
+// (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.
 template <class T, bool DAG>
 __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p0) {
   const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
-  float* sraw = reinterpret_cast<float*>(dyn_smem);                                  // k4 * 144 floats
-  float4* sUx = reinterpret_cast<float4*>(dyn_smem + size_t(p.k4) * 144 * sizeof(float));  // k4 * kUxStride
+  float* slink = reinterpret_cast<float*>(dyn_smem);  // k4 * kLinkStride floats
   __shared__ __align__(8) uint64_t bar;
 
   const int t = threadIdx.x;
@@ -371,9 +368,9 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
   if (t == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (t == 0) {
-    const uint32_t bytes = uint32_t(nsite) * 144u * uint32_t(sizeof(float));
-    mbar_expect_tx(&bar, bytes);
-    bulk_g2s(sraw, static_cast<const float*>(p.links) + x0 * 144, bytes, &bar);
+    mbar_expect_tx(&bar, uint32_t(nsite) * 576u);
+    const float* src = static_cast<const float*>(p.links) + x0 * 144;
+    for (int k = 0; k < nsite; k++) bulk_g2s(slink + k * kLinkStride, src + k * 144, 576u, &bar);
   }
   const int j = t / hc;
   const int sp = int(blockIdx.y) * hc + (t - j * hc);
@@ -385,166 +382,24 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
     nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
     nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
   }
-  const bool ok = mbar_wait_bounded(&bar, 0);
-  if (!ok && t == 0) atomicExch(p.err, 1);
-  // expand (re, im) -> (re, re, im, im); every thread takes part in the barrier
-  if (ok) {
-    for (int e = t; e < nsite * 72; e += blockDim.x) {
-      const int site = e / 72, el = e - site * 72;
-      const float re = sraw[2 * e], im = sraw[2 * e + 1];
-      sUx[site * kUxStride + el] = make_float4(re, re, im, im);
-    }
+  // every thread waits for the links, so none leaves while the copy is in flight
+  if (!mbar_wait_bounded(&bar, 0)) {
+    atomicExch(p.err, 1);
+    return;
   }
-  __syncthreads();
-  if (!ok || !active) return;
+  if (!active) return;
   const size_t np = p.n5 >> 1;
-  const float4* Ux = sUx + j * kUxStride;
+  const float2* U = reinterpret_cast<const float2*>(slink + j * kLinkStride);
   Pair12 acc;
-#if GB_DHOP_ORDER == 1
-  dhop_pair_leg<T, DAG, 0, true>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 4, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 1, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 5, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 2, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 6, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 3, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 7, false>(p, nb, sp, np, hl, Ux, acc);
-#else
-  dhop_pair_leg<T, DAG, 0, true>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 1, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 2, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 3, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 4, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 5, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 6, false>(p, nb, sp, np, hl, Ux, acc);
-  dhop_pair_leg<T, DAG, 7, false>(p, nb, sp, np, hl, Ux, acc);
-#endif
+  dhop_pair_leg<T, DAG, 0, true>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 4, false>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 1, false>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 5, false>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 2, false>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 6, false>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 3, false>(p, nb, sp, np, hl, U, acc);
+  dhop_pair_leg<T, DAG, 7, false>(p, nb, sp, np, hl, U, acc);
   PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
-}
-
-// ---------------------------------------------------------------------------------------
-// FP32 with the neighbour spinors of the next legs in flight without holding registers:
-// each thread copies its own neighbour pair (12 x 16 B) of leg l+DEPTH into its own
-// shared-memory slots with cp.async (L2-only, 16 B per copy) while it computes leg l.
-// A thread only reads slots it wrote, so the pipeline needs no CTA barrier.  Slots are
-// laid out [stage][component][thread] so consecutive threads hit consecutive banks.
-// The links arrive by one TMA bulk copy per CTA as in the other kernels.
-// ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
-constexpr int kCpaDepth = 3;
-static int pick_k4_pair(int hc);
-
-template <bool DAG, int LEG>
-__device__ __forceinline__ void dhop_slot_leg(const float4* __restrict__ slot, int nthr, const float4* Ux, Pair12& acc) {
-  constexpr int MU = LEG & 3;
-  constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
-  Pair12 f;
-#pragma unroll
-  for (int k = 0; k < 12; k++) {
-    const float4 v = slot[k * nthr];
-    f.re[k] = make_float2(v.x, v.y);
-    f.im[k] = make_float2(v.z, v.w);
-  }
-  float2 hr[6], hi[6], ur[6], ui[6];
-  project2<MU, S>(f, hr, hi);
-  su3_mul2(Ux + LEG * 9, hr, hi, ur, ui);
-  reconstruct2<MU, S, LEG == 0>(acc, ur, ui);
-}
-
-template <bool DAG>
-__global__ void __launch_bounds__(128, 2) dhop_cpa_kernel(const DhopParams p0) {
-  const DhopParams p = dhop_side(p0);
-  extern __shared__ __align__(128) unsigned char dyn_smem[];
-  const int k4 = p.k4;
-  const int hl = p.L5 >> 1, hc = p.L5c >> 1;
-  const int nthr = blockDim.x;
-  float* sraw = reinterpret_cast<float*>(dyn_smem);                     // k4*144 floats
-  float4* sUx = reinterpret_cast<float4*>(dyn_smem + size_t(k4) * 576);  // k4*kUxStride
-  float4* slots = sUx + size_t(k4) * kUxStride;                         // [kCpaDepth][12][nthr]
-  __shared__ __align__(8) uint64_t bar;
-
-  const int t = threadIdx.x;
-  const int64_t x0 = int64_t(blockIdx.x) * k4;
-  const int nsite = int(min(int64_t(k4), p.n4h - x0));
-  if (t == 0) mbar_init(&bar, 1);
-  __syncthreads();
-  if (t == 0) {
-    const uint32_t bytes = uint32_t(nsite) * 576u;
-    mbar_expect_tx(&bar, bytes);
-    bulk_g2s(sraw, static_cast<const float*>(p.links) + x0 * 144, bytes, &bar);
-  }
-  const int j = t / hc;
-  const int sp = int(blockIdx.y) * hc + (t - j * hc);
-  const bool active = j < nsite && sp < hl;
-  const size_t np = p.n5 >> 1;
-  const float4* gin = static_cast<const float4*>(p.in);
-  int nb[8];
-  if (active) {
-    const int4* q = reinterpret_cast<const int4*>(p.nbr + (x0 + j) * 8);
-    const int4 a = __ldg(q), b = __ldg(q + 1);
-    nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
-    nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
-  }
-  auto issue = [&](int leg, int stage) {
-    if (active) {
-      const float4* src = gin + size_t(nb[leg]) * hl + sp;
-      float4* dst = slots + size_t(stage) * 12 * nthr + t;
-#pragma unroll
-      for (int k = 0; k < 12; k++) cp_async16(dst + size_t(k) * nthr, src + size_t(k) * np);
-    }
-    cp_async_commit();  // empty groups keep the per-thread group count uniform
-  };
-  issue(0, 0);
-  issue(1, 1);
-  issue(2, 2);
-  const bool ok = mbar_wait_bounded(&bar, 0);
-  if (!ok && t == 0) atomicExch(p.err, 1);
-  if (ok) {
-    for (int e = t; e < nsite * 72; e += nthr) {
-      const int site = e / 72, el = e - site * 72;
-      const float re = sraw[2 * e], im = sraw[2 * e + 1];
-      sUx[site * kUxStride + el] = make_float4(re, re, im, im);
-    }
-  }
-  __syncthreads();
-  const float4* Ux = sUx + j * kUxStride;
-  Pair12 acc;
-#define GB_CPA_LEG(L, WAITN)                                                       \
-  {                                                                                \
-    cp_async_wait<WAITN>();                                                        \
-    if (ok && active) dhop_slot_leg<DAG, L>(slots + size_t((L) % kCpaDepth) * 12 * nthr + t, nthr, Ux, acc); \
-    if ((L) + kCpaDepth < 8) issue((L) + kCpaDepth, (L) % kCpaDepth);              \
-  }
-  // groups in flight after leg L's issue: 3 until the last issues, then 2, 1, 0
-  GB_CPA_LEG(0, 2) GB_CPA_LEG(1, 2) GB_CPA_LEG(2, 2) GB_CPA_LEG(3, 2) GB_CPA_LEG(4, 2)
-  GB_CPA_LEG(5, 2) GB_CPA_LEG(6, 1) GB_CPA_LEG(7, 0)
-#undef GB_CPA_LEG
-  if (ok && active) PairIO<float>::store(p.out, nullptr, np, size_t(x0 + j) * hl + sp, acc);
-}
-
-template <bool DAG> static int launch_dhop_cpa(Op* op, DhopParams p) {
-  p.L5c = p.L5 > 256 ? 256 : p.L5;
-  const int hc = p.L5c / 2;
-  p.k4 = pick_k4_pair(hc);
-  const int threads = hc * p.k4;
-  const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
-  const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
-  const size_t smem = size_t(p.k4) * (576 + kUxStride * 16) + size_t(kCpaDepth) * 12 * threads * 16;
-  static bool configured = false;
-  if (!configured) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_cpa_kernel<DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    configured = true;
-  }
-  dhop_cpa_kernel<DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
-  GB_CHECK_CUDA(cudaGetLastError());
-  return GB_OK;
 }
 
 // CTA = k4 4D sites x (L5c/2) pair threads, about 128 threads
@@ -553,7 +408,7 @@ static int pick_k4_pair(int hc) {
   int k4 = 128 / hc;
   while (k4 > 1 && (hc * k4) % 32 != 0) k4--;
   if ((hc * k4) % 32 != 0) k4 = 128 / hc;
-  if (k4 > 48) k4 = 48;  // shared memory: 48 x (576 + 1168) B
+  if (k4 > 64) k4 = 64;  // shared memory: 64 x 592 B
   return k4 < 1 ? 1 : k4;
 }
 
@@ -563,12 +418,7 @@ template <class T, bool DAG> static int launch_dhop_pair_t(Op* op, DhopParams p)
   const int threads = (p.L5c / 2) * p.k4;
   const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
   const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
-  const size_t smem = size_t(p.k4) * (144 * sizeof(float) + kUxStride * sizeof(float4));
-  static bool configured = false;
-  if (!configured) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_pair_kernel<T, DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    configured = true;
-  }
+  const size_t smem = size_t(p.k4) * kLinkStride * sizeof(float);
   dhop_pair_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
@@ -605,11 +455,7 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
   p.err = op->d_err;
   switch (op->prec) {
     case GB_F64: return dag ? launch_dhop_t<double, true>(op, p) : launch_dhop_t<double, false>(op, p);
-#ifdef GB_DHOP_CPA
-    case GB_F32: return dag ? launch_dhop_cpa<true>(op, p) : launch_dhop_cpa<false>(op, p);
-#else
     case GB_F32: return dag ? launch_dhop_pair_t<float, true>(op, p) : launch_dhop_pair_t<float, false>(op, p);
-#endif
     case GB_F16: return dag ? launch_dhop_pair_t<__half, true>(op, p) : launch_dhop_pair_t<__half, false>(op, p);
   }
   return GB_ERR_BAD_ARG;
