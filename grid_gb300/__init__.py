@@ -10,6 +10,6 @@ from .api import (  # noqa: F401
     FermionField, WilsonFermion, MobiusFermion, MdagMLinearOperator, SchurDiagMooeeOperator,
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
-    antiperiodic_t, periodic, set_device, PinnedArray, norm2, innerProduct, axpy, axpby, axpy_norm,
+    antiperiodic_t, periodic, set_device, PinnedArray, Stream, norm2, innerProduct, axpy, axpby, axpy_norm,
     pickCheckerboard, setCheckerboard, Server, Request, make_request, request_bytes,
 )

@@ -121,6 +121,13 @@ _proto("gb_op_event_record", [_vp, _i])
 _proto("gb_op_event_elapsed", [_vp, _i, _i, _dp])
 _proto("gb_host_alloc", [_sz, C.POINTER(_vp)])
 _proto("gb_host_free", [_vp])
+_proto("gb_stream_create", [C.POINTER(_vp)])
+_proto("gb_stream_destroy", [_vp])
+_proto("gb_Dminus", [_vp, _vp, _vp, _i])
+for _n in ("gb_import_physical_source", "gb_import_unphysical_fermion"):
+    _proto(_n, [_vp, _vp, _i, _vp])
+for _n in ("gb_export_physical_solution", "gb_export_physical_source"):
+    _proto(_n, [_vp, _vp, _vp, _i])
 
 
 def set_device(d: int):
@@ -141,6 +148,21 @@ class PinnedArray:
         if getattr(self, "ptr", None):
             self.array = None
             lib.gb_host_free(self.ptr)
+            self.ptr = None
+
+
+class Stream:
+    """A non-blocking CUDA stream owned by the library (for operators that should not use
+    the legacy default stream); `ptr` is the cudaStream_t value."""
+
+    def __init__(self):
+        p = _vp()
+        _check(lib.gb_stream_create(C.byref(p)))
+        self.ptr = p.value
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib.gb_stream_destroy(_vp(self.ptr))
             self.ptr = None
 
 
@@ -410,6 +432,33 @@ class MobiusFermion(_FermionOperator):
         _check(lib.gb_op_cayley_coeffs(self.h, _dptr(out)))
         names = ["bs", "cs", "bee", "cee", "dee", "lee", "leem", "uee", "ueem"]
         return {n: out[k * self.Ls:(k + 1) * self.Ls].copy() for k, n in enumerate(names)}
+
+    # CayleyFermion5D (CayleyFermion5DImplementation.h:57-153)
+    def Dminus(self, i, o): _check(lib.gb_Dminus(self.h, i.h, o.h, 0))
+    def DminusDag(self, i, o): _check(lib.gb_Dminus(self.h, i.h, o.h, 1))
+
+    def _surface_in(self, fn, src4d, out5d):
+        a = np.ascontiguousarray(src4d, dtype=np.complex128).reshape(-1)
+        if a.size != self.vol4 * 12 * self.nrhs:
+            raise GridError(1, "4D field has the wrong size")
+        _check(fn(self.h, a.ctypes.data, 0, out5d.h))
+
+    def _surface_out(self, fn, in5d):
+        out = np.empty(self.vol4 * 12 * self.nrhs, dtype=np.complex128)
+        _check(fn(self.h, in5d.h, out.ctypes.data, 0))
+        return out
+
+    def ImportPhysicalFermionSource(self, src4d, out5d):
+        self._surface_in(lib.gb_import_physical_source, src4d, out5d)
+
+    def ImportUnphysicalFermion(self, src4d, out5d):
+        self._surface_in(lib.gb_import_unphysical_fermion, src4d, out5d)
+
+    def ExportPhysicalFermionSolution(self, sol5d):
+        return self._surface_out(lib.gb_export_physical_solution, sol5d)
+
+    def ExportPhysicalFermionSource(self, src5d):
+        return self._surface_out(lib.gb_export_physical_source, src5d)
 
 
 # ---- linear operators and solvers -----------------------------------------------------

@@ -42,7 +42,7 @@ static int check_op(const Op* op) {
 }
 static int check_conf(const Field* a, const Field* b) {
   if (!a || !b) { set_error("null field"); return GB_ERR_BAD_ARG; }
-  if (a->op != b->op || a->n5 != b->n5) { set_error("fields are not conformable"); return GB_ERR_BAD_ARG; }
+  if (!ops_conformable(a->op, b->op) || a->n5 != b->n5) { set_error("fields are not conformable"); return GB_ERR_BAD_ARG; }
   return GB_OK;
 }
 static int check_subset(const Field* f, int subset, const char* what) {
@@ -270,6 +270,7 @@ int op_meooe(Op* op, Field* in, Field* out, int dag) {
 }
 
 int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
+  if (in->full() != out->full()) { set_error("Mooee: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
   if (op->kind == 0) {
     if (z) return field_axpby(out, op->diag_mass, zc, in, z);
@@ -281,6 +282,7 @@ int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
 }
 
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
+  if (in->full() != out->full()) { set_error("MooeeInv: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
   if (op->kind == 0) return field_scale(out, 1.0 / op->diag_mass, in);
   const int halves = in->full() ? 2 : 1;
@@ -340,6 +342,18 @@ int op_mdagm(Op* op, Field* in, Field* out) {
   GB_TRY(ws_get(op, GB_FULL, in->prec, WS_MDAGM, &t));
   GB_TRY(op_m(op, in, t, 0));
   return op_m(op, t, out, 1);
+}
+
+// Dminus / DminusDag (CayleyFermion5DImplementation.h:131-153):
+// chi = psi - cs (DW psi), DW = Dhop + (4 - M5); cs = c for every s of a Moebius operator.
+int op_dminus(Op* op, Field* in, Field* out, int dag) {
+  if (op->kind != 1) { set_error("Dminus: Moebius operators only"); return GB_ERR_UNSUPPORTED; }
+  if (!in->full() || !out->full()) { set_error("Dminus: full fields expected"); return GB_ERR_BAD_PARITY; }
+  Field* t;
+  GB_TRY(ws_get(op, GB_FULL, in->prec, WS_DMINUS, &t));
+  GB_TRY(op_dhop_full(op, in, t, dag));
+  const double c = op->cs[0];
+  return field_axpby(out, 1.0 - c * (4.0 - op->M5), -c, in, t);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -745,7 +759,7 @@ int gb_field_set_checkerboard(gb_field_t full, gb_field_t half) {
 #define GB_OP_PRE(op, in, out)                                                     \
   GB_TRY(check_op(op));                                                            \
   GB_TRY(check_conf(in, out));                                                     \
-  if (in->op != op) { set_error("field belongs to another operator"); return GB_ERR_BAD_ARG; } \
+  if (!ops_conformable(in->op, op)) { set_error("field is not conformable to the operator"); return GB_ERR_BAD_ARG; } \
   if (in == out) { set_error("in and out must be distinct fields"); return GB_ERR_BAD_ARG; }
 
 int gb_M(gb_op_t op, gb_field_t in, gb_field_t out) { GB_OP_PRE(op, in, out); return op_m(op, in, out, 0); }
@@ -778,6 +792,64 @@ int gb_MpcDagMpc(gb_op_t op, gb_field_t in, gb_field_t out) {
   GB_TRY(check_subset(in, GB_ODD, "MpcDagMpc"));
   out->subset = GB_ODD;
   return op_mpcdagmpc(op, in, out);
+}
+int gb_Dminus(gb_op_t op, gb_field_t in, gb_field_t out, int dag) {
+  GB_OP_PRE(op, in, out);
+  return op_dminus(op, in, out, dag ? 1 : 0);
+}
+
+// ---- 4D <-> 5D surface fields (CayleyFermion5DImplementation.h:57-129) ----
+static int surface_checks(gb_op_t op, gb_field_t f, const double* p4) {
+  GB_TRY(check_op(op));
+  if (!f || !p4) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (op->kind != 1) { set_error("physical fields: Moebius operators only"); return GB_ERR_UNSUPPORTED; }
+  if (!ops_conformable(f->op, op)) { set_error("field is not conformable to the operator"); return GB_ERR_BAD_ARG; }
+  if (!f->full()) { set_error("physical fields: a full 5D field expected"); return GB_ERR_BAD_PARITY; }
+  return GB_OK;
+}
+static size_t surface_bytes(const Op* op) { return size_t(op->vol4) * op->nrhs_user * 24 * sizeof(double); }
+
+static int import_surface(gb_op_t op, const double* src4d, int on_device, gb_field_t out, bool physical) {
+  GB_TRY(surface_checks(op, out, src4d));
+  const double* d = src4d;
+  if (!on_device) {
+    GB_TRY(ensure_stage(op, surface_bytes(op)));
+    GB_CHECK_CUDA(cudaMemcpyAsync(op->d_stage, src4d, surface_bytes(op), cudaMemcpyHostToDevice, op->stream));
+    d = op->d_stage;
+  }
+  Field* t = out;
+  if (physical) GB_TRY(ws_get(op, GB_FULL, out->prec, WS_PHYS, &t));
+  GB_TRY(field_zero(t));
+  GB_TRY(launch_surface_insert(op, d, half_view(t, 0), half_view(t, 1)));
+  if (physical) GB_TRY(op_dminus(op, t, out, 0));
+  if (!on_device) GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  return GB_OK;
+}
+static int export_surface(gb_op_t op, gb_field_t in, double* out4d, int on_device, int solution) {
+  GB_TRY(surface_checks(op, in, out4d));
+  double* d = out4d;
+  if (!on_device) {
+    GB_TRY(ensure_stage(op, surface_bytes(op)));
+    d = op->d_stage;
+  }
+  GB_TRY(launch_surface_extract(op, half_view(in, 0), half_view(in, 1), d, solution));
+  if (!on_device) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(out4d, d, surface_bytes(op), cudaMemcpyDeviceToHost, op->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  }
+  return GB_OK;
+}
+int gb_import_physical_source(gb_op_t op, const double* src4d, int on_device, gb_field_t out5d) {
+  return import_surface(op, src4d, on_device, out5d, true);
+}
+int gb_import_unphysical_fermion(gb_op_t op, const double* src4d, int on_device, gb_field_t out5d) {
+  return import_surface(op, src4d, on_device, out5d, false);
+}
+int gb_export_physical_solution(gb_op_t op, gb_field_t sol5d, double* out4d, int on_device) {
+  return export_surface(op, sol5d, out4d, on_device, 1);
+}
+int gb_export_physical_source(gb_op_t op, gb_field_t src5d, double* out4d, int on_device) {
+  return export_surface(op, src5d, out4d, on_device, 0);
 }
 
 }  // extern "C"

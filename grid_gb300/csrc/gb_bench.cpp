@@ -82,5 +82,16 @@ int gb_host_free(void* ptr) {
   GB_CHECK_CUDA(cudaFreeHost(ptr));
   return GB_OK;
 }
+int gb_stream_create(void** stream) {
+  if (!stream) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  cudaStream_t s = nullptr;
+  GB_CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *stream = s;
+  return GB_OK;
+}
+int gb_stream_destroy(void* stream) {
+  if (stream) GB_CHECK_CUDA(cudaStreamDestroy(static_cast<cudaStream_t>(stream)));
+  return GB_OK;
+}
 
 }  // extern "C"

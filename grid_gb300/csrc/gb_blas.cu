@@ -522,6 +522,76 @@ int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon
 }
 
 // ---------------------------------------------------------------------------------------
+// 4D <-> 5D surface fields of a Moebius operator (CayleyFermion5DImplementation.h:57-129).
+// One thread per (rhs, 4D site) of a canonical 4D field c4[rhs][site][12].  INSERT writes
+// spins 0,1 (P+) of the 4D spinor at s = 0 and spins 2,3 (P-) at s = Ls-1, zeros in the
+// other halves of those two sites, and leaves every other s untouched (the caller zeroes
+// the field first).  EXTRACT reads the 4D spinor back: with `solution` spins 0,1 come from
+// s = Ls-1 and spins 2,3 from s = 0 (ExportPhysicalFermionSolution), otherwise the
+// reverse (ExportPhysicalFermionSource).
+// ---------------------------------------------------------------------------------------
+template <class T, bool INSERT>
+__global__ void __launch_bounds__(256) surface_kernel(const GeoParams g, double* c4, void* even, float* even_n,
+                                                      void* odd, float* odd_n, int solution) {
+  using R = typename Arith<T>::type;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= size_t(g.vol4) * g.nrhs_user) return;
+  const int rhs = int(t / size_t(g.vol4));
+  const int64_t site = int64_t(t - size_t(rhs) * g.vol4);
+  int sum = 0;
+  {
+    int64_t r = site;
+    for (int k = 0; k < 4; k++) { sum += int(r % g.L[k]); r /= g.L[k]; }
+  }
+  const int parity = sum & 1;
+  void* base = parity ? odd : even;
+  float* nrm = parity ? odd_n : even_n;
+  const size_t n5 = size_t(g.half4) * g.L5;
+  const size_t i0 = size_t(site >> 1) * g.L5 + size_t(rhs) * g.Ls;  // s = 0
+  const size_t i1 = i0 + g.Ls - 1;                                   // s = Ls-1
+  double2* c = reinterpret_cast<double2*>(c4) + (size_t(rhs) * g.vol4 + site) * 12;
+  Spinor<R> a, b;
+  if (INSERT) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const double2 v = c[k];
+      const bool up = k < 6;
+      a.re[k] = up ? R(v.x) : R(0); a.im[k] = up ? R(v.y) : R(0);
+      b.re[k] = up ? R(0) : R(v.x); b.im[k] = up ? R(0) : R(v.y);
+    }
+    SpinorIO<T>::store(base, nrm, n5, i0, a);
+    SpinorIO<T>::store(base, nrm, n5, i1, b);
+  } else {
+    SpinorIO<T>::load(base, nrm, n5, i0, a);
+    SpinorIO<T>::load(base, nrm, n5, i1, b);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const bool from_last = (k < 6) == (solution != 0);
+      c[k] = from_last ? make_double2(double(b.re[k]), double(b.im[k])) : make_double2(double(a.re[k]), double(a.im[k]));
+    }
+  }
+}
+
+template <bool INSERT>
+static int surface_p(Op* op, double* c4, HalfView even, HalfView odd, int solution) {
+  const GeoParams g = geo(op);
+  const size_t n = size_t(op->vol4) * op->nrhs_user;
+  switch (even.prec) {
+    case GB_F64: surface_kernel<double, INSERT><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, solution); break;
+    case GB_F32: surface_kernel<float, INSERT><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, solution); break;
+    case GB_F16: surface_kernel<__half, INSERT><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, solution); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+int launch_surface_insert(Op* op, const double* c4, HalfView even, HalfView odd) {
+  return surface_p<true>(op, const_cast<double*>(c4), even, odd, 0);
+}
+int launch_surface_extract(Op* op, HalfView even, HalfView odd, double* c4, int solution) {
+  return surface_p<false>(op, c4, even, odd, solution);
+}
+
+// ---------------------------------------------------------------------------------------
 // DoubleStore (Grid/qcd/action/fermion/WilsonImpl.h:127-171) with ImportGauge's -1/2
 // (WilsonFermion5DImplementation.h:149-180), for the links of output parity p.
 // ---------------------------------------------------------------------------------------

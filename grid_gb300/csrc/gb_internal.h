@@ -2,13 +2,14 @@
 //
 // Device layout of a fermion field (one checkerboard, "half"):
 //   5D site index   i = s5 + L5 * x_cb,  s5 = rhs*Ls + s,  x_cb = site4 >> 1
-//   FP64            12 planes of double2, plane k = complex component spin*3+colour
-//   FP32            6 planes of float4,  plane g = complex components 2g, 2g+1
-//   FP16            3 planes of 16-byte vectors of 8 halves (4 complex components each)
-//                   plus one float norm per 5D site
-//   Each plane holds n5 = half_sites4 * L5 vectors; a full field is the even half
-//   followed by the odd half.  Planes 0..(P/2-1) hold spins 0,1 (the P+ chirality),
-//   the rest spins 2,3 (P-), so the 5D chiral projections read half the planes.
+//   FP64            12 planes of n5 double2, plane k = complex component spin*3+colour
+//   FP32            12 planes of n5/2 float4: component k of the site pair (i, i+1),
+//                   i even, as (re_i, re_i+1, im_i, im_i+1)
+//   FP16            6 planes of n5/2 16-byte vectors: components 2q, 2q+1 of the site
+//                   pair, each site scaled by its own float norm (one per 5D site)
+//   A full field is the even half followed by the odd half.  The first half of the
+//   planes holds spins 0,1 (the P+ chirality), the rest spins 2,3 (P-), so the 5D
+//   chiral projections read half the planes.
 // Gauge links (per output parity p): [x_cb][leg 0..7][3][3] complex in link precision,
 //   legs 0..3 = Ud_mu(x) (forward), 4..7 = Ud_{mu}(x-mu)^dagger (backward), with the
 //   -1/2 and boundary phases folded in (Grid's DoubleStore).  Neighbour table per parity:
@@ -103,6 +104,17 @@ struct Op {
   size_t link_bytes_per_parity() const;
 };
 
+// Fields created on one operator may be used with another of the same geometry (4D
+// extents, Ls, right-hand sides) on the same stream: the device layout is identical and
+// the work of both is ordered on that one stream.
+inline bool ops_conformable(const Op* a, const Op* b) {
+  if (a == b) return true;
+  if (!a || !b) return false;
+  for (int k = 0; k < 4; k++)
+    if (a->dims[k] != b->dims[k]) return false;
+  return a->Ls == b->Ls && a->nrhs == b->nrhs && a->nrhs_user == b->nrhs_user && a->stream == b->stream;
+}
+
 struct Field {
   Op* op = nullptr;
   int subset = GB_EVEN;
@@ -169,6 +181,9 @@ inline int red_parts(Op* op, int prec) {
 int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full);
 int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon_is_full);
 int launch_double_store(Op* op, const double* U_canon, int parity);
+// 4D <-> 5D surface fields (Moebius): canonical FP64 4D field in device memory
+int launch_surface_insert(Op* op, const double* c4, HalfView even, HalfView odd);
+int launch_surface_extract(Op* op, HalfView even, HalfView odd, double* c4, int solution);
 int build_neighbours(Op* op);
 
 // CG kernels (gb_blas.cu)

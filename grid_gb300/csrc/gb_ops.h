@@ -14,7 +14,8 @@ enum {
   WS_SCHUR_A = 16, WS_SCHUR_B = 17, WS_SCHUR_C = 18, WS_SCHUR_D = 19,
 };
 enum { WS_M_DIN = 0, WS_M_T = 1, WS_MDAGM = 2, WS_FCG_P = 3, WS_FCG_MMP = 4, WS_FCG_R = 5, WS_FCG_T = 6,
-       WS_FRU_PF = 7, WS_FRU_MMPF = 8, WS_FRU_RF = 9, WS_FRU_XF = 10, WS_SCHUR_RES = 11 };
+       WS_FRU_PF = 7, WS_FRU_MMPF = 8, WS_FRU_RF = 9, WS_FRU_XF = 10, WS_SCHUR_RES = 11, WS_DMINUS = 12,
+       WS_PHYS = 13 };
 
 int field_alloc(Op* op, int subset, int prec, Field** out);
 void field_free(Field* f);
@@ -45,6 +46,7 @@ int op_mpc(Op* op, Field* in, Field* out, int dag);
 int op_mpcdagmpc(Op* op, Field* in, Field* out);
 int op_m(Op* op, Field* in, Field* out, int dag);
 int op_mdagm(Op* op, Field* in, Field* out);
+int op_dminus(Op* op, Field* in, Field* out, int dag);
 
 // kind 0: MdagM on full fields; kind 1: MpcDagMpc on odd half fields
 inline int op_hermop(Op* op, int kind, Field* in, Field* out) {

@@ -143,10 +143,19 @@ struct ChunkRunner {
 // a private stream for a graph-captured solve on an operator bound to the legacy
 // default stream (which cannot be captured); restored and released on scope exit
 struct SolveStream {
-  Op* ops[2];
-  cudaStream_t saved[2];
+  // the solver's operators and the operators owning the caller's fields (which may be
+  // other operators of the same geometry and stream): all move to the private stream
+  Op* ops[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t saved[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t own = nullptr;
-  SolveStream(Op* a, Op* b, bool want) : ops{a, b}, saved{a ? a->stream : nullptr, b ? b->stream : nullptr} {
+  SolveStream(Op* a, Op* b, Field* f0, Field* f1, bool want) {
+    Op* cand[4] = {a, b, f0 ? f0->op : nullptr, f1 ? f1->op : nullptr};
+    int n = 0;
+    for (Op* o : cand) {
+      bool seen = !o;
+      for (int i = 0; i < n; i++) seen = seen || ops[i] == o;
+      if (!seen) { ops[n] = o; saved[n] = o->stream; n++; }
+    }
     if (!want || (a && a->stream)) return;
     cudaDeviceSynchronize();
     if (cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking) != cudaSuccess) { own = nullptr; return; }
@@ -155,7 +164,7 @@ struct SolveStream {
   ~SolveStream() {
     if (!own) return;
     cudaStreamSynchronize(own);
-    for (int i = 0; i < 2; i++) if (ops[i]) ops[i]->stream = saved[i];
+    for (int i = 0; i < 4; i++) if (ops[i]) ops[i]->stream = saved[i];
     cudaStreamDestroy(own);
   }
 };
@@ -394,7 +403,10 @@ void gb_cg_params_default(gb_cg_params* p) {
 static int solve_checks(gb_op_t op, gb_field_t a, gb_field_t b, const gb_cg_params* p, gb_cg_result* r) {
   if (!op || !a || !b || !p || !r) { set_error("null argument"); return GB_ERR_BAD_ARG; }
   if (!op->gauge_loaded) { set_error("operator has no gauge field"); return GB_ERR_BAD_ARG; }
-  if (a->op != op || b->op != op) { set_error("field belongs to another operator"); return GB_ERR_BAD_ARG; }
+  if (!ops_conformable(a->op, op) || !ops_conformable(b->op, op)) {
+    set_error("field is not conformable to the operator");
+    return GB_ERR_BAD_ARG;
+  }
   if (a->prec != op->prec || b->prec != op->prec) { set_error("field precision differs from the operator's"); return GB_ERR_BAD_ARG; }
   if (p->tolerance <= 0 || p->max_iterations < 1) { set_error("bad tolerance or max_iterations"); return GB_ERR_BAD_ARG; }
   std::memset(r, 0, sizeof(*r));
@@ -409,7 +421,7 @@ static int finish(int rc, const gb_cg_params* p) {
 int gb_cg_mdagm(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* p, gb_cg_result* res) {
   GB_TRY(solve_checks(op, src, psi, p, res));
   if (!src->full() || !psi->full()) { set_error("MdagM CG: full fields expected"); return GB_ERR_BAD_PARITY; }
-  SolveStream ss(op, nullptr, p->use_graphs != 0);
+  SolveStream ss(op, nullptr, src, psi, p->use_graphs != 0);
   return finish(cg_solve(op, 0, src, psi, p, res), p);
 }
 
@@ -417,7 +429,7 @@ int gb_cg_schur(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* 
   GB_TRY(solve_checks(op, src, psi, p, res));
   if (src->subset != GB_ODD) { set_error("Schur CG: odd source expected"); return GB_ERR_BAD_PARITY; }
   psi->subset = GB_ODD;
-  SolveStream ss(op, nullptr, p->use_graphs != 0);
+  SolveStream ss(op, nullptr, src, psi, p->use_graphs != 0);
   return finish(cg_solve(op, 1, src, psi, p, res), p);
 }
 
@@ -438,7 +450,7 @@ int gb_cg_reliable(gb_op_t op_d, gb_op_t op_lo, int kind, gb_field_t src, gb_fie
   if (kind == 0 && (!src->full() || !psi->full())) { set_error("reliable CG: full fields expected"); return GB_ERR_BAD_PARITY; }
   if (kind == 1 && src->subset != GB_ODD) { set_error("reliable CG: odd source expected"); return GB_ERR_BAD_PARITY; }
   if (kind == 1) psi->subset = GB_ODD;
-  SolveStream ss(op_d, op_lo, p->use_graphs != 0);
+  SolveStream ss(op_d, op_lo, src, psi, p->use_graphs != 0);
   return finish(cg_reliable(op_d, op_lo, kind, src, psi, p, res), p);
 }
 
@@ -447,7 +459,7 @@ int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, co
   GB_TRY(solve_checks(op, src, sol, p, res));
   if (!src->full() || !sol->full()) { set_error("Schur solve: full fields expected"); return GB_ERR_BAD_PARITY; }
   if (op_lo && (op->prec != GB_F64 || op_lo->prec == GB_F64)) { set_error("Schur solve: mixed needs FP64 op and FP32/FP16 op_lo"); return GB_ERR_BAD_ARG; }
-  SolveStream ss(op, op_lo, p->use_graphs != 0);
+  SolveStream ss(op, op_lo, src, sol, p->use_graphs != 0);
   return finish(schur_solve(op, op_lo, src, sol, p, res, unprec_resid), p);
 }
 

@@ -14,7 +14,7 @@
  * A multi-RHS operator (nrhs > 1) takes nrhs such fields back to back.
  *
  * Device layout is private to the library: structure-of-arrays, 5D site fastest, in
- * 16-byte vectors (see the design doc in the source tree).
+ * 16-byte vectors.
  */
 #ifndef GBDWF_H
 #define GBDWF_H
@@ -84,6 +84,9 @@ int gb_op_cayley_coeffs(gb_op_t op, double* out);
 /* ---- fields ---------------------------------------------------------------------
  * Lattice<vobj>(grid) on the op's FermionGrid (GB_FULL) or FermionRedBlackGrid
  * (GB_EVEN / GB_ODD).  precision may differ from the op's (for precisionChange).
+ * A field may be used with any operator of the same geometry (4D extents, Ls, nrhs) on
+ * the same stream as the one that created it (Grid: fields belong to a grid, not to an
+ * operator); the operator that created it must outlive it.
  */
 int gb_field_create(gb_op_t op, int subset, int precision, gb_field_t* out);
 int gb_field_destroy(gb_field_t f);
@@ -144,6 +147,23 @@ int gb_MooeeInvDag(gb_op_t op, gb_field_t in, gb_field_t out);
 int gb_Mpc(gb_op_t op, gb_field_t in, gb_field_t out);
 int gb_MpcDag(gb_op_t op, gb_field_t in, gb_field_t out);
 int gb_MpcDagMpc(gb_op_t op, gb_field_t in, gb_field_t out);
+/* CayleyFermion5D::Dminus / DminusDag (CayleyFermion5DImplementation.h:131-153), full
+ * fields: chi = psi - c (DW psi), DW = Dhop + (4 - M5).  Moebius operators only. */
+int gb_Dminus(gb_op_t op, gb_field_t in, gb_field_t out, int dag);
+
+/* ---- 4D <-> 5D surface fields (CayleyFermion5DImplementation.h:57-129) ------------
+ * The 4D side is a canonical FP64 4D fermion (nrhs fields back to back), in host memory
+ * (on_device = 0; the call returns when it is done) or device memory (on_device = 1; the
+ * work is queued on the operator's stream).  The 5D side is a full field.  Moebius only.
+ *   import_physical_source    ImportPhysicalFermionSource: P+ src at s=0, P- src at
+ *                             s=Ls-1, then Dminus (P+- = (1 +- gamma5)/2)
+ *   import_unphysical_fermion ImportUnphysicalFermion: the same without Dminus
+ *   export_physical_solution  ExportPhysicalFermionSolution: P- psi(0) + P+ psi(Ls-1)
+ *   export_physical_source    ExportPhysicalFermionSource:   P+ psi(0) + P- psi(Ls-1)  */
+int gb_import_physical_source(gb_op_t op, const double* src4d, int on_device, gb_field_t out5d);
+int gb_import_unphysical_fermion(gb_op_t op, const double* src4d, int on_device, gb_field_t out5d);
+int gb_export_physical_solution(gb_op_t op, gb_field_t sol5d, double* out4d, int on_device);
+int gb_export_physical_source(gb_op_t op, gb_field_t src5d, double* out4d, int on_device);
 
 /* ---- solvers ------------------------------------------------------------------- */
 typedef struct {
@@ -252,6 +272,8 @@ int gb_request_bytes(const gb_request* r, size_t* bytes); /* the admission estim
 
 /* ---- device, stream and host-buffer utilities ------------------------------------ */
 int gb_set_device(int device);                       /* cudaSetDevice for this thread        */
+int gb_stream_create(void** stream);                 /* a non-blocking CUDA stream           */
+int gb_stream_destroy(void* stream);
 int gb_op_sync(gb_op_t op);                          /* wait for the op's stream             */
 int gb_op_event_record(gb_op_t op, int slot);        /* slot in [0, 16): event on op stream  */
 int gb_op_event_elapsed(gb_op_t op, int slot0, int slot1, double* ms); /* waits for slot1   */

@@ -1,0 +1,749 @@
+/* gbgrid.h -- Grid-shaped C++ adapter over the C ABI of gbdwf.h (header only).
+ *
+ * Code written against Grid's fermion-operator path compiles against these classes
+ * unchanged for that path: grids from SpaceTimeGrid, LatticeFermion / LatticeGaugeField,
+ * WilsonFermion / MobiusFermion (FermionOperator interface), MdagMLinearOperator,
+ * SchurDiagMooeeOperator, ConjugateGradient, ConjugateGradientReliableUpdate and
+ * SchurRedBlackDiagMooeeSolve, plus norm2 / innerProduct / axpy / axpby / axpy_norm /
+ * pickCheckerboard / setCheckerboard / precisionChange.  Every call forwards to the C ABI;
+ * the fields live in device memory.  Reference interfaces:
+ *   Grid/qcd/action/fermion/FermionOperator.h:40-192, MobiusFermion.h:45-56,
+ *   WilsonFermion.h:139-142, Grid/algorithms/LinearOperator.h:44-105,286-349,590-616,
+ *   Grid/algorithms/iterative/ConjugateGradient.h:55-257, ConjugateGradientReliableUpdate.h,
+ *   SchurRedBlack.h:373-436, Grid/qcd/utils/SpaceTimeGrid.cc:49-80.
+ *
+ * Differences from Grid, by design:
+ *   - errors throw Grid::GridError carrying the C status (Grid asserts);
+ *   - fields of one geometry (4D extents, Ls) are created through one hidden "context"
+ *     operator of that geometry, so they work with every operator built on their grid;
+ *     all adapter objects share one non-blocking stream, so their work is ordered;
+ *   - random fields come from the library's seeded generators (Grid's RNG streams
+ *     cannot be reproduced); gaussian() draws N(0,1) per real component;
+ *   - single process, single GPU: no MPI decomposition (simd / mpi layouts are accepted
+ *     and ignored).
+ */
+#ifndef GBGRID_H
+#define GBGRID_H
+
+#ifndef __cplusplus
+#error "gbgrid.h is C++; C callers use gbdwf.h"
+#endif
+
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gbdwf.h"
+
+namespace Grid {
+
+typedef double RealD;
+typedef float RealF;
+typedef RealD Real;
+typedef std::complex<double> ComplexD;
+typedef ComplexD Complex;
+typedef int32_t Integer;
+typedef std::vector<int> Coordinate;
+
+enum { Even = 0, Odd = 1 };
+enum { DaggerNo = 0, DaggerYes = 1 };
+static constexpr int Nd = 4, Nc = 3, Ns = 4;
+struct Zero {};
+
+class GridError : public std::runtime_error {
+ public:
+  int status;
+  GridError(int st, const std::string& msg) : std::runtime_error(msg), status(st) {}
+};
+
+namespace gbdetail {
+inline void check(int rc, const char* what) {
+  if (rc != GB_OK) {
+    const char* e = gb_last_error();
+    throw GridError(rc, std::string(what) + ": " + (e && *e ? e : gb_status_string(rc)));
+  }
+}
+// the stream shared by every operator and field of the adapter
+inline void* stream() {
+  static void* s = [] {
+    void* p = nullptr;
+    check(gb_stream_create(&p), "gb_stream_create");
+    return p;
+  }();
+  return s;
+}
+// One operator per geometry creates the device fields of every grid with that geometry.
+// It is never destroyed: grids, like Grid's, live until the process ends.
+inline gb_op_t context(const Coordinate& d4, int Ls) {
+  static std::mutex m;
+  static auto* reg = new std::map<std::vector<int>, gb_op_t>();
+  std::lock_guard<std::mutex> lk(m);
+  std::vector<int> key(d4);
+  key.push_back(Ls);
+  auto it = reg->find(key);
+  if (it != reg->end()) return it->second;
+  gb_op_t op = nullptr;
+  if (Ls == 1) check(gb_wilson_create(d4.data(), 0.0, nullptr, GB_F32, 1, stream(), 0, &op), "gb_wilson_create");
+  else check(gb_mobius_create(d4.data(), Ls, 0.0, 1.0, 1.0, 0.0, nullptr, GB_F32, 1, stream(), 0, &op), "gb_mobius_create");
+  (*reg)[key] = op;
+  return op;
+}
+}  // namespace gbdetail
+
+// ---- grids (Grid/cartesian/Cartesian_full.h, Cartesian_red_black.h) ------------------
+class GridBase {
+ public:
+  Coordinate _fdimensions;  // full extents; a 5D grid lists s first, as Grid does
+  Coordinate _gdimensions;  // checkerboarded grids halve x
+  int _ndimension = 4;
+  int _isCheckerBoarded = 0;
+  int Ls = 1;               // 1 on 4D grids
+  Coordinate dims4;         // the 4D extents
+  virtual ~GridBase() {}
+  int Nd() const { return _ndimension; }
+  const Coordinate& FullDimensions() const { return _fdimensions; }
+  const Coordinate& GlobalDimensions() const { return _gdimensions; }
+  int64_t gSites() const {
+    int64_t n = 1;
+    for (int d : _gdimensions) n *= d;
+    return n;
+  }
+  int64_t lSites() const { return gSites(); }
+  gb_op_t context() const { return gbdetail::context(dims4, Ls); }
+
+ protected:
+  void init(const Coordinate& d4, int ls, int cb) {
+    dims4 = d4;
+    Ls = ls;
+    _isCheckerBoarded = cb;
+    _fdimensions.clear();
+    if (ls > 1) _fdimensions.push_back(ls);
+    for (int d : d4) _fdimensions.push_back(d);
+    _ndimension = int(_fdimensions.size());
+    _gdimensions = _fdimensions;
+    if (cb) _gdimensions[ls > 1 ? 1 : 0] /= 2;
+  }
+};
+class GridCartesian : public GridBase {
+ public:
+  explicit GridCartesian(const Coordinate& d4, int ls = 1) { init(d4, ls, 0); }
+};
+class GridRedBlackCartesian : public GridBase {
+ public:
+  explicit GridRedBlackCartesian(const GridBase* base) { init(base->dims4, base->Ls, 1); }
+};
+
+inline Coordinate GridDefaultSimd(int nd, int) { return Coordinate(nd, 1); }
+inline Coordinate GridDefaultMpi() { return Coordinate(4, 1); }
+
+// SpaceTimeGrid (Grid/qcd/utils/SpaceTimeGrid.cc:49-80); the caller owns the grids
+namespace SpaceTimeGrid {
+inline GridCartesian* makeFourDimGrid(const Coordinate& latt, const Coordinate& = Coordinate(),
+                                      const Coordinate& = Coordinate()) {
+  if (latt.size() != 4) throw GridError(GB_ERR_BAD_ARG, "makeFourDimGrid: 4 extents expected");
+  return new GridCartesian(latt);
+}
+inline GridRedBlackCartesian* makeFourDimRedBlackGrid(const GridCartesian* g) { return new GridRedBlackCartesian(g); }
+inline GridCartesian* makeFiveDimGrid(int Ls, const GridCartesian* g) { return new GridCartesian(g->dims4, Ls); }
+inline GridRedBlackCartesian* makeFiveDimRedBlackGrid(int Ls, const GridCartesian* g) {
+  GridCartesian full(g->dims4, Ls);
+  return new GridRedBlackCartesian(&full);
+}
+}  // namespace SpaceTimeGrid
+
+// ---- fields --------------------------------------------------------------------------
+struct vSpinColourVectorD { static constexpr int precision = GB_F64; };
+struct vSpinColourVectorF { static constexpr int precision = GB_F32; };
+// FP16 storage with per-site FP32 norms (no Grid counterpart: Grid keeps half precision
+// for halo messages only)
+struct vSpinColourVectorH { static constexpr int precision = GB_F16; };
+struct vLorentzColourMatrixD {};
+struct vLorentzColourMatrixF {};
+
+// Checkerboard() of a field: readable as an int and assignable, like Grid's int&
+class CheckerboardRef {
+  gb_field_t h_;
+
+ public:
+  explicit CheckerboardRef(gb_field_t h) : h_(h) {}
+  operator int() const {
+    int s = 0;
+    gbdetail::check(gb_field_subset(h_, &s), "gb_field_subset");
+    return s == GB_FULL ? Even : s;
+  }
+  CheckerboardRef& operator=(int cb) {
+    int s = 0;
+    gbdetail::check(gb_field_subset(h_, &s), "gb_field_subset");
+    if (s != GB_FULL) gbdetail::check(gb_field_set_subset(h_, cb), "gb_field_set_subset");
+    return *this;
+  }
+};
+
+// A fermion field in device memory on a 4D or 5D, full or red-black grid.
+template <class vobj> class Lattice {
+  GridBase* grid_ = nullptr;
+  gb_field_t h_ = nullptr;
+
+ public:
+  typedef vobj vector_object;
+  explicit Lattice(GridBase* grid) : grid_(grid) {
+    gbdetail::check(gb_field_create(grid->context(), grid->_isCheckerBoarded ? GB_EVEN : GB_FULL, vobj::precision, &h_),
+                    "gb_field_create");
+  }
+  Lattice(const Lattice& o) : Lattice(o.grid_) { *this = o; }
+  Lattice(Lattice&& o) noexcept : grid_(o.grid_), h_(o.h_) { o.h_ = nullptr; }
+  ~Lattice() {
+    if (h_) gb_field_destroy(h_);
+  }
+  Lattice& operator=(const Lattice& o) {
+    if (this != &o) gbdetail::check(gb_field_copy(h_, o.h_), "gb_field_copy");
+    return *this;
+  }
+  Lattice& operator=(Lattice&& o) noexcept {
+    std::swap(grid_, o.grid_);
+    std::swap(h_, o.h_);
+    return *this;
+  }
+  Lattice& operator=(const Zero&) {
+    gbdetail::check(gb_field_zero(h_), "gb_field_zero");
+    return *this;
+  }
+  GridBase* Grid() const { return grid_; }
+  CheckerboardRef Checkerboard() const { return CheckerboardRef(h_); }
+  gb_field_t handle() const { return h_; }
+  // canonical host form (complex per site, s, spin, colour; one checkerboard's sites in
+  // lexicographic order for red-black fields) -- Grid's vectorizeFromLexOrdArray
+  size_t HostSize() const {
+    size_t n = 0;
+    gbdetail::check(gb_field_host_len(h_, &n), "gb_field_host_len");
+    return n / 2;
+  }
+  void ImportHost(const std::vector<ComplexD>& v) {
+    if (v.size() != HostSize()) throw GridError(GB_ERR_BAD_ARG, "ImportHost: wrong size");
+    gbdetail::check(gb_field_import(h_, reinterpret_cast<const double*>(v.data())), "gb_field_import");
+  }
+  std::vector<ComplexD> ExportHost() const {
+    std::vector<ComplexD> v(HostSize());
+    gbdetail::check(gb_field_export(h_, reinterpret_cast<double*>(v.data())), "gb_field_export");
+    return v;
+  }
+};
+
+typedef Lattice<vSpinColourVectorD> LatticeFermionD;
+typedef Lattice<vSpinColourVectorF> LatticeFermionF;
+typedef Lattice<vSpinColourVectorH> LatticeFermionH;
+typedef LatticeFermionD LatticeFermion;
+
+// The gauge field stays on the host in canonical form U[site][mu][3][3]; operators copy
+// it to the device in ImportGauge.
+template <class Tag> class GaugeLattice {
+  GridBase* grid_;
+
+ public:
+  std::vector<ComplexD> data;
+  explicit GaugeLattice(GridBase* grid) : grid_(grid), data(size_t(grid->gSites()) * Nd * Nc * Nc) {}
+  GridBase* Grid() const { return grid_; }
+  template <class T2> GaugeLattice& operator=(const GaugeLattice<T2>& o) {
+    data = o.data;
+    return *this;
+  }
+};
+typedef GaugeLattice<vLorentzColourMatrixD> LatticeGaugeFieldD;
+typedef GaugeLattice<vLorentzColourMatrixF> LatticeGaugeFieldF;
+typedef LatticeGaugeFieldD LatticeGaugeField;
+
+// ---- field linear algebra (Grid/lattice/Lattice_arith.h, Lattice_reduction.h) --------
+template <class v> RealD norm2(const Lattice<v>& x) {
+  double n = 0;
+  gbdetail::check(gb_field_norm2(x.handle(), &n), "gb_field_norm2");
+  return n;
+}
+template <class v> ComplexD innerProduct(const Lattice<v>& a, const Lattice<v>& b) {
+  double r[2] = {0, 0};
+  gbdetail::check(gb_field_inner(a.handle(), b.handle(), r), "gb_field_inner");
+  return ComplexD(r[0], r[1]);
+}
+inline double real_coeff(ComplexD a) {
+  if (a.imag() != 0) throw GridError(GB_ERR_UNSUPPORTED, "complex field coefficients are not supported");
+  return a.real();
+}
+template <class v> void axpy(Lattice<v>& ret, ComplexD a, const Lattice<v>& x, const Lattice<v>& y) {
+  gbdetail::check(gb_field_axpy(ret.handle(), real_coeff(a), x.handle(), y.handle()), "gb_field_axpy");
+}
+template <class v> void axpby(Lattice<v>& ret, ComplexD a, ComplexD b, const Lattice<v>& x, const Lattice<v>& y) {
+  gbdetail::check(gb_field_axpby(ret.handle(), real_coeff(a), real_coeff(b), x.handle(), y.handle()), "gb_field_axpby");
+}
+template <class v> RealD axpy_norm(Lattice<v>& ret, ComplexD a, const Lattice<v>& x, const Lattice<v>& y) {
+  double n = 0;
+  gbdetail::check(gb_field_axpy_norm(ret.handle(), real_coeff(a), x.handle(), y.handle(), &n), "gb_field_axpy_norm");
+  return n;
+}
+template <class v> void pickCheckerboard(int cb, Lattice<v>& half, const Lattice<v>& full) {
+  half.Checkerboard() = cb;
+  gbdetail::check(gb_field_pick_checkerboard(half.handle(), full.handle()), "gb_field_pick_checkerboard");
+}
+template <class v> void setCheckerboard(Lattice<v>& full, const Lattice<v>& half) {
+  gbdetail::check(gb_field_set_checkerboard(full.handle(), half.handle()), "gb_field_set_checkerboard");
+}
+template <class vo, class vi> void precisionChange(Lattice<vo>& out, const Lattice<vi>& in) {
+  gbdetail::check(gb_field_copy(out.handle(), in.handle()), "gb_field_copy");
+}
+template <class T1, class T2> void precisionChange(GaugeLattice<T1>& out, const GaugeLattice<T2>& in) {
+  out.data = in.data;
+}
+// a - b, a + b and scalar * a as new fields (Grid's expression templates, evaluated eagerly)
+template <class v> Lattice<v> operator-(const Lattice<v>& a, const Lattice<v>& b) {
+  Lattice<v> r(a.Grid());
+  axpby(r, 1.0, -1.0, a, b);
+  return r;
+}
+template <class v> Lattice<v> operator+(const Lattice<v>& a, const Lattice<v>& b) {
+  Lattice<v> r(a.Grid());
+  axpby(r, 1.0, 1.0, a, b);
+  return r;
+}
+template <class v> Lattice<v> operator*(RealD s, const Lattice<v>& a) {
+  Lattice<v> r(a.Grid());
+  axpby(r, s, 0.0, a, a);
+  return r;
+}
+
+// ---- seeded synthetic inputs (GridParallelRNG + gaussian + SU3 configurations) --------
+class GridParallelRNG {
+  uint64_t seed_ = 0x9E3779B97F4A7C15ull, draws_ = 0;
+
+ public:
+  explicit GridParallelRNG(GridBase*) {}
+  void SeedFixedIntegers(const std::vector<int>& seeds) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the seed integers
+    for (int s : seeds) {
+      for (int k = 0; k < 4; k++) {
+        h ^= uint64_t((uint32_t(s) >> (8 * k)) & 0xff);
+        h *= 1099511628211ull;
+      }
+    }
+    seed_ = h;
+    draws_ = 0;
+  }
+  uint64_t next() { return seed_ + 0x632BE59BD9B4E019ull * ++draws_; }
+};
+template <class v> void gaussian(GridParallelRNG& rng, Lattice<v>& f) {
+  std::vector<ComplexD> buf(f.HostSize());
+  gbdetail::check(gb_random_gaussian(buf.size(), rng.next(), reinterpret_cast<double*>(buf.data())), "gb_random_gaussian");
+  f.ImportHost(buf);
+}
+template <class v> void random(GridParallelRNG& rng, Lattice<v>& f) { gaussian(rng, f); }
+
+template <int N> struct SU {
+  static_assert(N == 3, "SU(3) only");
+  // U = exp(i eps H), H traceless Hermitian with N(0,1) entries, reunitarised
+  template <class T> static void ExpiHConfiguration(GridParallelRNG& rng, GaugeLattice<T>& U, RealD eps) {
+    gbdetail::check(gb_random_gauge(U.Grid()->dims4.data(), eps, rng.next(), reinterpret_cast<double*>(U.data.data())),
+                    "gb_random_gauge");
+  }
+  template <class T> static void HotConfiguration(GridParallelRNG& rng, GaugeLattice<T>& U) {
+    ExpiHConfiguration(rng, U, 1.0);
+  }
+  template <class T> static void TepidConfiguration(GridParallelRNG& rng, GaugeLattice<T>& U) {
+    ExpiHConfiguration(rng, U, 0.01);
+  }
+  template <class T> static void ColdConfiguration(GaugeLattice<T>& U) {
+    gbdetail::check(gb_unit_gauge(U.Grid()->dims4.data(), reinterpret_cast<double*>(U.data.data())), "gb_unit_gauge");
+  }
+  template <class T> static void ColdConfiguration(GridParallelRNG&, GaugeLattice<T>& U) { ColdConfiguration(U); }
+};
+typedef SU<3> SU3;
+
+// ---- fermion operators (FermionOperator.h:40-192) ------------------------------------
+struct WilsonImplParams {
+  std::vector<ComplexD> boundary_phases = std::vector<ComplexD>(Nd, ComplexD(1, 0));
+  WilsonImplParams() {}
+  explicit WilsonImplParams(const std::vector<ComplexD>& phi) : boundary_phases(phi) {}
+};
+template <class vobj, class GaugeTag> struct WilsonImplT {
+  typedef Lattice<vobj> FermionField;
+  typedef GaugeLattice<GaugeTag> GaugeField;
+  typedef WilsonImplParams ImplParams;
+  static constexpr int precision = vobj::precision;
+};
+typedef WilsonImplT<vSpinColourVectorD, vLorentzColourMatrixD> WilsonImplD;
+typedef WilsonImplT<vSpinColourVectorF, vLorentzColourMatrixF> WilsonImplF;
+typedef WilsonImplT<vSpinColourVectorH, vLorentzColourMatrixF> WilsonImplH;
+typedef WilsonImplD WilsonImplR;
+
+// CheckerBoardedSparseMatrixBase / FermionOperator<Impl>
+template <class Impl> class FermionOperator {
+ public:
+  typedef typename Impl::FermionField FermionField;
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+
+  FermionOperator(const FermionOperator&) = delete;
+  FermionOperator& operator=(const FermionOperator&) = delete;
+  virtual ~FermionOperator() {
+    if (op_) gb_op_destroy(op_);
+  }
+  gb_op_t handle() const { return op_; }
+  GridBase* FermionGrid() const { return fgrid_; }
+  GridBase* FermionRedBlackGrid() const { return frbgrid_; }
+  GridBase* GaugeGrid() const { return ugrid_; }
+  GridBase* GaugeRedBlackGrid() const { return urbgrid_; }
+  RealD Mass() const { return mass_; }
+
+  void ImportGauge(const GaugeField& U) {
+    gbdetail::check(gb_op_import_gauge(op_, reinterpret_cast<const double*>(U.data.data())), "ImportGauge");
+  }
+  void M(const FermionField& in, FermionField& out) { run(gb_M(op_, in.handle(), out.handle()), "M"); }
+  void Mdag(const FermionField& in, FermionField& out) { run(gb_Mdag(op_, in.handle(), out.handle()), "Mdag"); }
+  void MdagM(const FermionField& in, FermionField& out) { run(gb_MdagM(op_, in.handle(), out.handle()), "MdagM"); }
+  void Dhop(const FermionField& in, FermionField& out, int dag) {
+    run(gb_Dhop(op_, in.handle(), out.handle(), dag), "Dhop");
+  }
+  void DhopEO(const FermionField& in, FermionField& out, int dag) {
+    run(gb_DhopEO(op_, in.handle(), out.handle(), dag), "DhopEO");
+  }
+  void DhopOE(const FermionField& in, FermionField& out, int dag) {
+    run(gb_DhopOE(op_, in.handle(), out.handle(), dag), "DhopOE");
+  }
+  void Meooe(const FermionField& in, FermionField& out) { run(gb_Meooe(op_, in.handle(), out.handle()), "Meooe"); }
+  void MeooeDag(const FermionField& in, FermionField& out) {
+    run(gb_MeooeDag(op_, in.handle(), out.handle()), "MeooeDag");
+  }
+  void Mooee(const FermionField& in, FermionField& out) { run(gb_Mooee(op_, in.handle(), out.handle()), "Mooee"); }
+  void MooeeDag(const FermionField& in, FermionField& out) {
+    run(gb_MooeeDag(op_, in.handle(), out.handle()), "MooeeDag");
+  }
+  void MooeeInv(const FermionField& in, FermionField& out) {
+    run(gb_MooeeInv(op_, in.handle(), out.handle()), "MooeeInv");
+  }
+  void MooeeInvDag(const FermionField& in, FermionField& out) {
+    run(gb_MooeeInvDag(op_, in.handle(), out.handle()), "MooeeInvDag");
+  }
+  // SchurDiagMooeeOperator's pieces (LinearOperator.h:325-349)
+  void Mpc(const FermionField& in, FermionField& out) { run(gb_Mpc(op_, in.handle(), out.handle()), "Mpc"); }
+  void MpcDag(const FermionField& in, FermionField& out) { run(gb_MpcDag(op_, in.handle(), out.handle()), "MpcDag"); }
+  void MpcDagMpc(const FermionField& in, FermionField& out) {
+    run(gb_MpcDagMpc(op_, in.handle(), out.handle()), "MpcDagMpc");
+  }
+
+ protected:
+  gb_op_t op_ = nullptr;
+  GridBase *fgrid_, *frbgrid_, *ugrid_, *urbgrid_;
+  RealD mass_;
+  FermionOperator(GridBase* f, GridBase* frb, GridBase* u, GridBase* urb, RealD mass)
+      : fgrid_(f), frbgrid_(frb), ugrid_(u), urbgrid_(urb), mass_(mass) {}
+  static std::vector<double> phases(const ImplParams& p) {
+    std::vector<double> ph(2 * Nd);
+    for (int k = 0; k < Nd; k++) {
+      ph[2 * k] = p.boundary_phases[k].real();
+      ph[2 * k + 1] = p.boundary_phases[k].imag();
+    }
+    return ph;
+  }
+  static void run(int rc, const char* what) { gbdetail::check(rc, what); }
+};
+
+// WilsonFermion(U, Fgrid, Hgrid, mass, ImplParams) (WilsonFermion.h:139-142)
+template <class Impl> class WilsonFermion : public FermionOperator<Impl> {
+  typedef FermionOperator<Impl> Base;
+
+ public:
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  WilsonFermion(const GaugeField& U, GridCartesian& Fgrid, GridRedBlackCartesian& Hgrid, RealD mass,
+                const ImplParams& p = ImplParams())
+      : Base(&Fgrid, &Hgrid, &Fgrid, &Hgrid, mass) {
+    const std::vector<double> ph = Base::phases(p);
+    gbdetail::check(gb_wilson_create(Fgrid.dims4.data(), mass, ph.data(), Impl::precision, 1, gbdetail::stream(), 0,
+                                     &this->op_),
+                    "WilsonFermion");
+    this->ImportGauge(U);
+  }
+};
+
+// MobiusFermion(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, b, c, ImplParams)
+// (MobiusFermion.h:45-56) with the CayleyFermion5D extras
+template <class Impl> class MobiusFermion : public FermionOperator<Impl> {
+  typedef FermionOperator<Impl> Base;
+
+ public:
+  typedef typename Impl::FermionField FermionField;
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  int Ls;
+  RealD M5, b, c;
+  MobiusFermion(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
+                RealD b_, RealD c_, const ImplParams& p = ImplParams())
+      : Base(&FiveDimGrid, &FiveDimRedBlackGrid, &FourDimGrid, &FourDimRedBlackGrid, mass),
+        Ls(FiveDimGrid.Ls), M5(M5_), b(b_), c(c_) {
+    const std::vector<double> ph = Base::phases(p);
+    gbdetail::check(gb_mobius_create(FourDimGrid.dims4.data(), Ls, mass, M5_, b_, c_, ph.data(), Impl::precision, 1,
+                                     gbdetail::stream(), 0, &this->op_),
+                    "MobiusFermion");
+    this->ImportGauge(U);
+  }
+  void Dminus(const FermionField& in, FermionField& out) {
+    Base::run(gb_Dminus(this->op_, in.handle(), out.handle(), 0), "Dminus");
+  }
+  void DminusDag(const FermionField& in, FermionField& out) {
+    Base::run(gb_Dminus(this->op_, in.handle(), out.handle(), 1), "DminusDag");
+  }
+  // 4D <-> 5D surface fields (CayleyFermion5DImplementation.h:57-129); the 4D field is
+  // any fermion field on the gauge grid
+  template <class F4> void ImportPhysicalFermionSource(const F4& input4d, FermionField& imported5d) {
+    const std::vector<ComplexD> v = input4d.ExportHost();
+    Base::run(gb_import_physical_source(this->op_, reinterpret_cast<const double*>(v.data()), 0, imported5d.handle()),
+              "ImportPhysicalFermionSource");
+  }
+  template <class F4> void ImportUnphysicalFermion(const F4& input4d, FermionField& imported5d) {
+    const std::vector<ComplexD> v = input4d.ExportHost();
+    Base::run(gb_import_unphysical_fermion(this->op_, reinterpret_cast<const double*>(v.data()), 0,
+                                           imported5d.handle()),
+              "ImportUnphysicalFermion");
+  }
+  template <class F4> void ExportPhysicalFermionSolution(const FermionField& solution5d, F4& exported4d) {
+    std::vector<ComplexD> v(exported4d.HostSize());
+    Base::run(gb_export_physical_solution(this->op_, solution5d.handle(), reinterpret_cast<double*>(v.data()), 0),
+              "ExportPhysicalFermionSolution");
+    exported4d.ImportHost(v);
+  }
+  template <class F4> void ExportPhysicalFermionSource(const FermionField& solution5d, F4& exported4d) {
+    std::vector<ComplexD> v(exported4d.HostSize());
+    Base::run(gb_export_physical_source(this->op_, solution5d.handle(), reinterpret_cast<double*>(v.data()), 0),
+              "ExportPhysicalFermionSource");
+    exported4d.ImportHost(v);
+  }
+};
+
+typedef WilsonFermion<WilsonImplD> WilsonFermionD;
+typedef WilsonFermion<WilsonImplF> WilsonFermionF;
+typedef WilsonFermionD WilsonFermionR;
+typedef MobiusFermion<WilsonImplD> MobiusFermionD;
+typedef MobiusFermion<WilsonImplF> MobiusFermionF;
+typedef MobiusFermion<WilsonImplH> MobiusFermionH;
+typedef MobiusFermionD MobiusFermionR;
+
+// ---- linear operators (Grid/algorithms/LinearOperator.h:44-105,286-349) --------------
+template <class Field> class LinearOperatorBase {
+ public:
+  virtual ~LinearOperatorBase() {}
+  virtual void Op(const Field& in, Field& out) = 0;
+  virtual void AdjOp(const Field& in, Field& out) = 0;
+  virtual void HermOp(const Field& in, Field& out) = 0;
+  virtual void HermOpAndNorm(const Field& in, Field& out, RealD& n1, RealD& n2) {
+    HermOp(in, out);
+    const ComplexD dot = innerProduct(in, out);
+    n1 = dot.real();
+    n2 = norm2(out);
+  }
+  virtual void OpDiag(const Field&, Field&) { throw GridError(GB_ERR_UNSUPPORTED, "OpDiag"); }
+  virtual void OpDir(const Field&, Field&, int, int) { throw GridError(GB_ERR_UNSUPPORTED, "OpDir"); }
+  virtual void OpDirAll(const Field&, std::vector<Field>&) { throw GridError(GB_ERR_UNSUPPORTED, "OpDirAll"); }
+  // the library operator behind this linear operator and its kind (0 MdagM, 1 Schur), or
+  // null for a user-defined operator (solved by the host-driven CG below)
+  virtual gb_op_t library_op() const { return nullptr; }
+  virtual int library_kind() const { return -1; }
+};
+
+template <class Matrix, class Field> class MdagMLinearOperator : public LinearOperatorBase<Field> {
+  Matrix& _Mat;
+
+ public:
+  explicit MdagMLinearOperator(Matrix& Mat) : _Mat(Mat) {}
+  void Op(const Field& in, Field& out) override { _Mat.M(in, out); }
+  void AdjOp(const Field& in, Field& out) override { _Mat.Mdag(in, out); }
+  void HermOp(const Field& in, Field& out) override { _Mat.MdagM(in, out); }
+  gb_op_t library_op() const override { return _Mat.handle(); }
+  int library_kind() const override { return 0; }
+};
+
+template <class Matrix, class Field> class SchurDiagMooeeOperator : public LinearOperatorBase<Field> {
+  Matrix& _Mat;
+
+ public:
+  explicit SchurDiagMooeeOperator(Matrix& Mat) : _Mat(Mat) {}
+  void Mpc(const Field& in, Field& out) { _Mat.Mpc(in, out); }
+  void MpcDag(const Field& in, Field& out) { _Mat.MpcDag(in, out); }
+  void MpcDagMpc(const Field& in, Field& out) { _Mat.MpcDagMpc(in, out); }
+  void Op(const Field& in, Field& out) override { Mpc(in, out); }
+  void AdjOp(const Field& in, Field& out) override { MpcDag(in, out); }
+  void HermOp(const Field& in, Field& out) override { MpcDagMpc(in, out); }
+  gb_op_t library_op() const override { return _Mat.handle(); }
+  int library_kind() const override { return 1; }
+};
+
+// ---- solvers ---------------------------------------------------------------------------
+template <class Field> class OperatorFunction {
+ public:
+  virtual ~OperatorFunction() {}
+  virtual void operator()(LinearOperatorBase<Field>& Linop, const Field& in, Field& out) = 0;
+};
+template <class Field> class LinearFunction {
+ public:
+  virtual ~LinearFunction() {}
+  virtual void operator()(const Field& in, Field& out) = 0;
+};
+
+// ConjugateGradient<Field>(tol, maxit, err_on_no_conv) (ConjugateGradient.h:55-257).  A
+// library operator runs the device-resident CG of the C ABI; any other linear operator
+// runs Grid's iteration driven from the host over the device field algebra.
+template <class Field> class ConjugateGradient : public OperatorFunction<Field> {
+ public:
+  RealD Tolerance;
+  Integer MaxIterations;
+  bool ErrorOnNoConverge;
+  Integer IterationsToComplete = 0;
+  RealD TrueResidual = 0;
+  bool UseGraphs = false;  // capture iteration chunks as CUDA graphs
+  ConjugateGradient(RealD tol, Integer maxit, bool err_on_no_conv = true)
+      : Tolerance(tol), MaxIterations(maxit), ErrorOnNoConverge(err_on_no_conv) {}
+
+  gb_cg_params params() const {
+    gb_cg_params p;
+    gb_cg_params_default(&p);
+    p.tolerance = Tolerance;
+    p.max_iterations = MaxIterations;
+    p.err_on_no_conv = ErrorOnNoConverge ? 1 : 0;
+    p.use_graphs = UseGraphs ? 1 : 0;
+    return p;
+  }
+  void operator()(LinearOperatorBase<Field>& Linop, const Field& src, Field& psi) override {
+    if (gb_op_t op = Linop.library_op()) {
+      const gb_cg_params p = params();
+      gb_cg_result r;
+      const int rc = Linop.library_kind() == 1 ? gb_cg_schur(op, src.handle(), psi.handle(), &p, &r)
+                                               : gb_cg_mdagm(op, src.handle(), psi.handle(), &p, &r);
+      IterationsToComplete = r.iterations;
+      TrueResidual = r.true_residual;
+      gbdetail::check(rc, "ConjugateGradient");
+      return;
+    }
+    generic(Linop, src, psi);
+  }
+
+ private:
+  // ConjugateGradient.h:68-257, with every vector operation on the device
+  void generic(LinearOperatorBase<Field>& Linop, const Field& src, Field& psi) {
+    Field p(src.Grid()), mmp(src.Grid()), r(src.Grid());
+    p.Checkerboard() = int(src.Checkerboard());
+    mmp.Checkerboard() = int(src.Checkerboard());
+    r.Checkerboard() = int(src.Checkerboard());
+    const RealD ssq = norm2(src);
+    RealD d, b, c, cp;
+    Linop.HermOpAndNorm(psi, mmp, d, b);
+    axpby(r, 1.0, -1.0, src, mmp);  // r = src - A psi
+    p = r;
+    cp = norm2(r);
+    const RealD rsq = Tolerance * Tolerance * ssq;
+    IterationsToComplete = 0;
+    if (cp <= rsq) {
+      TrueResidual = ssq > 0 ? std::sqrt(cp / ssq) : 0;
+      return;
+    }
+    for (int k = 1; k <= MaxIterations; k++) {
+      c = cp;
+      Linop.HermOpAndNorm(p, mmp, d, b);
+      const RealD a = c / d;
+      cp = axpy_norm(r, -a, mmp, r);
+      b = cp / c;
+      axpy(psi, a, p, psi);
+      axpby(p, b, 1.0, p, r);
+      if (cp <= rsq) {
+        Linop.HermOp(psi, mmp);
+        axpby(p, 1.0, -1.0, mmp, src);
+        TrueResidual = std::sqrt(norm2(p) / ssq);
+        IterationsToComplete = k;
+        return;
+      }
+    }
+    IterationsToComplete = MaxIterations;
+    if (ErrorOnNoConverge) throw GridError(GB_ERR_NOT_CONVERGED, "ConjugateGradient did not converge");
+  }
+};
+
+// ConjugateGradientReliableUpdate<FieldD, FieldF>(tol, maxit, delta, sp_grid, Linop_f,
+// Linop_d, err_on_nonconv) (ConjugateGradientReliableUpdate.h:33-270): FP32 (or FP16)
+// inner CG with FP64 reliable updates.  Both linear operators must be library operators
+// of the same kind.
+template <class FieldD, class FieldF> class ConjugateGradientReliableUpdate : public LinearFunction<FieldD> {
+ public:
+  RealD Tolerance, Delta;
+  Integer MaxIterations;
+  bool ErrorOnNoConverge, DoFinalCleanup = true;
+  Integer IterationsToComplete = 0, IterationsToCleanup = 0, ReliableUpdatesPerformed = 0;
+  RealD TrueResidual = 0;
+  Integer ReliableUpdateEvery = 100;  // also update at least this often (0 = only on Delta)
+  bool UseGraphs = false;
+  LinearOperatorBase<FieldF>& Linop_f;
+  LinearOperatorBase<FieldD>& Linop_d;
+
+  ConjugateGradientReliableUpdate(RealD tol, Integer maxit, RealD delta, GridBase*, LinearOperatorBase<FieldF>& lf,
+                                  LinearOperatorBase<FieldD>& ld, bool err_on_nonconv = true)
+      : Tolerance(tol), Delta(delta), MaxIterations(maxit), ErrorOnNoConverge(err_on_nonconv), Linop_f(lf),
+        Linop_d(ld) {}
+
+  void operator()(const FieldD& src, FieldD& psi) override {
+    gb_op_t od = Linop_d.library_op(), of = Linop_f.library_op();
+    if (!od || !of || Linop_d.library_kind() != Linop_f.library_kind())
+      throw GridError(GB_ERR_UNSUPPORTED, "ConjugateGradientReliableUpdate: library operators of one kind expected");
+    gb_cg_params p;
+    gb_cg_params_default(&p);
+    p.tolerance = Tolerance;
+    p.max_iterations = MaxIterations;
+    p.err_on_no_conv = ErrorOnNoConverge ? 1 : 0;
+    p.delta = Delta;
+    p.relup_every = ReliableUpdateEvery;
+    p.final_cleanup = DoFinalCleanup ? 1 : 0;
+    p.use_graphs = UseGraphs ? 1 : 0;
+    gb_cg_result r;
+    const int rc = gb_cg_reliable(od, of, Linop_d.library_kind(), src.handle(), psi.handle(), &p, &r);
+    IterationsToComplete = r.iterations;
+    IterationsToCleanup = r.cleanup_iterations;
+    ReliableUpdatesPerformed = r.reliable_updates;
+    TrueResidual = r.true_residual;
+    gbdetail::check(rc, "ConjugateGradientReliableUpdate");
+  }
+};
+
+// SchurRedBlackDiagMooeeSolve(OperatorFunction&) (SchurRedBlack.h:373-436).  The CG is a
+// library ConjugateGradient; an optional lower-precision operator of the same action
+// turns the inner solve into the mixed-precision reliable-update CG.
+template <class Field> class SchurRedBlackDiagMooeeSolve {
+  OperatorFunction<Field>& solver_;
+
+ public:
+  Integer IterationsToComplete = 0;
+  RealD TrueResidual = 0, UnpreconditionedResidual = 0;
+  explicit SchurRedBlackDiagMooeeSolve(OperatorFunction<Field>& HermitianRBSolver, bool = false, bool = false)
+      : solver_(HermitianRBSolver) {}
+  template <class Matrix> void operator()(Matrix& _Matrix, const Field& in, Field& out) { solve(_Matrix, nullptr, in, out); }
+  template <class Matrix, class MatrixLo>
+  void operator()(Matrix& _Matrix, MatrixLo& lower_precision, const Field& in, Field& out) {
+    solve(_Matrix, lower_precision.handle(), in, out);
+  }
+
+ private:
+  template <class Matrix> void solve(Matrix& M, gb_op_t lo, const Field& in, Field& out) {
+    auto* cg = dynamic_cast<ConjugateGradient<Field>*>(&solver_);
+    if (!cg) throw GridError(GB_ERR_UNSUPPORTED, "SchurRedBlackDiagMooeeSolve: a ConjugateGradient solver expected");
+    const gb_cg_params p = cg->params();
+    gb_cg_result r;
+    double unprec = 0;
+    const int rc = gb_schur_solve(M.handle(), lo, in.handle(), out.handle(), &p, &r, &unprec);
+    IterationsToComplete = cg->IterationsToComplete = r.iterations;
+    TrueResidual = cg->TrueResidual = r.true_residual;
+    UnpreconditionedResidual = unprec;
+    gbdetail::check(rc, "SchurRedBlackDiagMooeeSolve");
+  }
+};
+
+}  // namespace Grid
+
+#endif  // GBGRID_H

@@ -430,6 +430,49 @@ template <class R> struct Mobius : Op<R> {
   void DW(const Field<R>& in, Field<R>& out, int dag) {
     this->Dhop(in, out, dag); axpy<R>(out, R(4.0 - cf.M5), in, out);
   }
+  // Dminus / DminusDag (CayleyFermion5DImplementation.h:131-153): chi_s = psi_s - cs[s] (DW psi)_s
+  // (cs is real for Moebius, so the dagger only changes DW)
+  void Dminus(const Field<R>& psi, Field<R>& chi, int dag) {
+    Field<R> t;
+    DW(psi, t, dag);
+    chi.resize(psi.size());
+    const int64_t n = n4(psi);
+    for (int64_t x = 0; x < n; x++)
+      for (int s = 0; s < Ls; s++)
+        for (int k = 0; k < Nsc; k++) {
+          const size_t i = (size_t(x) * Ls + s) * Nsc + k;
+          chi[i] = psi[i] - R(cf.cs[s]) * t[i];
+        }
+  }
+  // ImportUnphysicalFermion (:101-114): s = 0 takes P+ in4, s = Ls-1 takes P- in4, the
+  // rest is zero.  P+ keeps spins 0,1 and P- spins 2,3 (gamma5 = diag(1,1,-1,-1)).
+  void ImportUnphysical(const Field<R>& in4, Field<R>& out5) const {
+    const int64_t n = int64_t(in4.size() / Nsc);
+    out5.assign(size_t(n) * Ls * Nsc, cplx<R>(0, 0));
+    for (int64_t x = 0; x < n; x++)
+      for (int k = 0; k < Nsc; k++) {
+        const size_t s = k < 6 ? 0 : size_t(Ls - 1);
+        out5[(size_t(x) * Ls + s) * Nsc + k] = in4[size_t(x) * Nsc + k];
+      }
+  }
+  // ImportPhysicalFermionSource (:116-129) = Dminus of the unphysical import
+  void ImportPhysicalSource(const Field<R>& in4, Field<R>& out5) {
+    Field<R> t;
+    ImportUnphysical(in4, t);
+    Dminus(t, out5, 0);
+  }
+  // ExportPhysicalFermionSolution (:57-68): P- psi(s=0) + P+ psi(s=Ls-1);
+  // ExportPhysicalFermionSource (:89-100): P+ psi(s=0) + P- psi(s=Ls-1)
+  void ExportPhysical(const Field<R>& in5, Field<R>& out4, bool solution) const {
+    const int64_t n = n4(in5);
+    out4.resize(size_t(n) * Nsc);
+    for (int64_t x = 0; x < n; x++)
+      for (int k = 0; k < Nsc; k++) {
+        const bool upper = k < 6;
+        const size_t s = (upper == solution) ? size_t(Ls - 1) : 0;
+        out4[size_t(x) * Nsc + k] = in5[(size_t(x) * Ls + s) * Nsc + k];
+      }
+  }
   void Meooe5D(const Field<R>& psi, Field<R>& Din) {
     std::vector<double> diag = cf.bs, upper = cf.cs, lower = cf.cs;
     upper[Ls - 1] = -cf.mf * upper[Ls - 1];

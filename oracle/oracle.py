@@ -19,6 +19,9 @@ OP_M, OP_MDAG, OP_DHOP, OP_DHOP_DAG = 0, 1, 2, 3
 OP_MEOOE, OP_MEOOE_DAG, OP_MOOEE, OP_MOOEE_DAG = 4, 5, 6, 7
 OP_MOOEE_INV, OP_MOOEE_INV_DAG, OP_MPC, OP_MPC_DAG = 8, 9, 10, 11
 OP_MPCDAGMPC, OP_MDAGM, OP_MEOOE5D, OP_MEOOE_DAG5D = 12, 13, 14, 15
+OP_DMINUS, OP_DMINUS_DAG = 16, 17
+# orc_physical modes (CayleyFermion5DImplementation.h:57-129)
+IMPORT_PHYSICAL_SOURCE, IMPORT_UNPHYSICAL, EXPORT_PHYSICAL_SOLUTION, EXPORT_PHYSICAL_SOURCE = 0, 1, 2, 3
 
 
 def build():
@@ -49,6 +52,7 @@ def lib():
         L.orc_cg.argtypes = [vp, i, dp, dp, d, i, ip, dp]
         L.orc_schur_solve.argtypes = [vp, dp, dp, d, i, ip, dp]
         L.orc_cg_reliable.argtypes = [vp, vp, i, dp, dp, d, i, d, i, i, ip, dp]
+        L.orc_physical.argtypes = [vp, i, dp, dp]
         L.orc_set_threads.argtypes = [i]
         L.orc_max_threads.restype = i
         _lib = L
@@ -110,6 +114,15 @@ class OracleOp:
         x = np.ascontiguousarray(x, dtype=np.complex128)
         out = np.empty_like(x)
         lib().orc_dhop_cb(self.h, _p(x), _p(out), in_parity, dag)
+        return out
+
+    def physical(self, mode, x):
+        """4D <-> 5D surface fields (Moebius, FP64): modes IMPORT_* take a 4D field and
+        return a 5D one, EXPORT_* the reverse."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        n = self.vol * 12 * (self.L5 if mode < 2 else 1)
+        out = np.empty(n, dtype=np.complex128)
+        assert lib().orc_physical(self.h, mode, _p(x), _p(out)) == 0
         return out
 
     def doubled_links(self):

@@ -33,13 +33,15 @@ template <class R> void store(const Field<R>& f, double* p) {
 enum Opcode {
   OP_M = 0, OP_MDAG = 1, OP_DHOP = 2, OP_DHOP_DAG = 3, OP_MEOOE = 4, OP_MEOOE_DAG = 5, OP_MOOEE = 6,
   OP_MOOEE_DAG = 7, OP_MOOEE_INV = 8, OP_MOOEE_INV_DAG = 9, OP_MPC = 10, OP_MPC_DAG = 11,
-  OP_MPCDAGMPC = 12, OP_MDAGM = 13, OP_MEOOE5D = 14, OP_MEOOE_DAG5D = 15
+  OP_MPCDAGMPC = 12, OP_MDAGM = 13, OP_MEOOE5D = 14, OP_MEOOE_DAG5D = 15, OP_DMINUS = 16,
+  OP_DMINUS_DAG = 17
 };
 
 // returns the input length (in complex numbers) that the opcode expects
 template <class R> size_t in_len(Op<R>* op, int opcode) {
   switch (opcode) {
-    case OP_M: case OP_MDAG: case OP_DHOP: case OP_DHOP_DAG: case OP_MDAGM: return op->full_len();
+    case OP_M: case OP_MDAG: case OP_DHOP: case OP_DHOP_DAG: case OP_MDAGM: case OP_DMINUS: case OP_DMINUS_DAG:
+      return op->full_len();
     default: return op->half_len();
   }
 }
@@ -67,6 +69,12 @@ template <class R> int apply(Op<R>* op, int kind, int opcode, const double* in, 
       if (kind != 1) return 1;
       auto* m = static_cast<Mobius<R>*>(op);
       if (opcode == OP_MEOOE5D) m->Meooe5D(a, b); else m->MeooeDag5D(a, b);
+      break;
+    }
+    case OP_DMINUS:
+    case OP_DMINUS_DAG: {
+      if (kind != 1) return 1;
+      static_cast<Mobius<R>*>(op)->Dminus(a, b, opcode == OP_DMINUS_DAG);
       break;
     }
     default: return 1;
@@ -119,6 +127,27 @@ int orc_apply(void* p, int opcode, const double* in, double* out, int parity) {
   Handle* h = static_cast<Handle*>(p);
   if (h->prec == 0) return apply<double>(h->d, h->kind, opcode, in, out, parity);
   return apply<float>(h->f, h->kind, opcode, in, out, parity);
+}
+
+// 4D <-> 5D surface fields of a Moebius operator (CayleyFermion5DImplementation.h:57-129).
+// mode 0: ImportPhysicalFermionSource, 1: ImportUnphysicalFermion (in4: full 4D field,
+// out5: full 5D field); mode 2: ExportPhysicalFermionSolution, 3: ExportPhysicalFermionSource
+// (in = 5D, out = 4D).
+int orc_physical(void* p, int mode, const double* in, double* out) {
+  Handle* h = static_cast<Handle*>(p);
+  if (h->kind != 1 || h->prec != 0) return 1;
+  auto* m = static_cast<Mobius<double>*>(h->d);
+  const size_t n5 = m->full_len(), n4 = n5 / size_t(m->Ls);
+  Field<double> a = load<double>(in, mode < 2 ? n4 : n5), b;
+  switch (mode) {
+    case 0: m->ImportPhysicalSource(a, b); break;
+    case 1: m->ImportUnphysical(a, b); break;
+    case 2: m->ExportPhysical(a, b, true); break;
+    case 3: m->ExportPhysical(a, b, false); break;
+    default: return 1;
+  }
+  store<double>(b, out);
+  return 0;
 }
 
 // DhopEO / DhopOE: in has parity in_parity, out the other one

@@ -130,3 +130,19 @@ def mobius_free_solve(dims, Ls, mf, M5, b, c, eta, antiperiodic_t=True):
     if antiperiodic_t:
         o = o * np.exp(1j * np.pi * np.arange(Lt) / Lt)[:, None, None, None, None, None]
     return o.reshape(-1)
+
+
+def dminus_free(dims, Ls, c, M5, psi, dag=False, antiperiodic_t=True):
+    """Dminus psi = (1 - c D_W) psi on every s at U = 1 (CayleyFermion5DImplementation.h:131-153),
+    with D_W(k) = D(k) - M5 in momentum space; dag uses D_W(k)^dagger."""
+    DW = wilson_dirac_k(dims, antiperiodic_t) - M5 * np.eye(4)
+    if dag:
+        DW = np.conj(np.swapaxes(DW, -1, -2))
+    A = np.eye(4) - c * DW
+    Lx, Ly, Lz, Lt = dims
+    f = psi.reshape(Lt, Lz, Ly, Lx, Ls, 4, 3)
+    ph = np.exp(-1j * np.pi * np.arange(Lt) / Lt) if antiperiodic_t else np.ones(Lt)
+    fk = np.fft.fftn(f * ph[:, None, None, None, None, None, None], axes=(0, 1, 2, 3))
+    ok = np.einsum("tzyxij,tzyxsjc->tzyxsic", A, fk)
+    o = np.fft.ifftn(ok, axes=(0, 1, 2, 3)) * np.conj(ph)[:, None, None, None, None, None, None]
+    return o.reshape(-1)

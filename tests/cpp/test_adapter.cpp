@@ -1,0 +1,167 @@
+// Grid-style program on the C++ adapter (include/gbgrid.h): the even-odd identities of
+// tests/core/Test_mobius_even_odd.cc, the Schur red-black solve, the mixed-precision
+// reliable-update CG of tests/Test_dwf_mixedcg_prec.cc, the unpreconditioned Wilson CG of
+// tests/solver/Test_wilson_cg_unprec.cc, a user-defined linear operator through the
+// host-driven CG, and the 4D <-> 5D surface fields.  Exit status 0 when every check holds.
+#include <cstdio>
+#include <cstdlib>
+
+#include "gbgrid.h"
+
+using namespace Grid;
+
+static int failures = 0;
+static void expect(bool ok, const char* what, double v) {
+  std::printf("%-58s %-4s %.3e\n", what, ok ? "ok" : "FAIL", v);
+  if (!ok) failures++;
+}
+
+// a user-defined Hermitian operator: MdagM + shift (no library counterpart)
+template <class Matrix, class Field> class ShiftedMdagM : public LinearOperatorBase<Field> {
+  Matrix& m_;
+  RealD shift_;
+
+ public:
+  ShiftedMdagM(Matrix& m, RealD s) : m_(m), shift_(s) {}
+  void Op(const Field& in, Field& out) override { HermOp(in, out); }
+  void AdjOp(const Field& in, Field& out) override { HermOp(in, out); }
+  void HermOp(const Field& in, Field& out) override {
+    m_.MdagM(in, out);
+    axpy(out, shift_, in, out);
+  }
+};
+
+int main() {
+  const int Ls = 8;
+  const RealD mass = 0.05, M5 = 1.8, b = 1.5, c = 0.5;
+  GridCartesian* UGrid = SpaceTimeGrid::makeFourDimGrid({8, 8, 8, 8}, GridDefaultSimd(Nd, 1), GridDefaultMpi());
+  GridRedBlackCartesian* UrbGrid = SpaceTimeGrid::makeFourDimRedBlackGrid(UGrid);
+  GridCartesian* FGrid = SpaceTimeGrid::makeFiveDimGrid(Ls, UGrid);
+  GridRedBlackCartesian* FrbGrid = SpaceTimeGrid::makeFiveDimRedBlackGrid(Ls, UGrid);
+
+  GridParallelRNG RNG4(UGrid), RNG5(FGrid);
+  RNG4.SeedFixedIntegers({1, 2, 3, 4});
+  RNG5.SeedFixedIntegers({5, 6, 7, 8});
+  LatticeGaugeField Umu(UGrid);
+  SU<Nc>::ExpiHConfiguration(RNG4, Umu, 0.5);
+  LatticeGaugeFieldF UmuF(UGrid);
+  precisionChange(UmuF, Umu);
+
+  WilsonImplParams params;
+  params.boundary_phases[3] = ComplexD(-1, 0);  // antiperiodic in time
+  MobiusFermionD Ddwf(Umu, *FGrid, *FrbGrid, *UGrid, *UrbGrid, mass, M5, b, c, params);
+  MobiusFermionF DdwfF(UmuF, *FGrid, *FrbGrid, *UGrid, *UrbGrid, mass, M5, b, c, params);
+
+  // ---- even-odd identities (Test_mobius_even_odd.cc) ----
+  LatticeFermion src(FGrid), phi(FGrid), ref(FGrid), tmp(FGrid);
+  gaussian(RNG5, src);
+  gaussian(RNG5, phi);
+  LatticeFermion src_e(FrbGrid), src_o(FrbGrid), r_e(FrbGrid), r_o(FrbGrid), r_eo(FGrid);
+  pickCheckerboard(Even, src_e, src);
+  pickCheckerboard(Odd, src_o, src);
+  Ddwf.Meooe(src_e, r_o);
+  Ddwf.Meooe(src_o, r_e);
+  LatticeFermion t_e(FrbGrid), t_o(FrbGrid);
+  Ddwf.Mooee(src_e, t_e);
+  Ddwf.Mooee(src_o, t_o);
+  axpy(r_e, 1.0, t_e, r_e);
+  axpy(r_o, 1.0, t_o, r_o);
+  setCheckerboard(r_eo, r_e);
+  setCheckerboard(r_eo, r_o);
+  Ddwf.M(src, ref);
+  tmp = ref - r_eo;
+  expect(std::sqrt(norm2(tmp) / norm2(ref)) < 1e-13, "Meooe + Mooee == M", std::sqrt(norm2(tmp) / norm2(ref)));
+
+  Ddwf.Mooee(src_o, t_o);
+  Ddwf.MooeeInv(t_o, r_o);
+  LatticeFermion d_o = r_o - src_o;
+  expect(std::sqrt(norm2(d_o) / norm2(src_o)) < 1e-13, "MooeeInv Mooee == 1", std::sqrt(norm2(d_o) / norm2(src_o)));
+
+  LatticeFermion phi_o(FrbGrid), Mpc_src(FrbGrid), MpcDag_phi(FrbGrid);
+  pickCheckerboard(Odd, phi_o, phi);
+  SchurDiagMooeeOperator<MobiusFermionD, LatticeFermion> HermOpEO(Ddwf);
+  HermOpEO.Mpc(src_o, Mpc_src);
+  HermOpEO.MpcDag(phi_o, MpcDag_phi);
+  const ComplexD pMs = innerProduct(phi_o, Mpc_src), Mdps = innerProduct(MpcDag_phi, src_o);
+  expect(std::abs(pMs - Mdps) / std::abs(pMs) < 1e-12, "<phi|Mpc src> == <MpcDag phi|src>", std::abs(pMs - Mdps) / std::abs(pMs));
+
+  // ---- Schur red-black solve, FP64 and mixed precision ----
+  ConjugateGradient<LatticeFermion> CG(1e-10, 10000);
+  SchurRedBlackDiagMooeeSolve<LatticeFermion> SchurSolver(CG);
+  LatticeFermion sol(FGrid), sol_mixed(FGrid);
+  sol = Zero();
+  SchurSolver(Ddwf, src, sol);
+  Ddwf.M(sol, tmp);
+  tmp = tmp - src;
+  const RealD res = std::sqrt(norm2(tmp) / norm2(src));
+  std::printf("Schur CG: %d iterations, true residual %.3e\n", CG.IterationsToComplete, CG.TrueResidual);
+  expect(res < 1e-9, "Schur solve |M x - b| / |b|", res);
+
+  sol_mixed = Zero();
+  SchurSolver(Ddwf, DdwfF, src, sol_mixed);
+  tmp = sol_mixed - sol;
+  expect(std::sqrt(norm2(tmp) / norm2(sol)) < 1e-8, "mixed-precision Schur solve == FP64", std::sqrt(norm2(tmp) / norm2(sol)));
+
+  // ConjugateGradientReliableUpdate on the Schur operator (Test_dwf_mixedcg_prec.cc)
+  SchurDiagMooeeOperator<MobiusFermionF, LatticeFermionF> HermOpEO_f(DdwfF);
+  ConjugateGradientReliableUpdate<LatticeFermion, LatticeFermionF> mCG(1e-10, 10000, 1e-6, FrbGrid, HermOpEO_f, HermOpEO);
+  LatticeFermion psi_o(FrbGrid), psi_d(FrbGrid);
+  psi_o = Zero();
+  psi_o.Checkerboard() = Odd;
+  mCG(src_o, psi_o);
+  psi_d = Zero();
+  psi_d.Checkerboard() = Odd;
+  CG(HermOpEO, src_o, psi_d);
+  LatticeFermion dpsi = psi_o - psi_d;
+  std::printf("reliable update CG: %d iterations, %d updates; FP64 CG %d iterations\n", mCG.IterationsToComplete,
+              mCG.ReliableUpdatesPerformed, CG.IterationsToComplete);
+  expect(std::sqrt(norm2(dpsi) / norm2(psi_d)) < 1e-8, "ReliableUpdate CG == FP64 CG", std::sqrt(norm2(dpsi) / norm2(psi_d)));
+
+  // ---- user-defined operator: host-driven CG on device fields ----
+  ShiftedMdagM<MobiusFermionD, LatticeFermion> Shifted(Ddwf, 0.5);
+  ConjugateGradient<LatticeFermion> CGu(1e-10, 2000);
+  LatticeFermion x(FGrid), Ax(FGrid);
+  x = Zero();
+  CGu(Shifted, src, x);
+  Shifted.HermOp(x, Ax);
+  Ax = Ax - src;
+  expect(std::sqrt(norm2(Ax) / norm2(src)) < 1e-9, "host-driven CG on a user operator", std::sqrt(norm2(Ax) / norm2(src)));
+
+  // ---- unpreconditioned Wilson CG (Test_wilson_cg_unprec.cc) ----
+  WilsonFermionD Dw(Umu, *UGrid, *UrbGrid, 0.1, params);
+  LatticeFermion wsrc(UGrid), wsol(UGrid), wtmp(UGrid);
+  gaussian(RNG4, wsrc);
+  wsol = Zero();
+  MdagMLinearOperator<WilsonFermionD, LatticeFermion> HermOp(Dw);
+  ConjugateGradient<LatticeFermion> CGw(1e-8, 10000);
+  CGw(HermOp, wsrc, wsol);
+  HermOp.HermOp(wsol, wtmp);
+  wtmp = wtmp - wsrc;
+  expect(std::sqrt(norm2(wtmp) / norm2(wsrc)) < 1e-7, "Wilson MdagM CG", std::sqrt(norm2(wtmp) / norm2(wsrc)));
+
+  // ---- 4D <-> 5D surface fields ----
+  LatticeFermion eta(UGrid), eta_back(UGrid), eta5(FGrid), prop5(FGrid), prop4(UGrid);
+  gaussian(RNG4, eta);
+  Ddwf.ImportUnphysicalFermion(eta, eta5);
+  Ddwf.ExportPhysicalFermionSource(eta5, eta_back);
+  eta_back = eta_back - eta;
+  expect(norm2(eta_back) == 0.0, "ExportPhysicalFermionSource(ImportUnphysical(eta)) == eta", norm2(eta_back));
+  Ddwf.ImportPhysicalFermionSource(eta, eta5);
+  prop5 = Zero();
+  SchurSolver(Ddwf, eta5, prop5);
+  Ddwf.ExportPhysicalFermionSolution(prop5, prop4);
+  expect(norm2(prop4) > 0 && SchurSolver.UnpreconditionedResidual < 1e-9, "physical propagator solve",
+         SchurSolver.UnpreconditionedResidual);
+
+  // ---- errors come back as exceptions ----
+  bool threw = false;
+  try {
+    Ddwf.DhopEO(src, tmp, DaggerNo);  // full fields where an odd half field is expected
+  } catch (const GridError& e) {
+    threw = e.status == GB_ERR_BAD_PARITY;
+  }
+  expect(threw, "checkerboard mismatch throws GridError", 0.0);
+
+  std::printf("%s (%d failures)\n", failures ? "FAILED" : "PASSED", failures);
+  return failures ? 1 : 0;
+}

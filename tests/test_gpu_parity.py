@@ -328,3 +328,52 @@ def test_multi_rhs_cg_each_equals_single(gpu_available):
         assert abs(cg.per_rhs_iterations[r] - c1.IterationsToComplete) <= 1
         assert cg.per_rhs_true_residual[r] < 1e-10 * 1.5 and c1.TrueResidual < 1e-10 * 1.5
         assert o.rel_l2(got[r], x1.export()) < 1e-8
+
+
+@pytest.mark.parametrize("prec", [g.F64, g.F32])
+@pytest.mark.parametrize("nrhs", [1, 2])
+def test_dminus_and_physical_fields(gpu_available, prec, nrhs):
+    """Dminus/DminusDag and the 4D <-> 5D surface fields (CayleyFermion5DImplementation.h:57-153)
+    against the oracle, one right-hand side at a time for nrhs = 2."""
+    dims, Ls = (4, 4, 4, 6), 8
+    op, ref, U = mobius_pair(dims, Ls, 0.05, prec, nrhs=nrhs)
+    vol = int(np.prod(dims))
+    xs = [fermion(vol, Ls, 40 + r) for r in range(nrhs)]
+    fin = op.FermionField().import_(np.concatenate(xs))
+    fout = op.FermionField()
+    for name, code in (("Dminus", o.OP_DMINUS), ("DminusDag", o.OP_DMINUS_DAG)):
+        getattr(op, name)(fin, fout)
+        got = fout.export().reshape(nrhs, -1)
+        for r in range(nrhs):
+            assert o.rel_l2(got[r], ref.apply(code, xs[r])) < TOL[prec], (name, r)
+    etas = [fermion(vol, 1, 50 + r) for r in range(nrhs)]
+    for fn, mode in ((op.ImportPhysicalFermionSource, o.IMPORT_PHYSICAL_SOURCE),
+                     (op.ImportUnphysicalFermion, o.IMPORT_UNPHYSICAL)):
+        fn(np.concatenate(etas), fout)
+        got = fout.export().reshape(nrhs, -1)
+        for r in range(nrhs):
+            assert o.rel_l2(got[r], ref.physical(mode, etas[r])) < TOL[prec], (mode, r)
+    for fn, mode in ((op.ExportPhysicalFermionSolution, o.EXPORT_PHYSICAL_SOLUTION),
+                     (op.ExportPhysicalFermionSource, o.EXPORT_PHYSICAL_SOURCE)):
+        got = fn(fin).reshape(nrhs, -1)
+        for r in range(nrhs):
+            assert o.rel_l2(got[r], ref.physical(mode, xs[r])) < TOL[prec], (mode, r)
+
+
+def test_fields_shared_between_operators(gpu_available):
+    """A field created on one operator works with another of the same geometry and stream
+    (Grid fields belong to a grid), and is refused by an operator on another stream."""
+    dims, Ls = (4, 4, 4, 4), 8
+    op_a, _, U = mobius_pair(dims, Ls, 0.05, g.F64)
+    op_b = g.MobiusFermion(U, dims, Ls, 0.2, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], precision=g.F64)
+    ref_b = o.OracleOp(1, 0, dims, Ls, [0.2, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t())
+    x = fermion(int(np.prod(dims)), Ls, 60)
+    fin = op_a.FermionField().import_(x)
+    fout = op_a.FermionField()
+    op_b.M(fin, fout)
+    assert o.rel_l2(fout.export(), ref_b.apply(o.OP_M, x)) < TOL[g.F64]
+    s = g.Stream()
+    op_c = g.MobiusFermion(U, dims, Ls, 0.2, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], precision=g.F64, stream=s.ptr)
+    with pytest.raises(g.GridError):
+        op_c.M(fin, fout)
+    del op_c

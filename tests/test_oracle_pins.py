@@ -13,7 +13,8 @@ import pytest
 
 import grid_gb300 as g
 from oracle import oracle as o
-from tests._common import GAMMA, GAMMA5, MOBIUS, fermion, mobius_free_apply, mobius_free_solve, wilson_free_solve
+from tests._common import (GAMMA, GAMMA5, MOBIUS, dminus_free, fermion, mobius_free_apply, mobius_free_solve,
+                           wilson_free_solve)
 
 DIMS = (4, 4, 4, 4)
 VOL = 256
@@ -198,3 +199,27 @@ def test_oracle_fp32_matches_fp64_dhop():
     xo = o.pick(DIMS, 6, x, 1)
     assert o.rel_l2(of.dhop_cb(xo, 1), od.dhop_cb(xo, 1)) < 1e-6
     assert o.rel_l2(of.apply(o.OP_MPCDAGMPC, xo), od.apply(o.OP_MPCDAGMPC, xo)) < 1e-6
+
+
+@pytest.mark.parametrize("dag", [0, 1])
+def test_physical_surface_fields_free_field(dag):
+    """ImportUnphysicalFermion puts P+ eta at s = 0 and P- eta at s = Ls-1; the source export
+    undoes it and the solution export annihilates it; Dminus = 1 - c D_W agrees with the
+    momentum-space restatement at U = 1; ImportPhysicalFermionSource = Dminus of the
+    unphysical import (CayleyFermion5DImplementation.h:57-153)."""
+    Ls, mf = 6, 0.1
+    ref, _ = _mobius(Ls=Ls, mf=mf, U=g.unit_gauge(DIMS))
+    eta = fermion(VOL, 1, 5)
+    e5 = ref.physical(o.IMPORT_UNPHYSICAL, eta)
+    X = np.zeros((VOL, Ls, 4, 3), dtype=np.complex128)
+    E = eta.reshape(VOL, 4, 3)
+    X[:, 0, :2], X[:, Ls - 1, 2:] = E[:, :2], E[:, 2:]
+    assert np.array_equal(e5, X.reshape(-1))
+    assert np.array_equal(ref.physical(o.EXPORT_PHYSICAL_SOURCE, e5), eta)
+    assert not np.any(ref.physical(o.EXPORT_PHYSICAL_SOLUTION, e5))
+    psi = fermion(VOL, Ls, 6)
+    want = dminus_free(DIMS, Ls, MOBIUS["c"], MOBIUS["M5"], psi, dag=bool(dag))
+    assert o.rel_l2(ref.apply(o.OP_DMINUS_DAG if dag else o.OP_DMINUS, psi), want) < 1e-12
+    if not dag:
+        want = dminus_free(DIMS, Ls, MOBIUS["c"], MOBIUS["M5"], e5)
+        assert o.rel_l2(ref.physical(o.IMPORT_PHYSICAL_SOURCE, eta), want) < 1e-12
