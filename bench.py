@@ -86,7 +86,7 @@ class ClockSampler:
                     self.samples.append(parts)
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(0.05)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
@@ -181,22 +181,28 @@ def run_reference(args, ws, rank):
     from oracle import oracle as o
     threads = o.max_threads()
     op = o.OracleOp(1, 1, DIMS, LS, [MF, M5, B, C], U, g.antiperiodic_t())
+    t0 = time.perf_counter()
     for _ in range(max(1, min(args.warmup, 1))):
         op.dhop_cb(xo, 1)
+        op.dhop_cb(xe, 0)
+    t_step = time.perf_counter() - t0
+    # a bounded sample: at most ~120 s of timed CPU work whatever --steps asks for
+    n = max(1, min(args.steps, int(120.0 / max(t_step, 1e-6))))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(n):
         op.dhop_cb(xo, 1)
         op.dhop_cb(xe, 0)
     dt = time.perf_counter() - t0
-    gbs = 2 * args.steps * nh * bytes_per_site(1, LS) / dt / 1e9
+    gbs = 2 * n * nh * bytes_per_site(1, LS) / dt / 1e9
     line = {"metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": dt / n * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": "mobius_dwf_16^4xLs16_dhop_eo_oe_fp32", "dims": list(DIMS), "Ls": LS,
                        "b": B, "c": C, "M5": M5, "mf": MF, "eps": EPS},
             "cpu_baseline": {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} DhopEO+DhopOE steps of the full workload (oracle, OpenMP)"},
+                             "sample": f"{n} of {args.steps} DhopEO+DhopOE steps of the full workload timed "
+                                       "(oracle, OpenMP; at most ~120 s of CPU work)"},
             "e2e": {"value": gbs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -208,18 +214,20 @@ def run_gpu(args, ws, rank, local, dist):
     op = g.MobiusFermion(U, DIMS, LS, MF, M5, B, C, precision=g.F32)
     nh = op.half_sites4 * LS
     NSET = 4
+    # full fields: one Dhop launch computes DhopEO (odd -> even) and DhopOE (even -> odd)
     sets = []
     for k in range(NSET):
-        xo = op.FermionRedBlackField(g.ODD).import_(g.random_gaussian(nh * 12, 10 + k))
-        ye = op.FermionRedBlackField(g.EVEN)
-        xe = op.FermionRedBlackField(g.EVEN).import_(g.random_gaussian(nh * 12, 20 + k))
-        yo = op.FermionRedBlackField(g.ODD)
-        sets.append((xo, ye, xe, yo))
+        x = op.FermionField().import_(g.random_gaussian(2 * nh * 12, 10 + k))
+        sets.append((x, op.FermionField()))
+    halves = []
+    for k in range(NSET):
+        xo = op.FermionRedBlackField(g.ODD).import_(g.random_gaussian(nh * 12, 30 + k))
+        xe = op.FermionRedBlackField(g.EVEN).import_(g.random_gaussian(nh * 12, 40 + k))
+        halves.append((xo, op.FermionRedBlackField(g.EVEN), xe, op.FermionRedBlackField(g.ODD)))
 
     def step(k):
-        xo, ye, xe, yo = sets[k % NSET]
-        op.DhopEO(xo, ye, 0)
-        op.DhopOE(xe, yo, 0)
+        x, y = sets[k % NSET]
+        op.Dhop(x, y, 0)
 
     for k in range(max(3, args.warmup)):
         step(k)
@@ -234,49 +242,48 @@ def run_gpu(args, ws, rank, local, dist):
         op.event(1)
         op.sync()
         dt_ms = op.elapsed_ms(0, 1)
-        # per-kernel average launch time of the dominant kernel (DhopEO), same rotation
-        ins = [s[0] for s in sets]
-        outs = [s[1] for s in sets]
-        eo_ms = op.bench_kernel(0, ins, outs, max(20, 4 * args.steps))
-        ins = [s[2] for s in sets]
-        outs = [s[3] for s in sets]
-        oe_ms = op.bench_kernel(1, ins, outs, max(20, 4 * args.steps))
+        # average launch time of the dominant kernel (the one-launch Dhop), same rotation,
+        # and of the single-checkerboard launches
+        reps = max(20, args.steps)
+        full_ms = op.bench_kernel(6, [s[0] for s in sets], [s[1] for s in sets], reps)
+        eo_ms = op.bench_kernel(0, [h[0] for h in halves], [h[1] for h in halves], reps)
+        oe_ms = op.bench_kernel(1, [h[2] for h in halves], [h[3] for h in halves], reps)
     dt_ms = dist_max(dist, dt_ms)
     step_bytes = 2 * nh * bpsite
     value = dist_sum(dist, step_bytes * args.steps) / (dt_ms / 1e3) / 1e9 if dist else step_bytes * args.steps / (dt_ms / 1e3) / 1e9
 
     # ---- extra kernels of the config (Mooee, MooeeInv) ----
-    m_ms = op.bench_kernel(2, [s[1] for s in sets], [s[0] for s in sets], 40)
-    mi_ms = op.bench_kernel(3, [s[1] for s in sets], [s[0] for s in sets], 40)
+    m_ms = op.bench_kernel(2, [h[1] for h in halves], [h[0] for h in halves], 40)
+    mi_ms = op.bench_kernel(3, [h[1] for h in halves], [h[0] for h in halves], 40)
 
-    # ---- e2e through the C ABI with pinned host buffers ----
-    host_in = g.PinnedArray(nh * 12)
-    host_out = g.PinnedArray(nh * 12)
-    host_in.array[:] = g.random_gaussian(nh * 12, 99)
-    fin = op.FermionRedBlackField(g.ODD)
-    fout = op.FermionRedBlackField(g.EVEN)
+    # ---- e2e through the C ABI with pinned host buffers: canonical FP64 full fields in
+    # and out (Grid's host layout), one Dhop per step ----
+    host_in = g.PinnedArray(2 * nh * 12)
+    host_out = g.PinnedArray(2 * nh * 12)
+    host_in.array[:] = g.random_gaussian(2 * nh * 12, 99)
+    fin, fout = op.FermionField(), op.FermionField()
     import ctypes as Cc
     pin = host_in.array.ctypes.data_as(Cc.POINTER(Cc.c_double))
     pout = host_out.array.ctypes.data_as(Cc.POINTER(Cc.c_double))
     for _ in range(2):
         g.lib.gb_field_import(fin.h, pin)
-        g.lib.gb_DhopEO(op.h, fin.h, fout.h, 0)
+        g.lib.gb_Dhop(op.h, fin.h, fout.h, 0)
         g.lib.gb_field_export(fout.h, pout)
     e2e_steps = max(3, min(args.steps, 20))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         assert g.lib.gb_field_import(fin.h, pin) == 0
-        assert g.lib.gb_DhopEO(op.h, fin.h, fout.h, 0) == 0
+        assert g.lib.gb_Dhop(op.h, fin.h, fout.h, 0) == 0
         assert g.lib.gb_field_export(fout.h, pout) == 0
     e2e_dt = (time.perf_counter() - t0) / e2e_steps
     e2e_dt = dist_max(dist, e2e_dt)
-    e2e_value = nh * bpsite / e2e_dt / 1e9 * (ws if dist else 1)
+    e2e_value = step_bytes / e2e_dt / 1e9 * (ws if dist else 1)
 
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
-    achieved = nh * bpsite / (eo_ms / 1e3) / 1e9
-    traffic = profile_traffic("dhop_eo_dwf16_fp32.txt")
+    achieved = step_bytes / (full_ms / 1e3) / 1e9
+    traffic = profile_traffic("dhop_full_dwf16_fp32.txt")
     cpu = cpu_baseline_oracle(U, g.random_gaussian(nh * 12, 10), g.random_gaussian(nh * 12, 20)) if ws == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -284,18 +291,22 @@ def run_gpu(args, ws, rank, local, dist):
         "dtype": "f32", "data": "synthetic: seeded exp(i*0.5*H) gauge field, Gaussian spinors",
         "config": {"workload": "mobius_dwf_16^4xLs16_dhop_eo_oe_fp32", "dims": list(DIMS), "Ls": LS, "b": B, "c": C,
                    "M5": M5, "mf": MF, "eps": EPS, "boundary": "antiperiodic t",
-                   "l2": "4 rotating input/output sets, 800 MB total (> 129 MB L2)", "parallelism": f"replicas{ws}"},
+                   "step": "DhopEO + DhopOE as one full-lattice Dhop launch",
+                   "l2": "4 rotating input/output full-field sets, 800 MB total (> 129 MB L2)",
+                   "parallelism": f"replicas{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "dhop_kernel<float> (DhopEO)", "peak_source": peak_kind,
-                     "bytes_per_site": bpsite, "sites_per_launch": nh},
-        "kernels_ms": {"DhopEO": eo_ms, "DhopOE": oe_ms, "Mooee": m_ms, "MooeeInv": mi_ms},
-        "kernels_gbs": {"DhopEO": achieved, "DhopOE": nh * bpsite / (oe_ms / 1e3) / 1e9,
+                     "traffic": traffic, "kernel": "dhop_pair_kernel<float> (full Dhop, both checkerboards)",
+                     "peak_source": peak_kind, "bytes_per_site": bpsite, "sites_per_launch": 2 * nh},
+        "kernels_ms": {"Dhop": full_ms, "DhopEO": eo_ms, "DhopOE": oe_ms, "Mooee": m_ms, "MooeeInv": mi_ms},
+        "kernels_gbs": {"Dhop": achieved, "DhopEO": nh * bpsite / (eo_ms / 1e3) / 1e9,
+                        "DhopOE": nh * bpsite / (oe_ms / 1e3) / 1e9,
                         "Mooee": nh * 192 / (m_ms / 1e3) / 1e9, "MooeeInv": nh * 192 / (mi_ms / 1e3) / 1e9},
-        "gflops_dhop": 1320.0 * nh / (eo_ms / 1e3) / 1e9,
+        "gflops_dhop": 1320.0 * 2 * nh / (full_ms / 1e3) / 1e9,
         "clocks": clk.summary(),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nh * 12 * 16, "d2h_bytes_per_step": nh * 12 * 16,
-                "path": "gb_field_import (H2D canonical FP64) + gb_DhopEO + gb_field_export (D2H)"},
-        "gpu_launches": 2 * args.steps,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nh * 12 * 16,
+                "d2h_bytes_per_step": 2 * nh * 12 * 16,
+                "path": "gb_field_import (H2D canonical FP64 full field) + gb_Dhop + gb_field_export (D2H)"},
+        "gpu_launches": args.steps,
         "cpu_baseline": cpu,
     }
     if ws == 1 and not args.no_extras:
@@ -460,7 +471,7 @@ def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="only the headline DhopEO/DhopOE measurement")

@@ -147,6 +147,22 @@ struct Pair12 {
 
 template <class T> struct PairIO;
 template <> struct PairIO<float> {
+  // the loaded vectors of one site pair, before conversion (a prefetch buffer)
+  struct Raw {
+    float4 v[12];
+  };
+  static __device__ __forceinline__ void load_raw(const void* base, const float2*, size_t np, size_t q, Raw& r) {
+    const float4* p = static_cast<const float4*>(base) + q;
+#pragma unroll
+    for (int k = 0; k < 12; k++) r.v[k] = __ldg(p + size_t(k) * np);
+  }
+  static __device__ __forceinline__ void decode(const Raw& r, Pair12& f) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      f.re[k] = make_float2(r.v[k].x, r.v[k].y);
+      f.im[k] = make_float2(r.v[k].z, r.v[k].w);
+    }
+  }
   // q = pair index (= i/2), np = pairs per plane
   static __device__ __forceinline__ void load(const void* base, const float2*, size_t np, size_t q, Pair12& f) {
     const float4* p = static_cast<const float4*>(base) + q;
@@ -175,6 +191,26 @@ template <> struct PairIO<float> {
 };
 
 template <> struct PairIO<__half> {
+  struct Raw {
+    uint4 v[6];
+    float2 n;
+  };
+  static __device__ __forceinline__ void load_raw(const void* base, const float2* norms, size_t np, size_t q, Raw& r) {
+    const uint4* p = static_cast<const uint4*>(base) + q;
+    r.n = __ldg(norms + q);
+#pragma unroll
+    for (int g = 0; g < 6; g++) r.v[g] = __ldg(p + size_t(g) * np);
+  }
+  static __device__ __forceinline__ void decode(const Raw& r, Pair12& f) {
+#pragma unroll
+    for (int g = 0; g < 6; g++) {
+      const __half2* h = reinterpret_cast<const __half2*>(&r.v[g]);
+      f.re[2 * g] = __fmul2_rn(__half22float2(h[0]), r.n);
+      f.im[2 * g] = __fmul2_rn(__half22float2(h[1]), r.n);
+      f.re[2 * g + 1] = __fmul2_rn(__half22float2(h[2]), r.n);
+      f.im[2 * g + 1] = __fmul2_rn(__half22float2(h[3]), r.n);
+    }
+  }
   static __device__ __forceinline__ void load(const void* base, const float2* norms, size_t np, size_t q, Pair12& f) {
     const uint4* p = static_cast<const uint4*>(base) + q;
     const float2 n = __ldg(norms + q);

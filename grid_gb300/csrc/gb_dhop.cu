@@ -333,17 +333,31 @@ __device__ __forceinline__ void su3_mul2(const float2* __restrict__ U, const flo
   }
 }
 
-template <class T, bool DAG, int LEG, bool FIRST>
-__device__ __forceinline__ void dhop_pair_leg(const DhopParams& p, const int (&nb)[8], int sp, size_t np, int hl,
-                                              const float2* U, Pair12& acc) {
+// legs in visiting order: +mu and -mu back to back, x and y first (the +-x and +-y
+// neighbour rows of a CTA's x-rows overlap, so the second visit can hit in L1)
+__device__ constexpr int kLegOrder[8] = {0, 4, 1, 5, 2, 6, 3, 7};
+
+// neighbour spinors of GB_DHOP_PF legs ahead are in flight while a leg computes
+#ifndef GB_DHOP_PF
+#define GB_DHOP_PF 0
+#endif
+
+template <class T, bool DAG, int PF, int I>
+__device__ __forceinline__ void dhop_pair_step(const DhopParams& p, const int (&nb)[8], int sp, size_t np, int hl,
+                                               const float2* U, typename PairIO<T>::Raw (&buf)[PF + 1], Pair12& acc) {
+  constexpr int LEG = kLegOrder[I];
   constexpr int MU = LEG & 3;
   constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
+  if constexpr (I + PF < 8)
+    PairIO<T>::load_raw(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[kLegOrder[I + PF]]) * hl + sp,
+                        buf[(I + PF) % (PF + 1)]);
   Pair12 f;
-  PairIO<T>::load(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[LEG]) * hl + sp, f);
+  PairIO<T>::decode(buf[I % (PF + 1)], f);
   float2 hr[6], hi[6], ur[6], ui[6];
   project2<MU, S>(f, hr, hi);
   su3_mul2(U + LEG * 9, hr, hi, ur, ui);
-  reconstruct2<MU, S, FIRST>(acc, ur, ui);
+  reconstruct2<MU, S, I == 0>(acc, ur, ui);
+  if constexpr (I + 1 < 8) dhop_pair_step<T, DAG, PF, I + 1>(p, nb, sp, np, hl, U, buf, acc);
 }
 
 // resident CTAs of 128 threads per SM the register allocation targets
@@ -391,14 +405,12 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
   const size_t np = p.n5 >> 1;
   const float2* U = reinterpret_cast<const float2*>(slink + j * kLinkStride);
   Pair12 acc;
-  dhop_pair_leg<T, DAG, 0, true>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 4, false>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 1, false>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 5, false>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 2, false>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 6, false>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 3, false>(p, nb, sp, np, hl, U, acc);
-  dhop_pair_leg<T, DAG, 7, false>(p, nb, sp, np, hl, U, acc);
+  typename PairIO<T>::Raw buf[GB_DHOP_PF + 1];
+#pragma unroll
+  for (int i = 0; i < GB_DHOP_PF; i++)
+    PairIO<T>::load_raw(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[kLegOrder[i]]) * hl + sp,
+                        buf[i]);
+  dhop_pair_step<T, DAG, GB_DHOP_PF, 0>(p, nb, sp, np, hl, U, buf, acc);
   PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
 }
 
