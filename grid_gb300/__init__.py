@@ -9,6 +9,7 @@ from .api import (  # noqa: F401
     GridError, lib, LIB_PATH, F64, F32, F16, EVEN, ODD, FULL, DaggerNo, DaggerYes,
     FermionField, WilsonFermion, MobiusFermion, MdagMLinearOperator, SchurDiagMooeeOperator,
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
+    ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
     antiperiodic_t, periodic, set_device, PinnedArray, Stream, norm2, innerProduct, axpy, axpby, axpy_norm,
     pickCheckerboard, setCheckerboard, Server, Request, make_request, request_bytes,

@@ -565,6 +565,73 @@ class ConjugateGradientReliableUpdate(ConjugateGradient):
         return r
 
 
+MAX_SHIFTS = 32
+
+
+class MultiShiftResult(C.Structure):
+    _fields_ = [("nshift", C.c_int), ("iterations", C.c_int), ("converged", C.c_int),
+                ("iterations_shift", C.c_int * MAX_SHIFTS), ("true_residual_shift", C.c_double * MAX_SHIFTS),
+                ("seconds", C.c_double), ("flops", C.c_double)]
+
+
+_proto("gb_cg_multishift", [_vp, _i, _vp, _i, _dp, _dp, C.POINTER(_vp), _i, _i, C.POINTER(MultiShiftResult)])
+
+
+class MultiShiftFunction:
+    """MultiShiftFunction (Grid/algorithms/approx/MultiShiftFunction.h:34-64): the poles
+    (shifts, lightest first), residues, per-shift tolerances and norm of a partial-fraction
+    rational function  f(x) = norm + sum_s residues[s] / (x + poles[s])."""
+
+    def __init__(self, poles, residues=None, tolerances=1e-10, norm=0.0):
+        self.order = len(poles)
+        self.poles = [float(p) for p in poles]
+        self.residues = [1.0] * self.order if residues is None else [float(r) for r in residues]
+        self.tolerances = ([float(tolerances)] * self.order if np.isscalar(tolerances)
+                           else [float(t) for t in tolerances])
+        self.norm = float(norm)
+
+
+class ConjugateGradientMultiShift:
+    """ConjugateGradientMultiShift(maxit, shifts) (ConjugateGradientMultiShift.h:44-75):
+    called with a list of output fields it solves (A + poles[s]) psi[s] = src for every
+    shift; called with one output field it returns norm src + sum_s residues[s] psi[s]."""
+
+    def __init__(self, maxit, shifts: MultiShiftFunction, check_every=10):
+        self.MaxIterations = maxit
+        self.shifts = shifts
+        self.check_every = check_every
+        self.IterationsToComplete = 0
+        self.IterationsToCompleteShift = []
+        self.TrueResidualShift = []
+
+    def __call__(self, linop, src, psi):
+        if isinstance(psi, FermionField):
+            results = [FermionField(src.op, src.checkerboard, src.precision)
+                       for _ in range(self.shifts.order)]
+            self.solve(linop, src, results)
+            axpby(psi, self.shifts.norm, 0.0, src, src)
+            for res, r in zip(self.shifts.residues, results):
+                axpby(psi, 1.0, res, psi, r)
+            return psi
+        return self.solve(linop, src, psi)
+
+    def solve(self, linop, src, psi_list):
+        ns = self.shifts.order
+        if len(psi_list) != ns:
+            raise GridError(1, "one output field per shift expected")
+        m = np.ascontiguousarray(self.shifts.poles, dtype=np.float64)
+        t = np.ascontiguousarray(self.shifts.tolerances, dtype=np.float64)
+        ptrs = (_vp * ns)(*[f.h for f in psi_list])
+        r = MultiShiftResult()
+        _check(lib.gb_cg_multishift(linop.op.h, linop.kind, src.h, ns, _dptr(m), _dptr(t), ptrs,
+                                    int(self.MaxIterations), int(self.check_every), C.byref(r)))
+        self.IterationsToComplete = r.iterations
+        self.IterationsToCompleteShift = list(r.iterations_shift[:ns])
+        self.TrueResidualShift = list(r.true_residual_shift[:ns])
+        self.result = r
+        return r
+
+
 class SchurRedBlackDiagMooeeSolve:
     """SchurRedBlackDiagMooeeSolve(solver)(op, src, sol).  `solver` is a ConjugateGradient
     (plain, in op's precision) or a ConjugateGradientReliableUpdate (mixed precision, whose

@@ -233,6 +233,17 @@ static int m5d_field(Op* op, Field* psi, Field* phi, Field* chi, const std::vect
   return GB_OK;
 }
 
+// a fused s-column program on every checkerboard half of the fields (FP32 Moebius)
+static int col_field(Op* op, int opa, int opb, int dag, Field* x, Field* y, Field* out, double zc,
+                     const ColCoefsHost& h) {
+  const int halves = out->full() ? 2 : 1;
+  for (int k = 0; k < halves; k++) {
+    const HalfView yv = y ? half_view(y, k) : HalfView{nullptr, nullptr, x->prec};
+    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h));
+  }
+  return GB_OK;
+}
+
 int op_meooe5d(Op* op, Field* in, Field* out, int dag) {
   std::vector<double> l, d, u;
   coeffs_meooe5d(op, dag, l, d, u);
@@ -285,6 +296,7 @@ int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
   if (in->full() != out->full()) { set_error("MooeeInv: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
   if (op->kind == 0) return field_scale(out, 1.0 / op->diag_mass, in);
+  if (col_available(op, in->prec)) return col_field(op, COL_INV, COLB_NONE, dag, in, nullptr, out, 0.0, ColCoefsHost());
   const int halves = in->full() ? 2 : 1;
   for (int h = 0; h < halves; h++)
     GB_TRY(launch_mooee_inv(op, half_view(in, h), half_view(out, h), dag, size_t(op->half4)));
@@ -298,6 +310,30 @@ int op_mpc(Op* op, Field* in, Field* out, int dag) {
   GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E1, &te1));
   GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E2, &te2));
   GB_TRY(ws_get(op, GB_ODD, in->prec, WS_MPC_O, &to));
+  if (col_available(op, in->prec)) {
+    // the same sequence with the 5D steps fused into s-column programs:
+    //   Mpc    = Mooee in - DhopOE M5D MooeeInv DhopEO M5D in            (5 launches)
+    //   MpcDag = MooeeDag in - M5Ddag DhopOE^dag MooeeInvDag M5Ddag DhopEO^dag in  (4)
+    // (a lone M5D stays on the site-pair kernel, which is faster for it)
+    ColCoefsHost meo;
+    coeffs_meooe5d(op, dag, meo.l1, meo.d1, meo.u1);
+    te1->subset = te2->subset = GB_EVEN;
+    to->subset = out->subset = GB_ODD;
+    if (!dag) {
+      GB_TRY(op_meooe5d(op, in, to, 0));
+      GB_TRY(op_dhop_cb(op, to, te1, 0));
+      GB_TRY(col_field(op, COL_INV_M5D, COLB_NONE, 0, te1, nullptr, te2, 0.0, meo));
+      GB_TRY(op_dhop_cb(op, te2, to, 0));
+      return op_mooee(op, in, out, 0, to, -1.0);
+    }
+    GB_TRY(op_dhop_cb(op, in, te1, 1));
+    GB_TRY(col_field(op, COL_M5D_INV, COLB_NONE, 1, te1, nullptr, te2, 0.0, meo));
+    GB_TRY(op_dhop_cb(op, te2, to, 1));
+    ColCoefsHost h;
+    coeffs_mooee(op, 1, h.l1, h.d1, h.u1);
+    h.l2 = meo.l1; h.d2 = meo.d1; h.u2 = meo.u1;
+    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h);
+  }
   GB_TRY(op_meooe(op, in, te1, dag));
   GB_TRY(op_mooee_inv(op, te1, te2, dag));
   GB_TRY(op_meooe(op, te2, to, dag));

@@ -1,0 +1,259 @@
+// gb_col.cu -- fused s-column kernels of the Cayley 5D operators (FP32 site-pair layout).
+//
+// Every Cayley 5D operator acts on each spin-colour component of each (4D site, rhs)
+// column of Ls values on its own, because the chiral projectors P+- are diagonal in spin:
+// M5D (CayleyFermion5Dcache.h:41-115) couples s to s-1 (P+ components, non-dagger) or
+// s+1 (P- components), and MooeeInv (CayleyFermion5Dcache.h:117-230) is an LDU solve
+// along s.  A CTA stages Q columns x 12 components of its input(s) in shared memory with
+// coalesced 16-byte loads, one thread per (component, column) runs a short program of
+// these operators on its column in registers, and the CTA stores the result coalesced.
+//
+// Programs: out = A(x) + zc * B(y) with
+//   A in {M5D, INV, M5D(INV(x)), INV(M5D(x))},  B in {none, y, M5D(y)},
+// one dagger flag for the whole program.  They fuse the steps of
+// SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349) that touch no
+// neighbour in 4D: Mpc = Mooee - DhopOE M5D MooeeInv DhopEO M5D, and
+// MpcDag = MooeeDag - M5Ddag DhopOE^dag MooeeInvDag M5Ddag DhopEO^dag.
+#include <atomic>
+
+#include "gb_device.cuh"
+#include "gb_ops.h"
+
+namespace gb {
+
+template <int LS> struct ColCoef {
+  float d1[LS], u1[LS], l1[LS];  // M5D of A
+  float d2[LS], u2[LS], l2[LS];  // M5D of B
+  float lee[LS], leem[LS], uee[LS], ueem[LS], dinv[LS];  // LDU factors (dagger-swapped)
+};
+
+struct ColParams {
+  const float4* x;
+  const float4* y;
+  float4* out;
+  size_t np;  // float4 per component plane (site pairs per half field)
+  size_t nq;  // columns: 4D sites x right-hand sides
+  float zc;
+};
+
+// columns per CTA and the shared-memory slot of one column (an odd number of float4, so
+// the column reads of a quarter warp fall on distinct banks)
+template <int LS> __host__ __device__ constexpr int col_q() { return LS >= 16 ? 16 : 32; }
+template <int LS> __host__ __device__ constexpr int col_stride() { return (LS / 2) % 2 == 0 ? LS / 2 + 1 : LS / 2; }
+
+// chi_s = d_s x_s + (l_s x_{s-1} | u_s x_{s+1}) with the wrap inside the column
+template <int LS, bool DAG>
+__device__ __forceinline__ void col_m5d(const float (&xr)[LS], const float (&xi)[LS], float (&yr)[LS], float (&yi)[LS],
+                                        const float* d, const float* u, const float* l, bool upper) {
+  const bool from_minus = DAG ? !upper : upper;
+#pragma unroll
+  for (int s = 0; s < LS; s++) {
+    const float c = from_minus ? l[s] : u[s];
+    const float nr = from_minus ? xr[(s + LS - 1) % LS] : xr[(s + 1) % LS];
+    const float ni = from_minus ? xi[(s + LS - 1) % LS] : xi[(s + 1) % LS];
+    yr[s] = fmaf(c, nr, d[s] * xr[s]);
+    yi[s] = fmaf(c, ni, d[s] * xi[s]);
+  }
+}
+
+// in place LDU solve along s: forward sweep with lee (first chirality) or the leem
+// column (second), backward sweep with uee (second) or the ueem column (first)
+template <int LS>
+__device__ __forceinline__ void col_inv(float (&r)[LS], float (&i)[LS], const ColCoef<LS>& c, bool first) {
+  float pr = 0.f, pi = 0.f, ar = 0.f, ai = 0.f;
+#pragma unroll
+  for (int s = 0; s < LS; s++) {
+    float xr = r[s], xi = i[s];
+    if (s < LS - 1) {
+      if (first) {
+        if (s > 0) { xr = fmaf(-c.lee[s - 1], pr, xr); xi = fmaf(-c.lee[s - 1], pi, xi); }
+      } else {
+        ar = fmaf(c.leem[s], xr, ar); ai = fmaf(c.leem[s], xi, ai);
+      }
+      pr = xr; pi = xi;
+    } else {
+      if (first) { xr = fmaf(-c.lee[LS - 2], pr, xr); xi = fmaf(-c.lee[LS - 2], pi, xi); }
+      else { xr -= ar; xi -= ai; }
+      xr *= c.dinv[LS - 1]; xi *= c.dinv[LS - 1];
+    }
+    r[s] = xr; i[s] = xi;
+  }
+  const float lr = r[LS - 1], li = i[LS - 1];
+  float nr = lr, ni = li;
+#pragma unroll
+  for (int s = LS - 2; s >= 0; s--) {
+    float xr = r[s] * c.dinv[s], xi = i[s] * c.dinv[s];
+    if (!first) { xr = fmaf(-c.uee[s], nr, xr); xi = fmaf(-c.uee[s], ni, xi); }
+    else { xr = fmaf(-c.ueem[s], lr, xr); xi = fmaf(-c.ueem[s], li, xi); }
+    r[s] = xr; i[s] = xi;
+    nr = xr; ni = xi;
+  }
+}
+
+template <int LS>
+__device__ __forceinline__ void col_read(const float4* slot, float (&r)[LS], float (&i)[LS]) {
+#pragma unroll
+  for (int m = 0; m < LS / 2; m++) {
+    const float4 v = slot[m];
+    r[2 * m] = v.x; r[2 * m + 1] = v.y;
+    i[2 * m] = v.z; i[2 * m + 1] = v.w;
+  }
+}
+
+template <int LS, bool DAG, int OPA, int OPB>
+__global__ void __launch_bounds__(12 * col_q<LS>()) col_kernel(const ColParams p, const ColCoef<LS> c) {
+  constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+  extern __shared__ float4 col_tile[];  // [inputs][12][Q][ST]
+  float4* tx = col_tile;
+  float4* ty = col_tile + 12 * Q * ST;
+  const int t = threadIdx.x;
+  const size_t q0 = size_t(blockIdx.x) * Q;
+  const int qn = p.nq - q0 < size_t(Q) ? int(p.nq - q0) : Q;
+  const int nv = qn * H;  // float4 of one component plane in this CTA
+#pragma unroll 4
+  for (int e = t; e < 12 * Q * H; e += 12 * Q) {
+    const int k = e / (Q * H), r = e - k * (Q * H);
+    if (r < nv) {
+      const int qq = r / H, m = r - qq * H;
+      const size_t g = size_t(k) * p.np + q0 * H + r;
+      tx[(k * Q + qq) * ST + m] = __ldg(p.x + g);
+      if (OPB != COLB_NONE) ty[(k * Q + qq) * ST + m] = __ldg(p.y + g);
+    }
+  }
+  __syncthreads();
+  const int k = t / Q, qq = t - k * Q;
+  if (qq < qn) {
+    const bool upper = k < 6;
+    const bool first = DAG ? !upper : upper;
+    float4* slot = tx + (k * Q + qq) * ST;
+    float xr[LS], xi[LS], orr[LS], oi[LS];
+    col_read<LS>(slot, xr, xi);
+    if (OPA == COL_M5D) {
+      col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
+    } else if (OPA == COL_INV) {
+      col_inv<LS>(xr, xi, c, first);
+#pragma unroll
+      for (int s = 0; s < LS; s++) { orr[s] = xr[s]; oi[s] = xi[s]; }
+    } else if (OPA == COL_INV_M5D) {
+      col_inv<LS>(xr, xi, c, first);
+      col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
+    } else {  // COL_M5D_INV
+      col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
+      col_inv<LS>(orr, oi, c, first);
+    }
+    if (OPB != COLB_NONE) {
+      float yr[LS], yi[LS];
+      col_read<LS>(ty + (k * Q + qq) * ST, yr, yi);
+      if (OPB == COLB_M5D) {
+        col_m5d<LS, DAG>(yr, yi, xr, xi, c.d2, c.u2, c.l2, upper);
+#pragma unroll
+        for (int s = 0; s < LS; s++) { yr[s] = xr[s]; yi[s] = xi[s]; }
+      }
+#pragma unroll
+      for (int s = 0; s < LS; s++) { orr[s] = fmaf(p.zc, yr[s], orr[s]); oi[s] = fmaf(p.zc, yi[s], oi[s]); }
+    }
+#pragma unroll
+    for (int m = 0; m < H; m++) slot[m] = make_float4(orr[2 * m], orr[2 * m + 1], oi[2 * m], oi[2 * m + 1]);
+  }
+  __syncthreads();
+#pragma unroll 4
+  for (int e = t; e < 12 * Q * H; e += 12 * Q) {
+    const int k2 = e / (Q * H), r = e - k2 * (Q * H);
+    if (r < nv) {
+      const int q2 = r / H, m = r - q2 * H;
+      p.out[size_t(k2) * p.np + q0 * H + r] = tx[(k2 * Q + q2) * ST + m];
+    }
+  }
+}
+
+template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost& h, ColCoef<LS>& c) {
+  const std::vector<double>& lee = dag ? op->uee : op->lee;
+  const std::vector<double>& leem = dag ? op->ueem : op->leem;
+  const std::vector<double>& uee = dag ? op->lee : op->uee;
+  const std::vector<double>& ueem = dag ? op->leem : op->ueem;
+  for (int s = 0; s < LS; s++) {
+    c.d1[s] = h.d1.empty() ? 0.f : float(h.d1[s]);
+    c.u1[s] = h.u1.empty() ? 0.f : float(h.u1[s]);
+    c.l1[s] = h.l1.empty() ? 0.f : float(h.l1[s]);
+    c.d2[s] = h.d2.empty() ? 0.f : float(h.d2[s]);
+    c.u2[s] = h.u2.empty() ? 0.f : float(h.u2[s]);
+    c.l2[s] = h.l2.empty() ? 0.f : float(h.l2[s]);
+    c.lee[s] = float(lee[s]); c.leem[s] = float(leem[s]);
+    c.uee[s] = float(uee[s]); c.ueem[s] = float(ueem[s]);
+    c.dinv[s] = float(1.0 / op->dee[s]);
+  }
+}
+
+template <int LS, bool DAG, int OPA, int OPB>
+static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
+  constexpr int Q = col_q<LS>();
+  const size_t smem = size_t(OPB != COLB_NONE ? 2 : 1) * 12 * Q * col_stride<LS>() * sizeof(float4);
+  static std::atomic<bool> configured{false};
+  if (!configured.load()) {
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_kernel<LS, DAG, OPA, OPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(smem)));
+    configured.store(true);
+  }
+  const unsigned blocks = unsigned((p.nq + Q - 1) / Q);
+  col_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * Q, smem, op->stream>>>(p, c);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// the programs the operators use; the others are not instantiated
+template <int LS>
+static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h) {
+  ColCoef<LS> c;
+  fill_col<LS>(op, dag, h, c);
+  const int key = (dag ? 100 : 0) + opa * 10 + opb;
+  switch (key) {
+    case 0 + COL_M5D * 10 + COLB_NONE: return col_go<LS, false, COL_M5D, COLB_NONE>(op, p, c);
+    case 100 + COL_M5D * 10 + COLB_NONE: return col_go<LS, true, COL_M5D, COLB_NONE>(op, p, c);
+    case 0 + COL_M5D * 10 + COLB_IDENT: return col_go<LS, false, COL_M5D, COLB_IDENT>(op, p, c);
+    case 100 + COL_M5D * 10 + COLB_IDENT: return col_go<LS, true, COL_M5D, COLB_IDENT>(op, p, c);
+    case 0 + COL_INV * 10 + COLB_NONE: return col_go<LS, false, COL_INV, COLB_NONE>(op, p, c);
+    case 100 + COL_INV * 10 + COLB_NONE: return col_go<LS, true, COL_INV, COLB_NONE>(op, p, c);
+    case 0 + COL_INV_M5D * 10 + COLB_NONE: return col_go<LS, false, COL_INV_M5D, COLB_NONE>(op, p, c);
+    case 100 + COL_M5D_INV * 10 + COLB_NONE: return col_go<LS, true, COL_M5D_INV, COLB_NONE>(op, p, c);
+    case 100 + COL_M5D * 10 + COLB_M5D: return col_go<LS, true, COL_M5D, COLB_M5D>(op, p, c);
+  }
+  set_error("column program (%d, %d, dag %d) is not instantiated", opa, opb, dag);
+  return GB_ERR_UNSUPPORTED;
+}
+
+bool col_available(const Op* op, int prec) {
+  if (op->kind != 1 || prec != GB_F32) return false;
+  switch (op->Ls) {
+    case 4: case 6: case 8: case 10: case 12: case 16: case 20: case 24: return true;
+  }
+  return false;
+}
+
+int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
+               const ColCoefsHost& h) {
+  if (!col_available(op, x.prec) || out.prec != x.prec || (opb != COLB_NONE && y.prec != x.prec)) {
+    set_error("column kernel: FP32 Moebius fields with an instantiated Ls expected");
+    return GB_ERR_UNSUPPORTED;
+  }
+  ColParams p;
+  p.x = static_cast<const float4*>(x.data);
+  p.y = static_cast<const float4*>(y.data);
+  p.out = static_cast<float4*>(out.data);
+  p.np = op->n5() >> 1;
+  p.nq = size_t(op->half4) * op->nrhs;
+  p.zc = float(zc);
+  switch (op->Ls) {
+    case 4: return col_ls<4>(op, opa, opb, dag, p, h);
+    case 6: return col_ls<6>(op, opa, opb, dag, p, h);
+    case 8: return col_ls<8>(op, opa, opb, dag, p, h);
+    case 10: return col_ls<10>(op, opa, opb, dag, p, h);
+    case 12: return col_ls<12>(op, opa, opb, dag, p, h);
+    case 16: return col_ls<16>(op, opa, opb, dag, p, h);
+    case 20: return col_ls<20>(op, opa, opb, dag, p, h);
+    case 24: return col_ls<24>(op, opa, opb, dag, p, h);
+  }
+  set_error("column kernel: Ls = %d not instantiated", op->Ls);
+  return GB_ERR_UNSUPPORTED;
+}
+
+}  // namespace gb

@@ -177,6 +177,18 @@ inline int red_parts(Op* op, int prec) {
   return g;
 }
 
+// fused s-column programs of the Cayley 5D operators (gb_col.cu, FP32 Moebius):
+// out = A(x) + zc * B(y), one dagger flag for the program
+enum { COL_M5D = 0, COL_INV = 1, COL_INV_M5D = 2, COL_M5D_INV = 3 };  // A: M5D, INV, M5D(INV x), INV(M5D x)
+enum { COLB_NONE = 0, COLB_IDENT = 1, COLB_M5D = 2 };                 // B: -, y, M5D(y)
+struct ColCoefsHost {
+  std::vector<double> l1, d1, u1;  // M5D of A (lower, diagonal, upper per s)
+  std::vector<double> l2, d2, u2;  // M5D of B
+};
+bool col_available(const Op* op, int prec);
+int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
+               const ColCoefsHost& h);
+
 // layout conversion between canonical FP64 (device) and the device layout
 int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full);
 int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon_is_full);

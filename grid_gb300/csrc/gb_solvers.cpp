@@ -81,6 +81,8 @@ int true_residual(Op* op, int kind, Field* src, Field* psi, Field* mmp, Field* t
   return GB_OK;
 }
 
+}  // namespace
+
 // flops per CG iteration in Grid's model: 1452 per half-checkerboard 5D site for each of
 // the four Meooe of MpcDagMpc plus 336 of linear algebra (Test_dwf_mixedcg_prec.cc:138-140,
 // ConjugateGradient.h:204-205); Wilson: 1320 per Dhop site; MdagM: two full M.
@@ -89,6 +91,8 @@ double hermop_flops(const Op* op, int kind) {
   if (kind == 0) return 2 * half5 * (2 * 1320.0 + (op->kind ? 2 * 120.0 : 48.0)) + 2 * half5 * 336.0;
   return half5 * (4 * (op->kind ? 1452.0 : 1320.0) + 336.0);
 }
+
+namespace {
 
 int field_for(Op* op, int kind, int subset_half, int prec, int slot_half, int slot_full, Field** out) {
   if (kind == 0) return ws_get(op, GB_FULL, prec, slot_full, out);

@@ -199,6 +199,26 @@ int gb_cg_last_per_rhs(gb_op_t op, int* iterations, double* true_residual);
  * same gauge field; kind 0 = MdagM (full fields), 1 = Schur (odd half fields). */
 int gb_cg_reliable(gb_op_t op_d, gb_op_t op_lo, int kind, gb_field_t src, gb_field_t psi, const gb_cg_params* p,
                    gb_cg_result* res);
+/* ConjugateGradientMultiShift (Grid/algorithms/iterative/ConjugateGradientMultiShift.h:76-330):
+ * solves (A + shifts[s]) psi[s] = src for nshift <= GB_MAX_SHIFTS shifts at once, A = MdagM
+ * (kind 0, full fields) or MpcDagMpc (kind 1, odd fields); shifts[0] must be the lightest
+ * (MultiShiftFunction::poles), tolerances[s] is shift s's target |r_s|/|src|.  FP64 or
+ * FP32 operators, one right-hand side.  psi[s] are outputs (no initial guess, as in Grid).
+ * The rational sum psi = norm src + sum_s residues[s] psi[s] is left to the caller
+ * (gb_field_axpby). */
+#define GB_MAX_SHIFTS 32
+typedef struct {
+  int nshift;
+  int iterations;                              /* IterationsToComplete                  */
+  int converged;                               /* 1 when every shift converged          */
+  int iterations_shift[GB_MAX_SHIFTS];         /* IterationsToCompleteShift             */
+  double true_residual_shift[GB_MAX_SHIFTS];   /* TrueResidualShift                     */
+  double seconds;
+  double flops;                                /* Grid's flop model of the A applications */
+} gb_multishift_result;
+int gb_cg_multishift(gb_op_t op, int kind, gb_field_t src, int nshift, const double* shifts, const double* tolerances,
+                     gb_field_t* psi, int max_iterations, int check_every, gb_multishift_result* res);
+
 /* SchurRedBlackDiagMooeeSolve(CG)(M, src, sol) (SchurRedBlack.h:236-291,373-436).
  * op_lo == NULL: plain CG in op's precision; else mixed precision (reliable update).
  * unprec_resid (may be NULL): |M sol - src| / |src| per right-hand side. */

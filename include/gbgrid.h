@@ -712,6 +712,69 @@ template <class FieldD, class FieldF> class ConjugateGradientReliableUpdate : pu
   }
 };
 
+// MultiShiftFunction (Grid/algorithms/approx/MultiShiftFunction.h:34-64): a partial-fraction
+// rational function f(x) = norm + sum_i residues[i] / (x + poles[i]).  The Remez
+// construction of Grid's AlgRemez is not part of this library: fill the arrays directly.
+class MultiShiftFunction {
+ public:
+  int order = 0;
+  std::vector<RealD> poles, residues, tolerances;
+  RealD norm = 0, lo = 0, hi = 0;
+  MultiShiftFunction() {}
+  MultiShiftFunction(int n, RealD _lo, RealD _hi) : order(n), poles(n), residues(n), tolerances(n), lo(_lo), hi(_hi) {}
+  RealD approx(RealD x) const {
+    RealD a = norm;
+    for (int i = 0; i < order; i++) a += residues[i] / (x + poles[i]);
+    return a;
+  }
+};
+
+// ConjugateGradientMultiShift(maxit, shifts) (ConjugateGradientMultiShift.h:44-75): solves
+// (A + poles[i]) results[i] = src for every pole at once on a library linear operator;
+// the one-field form returns norm src + sum_i residues[i] results[i].
+template <class Field> class ConjugateGradientMultiShift : public OperatorFunction<Field> {
+ public:
+  Integer MaxIterations;
+  Integer IterationsToComplete = 0;
+  std::vector<int> IterationsToCompleteShift;
+  std::vector<RealD> TrueResidualShift;
+  MultiShiftFunction shifts;
+  int CheckEvery = 10;
+  ConjugateGradientMultiShift(Integer maxit, const MultiShiftFunction& s)
+      : MaxIterations(maxit), IterationsToCompleteShift(s.order), TrueResidualShift(s.order), shifts(s) {}
+
+  void operator()(LinearOperatorBase<Field>& Linop, const Field& src, std::vector<Field>& results) {
+    gb_op_t op = Linop.library_op();
+    if (!op) throw GridError(GB_ERR_UNSUPPORTED, "ConjugateGradientMultiShift: a library linear operator expected");
+    if (int(results.size()) != shifts.order) throw GridError(GB_ERR_BAD_ARG, "one result field per pole expected");
+    std::vector<gb_field_t> h(results.size());
+    for (size_t i = 0; i < results.size(); i++) h[i] = results[i].handle();
+    gb_multishift_result r;
+    const int rc = gb_cg_multishift(op, Linop.library_kind(), src.handle(), shifts.order, shifts.poles.data(),
+                                    shifts.tolerances.data(), h.data(), MaxIterations, CheckEvery, &r);
+    IterationsToComplete = r.iterations;
+    for (int i = 0; i < shifts.order; i++) {
+      IterationsToCompleteShift[i] = r.iterations_shift[i];
+      TrueResidualShift[i] = r.true_residual_shift[i];
+    }
+    gbdetail::check(rc, "ConjugateGradientMultiShift");
+  }
+  void operator()(LinearOperatorBase<Field>& Linop, const Field& src, std::vector<Field>& results, Field& psi) {
+    (*this)(Linop, src, results);
+    axpby(psi, shifts.norm, 0.0, src, src);
+    for (int i = 0; i < shifts.order; i++) axpby(psi, 1.0, shifts.residues[i], psi, results[i]);
+  }
+  void operator()(LinearOperatorBase<Field>& Linop, const Field& src, Field& psi) override {
+    std::vector<Field> results;
+    results.reserve(shifts.order);
+    for (int i = 0; i < shifts.order; i++) {
+      results.emplace_back(src.Grid());
+      results.back().Checkerboard() = int(src.Checkerboard());
+    }
+    (*this)(Linop, src, results, psi);
+  }
+};
+
 // SchurRedBlackDiagMooeeSolve(OperatorFunction&) (SchurRedBlack.h:373-436).  The CG is a
 // library ConjugateGradient; an optional lower-precision operator of the same action
 // turns the inner solve into the mixed-precision reliable-update CG.

@@ -31,6 +31,8 @@
 //   red-black solve        Grid/algorithms/iterative/SchurRedBlack.h:236-291,373-436
 //   CG                     Grid/algorithms/iterative/ConjugateGradient.h:68-257
 //   reliable-update CG     Grid/algorithms/iterative/ConjugateGradientReliableUpdate.h:77-269
+//   multishift CG          Grid/algorithms/iterative/ConjugateGradientMultiShift.h:76-330
+//   Dminus, 4D<->5D        Grid/qcd/action/fermion/implementation/CayleyFermion5DImplementation.h:57-153
 //
 // Canonical host layout (also the library's C-ABI layout):
 //   4D site index  site = x + Lx*(y + Ly*(z + Lz*t))
@@ -41,6 +43,7 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -621,6 +624,103 @@ CGResult cg(HermOp&& A, const Field<R>& src, Field<R>& psi, double tol, int maxi
   A(psi, mmp);
   for (size_t i = 0; i < n; i++) p[i] = mmp[i] - src[i];
   res.true_residual = std::sqrt(norm2(p) / ssq);
+  return res;
+}
+
+// ConjugateGradientMultiShift (ConjugateGradientMultiShift.h:76-330): (A + m_s) psi_s = src
+// for every shift, m_0 the lightest; the same sequence of operations as Grid's.
+struct MultiShiftResult {
+  int iterations = 0;
+  int converged = 0;
+  std::vector<int> iterations_shift;
+  std::vector<double> true_residual;
+};
+
+template <class HermOp>
+MultiShiftResult cg_multishift(HermOp&& A, const Field<double>& src, std::vector<Field<double>>& psi,
+                               const std::vector<double>& mass, const std::vector<double>& tol, int maxit) {
+  MultiShiftResult res;
+  const int ns = int(mass.size());
+  const size_t n = src.size();
+  psi.assign(ns, Field<double>(n));
+  res.iterations_shift.assign(ns, 0);
+  res.true_residual.assign(ns, 0.0);
+  std::vector<Field<double>> ps(ns, src);
+  std::vector<double> bs(ns), rsq(ns);
+  std::vector<std::array<double, 2>> z(ns);
+  std::vector<int> conv(ns, 0);
+  Field<double> r = src, p = src, mmp(n), tmp(n);
+  double cp = norm2(src);
+  if (cp == 0.0) {
+    for (int s = 0; s < ns; s++) res.iterations_shift[s] = 1;
+    res.converged = 1;
+    return res;
+  }
+  const double ssq = cp;
+  for (int s = 0; s < ns; s++) rsq[s] = cp * tol[s] * tol[s];
+  auto apply = [&](const Field<double>& x, Field<double>& y, double m) {  // y = (A + m) x ; returns <x,y>
+    A(x, y);
+    for (size_t i = 0; i < n; i++) y[i] += m * x[i];
+    return inner(x, y).real();
+  };
+  double d = apply(p, mmp, mass[0]);
+  double b = -cp / d, a = 0, c = 0, bp = 0;
+  int iz = 0;
+  z[0][0] = z[0][1] = 1.0;
+  bs[0] = b;
+  for (int s = 1; s < ns; s++) {
+    z[s][1 - iz] = 1.0;
+    z[s][iz] = 1.0 / (1.0 - b * (mass[s] - mass[0]));
+    bs[s] = b * z[s][iz];
+  }
+  for (size_t i = 0; i < n; i++) r[i] += b * mmp[i];
+  c = norm2(r);
+  for (int s = 0; s < ns; s++)
+    for (size_t i = 0; i < n; i++) psi[s][i] = -bs[s] * src[i];
+  for (int k = 1; k <= maxit; k++) {
+    a = c / cp;
+    for (size_t i = 0; i < n; i++) p[i] = a * p[i] + r[i];
+    for (int s = 0; s < ns; s++) {
+      if (conv[s]) continue;
+      if (s == 0) {
+        for (size_t i = 0; i < n; i++) ps[s][i] = a * ps[s][i] + r[i];
+      } else {
+        const double as = a * z[s][iz] * bs[s] / (z[s][1 - iz] * b);
+        for (size_t i = 0; i < n; i++) ps[s][i] = z[s][iz] * r[i] + as * ps[s][i];
+      }
+    }
+    cp = c;
+    d = apply(p, mmp, mass[0]);
+    bp = b;
+    b = -cp / d;
+    for (size_t i = 0; i < n; i++) r[i] += b * mmp[i];
+    c = norm2(r);
+    bs[0] = b;
+    iz = 1 - iz;
+    for (int s = 1; s < ns; s++) {
+      if (conv[s]) continue;
+      const double z0 = z[s][1 - iz], z1 = z[s][iz];
+      z[s][iz] = z0 * z1 * bp / (b * a * (z1 - z0) + z1 * bp * (1 - (mass[s] - mass[0]) * b));
+      bs[s] = b * z[s][iz] / z0;
+    }
+    for (int s = 0; s < ns; s++)
+      if (!conv[s])
+        for (size_t i = 0; i < n; i++) psi[s][i] -= bs[s] * ps[s][i];
+    int all = 1;
+    for (int s = 0; s < ns; s++) {
+      if (conv[s]) continue;
+      res.iterations_shift[s] = k;
+      if (c * z[s][iz] * z[s][iz] < rsq[s]) conv[s] = 1;
+      else all = 0;
+    }
+    res.iterations = k;
+    if (all) { res.converged = 1; break; }
+  }
+  for (int s = 0; s < ns; s++) {
+    apply(psi[s], mmp, mass[s]);
+    for (size_t i = 0; i < n; i++) tmp[i] = mmp[i] - src[i];
+    res.true_residual[s] = std::sqrt(norm2(tmp) / ssq);
+  }
   return res;
 }
 

@@ -53,6 +53,7 @@ def lib():
         L.orc_schur_solve.argtypes = [vp, dp, dp, d, i, ip, dp]
         L.orc_cg_reliable.argtypes = [vp, vp, i, dp, dp, d, i, d, i, i, ip, dp]
         L.orc_physical.argtypes = [vp, i, dp, dp]
+        L.orc_cg_multishift.argtypes = [vp, i, dp, i, dp, dp, i, dp, ip, dp]
         L.orc_set_threads.argtypes = [i]
         L.orc_max_threads.restype = i
         _lib = L
@@ -137,6 +138,19 @@ class OracleOp:
         res = C.c_double()
         lib().orc_cg(self.h, kind, _p(src), _p(psi), float(tol), int(maxit), info, C.byref(res))
         return psi, info[0], res.value
+
+    def cg_multishift(self, kind, src, shifts, tols, maxit):
+        """(A + shifts[s]) psi_s = src for every shift (FP64); returns (psi list, iterations,
+        converged, iterations per shift, true residual per shift)."""
+        src = np.ascontiguousarray(src, dtype=np.complex128)
+        ns = len(shifts)
+        psi = np.zeros((ns, src.size), dtype=np.complex128)
+        info = (C.c_int * (2 + ns))()
+        res = (C.c_double * ns)()
+        m = np.ascontiguousarray(shifts, dtype=np.float64)
+        t = np.ascontiguousarray(tols, dtype=np.float64)
+        lib().orc_cg_multishift(self.h, kind, _p(src), ns, _p(m), _p(t), int(maxit), _p(psi), info, res)
+        return list(psi), info[0], info[1], list(info[2:]), list(res)
 
     def schur_solve(self, src, tol, maxit):
         src = np.ascontiguousarray(src, dtype=np.complex128)

@@ -275,3 +275,32 @@ int orc_cg_reliable(void* pd, void* pf, int kind, const double* src, double* psi
 }
 
 }  // extern "C"
+
+extern "C" {
+// ConjugateGradientMultiShift in double (ConjugateGradientMultiShift.h:76-330): kind 0
+// MdagM (full field), 1 MpcDagMpc (odd half field).  psi: nshift fields back to back.
+// info = {iterations, converged, iterations of shift 0, 1, ...}; resid: true residual per shift.
+int orc_cg_multishift(void* p, int kind, const double* src, int nshift, const double* mass, const double* tol,
+                      int maxit, double* psi, int* info, double* resid) {
+  Handle* h = static_cast<Handle*>(p);
+  if (h->prec != 0) return 1;
+  Op<double>* op = h->d;
+  const size_t n = kind == 0 ? op->full_len() : op->half_len();
+  Field<double> s = load<double>(src, n);
+  std::vector<Field<double>> x;
+  std::vector<double> m(mass, mass + nshift), t(tol, tol + nshift);
+  MultiShiftResult r;
+  if (kind == 0)
+    r = cg_multishift([&](const Field<double>& a, Field<double>& b) { op->MdagM(a, b); }, s, x, m, t, maxit);
+  else
+    r = cg_multishift([&](const Field<double>& a, Field<double>& b) { op->MpcDagMpc(a, b); }, s, x, m, t, maxit);
+  for (int k = 0; k < nshift; k++) {
+    store<double>(x[k], psi + size_t(k) * n * 2);
+    info[2 + k] = r.iterations_shift[k];
+    resid[k] = r.true_residual[k];
+  }
+  info[0] = r.iterations;
+  info[1] = r.converged;
+  return r.converged ? 0 : 5;
+}
+}

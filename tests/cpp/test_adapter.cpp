@@ -1,6 +1,6 @@
 // Grid-style program on the C++ adapter (include/gbgrid.h): the even-odd identities of
 // tests/core/Test_mobius_even_odd.cc, the Schur red-black solve, the mixed-precision
-// reliable-update CG of tests/Test_dwf_mixedcg_prec.cc, the unpreconditioned Wilson CG of
+// reliable-update CG of tests/Test_dwf_mixedcg_prec.cc, the multishift CG, the unpreconditioned Wilson CG of
 // tests/solver/Test_wilson_cg_unprec.cc, a user-defined linear operator through the
 // host-driven CG, and the 4D <-> 5D surface fields.  Exit status 0 when every check holds.
 #include <cstdio>
@@ -126,6 +126,38 @@ int main() {
   Shifted.HermOp(x, Ax);
   Ax = Ax - src;
   expect(std::sqrt(norm2(Ax) / norm2(src)) < 1e-9, "host-driven CG on a user operator", std::sqrt(norm2(Ax) / norm2(src)));
+
+  // ---- multishift CG on the Schur operator (tests/solver/Test_dwf_multishift_mixedprec.cc pattern) ----
+  MultiShiftFunction Sqrt(3, 0.01, 10.0);
+  Sqrt.poles = {0.01, 0.1, 1.0};
+  Sqrt.residues = {0.3, 0.6, 1.1};
+  Sqrt.tolerances = {1e-10, 1e-10, 1e-10};
+  Sqrt.norm = 0.2;
+  ConjugateGradientMultiShift<LatticeFermion> MSCG(5000, Sqrt);
+  std::vector<LatticeFermion> shifted;
+  for (int i = 0; i < 3; i++) {
+    shifted.emplace_back(FrbGrid);
+    shifted.back().Checkerboard() = Odd;
+  }
+  MSCG(HermOpEO, src_o, shifted);
+  RealD worst = 0;
+  for (int i = 0; i < 3; i++) {
+    LatticeFermion chk(FrbGrid);
+    HermOpEO.HermOp(shifted[i], chk);
+    axpy(chk, Sqrt.poles[i], shifted[i], chk);
+    chk = chk - src_o;
+    worst = std::max(worst, std::sqrt(norm2(chk) / norm2(src_o)));
+  }
+  std::printf("multishift CG: %d iterations\n", MSCG.IterationsToComplete);
+  expect(worst < 2e-10, "multishift (A + m_i) x_i == src", worst);
+  LatticeFermion rat(FrbGrid);
+  MSCG(HermOpEO, src_o, rat);
+  LatticeFermion want(FrbGrid);
+  axpby(want, Sqrt.norm, 0.0, src_o, src_o);
+  for (int i = 0; i < 3; i++) axpby(want, 1.0, Sqrt.residues[i], want, shifted[i]);
+  LatticeFermion drat = rat - want;
+  expect(std::sqrt(norm2(drat) / norm2(want)) < 1e-12, "rational sum norm src + sum residues x_i",
+         std::sqrt(norm2(drat) / norm2(want)));
 
   // ---- unpreconditioned Wilson CG (Test_wilson_cg_unprec.cc) ----
   WilsonFermionD Dw(Umu, *UGrid, *UrbGrid, 0.1, params);

@@ -223,3 +223,22 @@ def test_physical_surface_fields_free_field(dag):
     if not dag:
         want = dminus_free(DIMS, Ls, MOBIUS["c"], MOBIUS["M5"], e5)
         assert o.rel_l2(ref.physical(o.IMPORT_PHYSICAL_SOURCE, eta), want) < 1e-12
+
+
+def test_oracle_multishift_free_wilson():
+    """The multishift CG restatement (ConjugateGradientMultiShift.h:76-330) solves
+    (MdagM + sigma) psi = eta for every shift: checked at U = 1 against the momentum-space
+    solve of the free Wilson operator, M(k)^dagger M(k) + sigma."""
+    from tests._common import _from_k, _to_k, wilson_dirac_k
+    mass, shifts = 0.1, [0.0, 0.05, 0.3, 1.2]
+    ref, _ = _wilson(mass=mass, U=g.unit_gauge(DIMS))
+    eta = fermion(VOL, 1, 21)
+    psi, it, conv, its, res = ref.cg_multishift(0, eta, shifts, [1e-11] * 4, 3000)
+    assert conv == 1 and its[0] == it and all(i <= it for i in its)
+    Mk = wilson_dirac_k(DIMS) + mass * np.eye(4)
+    MdM = np.conj(np.swapaxes(Mk, -1, -2)) @ Mk
+    ek = _to_k(DIMS, eta, 4, True)
+    for s, x, r in zip(shifts, psi, res):
+        want = _from_k(DIMS, np.linalg.solve(MdM + s * np.eye(4), ek), True)
+        assert r < 1e-10
+        assert o.rel_l2(x, want) < 1e-9, s
