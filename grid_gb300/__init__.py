@@ -6,10 +6,11 @@ operator and solver classes over that ABI.  Importing the package loads the libr
 raises if it has not been built: there is no CPU fallback.
 """
 from .api import (  # noqa: F401
-    GridError, lib, LIB_PATH, F64, F32, F16, EVEN, ODD, FULL, DaggerNo, DaggerYes,
+    GridError, lib, LIB_PATH, F64, F32, F16, RECON12, EVEN, ODD, FULL, DaggerNo, DaggerYes,
     FermionField, WilsonFermion, MobiusFermion, MdagMLinearOperator, SchurDiagMooeeOperator,
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
+    NerscHeader, nersc_read_header, nersc_read, nersc_write, gauge_stats,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
     antiperiodic_t, periodic, set_device, PinnedArray, Stream, norm2, innerProduct, axpy, axpby, axpy_norm,
     pickCheckerboard, setCheckerboard, Server, Request, make_request, request_bytes,

@@ -26,6 +26,7 @@ import numpy as np
 LIB_PATH = Path(__file__).resolve().with_name("libgbdwf.so")
 
 F64, F32, F16 = 0, 1, 2
+RECON12 = 1  # gb_*_create flag GB_FLAG_RECON12: 12-real links
 EVEN, ODD, FULL = 0, 1, 2
 DaggerNo, DaggerYes = 0, 1
 
@@ -743,3 +744,51 @@ class Server:
 
     def __del__(self):
         self.close()
+
+
+# ---- NERSC gauge files (Grid/parallelIO/NerscIO.h) -------------------------------------
+class NerscHeader(C.Structure):
+    _fields_ = [("dims", C.c_int * 4), ("two_row", C.c_int), ("bits", C.c_int), ("big_endian", C.c_int),
+                ("sequence_number", C.c_int), ("data_start", C.c_int64), ("link_trace", C.c_double),
+                ("plaquette", C.c_double), ("checksum", C.c_uint32), ("checksum_computed", C.c_uint32),
+                ("link_trace_computed", C.c_double), ("plaquette_computed", C.c_double),
+                ("data_type", C.c_char * 64), ("floating_point", C.c_char * 32), ("ensemble_id", C.c_char * 64),
+                ("ensemble_label", C.c_char * 64), ("boundary", (C.c_char * 32) * 4)]
+
+
+_proto("gb_nersc_read_header", [C.c_char_p, C.POINTER(NerscHeader)])
+_proto("gb_nersc_read", [C.c_char_p, _vp, _i, C.POINTER(NerscHeader), _i])
+_proto("gb_nersc_write", [C.c_char_p, _vp, _i, _ip, _i, _i, _i, C.c_char_p, C.c_char_p, _i])
+_proto("gb_gauge_stats", [_ip, _vp, _i, _dp, _dp])
+
+
+def nersc_read_header(path) -> NerscHeader:
+    h = NerscHeader()
+    _check(lib.gb_nersc_read_header(str(path).encode(), C.byref(h)))
+    return h
+
+
+def nersc_read(path, check=True):
+    """NerscIO::readConfiguration: (canonical FP64 gauge field, header).  The checksum,
+    plaquette and link trace are verified when `check` (GridError otherwise)."""
+    h = nersc_read_header(path)
+    U = np.empty(int(np.prod(list(h.dims))) * 36, dtype=np.complex128)
+    _check(lib.gb_nersc_read(str(path).encode(), U.ctypes.data, 0, C.byref(h), int(bool(check))))
+    return U, h
+
+
+def nersc_write(path, U, dims, two_row=False, bits=64, big_endian=True, ensemble_id="UKQCD", ensemble_label="DWF",
+                sequence_number=1):
+    """NerscIO::writeConfiguration of a canonical FP64 gauge field."""
+    U = np.ascontiguousarray(U, dtype=np.complex128)
+    _check(lib.gb_nersc_write(str(path).encode(), U.ctypes.data, 0, _dims(dims), int(bool(two_row)), int(bits),
+                              int(bool(big_endian)), ensemble_id.encode(), ensemble_label.encode(),
+                              int(sequence_number)))
+
+
+def gauge_stats(dims, U):
+    """(avgPlaquette, linkTrace) of a canonical gauge field, computed on the device."""
+    U = np.ascontiguousarray(U, dtype=np.complex128)
+    p, t = C.c_double(), C.c_double()
+    _check(lib.gb_gauge_stats(_dims(dims), U.ctypes.data, 0, C.byref(p), C.byref(t)))
+    return p.value, t.value

@@ -22,7 +22,7 @@ void set_error(const char* fmt, ...) {
   va_end(ap);
 }
 
-size_t Op::link_bytes_per_parity() const { return size_t(half4) * 8 * 18 * (prec == GB_F64 ? 8 : 4); }
+size_t Op::link_bytes_per_parity() const { return size_t(half4) * 8 * (recon12 ? 12 : 18) * (prec == GB_F64 ? 8 : 4); }
 
 size_t Field::half_bytes() const { return n5 * spinor_bytes(prec); }
 void* Field::half_ptr(int parity) const {
@@ -507,6 +507,12 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
     const std::complex<double> z = op->phases[k];
     if (!(z.imag() == 0 && (z.real() == 1 || z.real() == -1))) op->phases_pm1 = false;
   }
+  op->recon12 = (flags & GB_FLAG_RECON12) != 0;
+  if (op->recon12 && !op->phases_pm1) {
+    delete op;
+    set_error("12-real links need real boundary phases (+1 or -1)");
+    return GB_ERR_UNSUPPORTED;
+  }
   if (kind == 1) cayley_setup(op);
   int rc = GB_OK;
   auto alloc = [&](void** p, size_t n) {
@@ -611,6 +617,7 @@ const char* gb_status_string(int s) {
     case GB_ERR_TIMEOUT: return "device wait timed out";
     case GB_ERR_NO_DEVICE: return "no CUDA device";
     case GB_ERR_UNSUPPORTED: return "unsupported";
+    case GB_ERR_IO: return "file I/O or format error";
   }
   return "unknown status";
 }

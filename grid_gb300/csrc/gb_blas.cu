@@ -601,7 +601,7 @@ struct PhaseParams {
 
 template <class L>
 __global__ void __launch_bounds__(256) double_store_kernel(const GeoParams g, const PhaseParams ph, const double2* U,
-                                                           L* out, int parity) {
+                                                           L* out, int parity, int recon12) {
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= size_t(g.half4) * 8) return;
   const int64_t xcb = int64_t(t >> 3);
@@ -624,8 +624,9 @@ __global__ void __launch_bounds__(256) double_store_kernel(const GeoParams g, co
     src = xs[0] + int64_t(g.L[0]) * (xs[1] + int64_t(g.L[1]) * (xs[2] + int64_t(g.L[2]) * xs[3]));
   }
   const double2* u = U + (size_t(src) * 4 + mu) * 9;
-  L* o = out + (size_t(xcb) * 8 + leg) * 18;
-  for (int a = 0; a < 3; a++)
+  const int rows = recon12 ? 2 : 3;  // 12-real links keep rows 0 and 1
+  L* o = out + (size_t(xcb) * 8 + leg) * (rows * 6);
+  for (int a = 0; a < rows; a++)
     for (int b = 0; b < 3; b++) {
       // forward: U[a][b]; backward: conj(U[b][a])
       const double2 v = leg < 4 ? u[a * 3 + b] : make_double2(u[b * 3 + a].x, -u[b * 3 + a].y);
@@ -643,9 +644,11 @@ int launch_double_store(Op* op, const double* U_canon, int parity) {
   const size_t n = size_t(op->half4) * 8;
   const double2* U = reinterpret_cast<const double2*>(U_canon);
   if (op->prec == GB_F64)
-    double_store_kernel<double><<<nblk(n), 256, 0, op->stream>>>(g, ph, U, static_cast<double*>(op->links[parity]), parity);
+    double_store_kernel<double><<<nblk(n), 256, 0, op->stream>>>(g, ph, U, static_cast<double*>(op->links[parity]), parity,
+                                                                 op->recon12 ? 1 : 0);
   else
-    double_store_kernel<float><<<nblk(n), 256, 0, op->stream>>>(g, ph, U, static_cast<float*>(op->links[parity]), parity);
+    double_store_kernel<float><<<nblk(n), 256, 0, op->stream>>>(g, ph, U, static_cast<float*>(op->links[parity]), parity,
+                                                                op->recon12 ? 1 : 0);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }

@@ -18,6 +18,8 @@
 //    time boundary is already folded into the stored links, as in Grid's DoubleStore).
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "gb_device.cuh"
 
 namespace gb {
@@ -42,6 +44,11 @@ struct DhopParams {
   float* out2_norms;
   const void* links2;
   const int* nbr2;
+  // 12-real links: geometry and boundary signs to rebuild the third rows
+  int L[4];
+  int sgn[4];     // the (real) boundary phase of each direction
+  int parity;     // output checkerboard (parity2 for blockIdx.z == 1)
+  int parity2;
 };
 
 // the parameters of this CTA's checkerboard (both parities of a full Dhop run in one grid)
@@ -49,9 +56,44 @@ __device__ __forceinline__ DhopParams dhop_side(const DhopParams& p) {
   DhopParams q = p;
   if (blockIdx.z) {
     q.in = p.in2; q.in_norms = p.in2_norms; q.out = p.out2; q.out_norms = p.out2_norms;
-    q.links = p.links2; q.nbr = p.nbr2;
+    q.links = p.links2; q.nbr = p.nbr2; q.parity = p.parity2;
   }
   return q;
+}
+
+// 12-real links: the doubled link is k V with V in SU(3) and k = -1/2 times the boundary
+// sign of that leg at that site, so row 2 = conj(row 0 x row 1) / k.  Expands one leg of
+// one staged 4D site from rows {0,1} (12 reals) into the full 3x3 (18 reals).
+template <class R>
+__device__ __forceinline__ void expand_link12(const DhopParams& p, int64_t xcb, int leg, const R* src, R* dst) {
+  const int Lxh = p.L[0] >> 1;
+  const int64_t row = xcb / Lxh;
+  const int xh = int(xcb - row * Lxh);
+  const int y = int(row % p.L[1]);
+  const int64_t zt = row / p.L[1];
+  const int z = int(zt % p.L[2]), t = int(zt / p.L[2]);
+  const int x = 2 * xh + ((p.parity + y + z + t) & 1);
+  int cm, Lm, sg;  // the coordinate, extent and boundary sign of the leg's direction
+  switch (leg & 3) {
+    case 0: cm = x; Lm = p.L[0]; sg = p.sgn[0]; break;
+    case 1: cm = y; Lm = p.L[1]; sg = p.sgn[1]; break;
+    case 2: cm = z; Lm = p.L[2]; sg = p.sgn[2]; break;
+    default: cm = t; Lm = p.L[3]; sg = p.sgn[3]; break;
+  }
+  const bool edge = leg < 4 ? (cm == Lm - 1) : (cm == 0);
+  const R inv_k = R(-2) * R(edge ? sg : 1);
+#pragma unroll
+  for (int e = 0; e < 12; e++) dst[e] = src[e];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+    const R ar = src[2 * j1], ai = src[2 * j1 + 1], br = src[6 + 2 * j2], bi = src[6 + 2 * j2 + 1];
+    const R cr = src[2 * j2], ci = src[2 * j2 + 1], dr = src[6 + 2 * j1], di = src[6 + 2 * j1 + 1];
+    const R re = (ar * br - ai * bi) - (cr * dr - ci * di);
+    const R im = (ar * bi + ai * br) - (cr * di + ci * dr);
+    dst[12 + 2 * j] = inv_k * re;
+    dst[12 + 2 * j + 1] = -inv_k * im;
+  }
 }
 
 // ---- spin projection (1 + S gamma_MU) f -> two-spinor h, Grid's spProj{X,Y,Z,T}{p,m} ----
@@ -147,12 +189,13 @@ __device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8]
   reconstruct<MU, S, LEG == 0>(acc, ur, ui);
 }
 
-template <class T, bool DAG>
+template <class T, bool DAG, bool RECON>
 __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
   const DhopParams p = dhop_side(p0);
   using R = typename Arith<T>::type;
   extern __shared__ __align__(128) unsigned char dyn_smem[];
-  R* sU = reinterpret_cast<R*>(dyn_smem);
+  R* sU = reinterpret_cast<R*>(dyn_smem);  // k4 * 144
+  R* sraw = sU + size_t(p.k4) * 144;        // RECON: k4 * 96 (rows 0, 1 of every leg)
   __shared__ __align__(8) uint64_t bar;
 
   const int t = threadIdx.x;
@@ -161,9 +204,10 @@ __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
   if (t == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (t == 0) {
-    const uint32_t bytes = uint32_t(nsite) * 8u * 18u * uint32_t(sizeof(R));
+    const uint32_t per_site = RECON ? 96u : 144u;
+    const uint32_t bytes = uint32_t(nsite) * per_site * uint32_t(sizeof(R));
     mbar_expect_tx(&bar, bytes);
-    bulk_g2s(sU, static_cast<const R*>(p.links) + x0 * 144, bytes, &bar);
+    bulk_g2s(RECON ? sraw : sU, static_cast<const R*>(p.links) + x0 * per_site, bytes, &bar);
   }
   const int j = t / p.L5c;
   const int s = int(blockIdx.y) * p.L5c + (t - j * p.L5c);
@@ -175,11 +219,15 @@ __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
     nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
     nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
   }
-  if (!mbar_wait_bounded(&bar, 0)) {
-    if (t == 0) atomicExch(p.err, 1);
-    return;
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (!ok) atomicExch(p.err, 1);
+  if (RECON) {
+    if (ok)
+      for (int e = t; e < nsite * 8; e += blockDim.x)
+        expand_link12<R>(p, x0 + (e >> 3), e & 7, sraw + (e >> 3) * 96 + (e & 7) * 12, sU + (e >> 3) * 144 + (e & 7) * 18);
+    __syncthreads();
   }
-  if (!active) return;
+  if (!ok || !active) return;
   const R* U = sU + j * 144;
   Spinor<R> acc;
   dhop_leg<T, DAG, 0>(p, nb, s, U, acc);
@@ -205,18 +253,19 @@ static int pick_k4(int L5, size_t link_bytes_per_site) {
   return k4 < 1 ? 1 : k4;
 }
 
-template <class T, bool DAG> static int launch_dhop_t(Op* op, const DhopParams& p) {
+template <class T, bool DAG, bool RECON> static int launch_dhop_t(Op* op, const DhopParams& p) {
   using R = typename Arith<T>::type;
   const int threads = p.L5c * p.k4;
   const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
   const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
-  const size_t smem = size_t(p.k4) * 144 * sizeof(R);
-  static bool configured = false;
-  if (!configured) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_kernel<T, DAG>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    configured = true;
+  const size_t smem = size_t(p.k4) * (RECON ? 240 : 144) * sizeof(R);
+  static std::atomic<bool> configured{false};
+  if (!configured.load()) {
+    GB_CHECK_CUDA(
+        cudaFuncSetAttribute(dhop_kernel<T, DAG, RECON>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    configured.store(true);
   }
-  dhop_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
+  dhop_kernel<T, DAG, RECON><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -224,8 +273,8 @@ template <class T, bool DAG> static int launch_dhop_t(Op* op, const DhopParams& 
 // =======================================================================================
 // FP32 / FP16 storage: two 5D sites (s5, s5+1) per thread in packed f32x2 arithmetic.
 // Every operation acts identically on both lanes, so the site-pair layout needs no lane
-// shuffles; the links are expanded in shared memory to (re, re, im, im) so one 16-byte
-// shared load gives both broadcast pairs.
+// shuffles; each link element is read once from shared memory and broadcast to both
+// lanes.
 // =======================================================================================
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
@@ -367,11 +416,12 @@ __device__ __forceinline__ void dhop_pair_step(const DhopParams& p, const int (&
 
 // CTA = k4 4D sites x hc pair threads.  Thread (j, sp) computes the 5D sites
 // (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.
-template <class T, bool DAG>
+template <class T, bool DAG, bool RECON>
 __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p0) {
   const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   float* slink = reinterpret_cast<float*>(dyn_smem);  // k4 * kLinkStride floats
+  float* sraw = slink + size_t(p.k4) * kLinkStride;   // RECON: k4 * 96 floats (rows 0, 1)
   __shared__ __align__(8) uint64_t bar;
 
   const int t = threadIdx.x;
@@ -382,9 +432,14 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
   if (t == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (t == 0) {
-    mbar_expect_tx(&bar, uint32_t(nsite) * 576u);
-    const float* src = static_cast<const float*>(p.links) + x0 * 144;
-    for (int k = 0; k < nsite; k++) bulk_g2s(slink + k * kLinkStride, src + k * 144, 576u, &bar);
+    if (RECON) {
+      mbar_expect_tx(&bar, uint32_t(nsite) * 384u);
+      bulk_g2s(sraw, static_cast<const float*>(p.links) + x0 * 96, uint32_t(nsite) * 384u, &bar);
+    } else {
+      mbar_expect_tx(&bar, uint32_t(nsite) * 576u);
+      const float* src = static_cast<const float*>(p.links) + x0 * 144;
+      for (int k = 0; k < nsite; k++) bulk_g2s(slink + k * kLinkStride, src + k * 144, 576u, &bar);
+    }
   }
   const int j = t / hc;
   const int sp = int(blockIdx.y) * hc + (t - j * hc);
@@ -397,11 +452,16 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
     nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
   }
   // every thread waits for the links, so none leaves while the copy is in flight
-  if (!mbar_wait_bounded(&bar, 0)) {
-    atomicExch(p.err, 1);
-    return;
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (!ok) atomicExch(p.err, 1);
+  if (RECON) {
+    if (ok)
+      for (int e = t; e < nsite * 8; e += blockDim.x)
+        expand_link12<float>(p, x0 + (e >> 3), e & 7, sraw + (e >> 3) * 96 + (e & 7) * 12,
+                             slink + (e >> 3) * kLinkStride + (e & 7) * 18);
+    __syncthreads();
   }
-  if (!active) return;
+  if (!ok || !active) return;
   const size_t np = p.n5 >> 1;
   const float2* U = reinterpret_cast<const float2*>(slink + j * kLinkStride);
   Pair12 acc;
@@ -424,14 +484,20 @@ static int pick_k4_pair(int hc) {
   return k4 < 1 ? 1 : k4;
 }
 
-template <class T, bool DAG> static int launch_dhop_pair_t(Op* op, DhopParams p) {
+template <class T, bool DAG, bool RECON> static int launch_dhop_pair_t(Op* op, DhopParams p) {
   p.L5c = p.L5 > 256 ? 256 : p.L5;  // even
   p.k4 = pick_k4_pair(p.L5c / 2);
   const int threads = (p.L5c / 2) * p.k4;
   const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
   const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
-  const size_t smem = size_t(p.k4) * kLinkStride * sizeof(float);
-  dhop_pair_kernel<T, DAG><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
+  const size_t smem = size_t(p.k4) * (kLinkStride + (RECON ? 96 : 0)) * sizeof(float);
+  static std::atomic<bool> configured{false};
+  if (!configured.load()) {  // up to 64 sites x 976 B with 12-real staging
+    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_pair_kernel<T, DAG, RECON>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       64 * 1024));
+    configured.store(true);
+  }
+  dhop_pair_kernel<T, DAG, RECON><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -463,12 +529,25 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
   p.n5 = op->n5();
   p.L5 = op->L5;
   p.L5c = op->L5 > 256 ? 256 : op->L5;
-  p.k4 = pick_k4(p.L5c, op->prec == GB_F64 ? 1152 : 576);
+  p.k4 = pick_k4(p.L5c, (op->prec == GB_F64 ? 1152 : 576) * (op->recon12 ? 5 : 3) / 3);  // links + 12-real staging
   p.err = op->d_err;
-  switch (op->prec) {
-    case GB_F64: return dag ? launch_dhop_t<double, true>(op, p) : launch_dhop_t<double, false>(op, p);
-    case GB_F32: return dag ? launch_dhop_pair_t<float, true>(op, p) : launch_dhop_pair_t<float, false>(op, p);
-    case GB_F16: return dag ? launch_dhop_pair_t<__half, true>(op, p) : launch_dhop_pair_t<__half, false>(op, p);
+  for (int k = 0; k < 4; k++) {
+    p.L[k] = op->dims[k];
+    p.sgn[k] = op->phases[k].real() < 0 ? -1 : 1;
+  }
+  p.parity = out_parity;
+  p.parity2 = 1 - out_parity;
+  const int key = (op->prec << 2) | (dag ? 2 : 0) | (op->recon12 ? 1 : 0);
+  switch (key) {
+#define GB_DHOP_CASE(PREC, LAUNCH, T)                                        \
+  case (PREC << 2) | 0: return LAUNCH<T, false, false>(op, p);              \
+  case (PREC << 2) | 1: return LAUNCH<T, false, true>(op, p);               \
+  case (PREC << 2) | 2: return LAUNCH<T, true, false>(op, p);               \
+  case (PREC << 2) | 3: return LAUNCH<T, true, true>(op, p);
+    GB_DHOP_CASE(GB_F64, launch_dhop_t, double)
+    GB_DHOP_CASE(GB_F32, launch_dhop_pair_t, float)
+    GB_DHOP_CASE(GB_F16, launch_dhop_pair_t, __half)
+#undef GB_DHOP_CASE
   }
   return GB_ERR_BAD_ARG;
 }

@@ -36,7 +36,8 @@ enum {
   GB_ERR_NOT_CONVERGED = 5, /* CG hit MaxIterations (ConjugateGradient.h:254)        */
   GB_ERR_TIMEOUT = 6,       /* a bounded device wait gave up                         */
   GB_ERR_NO_DEVICE = 7,     /* no CUDA device visible                                */
-  GB_ERR_UNSUPPORTED = 8
+  GB_ERR_UNSUPPORTED = 8,
+  GB_ERR_IO = 9             /* file I/O, format, or a checksum / plaquette mismatch (NerscIO.h asserts) */
 };
 
 /* ---- precisions and subsets ---- */
@@ -63,8 +64,11 @@ int gb_device_count(int* n);
  * precision: GB_F64 or GB_F32 (or GB_F16: FP16 spinors with per-site FP32 norms,
  * FP32 links and arithmetic).  nrhs >= 1 right-hand sides share the gauge field.
  * stream: a cudaStream_t (NULL = the default stream).
- * flags: bit 0 = store links as 12 reals and reconstruct the third row.
+ * flags: GB_FLAG_RECON12 = store the doubled links as 12 reals (rows 0, 1) and rebuild
+ * row 2 in the Dhop kernel (the optional 12-real reconstruction); needs real boundary
+ * phases (+1 / -1), else GB_ERR_UNSUPPORTED.
  */
+#define GB_FLAG_RECON12 1u
 int gb_wilson_create(const int dims[4], double mass, const double* phases, int precision, int nrhs, void* stream,
                      unsigned flags, gb_op_t* out);
 int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,
@@ -224,6 +228,35 @@ int gb_cg_multishift(gb_op_t op, int kind, gb_field_t src, int nshift, const dou
  * unprec_resid (may be NULL): |M sol - src| / |src| per right-hand side. */
 int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, const gb_cg_params* p,
                    gb_cg_result* res, double* unprec_resid);
+
+/* ---- NERSC gauge configurations (Grid/parallelIO/NerscIO.h:62-300) ---------------
+ * Canonical FP64 gauge fields U[site][mu][3][3] to and from NERSC files: DATATYPE
+ * 4D_SU3_GAUGE (two rows stored, the third rebuilt) or 4D_SU3_GAUGE_3x3; FLOATING_POINT
+ * IEEE32BIG, IEEE32, IEEE64BIG, IEEE64 / IEEE64LITTLE.  The byte swapping, row rebuild,
+ * checksum (32-bit wrapping sum of the payload words in host order) and the plaquette /
+ * link trace run on the device.  U may be host (on_device = 0) or device memory. */
+typedef struct {
+  int dims[4];
+  int two_row;                  /* 1: 4D_SU3_GAUGE, 0: 4D_SU3_GAUGE_3x3                   */
+  int bits;                     /* 32 or 64                                               */
+  int big_endian;
+  int sequence_number;
+  int64_t data_start;           /* byte offset of the payload                             */
+  double link_trace, plaquette; /* header values                                          */
+  uint32_t checksum;            /* header value                                           */
+  uint32_t checksum_computed;   /* gb_nersc_read: of the payload                          */
+  double link_trace_computed, plaquette_computed;  /* gb_nersc_read: of the field read     */
+  char data_type[64], floating_point[32], ensemble_id[64], ensemble_label[64], boundary[4][32];
+} gb_nersc_header;
+int gb_nersc_read_header(const char* path, gb_nersc_header* h);
+/* readConfiguration: check != 0 returns GB_ERR_IO when the checksum differs, the
+ * plaquette differs by >= 1e-5 or the link trace by >= 1e-6 (Grid asserts) */
+int gb_nersc_read(const char* path, double* U, int on_device, gb_nersc_header* h, int check);
+/* writeConfiguration: two_row selects 4D_SU3_GAUGE; bits 32/64; big_endian as IEEE*BIG */
+int gb_nersc_write(const char* path, const double* U, int on_device, const int dims[4], int two_row, int bits,
+                   int big_endian, const char* ensemble_id, const char* ensemble_label, int sequence_number);
+/* WilsonLoops::avgPlaquette and linkTrace (Grid/qcd/utils/WilsonLoops.h:88-126,203-218) */
+int gb_gauge_stats(const int dims[4], const double* U, int on_device, double* plaquette, double* link_trace);
 
 /* ---- seeded synthetic inputs (Grid: GridParallelRNG + SU3::HotConfiguration) ----
  * Counter-based generator keyed by (seed, site, element); independent of thread count.

@@ -377,3 +377,43 @@ def test_fields_shared_between_operators(gpu_available):
     with pytest.raises(g.GridError):
         op_c.M(fin, fout)
     del op_c
+
+
+@pytest.mark.parametrize("prec", [g.F64, g.F32, g.F16])
+@pytest.mark.parametrize("kind", ["wilson", "mobius"])
+@pytest.mark.parametrize("antiperiodic", [True, False])
+def test_recon12_links(gpu_available, prec, kind, antiperiodic):
+    """12-real links (rows 0, 1 stored, row 2 rebuilt with the -1/2 and the boundary sign)
+    give the same Dhop as the full links."""
+    dims = (4, 6, 4, 8)
+    ph = g.antiperiodic_t() if antiperiodic else g.periodic()
+    U = g.random_gauge(dims, 0.5, 17)
+    if kind == "wilson":
+        op = g.WilsonFermion(U, dims, 0.1, phases=ph, precision=prec, flags=g.RECON12)
+        ref = o.OracleOp(0, 0, dims, 1, [0.1], U, ph)
+        L5 = 1
+    else:
+        op = g.MobiusFermion(U, dims, 8, 0.05, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], phases=ph, precision=prec,
+                             flags=g.RECON12)
+        ref = o.OracleOp(1, 0, dims, 8, [0.05, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, ph)
+        L5 = 8
+    tol = {g.F64: 1e-13, g.F32: 1e-6, g.F16: 3e-3}[prec]
+    vol = int(np.prod(dims))
+    x = fermion(vol, L5, 70)
+    fin = op.FermionField().import_(x)
+    fout = op.FermionField()
+    for dag, code in ((0, o.OP_DHOP), (1, o.OP_DHOP_DAG)):
+        op.Dhop(fin, fout, dag)
+        assert o.rel_l2(fout.export(), ref.apply(code, x)) < tol, dag
+    xh = fermion(vol // 2, L5, 71)
+    out = op.FermionRedBlackField(g.EVEN)
+    op.DhopEO(half(op, g.ODD, xh), out, 0)
+    assert o.rel_l2(out.export(), ref.dhop_cb(xh, 1, 0)) < tol
+
+
+def test_recon12_needs_real_phases(gpu_available):
+    dims = (4, 4, 4, 4)
+    ph = np.array([1, 0, 1, 0, 1, 0, 0, 1], dtype=np.float64)  # a complex phase in time
+    with pytest.raises(g.GridError) as e:
+        g.WilsonFermion(g.random_gauge(dims, 0.3, 1), dims, 0.1, phases=ph, flags=g.RECON12)
+    assert e.value.status == 8

@@ -242,3 +242,25 @@ def test_oracle_multishift_free_wilson():
         want = _from_k(DIMS, np.linalg.solve(MdM + s * np.eye(4), ek), True)
         assert r < 1e-10
         assert o.rel_l2(x, want) < 1e-9, s
+
+
+@pytest.mark.parametrize("fmt", ["IEEE64BIG", "IEEE64", "IEEE32BIG", "IEEE32"])
+@pytest.mark.parametrize("two_row", [False, True])
+def test_oracle_nersc_round_trip(tmp_path, fmt, two_row):
+    """The NERSC restatement (NerscIO.h): write -> read reproduces the field (exactly for
+    64-bit 3x3, within float rounding otherwise; the rebuilt third row of an SU(3) link
+    equals the stored one), the header checksum is the payload's, and the unit field has
+    plaquette and link trace 1."""
+    from oracle import nersc
+    dims = (4, 4, 4, 6)
+    U = g.random_gauge(dims, 0.7, 3)
+    path = tmp_path / "cfg.nersc"
+    csum, plaq, tr = nersc.write(path, U, dims, two_row, fmt)
+    V, hdr, csum2 = nersc.read(path)
+    assert csum2 == csum == int(hdr["CHECKSUM"], 16)
+    tol = 0 if (fmt.startswith("IEEE64") and not two_row) else (1e-13 if fmt.startswith("IEEE64") else 1e-6)
+    assert np.max(np.abs(V - U)) <= tol
+    p2, t2 = nersc.plaquette_and_trace(V, dims)
+    assert abs(p2 - plaq) < 1e-6 and abs(t2 - tr) < 1e-6
+    one = g.unit_gauge(dims)
+    assert np.allclose(nersc.plaquette_and_trace(one, dims), (1.0, 1.0), atol=1e-15)
