@@ -129,6 +129,8 @@ for _n in ("gb_import_physical_source", "gb_import_unphysical_fermion"):
     _proto(_n, [_vp, _vp, _i, _vp])
 for _n in ("gb_export_physical_solution", "gb_export_physical_source"):
     _proto(_n, [_vp, _vp, _vp, _i])
+for _n in ("gb_DhopDeriv", "gb_MDeriv"):
+    _proto(_n, [_vp, _vp, _vp, _i, _vp, _i])
 
 
 def set_device(d: int):
@@ -379,6 +381,26 @@ class _FermionOperator:
     def Mpc(self, i, o): _check(lib.gb_Mpc(self.h, i.h, o.h))
     def MpcDag(self, i, o): _check(lib.gb_MpcDag(self.h, i.h, o.h))
     def MpcDagMpc(self, i, o): _check(lib.gb_MpcDagMpc(self.h, i.h, o.h))
+
+    # force terms (WilsonFermion5DImplementation.h:212-305, CayleyFermion5DImplementation.h:346-391)
+    def _deriv(self, fn, A, B, dag):
+        n = (self.vol4 if A.checkerboard == FULL else self.vol4 // 2) * 36
+        mat = np.empty(n, dtype=np.complex128)
+        _check(fn(self.h, A.h, B.h, int(dag), mat.ctypes.data, 0))
+        return mat
+
+    def DhopDeriv(self, A, B, dag):
+        """force [site][mu][3][3] (full fields) or [site>>1][mu][3][3] (DerivEO/OE: half fields)"""
+        return self._deriv(lib.gb_DhopDeriv, A, B, dag)
+
+    DhopDerivEO = DhopDeriv
+    DhopDerivOE = DhopDeriv
+
+    def MDeriv(self, U, V, dag):
+        return self._deriv(lib.gb_MDeriv, U, V, dag)
+
+    MoeDeriv = MDeriv
+    MeoDeriv = MDeriv
 
     def sync(self):
         _check(lib.gb_op_sync(self.h))

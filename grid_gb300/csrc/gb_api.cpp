@@ -841,6 +841,50 @@ int gb_Dminus(gb_op_t op, gb_field_t in, gb_field_t out, int dag) {
   return op_dminus(op, in, out, dag ? 1 : 0);
 }
 
+// ---- force terms (WilsonFermion5DImplementation.h:212-305, CayleyFermion5DImplementation.h:346-391) ----
+static int deriv_launch(Op* op, Field* A, Field* B, int dag, double* mat) {
+  if (A->full() != B->full()) { set_error("Deriv: A and B must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
+  if (A->full()) {
+    for (int p = 0; p < 2; p++) GB_TRY(launch_deriv(op, half_view(A, p), half_view(B, 1 - p), p, dag, mat, 0));
+    return GB_OK;
+  }
+  if (B->subset != 1 - A->subset) { set_error("DhopDerivEO/OE: B must be on the other checkerboard"); return GB_ERR_BAD_PARITY; }
+  return launch_deriv(op, half_view(A, 0), half_view(B, 0), A->subset, dag, mat, 1);
+}
+static int deriv_entry(gb_op_t op, gb_field_t A, gb_field_t B, int dag, double* mat, int on_device, bool mderiv) {
+  GB_TRY(check_op(op));
+  if (!A || !B || !mat) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  GB_TRY(check_conf(A, B));
+  if (!ops_conformable(A->op, op)) { set_error("field is not conformable to the operator"); return GB_ERR_BAD_ARG; }
+  const size_t bytes = size_t(A->full() ? op->vol4 : op->half4) * 36 * 16;
+  double* d = mat;
+  if (!on_device) GB_CHECK_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), bytes, op->stream));
+  struct Free { double* p; cudaStream_t s; ~Free() { if (p) cudaFreeAsync(p, s); } } guard{on_device ? nullptr : d, op->stream};
+  Field* a = A;
+  Field* b = B;
+  if (mderiv && op->kind == 1) {
+    // U d[D_w D5]/du V: Din = Meooe5D V (non-dag) or Meooe5D U (dag, the adjoint is implicit)
+    Field* din;
+    Field* src = dag ? A : B;
+    GB_TRY(ws_get(op, src->full() ? GB_FULL : src->subset, src->prec, src->full() ? WS_DERIV_FULL : WS_DERIV, &din));
+    din->subset = src->subset;
+    GB_TRY(op_meooe5d(op, src, din, 0));
+    (dag ? a : b) = din;
+  }
+  GB_TRY(deriv_launch(op, a, b, dag ? 1 : 0, d));
+  if (!on_device) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(mat, d, bytes, cudaMemcpyDeviceToHost, op->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  }
+  return GB_OK;
+}
+int gb_DhopDeriv(gb_op_t op, gb_field_t A, gb_field_t B, int dag, double* mat, int on_device) {
+  return deriv_entry(op, A, B, dag, mat, on_device, false);
+}
+int gb_MDeriv(gb_op_t op, gb_field_t U, gb_field_t V, int dag, double* mat, int on_device) {
+  return deriv_entry(op, U, V, dag, mat, on_device, true);
+}
+
 // ---- 4D <-> 5D surface fields (CayleyFermion5DImplementation.h:57-129) ----
 static int surface_checks(gb_op_t op, gb_field_t f, const double* p4) {
   GB_TRY(check_op(op));

@@ -560,4 +560,128 @@ int launch_dhop_full(Op* op, HalfView in_odd, HalfView out_even, HalfView in_eve
   return launch_dhop_sides(op, in_odd, out_even, 0, &in_even, &out_odd, dag);
 }
 
+// =======================================================================================
+// Force term: WilsonFermion5D::DerivInternal (WilsonFermion5DImplementation.h:212-246) with
+// WilsonImpl::InsertForce5D (WilsonImpl.h:193-238).  For each output site x and direction
+// mu:  mat[x][mu]_ab = sum_s sum_spin Bt(x,s)_{spin,a} conj(A(x,s)_{spin,b}),
+// Bt = (1 -+ gamma_mu) U~_mu(x) B(x + mu) -- the forward leg of Dhop (dag: of Dhop^dag).
+// One thread per (x, mu) walks the L5 slots (all right-hand sides are summed), so the sum
+// has a fixed order; the result is FP64 in the canonical gauge layout.
+// =======================================================================================
+struct DerivParams {
+  const void* A;
+  const float* An;
+  const void* B;
+  const float* Bn;
+  const void* links;
+  const int* nbr;
+  double2* mat;
+  size_t n5;
+  int64_t n4h;
+  int L5;
+  int half_out;   // 1: mat indexed by x_cb, 0: by the lexicographic site
+  DhopParams geo;  // L, sgn, parity (for the 12-real link rebuild and the site index)
+};
+
+template <class T, bool DAG, int MU, bool RECON>
+__device__ __forceinline__ void deriv_site(const DerivParams& q, int64_t x) {
+  using R = typename Arith<T>::type;
+  constexpr int S = DAG ? 1 : -1;
+  R Ul[18];
+  if (RECON) {
+    R raw[12];
+    const R* src = static_cast<const R*>(q.links) + (size_t(x) * 8 + MU) * 12;
+#pragma unroll
+    for (int e = 0; e < 12; e++) raw[e] = src[e];
+    expand_link12<R>(q.geo, x, MU, raw, Ul);
+  } else {
+    const R* src = static_cast<const R*>(q.links) + (size_t(x) * 8 + MU) * 18;
+#pragma unroll
+    for (int e = 0; e < 18; e++) Ul[e] = src[e];
+  }
+  const int nb = q.nbr[size_t(x) * 8 + MU];
+  double fr[9], fi[9];
+#pragma unroll
+  for (int e = 0; e < 9; e++) { fr[e] = 0; fi[e] = 0; }
+  for (int s = 0; s < q.L5; s++) {
+    Spinor<R> b, a, bt;
+    SpinorIO<T>::load(q.B, q.Bn, q.n5, size_t(nb) * q.L5 + s, b);
+    SpinorIO<T>::load(q.A, q.An, q.n5, size_t(x) * q.L5 + s, a);
+    R hr[6], hi[6], ur[6], ui[6];
+    project<MU, S>(b, hr, hi);
+    su3_mul<R>(Ul, hr, hi, ur, ui);
+    reconstruct<MU, S, true>(bt, ur, ui);
+#pragma unroll
+    for (int ca = 0; ca < 3; ca++)
+#pragma unroll
+      for (int cb = 0; cb < 3; cb++)
+#pragma unroll
+        for (int sp = 0; sp < 4; sp++) {
+          const double br = bt.re[sp * 3 + ca], bi = bt.im[sp * 3 + ca];
+          const double ar = a.re[sp * 3 + cb], ai = a.im[sp * 3 + cb];
+          fr[ca * 3 + cb] += br * ar + bi * ai;  // b conj(a)
+          fi[ca * 3 + cb] += bi * ar - br * ai;
+        }
+  }
+  int64_t idx = x;
+  if (!q.half_out) {  // lexicographic site of x_cb in the output parity
+    const int Lxh = q.geo.L[0] >> 1;
+    const int64_t row = x / Lxh;
+    const int xh = int(x - row * Lxh);
+    const int y = int(row % q.geo.L[1]);
+    const int64_t zt = row / q.geo.L[1];
+    const int z = int(zt % q.geo.L[2]), t = int(zt / q.geo.L[2]);
+    idx = row * q.geo.L[0] + 2 * xh + ((q.geo.parity + y + z + t) & 1);
+  }
+  double2* o = q.mat + (size_t(idx) * 4 + MU) * 9;
+#pragma unroll
+  for (int e = 0; e < 9; e++) o[e] = make_double2(fr[e], fi[e]);
+}
+
+template <class T, bool DAG, bool RECON>
+__global__ void __launch_bounds__(128) deriv_kernel(const DerivParams q) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= q.n4h * 4) return;
+  const int64_t x = t >> 2;
+  switch (int(t & 3)) {
+    case 0: deriv_site<T, DAG, 0, RECON>(q, x); break;
+    case 1: deriv_site<T, DAG, 1, RECON>(q, x); break;
+    case 2: deriv_site<T, DAG, 2, RECON>(q, x); break;
+    default: deriv_site<T, DAG, 3, RECON>(q, x); break;
+  }
+}
+
+int launch_deriv(Op* op, HalfView A, HalfView B, int out_parity, int dag, double* mat, int half_out) {
+  if (A.prec != op->prec || B.prec != op->prec) { set_error("DhopDeriv: field precision differs from the operator's"); return GB_ERR_BAD_ARG; }
+  if (op->prec == GB_F16) { set_error("DhopDeriv: FP64 or FP32 operators"); return GB_ERR_UNSUPPORTED; }
+  DerivParams q;
+  q.A = A.data; q.An = A.norms; q.B = B.data; q.Bn = B.norms;
+  q.links = op->links[out_parity];
+  q.nbr = op->nbr[out_parity];
+  q.mat = reinterpret_cast<double2*>(mat);
+  q.n5 = op->n5();
+  q.n4h = op->half4;
+  q.L5 = op->L5;
+  q.half_out = half_out;
+  for (int k = 0; k < 4; k++) {
+    q.geo.L[k] = op->dims[k];
+    q.geo.sgn[k] = op->phases[k].real() < 0 ? -1 : 1;
+  }
+  q.geo.parity = out_parity;
+  const unsigned blocks = unsigned((op->half4 * 4 + 127) / 128);
+  const int key = (op->prec == GB_F64 ? 4 : 0) | (dag ? 2 : 0) | (op->recon12 ? 1 : 0);
+  switch (key) {
+    case 0: deriv_kernel<float, false, false><<<blocks, 128, 0, op->stream>>>(q); break;
+    case 1: deriv_kernel<float, false, true><<<blocks, 128, 0, op->stream>>>(q); break;
+    case 2: deriv_kernel<float, true, false><<<blocks, 128, 0, op->stream>>>(q); break;
+    case 3: deriv_kernel<float, true, true><<<blocks, 128, 0, op->stream>>>(q); break;
+    case 4: deriv_kernel<double, false, false><<<blocks, 128, 0, op->stream>>>(q); break;
+    case 5: deriv_kernel<double, false, true><<<blocks, 128, 0, op->stream>>>(q); break;
+    case 6: deriv_kernel<double, true, false><<<blocks, 128, 0, op->stream>>>(q); break;
+    default: deriv_kernel<double, true, true><<<blocks, 128, 0, op->stream>>>(q); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 }  // namespace gb

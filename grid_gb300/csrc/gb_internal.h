@@ -146,6 +146,9 @@ inline HalfView half_view(const Field* f, int parity) { return HalfView{f->half_
 
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag);
 int launch_dhop_full(Op* op, HalfView in_odd, HalfView out_even, HalfView in_even, HalfView out_odd, int dag);
+// force term of the output parity's sites into mat (FP64 canonical gauge layout, indexed
+// by x_cb when half_out, else by the lexicographic site); A has the output parity
+int launch_deriv(Op* op, HalfView A, HalfView B, int out_parity, int dag, double* mat, int half_out);
 // chi = diag*phi + upper*P(-/+) psi[s+1] + lower*P(+/-) psi[s-1]   (per rhs block of Ls)
 int launch_m5d(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
                const double* upper, int dag, size_t n5);

@@ -13,11 +13,13 @@ enum {
   WS_RU_PF = 12, WS_RU_MMPF = 13, WS_RU_RF = 14, WS_RU_XF = 15,
   WS_SCHUR_A = 16, WS_SCHUR_B = 17, WS_SCHUR_C = 18, WS_SCHUR_D = 19,
   WS_MS_P = 20, WS_MS_MMP = 21, WS_MS_R = 22, WS_MS_T = 23, WS_MS_PS = 24,  // WS_MS_PS + shift, < 24 + 32
+  WS_DERIV = 56,
 };
 enum { WS_M_DIN = 0, WS_M_T = 1, WS_MDAGM = 2, WS_FCG_P = 3, WS_FCG_MMP = 4, WS_FCG_R = 5, WS_FCG_T = 6,
        WS_FRU_PF = 7, WS_FRU_MMPF = 8, WS_FRU_RF = 9, WS_FRU_XF = 10, WS_SCHUR_RES = 11, WS_DMINUS = 12,
        WS_PHYS = 13, WS_MS_P_FULL = 14, WS_MS_MMP_FULL = 15, WS_MS_R_FULL = 16, WS_MS_T_FULL = 17,
-       WS_MS_PS_FULL = 18 };  // WS_MS_PS_FULL + shift, < 18 + 32
+       WS_MS_PS_FULL = 18,  // WS_MS_PS_FULL + shift, < 18 + 32
+       WS_DERIV_FULL = 50 };
 
 int field_alloc(Op* op, int subset, int prec, Field** out);
 void field_free(Field* f);

@@ -155,6 +155,20 @@ int gb_MpcDagMpc(gb_op_t op, gb_field_t in, gb_field_t out);
  * fields: chi = psi - c (DW psi), DW = Dhop + (4 - M5).  Moebius operators only. */
 int gb_Dminus(gb_op_t op, gb_field_t in, gb_field_t out, int dag);
 
+/* ---- force terms ---------------------------------------------------------------------
+ * gb_DhopDeriv ~ WilsonFermion5D::DhopDeriv / DhopDerivEO / DhopDerivOE
+ * (WilsonFermion5DImplementation.h:212-305) with WilsonImpl::InsertForce5D (WilsonImpl.h:193-238):
+ *   mat[x][mu]_ab = sum_s sum_spin [(1 -+ gamma_mu) U~_mu(x) B(x+mu, s)]_{spin,a} conj(A(x,s)_{spin,b})
+ * (minus sign: dag = 0), summed over all L5 slots (every right-hand side), U~ the doubled
+ * link with -1/2 and the boundary phase.  A, B full fields (mat: full canonical gauge
+ * layout [site][mu][3][3]) or half fields on opposite checkerboards (DerivEO: A even,
+ * B odd; DerivOE: A odd, B even; mat indexed by site>>1 over A's checkerboard), FP64 out.
+ * gb_MDeriv ~ CayleyFermion5D::MDeriv / MoeDeriv / MeoDeriv (CayleyFermion5DImplementation.h:346-391):
+ * DhopDeriv(U, Meooe5D V) (dag = 0) or DhopDeriv(Meooe5D U, V) (dag = 1); for a Wilson
+ * operator MDeriv = DhopDeriv.  FP64 or FP32 operators.  mat: host (on_device = 0) or device. */
+int gb_DhopDeriv(gb_op_t op, gb_field_t A, gb_field_t B, int dag, double* mat, int on_device);
+int gb_MDeriv(gb_op_t op, gb_field_t U, gb_field_t V, int dag, double* mat, int on_device);
+
 /* ---- 4D <-> 5D surface fields (CayleyFermion5DImplementation.h:57-129) ------------
  * The 4D side is a canonical FP64 4D fermion (nrhs fields back to back), in host memory
  * (on_device = 0; the call returns when it is done) or device memory (on_device = 1; the

@@ -210,6 +210,47 @@ void dhop(const Geom& g, int L5, const std::vector<cplx<R>>& Ud, const Field<R>&
   }
 }
 
+// Force term, DerivInternal + InsertForce5D (WilsonFermion5DImplementation.h:212-246,
+// WilsonImpl.h:193-238) on full canonical fields, double precision:
+//   mat[x][mu]_ab = sum_s sum_spin [(1 -+ g_mu) Ud_mu(x) B(x+mu, s)]_{spin,a} conj(A(x,s)_{spin,b})
+// (minus: non-dagger) for the sites of out_parity (all sites when < 0); mat is
+// [site][mu][3][3] and untouched elsewhere.
+inline void dhop_deriv(const Geom& g, int L5, const std::vector<cplx<double>>& Ud, const Field<double>& A,
+                       const Field<double>& B, std::vector<cplx<double>>& mat, int dag, int out_parity = -1) {
+  mat.resize(size_t(g.vol) * 4 * 9);
+#pragma omp parallel for schedule(static)
+  for (int64_t site = 0; site < g.vol; site++) {
+    if (out_parity >= 0 && g.parity(site) != out_parity) continue;
+    for (int mu = 0; mu < 4; mu++) {
+      const int64_t nb = g.shift(site, mu, +1);
+      const cplx<double>* U = &Ud[(size_t(site) * 8 + mu) * 9];
+      const double sign = dag ? 1.0 : -1.0;
+      cplx<double> F[9] = {};
+      for (int s = 0; s < L5; s++) {
+        const cplx<double>* p = &B[(size_t(nb) * L5 + s) * Nsc];
+        const cplx<double>* a = &A[(size_t(site) * L5 + s) * Nsc];
+        cplx<double> phi[Nsc], bt[Nsc];
+        for (int sp = 0; sp < Ns; sp++)
+          for (int c = 0; c < Nc; c++) {
+            cplx<double> acc = 0;
+            for (int d = 0; d < Nc; d++) acc += U[c * 3 + d] * p[sp * 3 + d];
+            phi[sp * 3 + c] = acc;
+          }
+        for (int sp = 0; sp < Ns; sp++)
+          for (int c = 0; c < Nc; c++) {
+            cplx<double> gp = 0;
+            for (int sq = 0; sq < Ns; sq++) gp += gamma_el(mu, sp, sq) * phi[sq * 3 + c];
+            bt[sp * 3 + c] = phi[sp * 3 + c] + sign * gp;
+          }
+        for (int ca = 0; ca < 3; ca++)
+          for (int cb = 0; cb < 3; cb++)
+            for (int sp = 0; sp < Ns; sp++) F[ca * 3 + cb] += bt[sp * 3 + ca] * std::conj(a[sp * 3 + cb]);
+      }
+      std::copy_n(F, 9, &mat[(size_t(site) * 4 + mu) * 9]);
+    }
+  }
+}
+
 // Naive Cshift-form Dhop (benchmarks/Benchmark_dwf.cc:145-158 non-dagger, :235-261 dagger),
 // written from the undoubled links and the boundary phases, as an independent check of
 // DoubleStore + the site loop.

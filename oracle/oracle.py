@@ -54,6 +54,7 @@ def lib():
         L.orc_cg_reliable.argtypes = [vp, vp, i, dp, dp, d, i, d, i, i, ip, dp]
         L.orc_physical.argtypes = [vp, i, dp, dp]
         L.orc_cg_multishift.argtypes = [vp, i, dp, i, dp, dp, i, dp, ip, dp]
+        L.orc_deriv.argtypes = [vp, i, dp, dp, i, i, dp]
         L.orc_set_threads.argtypes = [i]
         L.orc_max_threads.restype = i
         _lib = L
@@ -125,6 +126,15 @@ class OracleOp:
         out = np.empty(n, dtype=np.complex128)
         assert lib().orc_physical(self.h, mode, _p(x), _p(out)) == 0
         return out
+
+    def deriv(self, A, B, dag=0, mderiv=False, out_parity=-1):
+        """DhopDeriv (or MDeriv) force of full fields A, B: [site][mu][3][3] complex; only the
+        sites of out_parity when >= 0 (zero elsewhere)."""
+        A = np.ascontiguousarray(A, dtype=np.complex128)
+        B = np.ascontiguousarray(B, dtype=np.complex128)
+        mat = np.zeros(self.vol * 36, dtype=np.complex128)
+        assert lib().orc_deriv(self.h, int(mderiv), _p(A), _p(B), int(dag), int(out_parity), _p(mat)) == 0
+        return mat
 
     def doubled_links(self):
         out = np.empty(self.vol * 8 * 9, dtype=np.complex128)

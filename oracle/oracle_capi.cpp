@@ -304,3 +304,27 @@ int orc_cg_multishift(void* p, int kind, const double* src, int nshift, const do
   return r.converged ? 0 : 5;
 }
 }
+
+extern "C" {
+// DhopDeriv / MDeriv in double on full canonical fields (DhopDeriv: A, B as given;
+// MDeriv of a Moebius operator: B -> Meooe5D B (dag = 0) or A -> Meooe5D A (dag = 1),
+// CayleyFermion5DImplementation.h:346-391).  out_parity < 0: all sites (the full-field
+// form); 0 / 1: only the sites of that parity (DerivEO / DerivOE with A on that parity).
+// mat: [site][mu][3][3] complex.
+int orc_deriv(void* p, int mderiv, const double* A, const double* B, int dag, int out_parity, double* mat) {
+  Handle* h = static_cast<Handle*>(p);
+  if (h->prec != 0) return 1;
+  Op<double>* op = h->d;
+  const size_t n = op->full_len();
+  Field<double> a = load<double>(A, n), b = load<double>(B, n), t;
+  if (mderiv && h->kind == 1) {
+    auto* m = static_cast<Mobius<double>*>(op);
+    if (!dag) { m->Meooe5D(b, t); b = t; }
+    else { m->Meooe5D(a, t); a = t; }
+  }
+  std::vector<cplx<double>> M(size_t(op->g.vol) * 36, cplx<double>(0));
+  dhop_deriv(op->g, op->L5, op->Ud, a, b, M, dag, out_parity);
+  store<double>(M, mat);
+  return 0;
+}
+}

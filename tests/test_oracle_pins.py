@@ -264,3 +264,38 @@ def test_oracle_nersc_round_trip(tmp_path, fmt, two_row):
     assert abs(p2 - plaq) < 1e-6 and abs(t2 - tr) < 1e-6
     one = g.unit_gauge(dims)
     assert np.allclose(nersc.plaquette_and_trace(one, dims), (1.0, 1.0), atol=1e-15)
+
+
+@pytest.mark.parametrize("dag", [0, 1])
+@pytest.mark.parametrize("kind", ["wilson", "mobius"])
+def test_oracle_force_is_the_link_derivative(dag, kind):
+    """DhopDeriv (WilsonFermion5DImplementation.h:212-246 + InsertForce5D) is the derivative
+    of <A|Dhop|B> by the link: with A = 0 at x0 + mu (so only the forward leg at x0 sees
+    the link), <A|Dhop(U + D)|B> - <A|Dhop(U)|B> = tr(D U^+ F[x0][mu]) for any 3x3 D, with
+    boundary phases +-1; exactly, since Dhop is linear in the link."""
+    Ls = 1 if kind == "wilson" else 4
+    rng = np.random.default_rng(5 + dag)
+    U = g.random_gauge(DIMS, 0.6, 21)
+    ph = g.antiperiodic_t()
+    mk = (lambda V: o.OracleOp(0, 0, DIMS, 1, [0.1], V, ph)) if kind == "wilson" else \
+        (lambda V: o.OracleOp(1, 0, DIMS, Ls, [0.05, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], V, ph))
+    ref = mk(U)
+    A = fermion(VOL, Ls, 31).reshape(VOL, Ls * 12)
+    B = fermion(VOL, Ls, 32)
+    for x0, mu in ((5, 0), (VOL - 1, 3), (77, 2)):   # x0 = VOL-1 sits on the time boundary
+        x = np.unravel_index(x0, DIMS[::-1])[::-1]
+        xp = list(x)
+        xp[mu] = (xp[mu] + 1) % DIMS[mu]
+        nb = xp[0] + DIMS[0] * (xp[1] + DIMS[1] * (xp[2] + DIMS[2] * xp[3]))
+        Az = A.copy()
+        Az[nb] = 0
+        Az = Az.reshape(-1)
+        F = ref.deriv(Az, B, dag).reshape(VOL, 4, 3, 3)
+        D = rng.normal(size=(3, 3)) + 1j * rng.normal(size=(3, 3))
+        U2 = U.reshape(VOL, 4, 3, 3).copy()
+        U2[x0, mu] += D
+        code = o.OP_DHOP_DAG if dag else o.OP_DHOP
+        d_num = np.vdot(Az, mk(U2.reshape(-1)).apply(code, B)) - np.vdot(Az, ref.apply(code, B))
+        Ux = U.reshape(VOL, 4, 3, 3)[x0, mu]
+        d_ana = np.trace(D @ Ux.conj().T @ F[x0, mu])
+        assert abs(d_num - d_ana) < 1e-10 * abs(d_ana), (x0, mu)
