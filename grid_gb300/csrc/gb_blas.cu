@@ -327,42 +327,60 @@ __global__ void cg_init_kernel(CGScalars* cg, const double* ssq, const double* c
   if (r == 0) { flags[0] = (nd == nrhs); flags[1] = 0; }
 }
 
-__global__ void cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs) {
-  const int r = threadIdx.x;
-  if (r >= nrhs) return;
-  double d = 0;
-  for (int b = 0; b < nparts; b++) d += partial[(size_t(b) * nrhs + r) * 2];
-  cg[r].d = d;
-  cg[r].a = cg[r].done ? 0.0 : cg[r].c / d;
+// sum over b of partial[b * stride + offset] by one CTA of 256 threads in a fixed order
+// (strided per-thread sums, then a tree); every thread gets the result
+__device__ double cta_sum_fixed(const double* partial, int nparts, int stride, int offset) {
+  __shared__ double sm[256];
+  double s = 0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += partial[size_t(b) * stride + offset];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sm[threadIdx.x] += sm[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double r = sm[0];
+  __syncthreads();
+  return r;
 }
 
-__global__ void cg_beta_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs, int* flags) {
-  const int r = threadIdx.x;
-  __shared__ int nd, nr;
-  if (r == 0) { nd = 0; nr = 0; }
-  __syncthreads();
-  if (r < nrhs) {
-    CGScalars s = cg[r];
-    if (!s.done) {
-      double cp = 0;
-      for (int b = 0; b < nparts; b++) cp += partial[size_t(b) * nrhs + r];
-      s.cp = cp;
-      s.b = cp / s.c;
-      s.cprev = s.c;
-      s.c = cp;
-      s.iter += 1;
-      if (cp > s.maxres) s.maxres = cp;
-      if (cp <= s.rsq) s.done = 1;
-      else if (cp < s.delta * s.maxres) s.relup = 1;
-    } else {
-      s.b = 0.0;
+// launched with 256 threads: the partial sums of every right-hand side are reduced by the
+// whole CTA (a single thread walking thousands of partials would take ~100 us)
+__global__ void __launch_bounds__(256) cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs) {
+  for (int r = 0; r < nrhs; r++) {
+    const double d = cta_sum_fixed(partial, nparts, nrhs * 2, r * 2);
+    if (threadIdx.x == 0) {
+      cg[r].d = d;
+      cg[r].a = cg[r].done ? 0.0 : cg[r].c / d;
     }
-    cg[r] = s;
-    if (s.done) atomicAdd(&nd, 1);
-    if (s.relup && !s.done) atomicAdd(&nr, 1);
   }
-  __syncthreads();
-  if (r == 0) { flags[0] = (nd == nrhs); flags[1] = nr; }
+}
+
+__global__ void __launch_bounds__(256) cg_beta_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs,
+                                                      int* flags) {
+  int nd = 0, nr = 0;
+  for (int r = 0; r < nrhs; r++) {
+    const double cp = cta_sum_fixed(partial, nparts, nrhs, r);
+    if (threadIdx.x == 0) {
+      CGScalars s = cg[r];
+      if (!s.done) {
+        s.cp = cp;
+        s.b = cp / s.c;
+        s.cprev = s.c;
+        s.c = cp;
+        s.iter += 1;
+        if (cp > s.maxres) s.maxres = cp;
+        if (cp <= s.rsq) s.done = 1;
+        else if (cp < s.delta * s.maxres) s.relup = 1;
+      } else {
+        s.b = 0.0;
+      }
+      cg[r] = s;
+      nd += s.done;
+      nr += (s.relup && !s.done);
+    }
+  }
+  if (threadIdx.x == 0) { flags[0] = (nd == nrhs); flags[1] = nr; }
 }
 
 __global__ void cg_relup_reset_kernel(CGScalars* cg, const double* cp_true, int nrhs) {
@@ -386,15 +404,14 @@ int launch_cg_init(Op* op, const double* d_ssq, const double* d_cp, double tol, 
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
-// the per-block partial sums are few (<= 2 * kRedBlocks); the scalar kernels read them
-// directly in a fixed order
+// the scalar kernels reduce the per-block partial sums themselves, in a fixed order
 int launch_cg_alpha(Op* op, const double* partial_inner, int nparts) {
-  cg_alpha_kernel<<<1, rhs_threads(op), 0, op->stream>>>(op->d_cg, partial_inner, nparts, op->nrhs);
+  cg_alpha_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial_inner, nparts, op->nrhs);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
 int launch_cg_beta(Op* op, const double* partial_norm, int nparts) {
-  cg_beta_kernel<<<1, rhs_threads(op), 0, op->stream>>>(op->d_cg, partial_norm, nparts, op->nrhs, op->d_all_done);
+  cg_beta_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial_norm, nparts, op->nrhs, op->d_all_done);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }

@@ -1,4 +1,4 @@
-// gb_col.cu -- fused s-column kernels of the Cayley 5D operators (FP32 site-pair layout).
+// gb_col.cu -- fused s-column kernels of the Cayley 5D operators (FP32 / FP16 site-pair layout).
 //
 // Every Cayley 5D operator acts on each spin-colour component of each (4D site, rhs)
 // column of Ls values on its own, because the chiral projectors P+- are diagonal in spin:
@@ -7,6 +7,8 @@
 // along s.  A CTA stages Q columns x 12 components of its input(s) in shared memory with
 // coalesced 16-byte loads, one thread per (component, column) runs a short program of
 // these operators on its column in registers, and the CTA stores the result coalesced.
+// FP16 fields are decoded with their per-site norms on the way in and get new norms (the
+// largest |re|, |im| of each 5D site) on the way out.
 //
 // Programs: out = A(x) + zc * B(y) with
 //   A in {M5D, INV, M5D(INV(x)), INV(M5D(x))},  B in {none, y, M5D(y)},
@@ -21,6 +23,11 @@
 
 namespace gb {
 
+// columns per CTA and the shared-memory slot of one column (an odd number of float4, so
+// the column reads of a quarter warp fall on distinct banks)
+template <int LS> __host__ __device__ constexpr int col_q() { return LS >= 16 ? 16 : 32; }
+template <int LS> __host__ __device__ constexpr int col_stride() { return (LS / 2) % 2 == 0 ? LS / 2 + 1 : LS / 2; }
+
 template <int LS> struct ColCoef {
   float d1[LS], u1[LS], l1[LS];  // M5D of A
   float d2[LS], u2[LS], l2[LS];  // M5D of B
@@ -28,18 +35,105 @@ template <int LS> struct ColCoef {
 };
 
 struct ColParams {
-  const float4* x;
-  const float4* y;
-  float4* out;
-  size_t np;  // float4 per component plane (site pairs per half field)
+  const void* x;
+  const void* y;
+  void* out;
+  const float* xn;  // FP16: per-5D-site norms
+  const float* yn;
+  float* outn;
+  size_t np;  // 16-byte vectors per plane (site pairs per half field)
   size_t nq;  // columns: 4D sites x right-hand sides
   float zc;
 };
 
-// columns per CTA and the shared-memory slot of one column (an odd number of float4, so
-// the column reads of a quarter warp fall on distinct banks)
-template <int LS> __host__ __device__ constexpr int col_q() { return LS >= 16 ? 16 : 32; }
-template <int LS> __host__ __device__ constexpr int col_stride() { return (LS / 2) % 2 == 0 ? LS / 2 + 1 : LS / 2; }
+// stage one input into the [12][Q][ST] float4 tile: FP32 copies the vectors, FP16 decodes
+// the two components of each vector with the norms of the pair's sites
+template <class T, int LS> struct ColIO;
+template <int LS> struct ColIO<float, LS> {
+  static __device__ __forceinline__ void load(const void* src, const float*, float*, float4* tile, size_t np, size_t q0,
+                                              int nv) {
+    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    const float4* x = static_cast<const float4*>(src);
+#pragma unroll 4
+    for (int e = threadIdx.x; e < 12 * Q * H; e += 12 * Q) {
+      const int k = e / (Q * H), r = e - k * (Q * H);
+      if (r < nv) {
+        const int qq = r / H, m = r - qq * H;
+        tile[(k * Q + qq) * ST + m] = __ldg(x + size_t(k) * np + q0 * H + r);
+      }
+    }
+  }
+  static __device__ __forceinline__ void store(void* dst, float*, float*, float4* tile, size_t np, size_t q0, int nv) {
+    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    float4* o = static_cast<float4*>(dst);
+#pragma unroll 4
+    for (int e = threadIdx.x; e < 12 * Q * H; e += 12 * Q) {
+      const int k = e / (Q * H), r = e - k * (Q * H);
+      if (r < nv) {
+        const int qq = r / H, m = r - qq * H;
+        o[size_t(k) * np + q0 * H + r] = tile[(k * Q + qq) * ST + m];
+      }
+    }
+  }
+};
+template <int LS> struct ColIO<__half, LS> {
+  // snorm: Q * LS floats of shared memory for the CTA's site norms
+  static __device__ __forceinline__ void load(const void* src, const float* norms, float* snorm, float4* tile,
+                                              size_t np, size_t q0, int nv) {
+    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    for (int e = threadIdx.x; e < 2 * nv; e += 12 * Q) snorm[e] = __ldg(norms + q0 * LS + e);
+    __syncthreads();
+    const uint4* x = static_cast<const uint4*>(src);
+    for (int e = threadIdx.x; e < 6 * Q * H; e += 12 * Q) {
+      const int g = e / (Q * H), r = e - g * (Q * H);
+      if (r < nv) {
+        const int qq = r / H, m = r - qq * H;
+        const uint4 v = __ldg(x + size_t(g) * np + q0 * H + r);
+        const __half2* h = reinterpret_cast<const __half2*>(&v);
+        const float n0 = snorm[qq * LS + 2 * m], n1 = snorm[qq * LS + 2 * m + 1];
+        const float2 a = __half22float2(h[0]), b = __half22float2(h[1]), c = __half22float2(h[2]),
+                     d = __half22float2(h[3]);
+        tile[((2 * g) * Q + qq) * ST + m] = make_float4(a.x * n0, a.y * n1, b.x * n0, b.y * n1);
+        tile[((2 * g + 1) * Q + qq) * ST + m] = make_float4(c.x * n0, c.y * n1, d.x * n0, d.y * n1);
+      }
+    }
+    __syncthreads();  // snorm is reused by the next input
+  }
+  static __device__ __forceinline__ void store(void* dst, float* norms, float* snorm, float4* tile, size_t np,
+                                               size_t q0, int nv) {
+    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    // the norm of each 5D site: the largest |re|, |im| over its 12 components
+    for (int e = threadIdx.x; e < 2 * nv; e += 12 * Q) {
+      const int qq = e / LS, sl = e - qq * LS, m = sl >> 1, l = sl & 1;
+      float mx = 0.f;
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        const float4 v = tile[(k * Q + qq) * ST + m];
+        mx = fmaxf(mx, fmaxf(fabsf(l ? v.y : v.x), fabsf(l ? v.w : v.z)));
+      }
+      snorm[e] = mx;
+      norms[q0 * LS + e] = mx;
+    }
+    __syncthreads();
+    uint4* o = static_cast<uint4*>(dst);
+    for (int e = threadIdx.x; e < 6 * Q * H; e += 12 * Q) {
+      const int g = e / (Q * H), r = e - g * (Q * H);
+      if (r < nv) {
+        const int qq = r / H, m = r - qq * H;
+        const float m0 = snorm[qq * LS + 2 * m], m1 = snorm[qq * LS + 2 * m + 1];
+        const float2 inv = make_float2(m0 > 0.f ? 1.0f / m0 : 0.f, m1 > 0.f ? 1.0f / m1 : 0.f);
+        const float4 a = tile[((2 * g) * Q + qq) * ST + m], b = tile[((2 * g + 1) * Q + qq) * ST + m];
+        uint4 v;
+        __half2* h = reinterpret_cast<__half2*>(&v);
+        h[0] = __float22half2_rn(__fmul2_rn(make_float2(a.x, a.y), inv));
+        h[1] = __float22half2_rn(__fmul2_rn(make_float2(a.z, a.w), inv));
+        h[2] = __float22half2_rn(__fmul2_rn(make_float2(b.x, b.y), inv));
+        h[3] = __float22half2_rn(__fmul2_rn(make_float2(b.z, b.w), inv));
+        o[size_t(g) * np + q0 * H + r] = v;
+      }
+    }
+  }
+};
 
 // chi_s = d_s x_s + (l_s x_{s-1} | u_s x_{s+1}) with the wrap inside the column
 template <int LS, bool DAG>
@@ -100,26 +194,19 @@ __device__ __forceinline__ void col_read(const float4* slot, float (&r)[LS], flo
   }
 }
 
-template <int LS, bool DAG, int OPA, int OPB>
+template <class T, int LS, bool DAG, int OPA, int OPB>
 __global__ void __launch_bounds__(12 * col_q<LS>()) col_kernel(const ColParams p, const ColCoef<LS> c) {
   constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
-  extern __shared__ float4 col_tile[];  // [inputs][12][Q][ST]
+  extern __shared__ float4 col_tile[];  // [inputs][12][Q][ST], then Q * LS norms (FP16)
   float4* tx = col_tile;
   float4* ty = col_tile + 12 * Q * ST;
+  float* snorm = reinterpret_cast<float*>(col_tile + (OPB != COLB_NONE ? 2 : 1) * 12 * Q * ST);
   const int t = threadIdx.x;
   const size_t q0 = size_t(blockIdx.x) * Q;
   const int qn = p.nq - q0 < size_t(Q) ? int(p.nq - q0) : Q;
-  const int nv = qn * H;  // float4 of one component plane in this CTA
-#pragma unroll 4
-  for (int e = t; e < 12 * Q * H; e += 12 * Q) {
-    const int k = e / (Q * H), r = e - k * (Q * H);
-    if (r < nv) {
-      const int qq = r / H, m = r - qq * H;
-      const size_t g = size_t(k) * p.np + q0 * H + r;
-      tx[(k * Q + qq) * ST + m] = __ldg(p.x + g);
-      if (OPB != COLB_NONE) ty[(k * Q + qq) * ST + m] = __ldg(p.y + g);
-    }
-  }
+  const int nv = qn * H;  // vectors of one plane in this CTA
+  ColIO<T, LS>::load(p.x, p.xn, snorm, tx, p.np, q0, nv);
+  if (OPB != COLB_NONE) ColIO<T, LS>::load(p.y, p.yn, snorm, ty, p.np, q0, nv);
   __syncthreads();
   const int k = t / Q, qq = t - k * Q;
   if (qq < qn) {
@@ -156,14 +243,7 @@ __global__ void __launch_bounds__(12 * col_q<LS>()) col_kernel(const ColParams p
     for (int m = 0; m < H; m++) slot[m] = make_float4(orr[2 * m], orr[2 * m + 1], oi[2 * m], oi[2 * m + 1]);
   }
   __syncthreads();
-#pragma unroll 4
-  for (int e = t; e < 12 * Q * H; e += 12 * Q) {
-    const int k2 = e / (Q * H), r = e - k2 * (Q * H);
-    if (r < nv) {
-      const int q2 = r / H, m = r - q2 * H;
-      p.out[size_t(k2) * p.np + q0 * H + r] = tx[(k2 * Q + q2) * ST + m];
-    }
-  }
+  ColIO<T, LS>::store(p.out, p.outn, snorm, tx, p.np, q0, nv);
 }
 
 template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost& h, ColCoef<LS>& c) {
@@ -184,45 +264,46 @@ template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost
   }
 }
 
-template <int LS, bool DAG, int OPA, int OPB>
+template <class T, int LS, bool DAG, int OPA, int OPB>
 static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
   constexpr int Q = col_q<LS>();
-  const size_t smem = size_t(OPB != COLB_NONE ? 2 : 1) * 12 * Q * col_stride<LS>() * sizeof(float4);
+  const size_t smem = size_t(OPB != COLB_NONE ? 2 : 1) * 12 * Q * col_stride<LS>() * sizeof(float4) +
+                      (sizeof(T) == 2 ? size_t(Q) * LS * sizeof(float) : 0);
   static std::atomic<bool> configured{false};
   if (!configured.load()) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(col_kernel<LS, DAG, OPA, OPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_kernel<T, LS, DAG, OPA, OPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(smem)));
     configured.store(true);
   }
   const unsigned blocks = unsigned((p.nq + Q - 1) / Q);
-  col_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * Q, smem, op->stream>>>(p, c);
+  col_kernel<T, LS, DAG, OPA, OPB><<<blocks, 12 * Q, smem, op->stream>>>(p, c);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
 
 // the programs the operators use; the others are not instantiated
-template <int LS>
+template <class T, int LS>
 static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h) {
   ColCoef<LS> c;
   fill_col<LS>(op, dag, h, c);
   const int key = (dag ? 100 : 0) + opa * 10 + opb;
   switch (key) {
-    case 0 + COL_M5D * 10 + COLB_NONE: return col_go<LS, false, COL_M5D, COLB_NONE>(op, p, c);
-    case 100 + COL_M5D * 10 + COLB_NONE: return col_go<LS, true, COL_M5D, COLB_NONE>(op, p, c);
-    case 0 + COL_M5D * 10 + COLB_IDENT: return col_go<LS, false, COL_M5D, COLB_IDENT>(op, p, c);
-    case 100 + COL_M5D * 10 + COLB_IDENT: return col_go<LS, true, COL_M5D, COLB_IDENT>(op, p, c);
-    case 0 + COL_INV * 10 + COLB_NONE: return col_go<LS, false, COL_INV, COLB_NONE>(op, p, c);
-    case 100 + COL_INV * 10 + COLB_NONE: return col_go<LS, true, COL_INV, COLB_NONE>(op, p, c);
-    case 0 + COL_INV_M5D * 10 + COLB_NONE: return col_go<LS, false, COL_INV_M5D, COLB_NONE>(op, p, c);
-    case 100 + COL_M5D_INV * 10 + COLB_NONE: return col_go<LS, true, COL_M5D_INV, COLB_NONE>(op, p, c);
-    case 100 + COL_M5D * 10 + COLB_M5D: return col_go<LS, true, COL_M5D, COLB_M5D>(op, p, c);
+    case 0 + COL_M5D * 10 + COLB_NONE: return col_go<T, LS, false, COL_M5D, COLB_NONE>(op, p, c);
+    case 100 + COL_M5D * 10 + COLB_NONE: return col_go<T, LS, true, COL_M5D, COLB_NONE>(op, p, c);
+    case 0 + COL_M5D * 10 + COLB_IDENT: return col_go<T, LS, false, COL_M5D, COLB_IDENT>(op, p, c);
+    case 100 + COL_M5D * 10 + COLB_IDENT: return col_go<T, LS, true, COL_M5D, COLB_IDENT>(op, p, c);
+    case 0 + COL_INV * 10 + COLB_NONE: return col_go<T, LS, false, COL_INV, COLB_NONE>(op, p, c);
+    case 100 + COL_INV * 10 + COLB_NONE: return col_go<T, LS, true, COL_INV, COLB_NONE>(op, p, c);
+    case 0 + COL_INV_M5D * 10 + COLB_NONE: return col_go<T, LS, false, COL_INV_M5D, COLB_NONE>(op, p, c);
+    case 100 + COL_M5D_INV * 10 + COLB_NONE: return col_go<T, LS, true, COL_M5D_INV, COLB_NONE>(op, p, c);
+    case 100 + COL_M5D * 10 + COLB_M5D: return col_go<T, LS, true, COL_M5D, COLB_M5D>(op, p, c);
   }
   set_error("column program (%d, %d, dag %d) is not instantiated", opa, opb, dag);
   return GB_ERR_UNSUPPORTED;
 }
 
 bool col_available(const Op* op, int prec) {
-  if (op->kind != 1 || prec != GB_F32) return false;
+  if (op->kind != 1 || (prec != GB_F32 && prec != GB_F16)) return false;
   switch (op->Ls) {
     case 4: case 6: case 8: case 10: case 12: case 16: case 20: case 24: return true;
   }
@@ -232,25 +313,21 @@ bool col_available(const Op* op, int prec) {
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
                const ColCoefsHost& h) {
   if (!col_available(op, x.prec) || out.prec != x.prec || (opb != COLB_NONE && y.prec != x.prec)) {
-    set_error("column kernel: FP32 Moebius fields with an instantiated Ls expected");
+    set_error("column kernel: FP32 or FP16 Moebius fields with an instantiated Ls expected");
     return GB_ERR_UNSUPPORTED;
   }
   ColParams p;
-  p.x = static_cast<const float4*>(x.data);
-  p.y = static_cast<const float4*>(y.data);
-  p.out = static_cast<float4*>(out.data);
+  p.x = x.data; p.y = y.data; p.out = out.data;
+  p.xn = x.norms; p.yn = y.norms; p.outn = out.norms;
   p.np = op->n5() >> 1;
   p.nq = size_t(op->half4) * op->nrhs;
   p.zc = float(zc);
+  const bool half = x.prec == GB_F16;
   switch (op->Ls) {
-    case 4: return col_ls<4>(op, opa, opb, dag, p, h);
-    case 6: return col_ls<6>(op, opa, opb, dag, p, h);
-    case 8: return col_ls<8>(op, opa, opb, dag, p, h);
-    case 10: return col_ls<10>(op, opa, opb, dag, p, h);
-    case 12: return col_ls<12>(op, opa, opb, dag, p, h);
-    case 16: return col_ls<16>(op, opa, opb, dag, p, h);
-    case 20: return col_ls<20>(op, opa, opb, dag, p, h);
-    case 24: return col_ls<24>(op, opa, opb, dag, p, h);
+#define GB_COL_LS(L) \
+  case L: return half ? col_ls<__half, L>(op, opa, opb, dag, p, h) : col_ls<float, L>(op, opa, opb, dag, p, h);
+    GB_COL_LS(4) GB_COL_LS(6) GB_COL_LS(8) GB_COL_LS(10) GB_COL_LS(12) GB_COL_LS(16) GB_COL_LS(20) GB_COL_LS(24)
+#undef GB_COL_LS
   }
   set_error("column kernel: Ls = %d not instantiated", op->Ls);
   return GB_ERR_UNSUPPORTED;

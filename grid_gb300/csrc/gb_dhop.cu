@@ -413,11 +413,15 @@ __device__ __forceinline__ void dhop_pair_step(const DhopParams& p, const int (&
 #ifndef GB_DHOP_MINB
 #define GB_DHOP_MINB 4
 #endif
+// threads per CTA the site-pair kernel aims at
+#ifndef GB_DHOP_THREADS
+#define GB_DHOP_THREADS 128
+#endif
 
 // CTA = k4 4D sites x hc pair threads.  Thread (j, sp) computes the 5D sites
 // (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.
 template <class T, bool DAG, bool RECON>
-__global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p0) {
+__global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p0) {
   const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   float* slink = reinterpret_cast<float*>(dyn_smem);  // k4 * kLinkStride floats
@@ -476,10 +480,10 @@ __global__ void __launch_bounds__(128, GB_DHOP_MINB) dhop_pair_kernel(const Dhop
 
 // CTA = k4 4D sites x (L5c/2) pair threads, about 128 threads
 static int pick_k4_pair(int hc) {
-  if (hc >= 64) return 1;
-  int k4 = 128 / hc;
+  if (hc >= GB_DHOP_THREADS / 2) return 1;
+  int k4 = GB_DHOP_THREADS / hc;
   while (k4 > 1 && (hc * k4) % 32 != 0) k4--;
-  if ((hc * k4) % 32 != 0) k4 = 128 / hc;
+  if ((hc * k4) % 32 != 0) k4 = GB_DHOP_THREADS / hc;
   if (k4 > 64) k4 = 64;  // shared memory: 64 x 592 B
   return k4 < 1 ? 1 : k4;
 }

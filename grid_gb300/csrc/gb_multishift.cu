@@ -150,16 +150,27 @@ __global__ void __launch_bounds__(256) ms_setup_kernel(const V* src, const MSFie
   }
 }
 
+// sum of partial[2 i + which] by the whole CTA (256 threads) in a fixed order
 __device__ double sum_partials(const double* partial, int n, int which) {
+  __shared__ double sm[256];
   double s = 0;
-  for (int i = 0; i < n; i++) s += partial[2 * i + which];
-  return s;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[2 * i + which];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sm[threadIdx.x] += sm[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double r = sm[0];
+  __syncthreads();
+  return r;
 }
 
 // after the first A p: d, b, z, bs (ConjugateGradientMultiShift.h:152-176)
 __global__ void ms_init_kernel(MSState* st, const double* partial, int nparts) {
-  if (threadIdx.x || blockIdx.x) return;
-  const double d = sum_partials(partial, nparts, 0) + st->m0 * sum_partials(partial, nparts, 1);
+  const double s0 = sum_partials(partial, nparts, 0), s1 = sum_partials(partial, nparts, 1);
+  if (threadIdx.x) return;
+  const double d = s0 + st->m0 * s1;
   st->d = d;
   st->b = -st->cp / d;
   st->iz = 0;
@@ -175,8 +186,9 @@ __global__ void ms_init_kernel(MSState* st, const double* partial, int nparts) {
 
 // after r = src + b A p: c, then this iteration's p/ps coefficients (loop top of Grid's)
 __global__ void ms_coef_kernel(MSState* st, const double* partial, int nparts) {
-  if (threadIdx.x || blockIdx.x) return;
-  st->c = sum_partials(partial, nparts, 0);
+  const double s0 = sum_partials(partial, nparts, 0);
+  if (threadIdx.x) return;
+  st->c = s0;
   const double a = st->c / st->cp;
   st->a = a;
   const int iz = st->iz;
@@ -191,20 +203,23 @@ __global__ void ms_coef_kernel(MSState* st, const double* partial, int nparts) {
 
 // after d = <p, A p>: d, b
 __global__ void ms_mid_kernel(MSState* st, const double* partial, int nparts) {
-  if (threadIdx.x || blockIdx.x || st->frozen) return;
+  if (st->frozen) return;  // uniform: read by every thread before any write
+  const double s0 = sum_partials(partial, nparts, 0), s1 = sum_partials(partial, nparts, 1);
+  if (threadIdx.x) return;
   if (st->all_done) {  // the update pass before this kernel applied the last psi update
     st->frozen = 1;
     return;
   }
-  st->d = sum_partials(partial, nparts, 0) + st->m0 * sum_partials(partial, nparts, 1);
+  st->d = s0 + st->m0 * s1;
   st->bp = st->b;
   st->b = -st->cp / st->d;
 }
 
 // after r += b A p: c, z, bs, convergence, then the next iteration's coefficients
 __global__ void ms_post_kernel(MSState* st, const double* partial, int nparts) {
-  if (threadIdx.x || blockIdx.x || st->frozen) return;
+  if (st->frozen) return;
   const double c = sum_partials(partial, nparts, 0);
+  if (threadIdx.x) return;
   st->c = c;
   const double b = st->b, bp = st->bp, a = st->a;
   st->bs[0] = b;
@@ -281,7 +296,7 @@ template <class V> struct MS {
     return GB_OK;
   }
   int scalar(void (*k)(MSState*, const double*, int)) {
-    k<<<1, 1, 0, op->stream>>>(st, partial, int(blocks()));
+    k<<<1, 256, 0, op->stream>>>(st, partial, int(blocks()));
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
   }
