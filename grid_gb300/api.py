@@ -76,6 +76,7 @@ _proto("gb_device_count", [_ip])
 _proto("gb_version", [])
 _proto("gb_wilson_create", [_ip, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
 _proto("gb_mobius_create", [_ip, _i, _d, _d, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
+_proto("gb_zmobius_create", [_ip, _i, _d, _d, _dp, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
 _proto("gb_op_destroy", [_vp])
 _proto("gb_op_import_gauge", [_vp, _dp])
 _proto("gb_op_import_gauge_device", [_vp, _vp])
@@ -482,6 +483,24 @@ class MobiusFermion(_FermionOperator):
 
     def ExportPhysicalFermionSource(self, src5d):
         return self._surface_out(lib.gb_export_physical_source, src5d)
+
+
+class ZMobiusFermion(MobiusFermion):
+    """ZMobiusFermion<WilsonImplD/F>(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, gamma, b, c)
+    (Grid/qcd/action/fermion/ZMobiusFermion.h): complex omega_s = gamma[s]."""
+
+    def __init__(self, U, dims, gamma, mf, M5, b, c, phases=None, precision=F64, nrhs=1, stream=None, flags=0):
+        self.dims = tuple(int(x) for x in dims)
+        self.mass = float(mf)
+        self.M5, self.b, self.c = float(M5), float(b), float(c)
+        self.gamma = [complex(z) for z in gamma]
+        self.kind = 1
+        ph = antiperiodic_t() if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        gm = np.ascontiguousarray([v for z in self.gamma for v in (z.real, z.imag)], dtype=np.float64)
+        h = _vp()
+        _check(lib.gb_zmobius_create(_dims(dims), len(self.gamma), float(mf), float(M5), _dptr(gm), float(b), float(c),
+                                     _dptr(ph), int(precision), int(nrhs), _vp(stream or 0), int(flags), C.byref(h)))
+        self._finish(h, U, stream)
 
 
 # ---- linear operators and solvers -----------------------------------------------------

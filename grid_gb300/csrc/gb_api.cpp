@@ -244,7 +244,79 @@ static int col_field(Op* op, int opa, int opb, int dag, Field* x, Field* y, Fiel
   return GB_OK;
 }
 
+// ---- ZMobius: the same coefficient sets with complex bs, cs (CayleyFermion5DImplementation.h:
+// 155-271); the dagger forms are conjugated as Grid assembles them ----
+using cplxd = std::complex<double>;
+static void conj_all(std::vector<cplxd>& v) {
+  for (auto& x : v) x = std::conj(x);
+}
+static void zcoeffs_meooe5d(const Op* op, int dag, ZCoefsHost& h) {
+  const int Ls = op->Ls;
+  const double mf = op->mass;
+  h.d = op->zbs;
+  h.u.assign(Ls, 0);
+  h.l.assign(Ls, 0);
+  if (!dag) {
+    h.u = op->zcs;
+    h.l = op->zcs;
+    h.u[Ls - 1] = -mf * h.u[Ls - 1];
+    h.l[0] = -mf * h.l[0];
+    return;
+  }
+  for (int s = 0; s < Ls; s++) {
+    if (s == 0) { h.u[s] = op->zcs[s + 1]; h.l[s] = -mf * op->zcs[Ls - 1]; }
+    else if (s == Ls - 1) { h.u[s] = -mf * op->zcs[0]; h.l[s] = op->zcs[s - 1]; }
+    else { h.u[s] = op->zcs[s + 1]; h.l[s] = op->zcs[s - 1]; }
+  }
+  conj_all(h.d); conj_all(h.u); conj_all(h.l);
+}
+static void zcoeffs_mooee(const Op* op, int dag, ZCoefsHost& h) {
+  const int Ls = op->Ls;
+  const double mf = op->mass;
+  h.d = op->zbee;
+  h.u.assign(Ls, 0);
+  h.l.assign(Ls, 0);
+  if (!dag) {
+    for (int i = 0; i < Ls; i++) { h.u[i] = -op->zcee[i]; h.l[i] = -op->zcee[i]; }
+    h.u[Ls - 1] = -mf * h.u[Ls - 1];
+    h.l[0] = -mf * h.l[0];
+    return;
+  }
+  for (int s = 0; s < Ls; s++) {
+    if (s == 0) { h.u[s] = -op->zcee[s + 1]; h.l[s] = mf * op->zcee[Ls - 1]; }
+    else if (s == Ls - 1) { h.u[s] = mf * op->zcee[0]; h.l[s] = -op->zcee[s - 1]; }
+    else { h.u[s] = -op->zcee[s + 1]; h.l[s] = -op->zcee[s - 1]; }
+  }
+  conj_all(h.d); conj_all(h.u); conj_all(h.l);
+}
+// MooeeInv / MooeeInvDag (CayleyFermion5Dcache.h:117-230): the dagger swaps the L and U
+// factors and conjugates them
+static void zcoeffs_inv(const Op* op, int dag, ZCoefsHost& h) {
+  const int Ls = op->Ls;
+  h.dinv.resize(Ls);
+  for (int s = 0; s < Ls; s++) h.dinv[s] = 1.0 / op->zdee[s];
+  if (!dag) {
+    h.lee = op->zlee; h.leem = op->zleem; h.uee = op->zuee; h.ueem = op->zueem;
+    return;
+  }
+  h.lee = op->zuee; h.leem = op->zueem; h.uee = op->zlee; h.ueem = op->zleem;
+  conj_all(h.lee); conj_all(h.leem); conj_all(h.uee); conj_all(h.ueem); conj_all(h.dinv);
+}
+static int zcol_field(Op* op, int prog, int dag, Field* x, Field* y, Field* out, double zc, const ZCoefsHost& h) {
+  const int halves = out->full() ? 2 : 1;
+  for (int k = 0; k < halves; k++) {
+    const HalfView yv = y ? half_view(y, k) : HalfView{nullptr, nullptr, x->prec};
+    GB_TRY(launch_zcol(op, prog, dag, half_view(x, k), y ? &yv : nullptr, half_view(out, k), zc, h));
+  }
+  return GB_OK;
+}
+
 int op_meooe5d(Op* op, Field* in, Field* out, int dag) {
+  if (op->zmobius) {
+    ZCoefsHost h;
+    zcoeffs_meooe5d(op, dag, h);
+    return zcol_field(op, ZPROG_M5D, dag, in, nullptr, out, 0.0, h);
+  }
   std::vector<double> l, d, u;
   coeffs_meooe5d(op, dag, l, d, u);
   return m5d_field(op, in, in, out, l, d, u, dag, nullptr, 0);
@@ -287,6 +359,11 @@ int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
     if (z) return field_axpby(out, op->diag_mass, zc, in, z);
     return field_scale(out, op->diag_mass, in);
   }
+  if (op->zmobius) {
+    ZCoefsHost h;
+    zcoeffs_mooee(op, dag, h);
+    return zcol_field(op, ZPROG_M5D, dag, in, z, out, zc, h);
+  }
   std::vector<double> l, d, u;
   coeffs_mooee(op, dag, l, d, u);
   return m5d_field(op, in, in, out, l, d, u, dag, z, zc);
@@ -296,6 +373,11 @@ int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
   if (in->full() != out->full()) { set_error("MooeeInv: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
   if (op->kind == 0) return field_scale(out, 1.0 / op->diag_mass, in);
+  if (op->zmobius) {
+    ZCoefsHost h;
+    zcoeffs_inv(op, dag, h);
+    return zcol_field(op, ZPROG_INV, dag, in, nullptr, out, 0.0, h);
+  }
   if (col_available(op, in->prec)) return col_field(op, COL_INV, COLB_NONE, dag, in, nullptr, out, 0.0, ColCoefsHost());
   const int halves = in->full() ? 2 : 1;
   for (int h = 0; h < halves; h++)
@@ -388,6 +470,13 @@ int op_dminus(Op* op, Field* in, Field* out, int dag) {
   Field* t;
   GB_TRY(ws_get(op, GB_FULL, in->prec, WS_DMINUS, &t));
   GB_TRY(op_dhop_full(op, in, t, dag));
+  if (op->zmobius) {  // chi_s = psi_s - cs_s (DW psi)_s, conj(cs_s) for the dagger
+    GB_TRY(field_axpby(t, 1.0, 4.0 - op->M5, t, in));
+    ZCoefsHost h;
+    h.e.resize(op->Ls);
+    for (int s = 0; s < op->Ls; s++) h.e[s] = dag ? -std::conj(op->zcs[s]) : -op->zcs[s];
+    return zcol_field(op, ZPROG_DIAG, dag, in, t, out, 0.0, h);
+  }
   const double c = op->cs[0];
   return field_axpby(out, 1.0 - c * (4.0 - op->M5), -c, in, t);
 }
@@ -448,6 +537,39 @@ static void cayley_setup(Op* op) {
   double delta_d = mf * op->cee[Ls - 1];
   for (int j = 0; j < Ls - 1; j++) delta_d *= op->cee[j] / op->bee[j];
   op->dee[Ls - 1] += delta_d;
+}
+
+// SetCoefficientsInternal with complex omega_s = gamma_s (ZMobiusFermion.h,
+// CayleyFermion5DImplementation.h:410-535)
+static void zcayley_setup(Op* op) {
+  const int Ls = op->Ls;
+  const double b = op->b, c = op->c, M5 = op->M5, mf = op->mass;
+  using C = std::complex<double>;
+  op->zbs.assign(Ls, 0); op->zcs.assign(Ls, 0); op->zbee.assign(Ls, 0); op->zcee.assign(Ls, 0);
+  op->zdee.assign(Ls, 0); op->zlee.assign(Ls, 0); op->zleem.assign(Ls, 0); op->zuee.assign(Ls, 0); op->zueem.assign(Ls, 0);
+  for (int i = 0; i < Ls; i++) {
+    const C omega = op->zgamma[i];
+    op->zbs[i] = 0.5 * ((b + c) / omega + (b - c));
+    op->zcs[i] = 0.5 * ((b + c) / omega - (b - c));
+    op->zbee[i] = op->zbs[i] * (4.0 - M5) + 1.0;
+    op->zcee[i] = 1.0 - op->zcs[i] * (4.0 - M5);
+  }
+  const std::vector<C>& aee = op->zcee;
+  for (int i = 0; i < Ls; i++) {
+    op->zdee[i] = op->zbee[i];
+    if (i < Ls - 1) {
+      op->zlee[i] = -op->zcee[i + 1] / op->zbee[i];
+      op->zleem[i] = mf * op->zcee[Ls - 1] / op->zbee[0];
+      for (int j = 0; j < i; j++) op->zleem[i] *= aee[j] / op->zbee[j + 1];
+      op->zuee[i] = -aee[i] / op->zbee[i];
+      op->zueem[i] = mf;
+      for (int j = 1; j <= i; j++) op->zueem[i] *= op->zcee[j] / op->zbee[j];
+      op->zueem[i] *= aee[0] / op->zbee[0];
+    }
+  }
+  C delta_d = mf * op->zcee[Ls - 1];
+  for (int j = 0; j < Ls - 1; j++) delta_d *= op->zcee[j] / op->zbee[j];
+  op->zdee[Ls - 1] += delta_d;
 }
 
 static void op_release(Op* op) {
@@ -636,6 +758,21 @@ int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, 
                      int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out) {
   return op_create(1, dims, Ls, mf, M5, b, c, phases, precision, nrhs, stream, flags, out);
 }
+int gb_zmobius_create(const int dims[4], int Ls, double mf, double M5, const double* gamma, double b, double c,
+                      const double* phases, int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out) {
+  if (!gamma || !out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (precision == GB_F16) { set_error("ZMobius: FP64 or FP32 operators"); return GB_ERR_UNSUPPORTED; }
+  if (!zmobius_ls_supported(Ls)) { set_error("ZMobius: Ls = %d is not supported", Ls); return GB_ERR_UNSUPPORTED; }
+  for (int s = 0; s < Ls; s++)
+    if (gamma[2 * s] == 0.0 && gamma[2 * s + 1] == 0.0) { set_error("ZMobius: gamma[%d] = 0", s); return GB_ERR_BAD_ARG; }
+  GB_TRY(op_create(1, dims, Ls, mf, M5, b, c, phases, precision, nrhs, stream, flags, out));
+  Op* op = *out;
+  op->zmobius = true;
+  op->zgamma.resize(Ls);
+  for (int s = 0; s < Ls; s++) op->zgamma[s] = std::complex<double>(gamma[2 * s], gamma[2 * s + 1]);
+  zcayley_setup(op);
+  return GB_OK;
+}
 int gb_op_destroy(gb_op_t op) {
   if (!op) return GB_OK;
   cudaStreamSynchronize(op->stream);
@@ -669,6 +806,7 @@ int gb_op_set_stream(gb_op_t op, void* stream) {
 }
 int gb_op_cayley_coeffs(gb_op_t op, double* out) {
   if (!op || !out || op->kind != 1) { set_error("not a Moebius operator"); return GB_ERR_BAD_ARG; }
+  if (op->zmobius) { set_error("ZMobius coefficients are complex"); return GB_ERR_UNSUPPORTED; }
   const std::vector<double>* v[9] = {&op->bs, &op->cs, &op->bee, &op->cee, &op->dee, &op->lee, &op->leem, &op->uee, &op->ueem};
   for (int k = 0; k < 9; k++) std::memcpy(out + k * op->Ls, v[k]->data(), op->Ls * sizeof(double));
   return GB_OK;

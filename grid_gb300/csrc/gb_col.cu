@@ -303,7 +303,7 @@ static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const C
 }
 
 bool col_available(const Op* op, int prec) {
-  if (op->kind != 1 || (prec != GB_F32 && prec != GB_F16)) return false;
+  if (op->kind != 1 || op->zmobius || (prec != GB_F32 && prec != GB_F16)) return false;
   switch (op->Ls) {
     case 4: case 6: case 8: case 10: case 12: case 16: case 20: case 24: return true;
   }

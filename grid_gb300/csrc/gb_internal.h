@@ -81,6 +81,10 @@ struct Op {
 
   // Cayley coefficients (Moebius) -- host copies
   std::vector<double> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
+  // ZMobius: complex omega_s, so complex Cayley coefficients (the real arrays above are
+  // then unused)
+  bool zmobius = false;
+  std::vector<std::complex<double>> zgamma, zbs, zcs, zbee, zcee, zdee, zlee, zleem, zuee, zueem;
 
   // reduction scratch
   double* d_partial = nullptr;  // kRedBlocks * nrhs * 2
@@ -189,6 +193,16 @@ struct ColCoefsHost {
   std::vector<double> l2, d2, u2;  // M5D of B
 };
 bool col_available(const Op* op, int prec);
+// complex-coefficient 5D programs of ZMobius operators (gb_zmobius.cu); coefficients as
+// the operator applies them (conjugated / swapped for the dagger forms by the host)
+struct ZCoefsHost {
+  std::vector<std::complex<double>> d, u, l;                    // M5D
+  std::vector<std::complex<double>> lee, leem, uee, ueem, dinv;  // MooeeInv
+  std::vector<std::complex<double>> e;                          // DIAG: out = x + e y
+};
+enum { ZPROG_M5D = 0, ZPROG_INV = 2, ZPROG_DIAG = 3 };
+bool zmobius_ls_supported(int Ls);
+int launch_zcol(Op* op, int prog, int dag, HalfView x, const HalfView* y, HalfView out, double zc, const ZCoefsHost& h);
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
                const ColCoefsHost& h);
 

@@ -73,6 +73,12 @@ int gb_wilson_create(const int dims[4], double mass, const double* phases, int p
                      unsigned flags, gb_op_t* out);
 int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,
                      int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out);
+/* ZMobiusFermion(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, gamma, b, c, ImplParams)
+ * (Grid/qcd/action/fermion/ZMobiusFermion.h): complex omega_s = gamma[s] (Ls complex
+ * numbers as re, im), hence complex Cayley coefficients.  FP64 or FP32; Ls even, 2..16,
+ * 20, 24 or 32. */
+int gb_zmobius_create(const int dims[4], int Ls, double mf, double M5, const double* gamma, double b, double c,
+                      const double* phases, int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out);
 int gb_op_destroy(gb_op_t op);
 /* ImportGauge (WilsonFermion5DImplementation.h:149-180): canonical FP64 host field. */
 int gb_op_import_gauge(gb_op_t op, const double* U_host);

@@ -321,22 +321,27 @@ void dhop_naive(const Geom& g, int L5, const cplx<double>* U, const cplx<double>
 // Cayley / Moebius coefficients (CayleyFermion5DImplementation.h:410-535) with the
 // Moebius tanh choice gamma_s = 1 (MobiusFermion.h:63-67; approx/Zolotarev.cc:471-473).
 // ---------------------------------------------------------------------------------------
-struct Cayley {
+// coefficient conjugation: the identity for real Moebius coefficients
+inline double cj(double x) { return x; }
+inline cplx<double> cj(const cplx<double>& x) { return std::conj(x); }
+
+// SetCoefficientsInternal (CayleyFermion5DImplementation.h:410-535) with omega_s = gamma_s:
+// 1 for Moebius (real coefficients), complex for ZMobius (ZMobiusFermion.h)
+template <class C> struct CayleyT {
   int Ls = 0;
   double mf = 0, M5 = 0, b = 0, c = 0;
-  std::vector<double> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
-  void setup(int Ls_, double mf_, double M5_, double b_, double c_) {
+  std::vector<C> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
+  void setup(int Ls_, double mf_, double M5_, double b_, double c_, const std::vector<C>& omega) {
     Ls = Ls_; mf = mf_; M5 = M5_; b = b_; c = c_;
-    bs.assign(Ls, 0); cs.assign(Ls, 0); bee.assign(Ls, 0); cee.assign(Ls, 0);
-    dee.assign(Ls, 0); lee.assign(Ls, 0); leem.assign(Ls, 0); uee.assign(Ls, 0); ueem.assign(Ls, 0);
+    bs.assign(Ls, C(0)); cs.assign(Ls, C(0)); bee.assign(Ls, C(0)); cee.assign(Ls, C(0));
+    dee.assign(Ls, C(0)); lee.assign(Ls, C(0)); leem.assign(Ls, C(0)); uee.assign(Ls, C(0)); ueem.assign(Ls, C(0));
     for (int i = 0; i < Ls; i++) {
-      double omega = 1.0;
-      bs[i] = 0.5 * ((b + c) / omega + (b - c));
-      cs[i] = 0.5 * ((b + c) / omega - (b - c));
+      bs[i] = 0.5 * ((b + c) / omega[i] + (b - c));
+      cs[i] = 0.5 * ((b + c) / omega[i] - (b - c));
       bee[i] = bs[i] * (4.0 - M5) + 1.0;
       cee[i] = 1.0 - cs[i] * (4.0 - M5);
     }
-    const std::vector<double>& aee = cee;
+    const std::vector<C>& aee = cee;
     for (int i = 0; i < Ls; i++) {
       dee[i] = bee[i];
       if (i < Ls - 1) {
@@ -344,24 +349,28 @@ struct Cayley {
         leem[i] = mf * cee[Ls - 1] / bee[0];
         for (int j = 0; j < i; j++) leem[i] *= aee[j] / bee[j + 1];
         uee[i] = -aee[i] / bee[i];
-        ueem[i] = mf;
+        ueem[i] = C(mf);
         for (int j = 1; j <= i; j++) ueem[i] *= cee[j] / bee[j];
         ueem[i] *= aee[0] / bee[0];
       }
     }
-    double delta_d = mf * cee[Ls - 1];
+    C delta_d = mf * cee[Ls - 1];
     for (int j = 0; j < Ls - 1; j++) delta_d *= cee[j] / bee[j];
     dee[Ls - 1] += delta_d;
   }
+  void setup(int Ls_, double mf_, double M5_, double b_, double c_) {  // Moebius: omega_s = 1
+    setup(Ls_, mf_, M5_, b_, c_, std::vector<C>(Ls_, C(1.0)));
+  }
 };
+using Cayley = CayleyT<double>;
 
 // M5D / M5Ddag (CayleyFermion5Dcache.h:41-115) on an n4 x Ls field (full or half):
 //   non-dag: chi[s] = diag[s] phi[s] + upper[s] P- psi[s+1] + lower[s] P+ psi[s-1]
 //   dag    : chi[s] = diag[s] phi[s] + upper[s] P+ psi[s+1] + lower[s] P- psi[s-1]
 // with P+ = spins {0,1}, P- = spins {2,3} (gamma_5 = diag(1,1,-1,-1)).
-template <class R>
-void m5d(int64_t n4, int Ls, const Field<R>& psi, const Field<R>& phi, Field<R>& chi, const std::vector<double>& lower,
-         const std::vector<double>& diag, const std::vector<double>& upper, int dag) {
+template <class R, class C = double>
+void m5d(int64_t n4, int Ls, const Field<R>& psi, const Field<R>& phi, Field<R>& chi, const std::vector<C>& lower,
+         const std::vector<C>& diag, const std::vector<C>& upper, int dag) {
   Field<R> res(psi.size());
 #pragma omp parallel for
   for (int64_t x = 0; x < n4; x++)
@@ -370,9 +379,9 @@ void m5d(int64_t n4, int Ls, const Field<R>& psi, const Field<R>& phi, Field<R>&
       size_t o = (size_t(x) * Ls + s) * Nsc, op = (size_t(x) * Ls + sp) * Nsc, om = (size_t(x) * Ls + sm) * Nsc;
       for (int k = 0; k < Nsc; k++) {
         bool upper_spin = k < 6;  // spins 0,1
-        cplx<R> v = R(diag[s]) * phi[o + k];
-        if (!dag) v += upper_spin ? R(lower[s]) * psi[om + k] : R(upper[s]) * psi[op + k];
-        else      v += upper_spin ? R(upper[s]) * psi[op + k] : R(lower[s]) * psi[om + k];
+        cplx<R> v = cplx<R>(diag[s]) * phi[o + k];
+        if (!dag) v += upper_spin ? cplx<R>(lower[s]) * psi[om + k] : cplx<R>(upper[s]) * psi[op + k];
+        else      v += upper_spin ? cplx<R>(upper[s]) * psi[op + k] : cplx<R>(lower[s]) * psi[om + k];
         res[o + k] = v;
       }
     }
@@ -463,20 +472,36 @@ template <class R> struct Wilson : Op<R> {
 
 // MobiusFermion / CayleyFermion5D (CayleyFermion5DImplementation.h:155-344,
 // CayleyFermion5Dcache.h:117-230).  L5 = Ls.
-template <class R> struct Mobius : Op<R> {
-  Cayley cf;
+// the Cayley-form operators (Moebius, ZMobius) beyond the common interface
+template <class R> struct CayleyBase : Op<R> {
+  CayleyBase(const int* dims, int L5) : Op<R>(dims, L5) {}
+  virtual void Meooe5D(const Field<R>& psi, Field<R>& Din) = 0;
+  virtual void MeooeDag5D(const Field<R>& psi, Field<R>& Din) = 0;
+  virtual void Dminus(const Field<R>& psi, Field<R>& chi, int dag) = 0;
+  virtual void ImportUnphysical(const Field<R>& in4, Field<R>& out5) const = 0;
+  virtual void ImportPhysicalSource(const Field<R>& in4, Field<R>& out5) = 0;
+  virtual void ExportPhysical(const Field<R>& in5, Field<R>& out4, bool solution) const = 0;
+};
+
+template <class R, class C = double> struct Mobius : CayleyBase<R> {
+  CayleyT<C> cf;
   int Ls;
-  Mobius(const int* dims, int Ls_, double mf, double M5, double b, double c) : Op<R>(dims, Ls_), Ls(Ls_) {
+  Mobius(const int* dims, int Ls_, double mf, double M5, double b, double c) : CayleyBase<R>(dims, Ls_), Ls(Ls_) {
     cf.setup(Ls_, mf, M5, b, c);
+  }
+  // ZMobius: complex omega_s = gamma_s
+  Mobius(const int* dims, int Ls_, double mf, double M5, double b, double c, const std::vector<C>& gamma)
+      : CayleyBase<R>(dims, Ls_), Ls(Ls_) {
+    cf.setup(Ls_, mf, M5, b, c, gamma);
   }
   int64_t n4(const Field<R>& f) const { return int64_t(f.size() / (size_t(Ls) * Nsc)); }
 
   void DW(const Field<R>& in, Field<R>& out, int dag) {
     this->Dhop(in, out, dag); axpy<R>(out, R(4.0 - cf.M5), in, out);
   }
-  // Dminus / DminusDag (CayleyFermion5DImplementation.h:131-153): chi_s = psi_s - cs[s] (DW psi)_s
-  // (cs is real for Moebius, so the dagger only changes DW)
-  void Dminus(const Field<R>& psi, Field<R>& chi, int dag) {
+  // Dminus / DminusDag (CayleyFermion5DImplementation.h:131-153): chi_s = psi_s - cs[s] (DW psi)_s,
+  // conj(cs[s]) and DW^dag for the dagger
+  void Dminus(const Field<R>& psi, Field<R>& chi, int dag) override {
     Field<R> t;
     DW(psi, t, dag);
     chi.resize(psi.size());
@@ -485,12 +510,12 @@ template <class R> struct Mobius : Op<R> {
       for (int s = 0; s < Ls; s++)
         for (int k = 0; k < Nsc; k++) {
           const size_t i = (size_t(x) * Ls + s) * Nsc + k;
-          chi[i] = psi[i] - R(cf.cs[s]) * t[i];
+          chi[i] = psi[i] - cplx<R>(dag ? cj(cf.cs[s]) : cf.cs[s]) * t[i];
         }
   }
   // ImportUnphysicalFermion (:101-114): s = 0 takes P+ in4, s = Ls-1 takes P- in4, the
   // rest is zero.  P+ keeps spins 0,1 and P- spins 2,3 (gamma5 = diag(1,1,-1,-1)).
-  void ImportUnphysical(const Field<R>& in4, Field<R>& out5) const {
+  void ImportUnphysical(const Field<R>& in4, Field<R>& out5) const override {
     const int64_t n = int64_t(in4.size() / Nsc);
     out5.assign(size_t(n) * Ls * Nsc, cplx<R>(0, 0));
     for (int64_t x = 0; x < n; x++)
@@ -500,14 +525,14 @@ template <class R> struct Mobius : Op<R> {
       }
   }
   // ImportPhysicalFermionSource (:116-129) = Dminus of the unphysical import
-  void ImportPhysicalSource(const Field<R>& in4, Field<R>& out5) {
+  void ImportPhysicalSource(const Field<R>& in4, Field<R>& out5) override {
     Field<R> t;
     ImportUnphysical(in4, t);
     Dminus(t, out5, 0);
   }
   // ExportPhysicalFermionSolution (:57-68): P- psi(s=0) + P+ psi(s=Ls-1);
   // ExportPhysicalFermionSource (:89-100): P+ psi(s=0) + P- psi(s=Ls-1)
-  void ExportPhysical(const Field<R>& in5, Field<R>& out4, bool solution) const {
+  void ExportPhysical(const Field<R>& in5, Field<R>& out4, bool solution) const override {
     const int64_t n = n4(in5);
     out4.resize(size_t(n) * Nsc);
     for (int64_t x = 0; x < n; x++)
@@ -517,38 +542,46 @@ template <class R> struct Mobius : Op<R> {
         out4[size_t(x) * Nsc + k] = in5[(size_t(x) * Ls + s) * Nsc + k];
       }
   }
-  void Meooe5D(const Field<R>& psi, Field<R>& Din) {
-    std::vector<double> diag = cf.bs, upper = cf.cs, lower = cf.cs;
+  void Meooe5D(const Field<R>& psi, Field<R>& Din) override {
+    std::vector<C> diag = cf.bs, upper = cf.cs, lower = cf.cs;
     upper[Ls - 1] = -cf.mf * upper[Ls - 1];
     lower[0] = -cf.mf * lower[0];
     m5d<R>(n4(psi), Ls, psi, psi, Din, lower, diag, upper, 0);
   }
-  void MeooeDag5D(const Field<R>& psi, Field<R>& Din) {
-    std::vector<double> diag = cf.bs, upper(Ls), lower(Ls);
+  void MeooeDag5D(const Field<R>& psi, Field<R>& Din) override {
+    std::vector<C> diag = cf.bs, upper(Ls), lower(Ls);
     for (int s = 0; s < Ls; s++) {
       if (s == 0) { upper[s] = cf.cs[s + 1]; lower[s] = -cf.mf * cf.cs[Ls - 1]; }
       else if (s == Ls - 1) { upper[s] = -cf.mf * cf.cs[0]; lower[s] = cf.cs[s - 1]; }
       else { upper[s] = cf.cs[s + 1]; lower[s] = cf.cs[s - 1]; }
     }
+    for (int s = 0; s < Ls; s++) { diag[s] = cj(diag[s]); upper[s] = cj(upper[s]); lower[s] = cj(lower[s]); }
     m5d<R>(n4(psi), Ls, psi, psi, Din, lower, diag, upper, 1);
   }
   void Mooee(const Field<R>& psi, Field<R>& chi) override {
-    std::vector<double> diag = cf.bee, upper(Ls), lower(Ls);
+    std::vector<C> diag = cf.bee, upper(Ls), lower(Ls);
     for (int i = 0; i < Ls; i++) { upper[i] = -cf.cee[i]; lower[i] = -cf.cee[i]; }
     upper[Ls - 1] = -cf.mf * upper[Ls - 1];
     lower[0] = -cf.mf * lower[0];
     m5d<R>(n4(psi), Ls, psi, psi, chi, lower, diag, upper, 0);
   }
   void MooeeDag(const Field<R>& psi, Field<R>& chi) override {
-    std::vector<double> diag = cf.bee, upper(Ls), lower(Ls);
+    std::vector<C> diag = cf.bee, upper(Ls), lower(Ls);
     for (int s = 0; s < Ls; s++) {
       if (s == 0) { upper[s] = -cf.cee[s + 1]; lower[s] = cf.mf * cf.cee[Ls - 1]; }
       else if (s == Ls - 1) { upper[s] = cf.mf * cf.cee[0]; lower[s] = -cf.cee[s - 1]; }
       else { upper[s] = -cf.cee[s + 1]; lower[s] = -cf.cee[s - 1]; }
     }
+    for (int s = 0; s < Ls; s++) { diag[s] = cj(diag[s]); upper[s] = cj(upper[s]); lower[s] = cj(lower[s]); }
     m5d<R>(n4(psi), Ls, psi, psi, chi, lower, diag, upper, 1);
   }
   // LDU solve along s (CayleyFermion5Dcache.h:117-170), component by component.
+  // MooeeInvDag conjugates the swapped factors (CayleyFermion5Dcache.h:172-230)
+  static cplx<R> cf_at(const std::vector<C>& v, int s, int dag) { return cplx<R>(dag ? cj(v[s]) : v[s]); }
+  static cplx<R> inv_dee(const std::vector<C>& d, int s, int dag) {
+    const C x = C(1.0) / d[s];
+    return cplx<R>(dag ? cj(x) : x);
+  }
   void MooeeInv(const Field<R>& psi, Field<R>& chi) override { mooee_inv(psi, chi, 0); }
   void MooeeInvDag(const Field<R>& psi, Field<R>& chi) override { mooee_inv(psi, chi, 1); }
   void mooee_inv(const Field<R>& psi, Field<R>& chi, int dag) {
@@ -571,23 +604,23 @@ template <class R> struct Mobius : Op<R> {
         cplx<R> prev = 0, acc = 0;
         for (int s = 0; s < Ls - 1; s++) {
           cplx<R> r = psi[at(s)];
-          if (s > 0 && first) r -= R(lee[s - 1]) * prev;
-          if (!first) acc += R(leem[s]) * r;
+          if (s > 0 && first) r -= cf_at(lee, s - 1, dag) * prev;
+          if (!first) acc += cf_at(leem, s, dag) * r;
           chi[at(s)] = r;
           prev = r;
         }
         cplx<R> r = psi[at(Ls - 1)];
-        if (first) r -= R(lee[Ls - 2]) * prev;
+        if (first) r -= cf_at(lee, Ls - 2, dag) * prev;
         else r -= acc;
         // backward: chi_{Ls-1} = r / dee ; chi_s = chi_s/dee[s] - uee[s] P_second chi_{s+1}
         //                                               - ueem[s] P_first chi_{Ls-1}
-        r = R(1.0 / dee[Ls - 1]) * r;
+        r = inv_dee(dee, Ls - 1, dag) * r;
         chi[at(Ls - 1)] = r;
         cplx<R> last = r, nxt = r;
         for (int s = Ls - 2; s >= 0; s--) {
-          cplx<R> v = R(1.0 / dee[s]) * chi[at(s)];
-          if (!first) v -= R(uee[s]) * nxt;
-          else v -= R(ueem[s]) * last;
+          cplx<R> v = inv_dee(dee, s, dag) * chi[at(s)];
+          if (!first) v -= cf_at(uee, s, dag) * nxt;
+          else v -= cf_at(ueem, s, dag) * last;
           chi[at(s)] = v;
           nxt = v;
         }

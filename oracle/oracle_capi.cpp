@@ -66,15 +66,15 @@ template <class R> int apply(Op<R>* op, int kind, int opcode, const double* in, 
     case OP_MDAGM: op->MdagM(a, b); break;
     case OP_MEOOE5D:
     case OP_MEOOE_DAG5D: {
-      if (kind != 1) return 1;
-      auto* m = static_cast<Mobius<R>*>(op);
+      if (kind == 0) return 1;
+      auto* m = static_cast<CayleyBase<R>*>(op);
       if (opcode == OP_MEOOE5D) m->Meooe5D(a, b); else m->MeooeDag5D(a, b);
       break;
     }
     case OP_DMINUS:
     case OP_DMINUS_DAG: {
-      if (kind != 1) return 1;
-      static_cast<Mobius<R>*>(op)->Dminus(a, b, opcode == OP_DMINUS_DAG);
+      if (kind == 0) return 1;
+      static_cast<CayleyBase<R>*>(op)->Dminus(a, b, opcode == OP_DMINUS_DAG);
       break;
     }
     default: return 1;
@@ -85,7 +85,11 @@ template <class R> int apply(Op<R>* op, int kind, int opcode, const double* in, 
 
 template <class R> Op<R>* make(int kind, const int* dims, int L5, const double* par) {
   if (kind == 0) return new Wilson<R>(dims, L5, par[0]);
-  return new Mobius<R>(dims, L5, par[0], par[1], par[2], par[3]);
+  if (kind == 1) return new Mobius<R>(dims, L5, par[0], par[1], par[2], par[3]);
+  // ZMobius: par[4 + 2 s], par[5 + 2 s] = gamma_s
+  std::vector<cplx<double>> gamma(L5);
+  for (int s = 0; s < L5; s++) gamma[s] = cplx<double>(par[4 + 2 * s], par[5 + 2 * s]);
+  return new Mobius<R, cplx<double>>(dims, L5, par[0], par[1], par[2], par[3], gamma);
 }
 
 }  // namespace
@@ -107,7 +111,8 @@ int orc_max_threads(void) {
 #endif
 }
 
-// kind 0: Wilson, par = {mass}; kind 1: Moebius, par = {mf, M5, b, c}, L5 = Ls.
+// kind 0: Wilson, par = {mf}; kind 1: Moebius, par = {mf, M5, b, c}, L5 = Ls; kind 2:
+// ZMobius, par = {mf, M5, b, c, gamma_0 (re, im), ..., gamma_{Ls-1}}.
 // U: canonical gauge field; phases: 4 complex boundary phases.
 void* orc_create(int kind, int prec, const int* dims, int L5, const double* par, const double* U,
                  const double* phases) {
@@ -135,9 +140,9 @@ int orc_apply(void* p, int opcode, const double* in, double* out, int parity) {
 // (in = 5D, out = 4D).
 int orc_physical(void* p, int mode, const double* in, double* out) {
   Handle* h = static_cast<Handle*>(p);
-  if (h->kind != 1 || h->prec != 0) return 1;
-  auto* m = static_cast<Mobius<double>*>(h->d);
-  const size_t n5 = m->full_len(), n4 = n5 / size_t(m->Ls);
+  if (h->kind == 0 || h->prec != 0) return 1;
+  auto* m = static_cast<CayleyBase<double>*>(h->d);
+  const size_t n5 = m->full_len(), n4 = n5 / size_t(m->L5);
   Field<double> a = load<double>(in, mode < 2 ? n4 : n5), b;
   switch (mode) {
     case 0: m->ImportPhysicalSource(a, b); break;
@@ -317,8 +322,8 @@ int orc_deriv(void* p, int mderiv, const double* A, const double* B, int dag, in
   Op<double>* op = h->d;
   const size_t n = op->full_len();
   Field<double> a = load<double>(A, n), b = load<double>(B, n), t;
-  if (mderiv && h->kind == 1) {
-    auto* m = static_cast<Mobius<double>*>(op);
+  if (mderiv && h->kind != 0) {
+    auto* m = static_cast<CayleyBase<double>*>(op);
     if (!dag) { m->Meooe5D(b, t); b = t; }
     else { m->Meooe5D(a, t); a = t; }
   }

@@ -25,6 +25,21 @@ def _mobius(prec=0, Ls=6, mf=0.1, dims=DIMS, U=None, eps=0.5, seed=11):
     return o.OracleOp(1, prec, dims, Ls, [mf, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t()), U
 
 
+# the Ls = 10 omegas of Grid's tests/core/Test_zmobius_even_odd.cc:97-106 (b = 1, c = 0)
+ZOMEGA = [1.45806438985048, 1.18231318389348, 0.830951166685955, 0.542352409156791, 0.341985020453729,
+          0.21137902619029, 0.126074299502912, 0.0990136651962626, 0.0686324988446592 + 0.0550658530827402j,
+          0.0686324988446592 - 0.0550658530827402j]
+
+
+def zparams(mf, M5, b, c, gamma):
+    return [mf, M5, b, c] + [v for z in gamma for v in (complex(z).real, complex(z).imag)]
+
+
+def _zmobius(prec=0, mf=0.1, dims=DIMS, U=None, eps=0.5, seed=13, gamma=ZOMEGA, b=1.0, c=0.0):
+    U = g.random_gauge(dims, eps, seed) if U is None else U
+    return o.OracleOp(2, prec, dims, len(gamma), zparams(mf, MOBIUS["M5"], b, c, gamma), U, g.antiperiodic_t()), U
+
+
 def _wilson(prec=0, L5=1, mass=0.1, dims=DIMS, U=None, eps=0.3, seed=7):
     U = g.random_gauge(dims, eps, seed) if U is None else U
     return o.OracleOp(0, prec, dims, L5, [mass], U, g.antiperiodic_t()), U
@@ -76,9 +91,9 @@ def test_dhop_eo_oe_equals_dhop():
     assert o.rel_l2(both, full) < 1e-14
 
 
-@pytest.mark.parametrize("kind", ["mobius", "wilson"])
+@pytest.mark.parametrize("kind", ["mobius", "wilson", "zmobius"])
 def test_even_odd_decomposition_identities(kind):
-    op, U = _mobius() if kind == "mobius" else _wilson()
+    op, U = {"mobius": _mobius, "wilson": _wilson, "zmobius": _zmobius}[kind]()
     L5 = op.L5
     chi = fermion(VOL, L5, 41)
     phi = fermion(VOL, L5, 42)
@@ -299,3 +314,26 @@ def test_oracle_force_is_the_link_derivative(dag, kind):
         Ux = U.reshape(VOL, 4, 3, 3)[x0, mu]
         d_ana = np.trace(D @ Ux.conj().T @ F[x0, mu])
         assert abs(d_num - d_ana) < 1e-10 * abs(d_ana), (x0, mu)
+
+
+def test_zmobius_with_real_unit_omega_is_moebius():
+    """ZMobius with omega_s = 1 has the Moebius coefficients: every operator agrees."""
+    U = g.random_gauge(DIMS, 0.5, 3)
+    Ls, mf = 6, 0.05
+    mob, _ = _mobius(Ls=Ls, mf=mf, U=U)
+    zmob, _ = _zmobius(mf=mf, U=U, gamma=[1.0] * Ls, b=MOBIUS["b"], c=MOBIUS["c"])
+    x = fermion(VOL, Ls, 5)
+    xo = o.pick(DIMS, Ls, x, 1)
+    for code in (o.OP_M, o.OP_MDAG, o.OP_MDAGM, o.OP_DMINUS, o.OP_DMINUS_DAG):
+        assert o.rel_l2(zmob.apply(code, x), mob.apply(code, x)) < 1e-14, code
+    for code in (o.OP_MOOEE, o.OP_MOOEE_DAG, o.OP_MOOEE_INV, o.OP_MOOEE_INV_DAG, o.OP_MPC, o.OP_MPC_DAG,
+                 o.OP_MPCDAGMPC, o.OP_MEOOE5D, o.OP_MEOOE_DAG5D):
+        assert o.rel_l2(zmob.apply(code, xo, 1), mob.apply(code, xo, 1)) < 1e-14, code
+
+
+def test_zmobius_dminus_adjoint():
+    op, _ = _zmobius()
+    a, b = fermion(VOL, 10, 7), fermion(VOL, 10, 8)
+    lhs = np.vdot(a, op.apply(o.OP_DMINUS, b)).conj()
+    rhs = np.vdot(b, op.apply(o.OP_DMINUS_DAG, a))
+    assert abs(lhs - rhs) < 1e-12 * abs(lhs)
