@@ -520,6 +520,41 @@ template <class Impl> class MobiusFermion : public FermionOperator<Impl> {
               "ExportPhysicalFermionSource");
     exported4d.ImportHost(v);
   }
+
+ protected:
+  // for derived operators that create the library operator themselves
+  struct Deferred {};
+  MobiusFermion(Deferred, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
+                RealD b_, RealD c_)
+      : Base(&FiveDimGrid, &FiveDimRedBlackGrid, &FourDimGrid, &FourDimRedBlackGrid, mass),
+        Ls(FiveDimGrid.Ls), M5(M5_), b(b_), c(c_) {}
+};
+
+// ZMobiusFermion<Impl> (Grid/qcd/action/fermion/ZMobiusFermion.h:44-90): complex omega_s =
+// gamma[s], bs = (b + c) omega_s / 2 + (b - c) / 2, cs = (b + c) omega_s / 2 - (b - c) / 2
+// (FP64 and FP32 storage)
+template <class Impl> class ZMobiusFermion : public MobiusFermion<Impl> {
+  typedef MobiusFermion<Impl> Base;
+
+ public:
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  std::vector<ComplexD> omega;
+  ZMobiusFermion(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                 GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
+                 const std::vector<ComplexD>& gamma, RealD b_, RealD c_, const ImplParams& p = ImplParams())
+      : Base(typename Base::Deferred(), FiveDimGrid, FiveDimRedBlackGrid, FourDimGrid, FourDimRedBlackGrid, mass,
+             M5_, b_, c_),
+        omega(gamma) {
+    if (int(gamma.size()) != this->Ls) throw GridError(GB_ERR_BAD_ARG, "ZMobiusFermion: gamma.size() != Ls");
+    const std::vector<double> ph = FermionOperator<Impl>::phases(p);
+    gbdetail::check(gb_zmobius_create(FourDimGrid.dims4.data(), this->Ls, mass, M5_,
+                                      reinterpret_cast<const double*>(gamma.data()), b_, c_, ph.data(),
+                                      Impl::precision, 1, gbdetail::stream(), 0, &this->op_),
+                    "ZMobiusFermion");
+    this->ImportGauge(U);
+  }
 };
 
 typedef WilsonFermion<WilsonImplD> WilsonFermionD;
@@ -529,6 +564,13 @@ typedef MobiusFermion<WilsonImplD> MobiusFermionD;
 typedef MobiusFermion<WilsonImplF> MobiusFermionF;
 typedef MobiusFermion<WilsonImplH> MobiusFermionH;
 typedef MobiusFermionD MobiusFermionR;
+// Grid's ZWilsonImpl carries the complex Cayley coefficients in the action; here the
+// operator does, so the implementation tags are the Wilson ones
+typedef WilsonImplD ZWilsonImplD;
+typedef WilsonImplF ZWilsonImplF;
+typedef ZMobiusFermion<ZWilsonImplD> ZMobiusFermionD;
+typedef ZMobiusFermion<ZWilsonImplF> ZMobiusFermionF;
+typedef ZMobiusFermionD ZMobiusFermionR;
 
 // ---- linear operators (Grid/algorithms/LinearOperator.h:44-105,286-349) --------------
 template <class Field> class LinearOperatorBase {

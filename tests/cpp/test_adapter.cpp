@@ -2,7 +2,7 @@
 // tests/core/Test_mobius_even_odd.cc, the Schur red-black solve, the mixed-precision
 // reliable-update CG of tests/Test_dwf_mixedcg_prec.cc, the multishift CG, the unpreconditioned Wilson CG of
 // tests/solver/Test_wilson_cg_unprec.cc, a user-defined linear operator through the
-// host-driven CG, and the 4D <-> 5D surface fields.  Exit status 0 when every check holds.
+// host-driven CG, the 4D <-> 5D surface fields and the ZMobius even-odd identities.  Exit status 0 when every check holds.
 #include <cstdio>
 #include <cstdlib>
 
@@ -184,6 +184,35 @@ int main() {
   Ddwf.ExportPhysicalFermionSolution(prop5, prop4);
   expect(norm2(prop4) > 0 && SchurSolver.UnpreconditionedResidual < 1e-9, "physical propagator solve",
          SchurSolver.UnpreconditionedResidual);
+
+  // ---- ZMobius, complex omega (tests/core/Test_zmobius_even_odd.cc pattern) ----
+  const std::vector<ComplexD> omega = {1.45806438985048, 1.18231318389348, 0.830951166685955, 0.542352409156791,
+                                       0.341985020453729, 0.21137902619029,
+                                       ComplexD(0.0686324988446592, 0.0550658530827402),
+                                       ComplexD(0.0686324988446592, -0.0550658530827402)};
+  ZMobiusFermionD Dz(Umu, *FGrid, *FrbGrid, *UGrid, *UrbGrid, mass, M5, omega, 1.0, 0.0, params);
+  Dz.Meooe(src_e, r_o);
+  Dz.Meooe(src_o, r_e);
+  Dz.Mooee(src_e, t_e);
+  Dz.Mooee(src_o, t_o);
+  axpy(r_e, 1.0, t_e, r_e);
+  axpy(r_o, 1.0, t_o, r_o);
+  setCheckerboard(r_eo, r_e);
+  setCheckerboard(r_eo, r_o);
+  Dz.M(src, ref);
+  tmp = ref - r_eo;
+  expect(std::sqrt(norm2(tmp) / norm2(ref)) < 1e-13, "ZMobius Meooe + Mooee == M", std::sqrt(norm2(tmp) / norm2(ref)));
+  Dz.MooeeDag(src_o, t_o);
+  Dz.MooeeInvDag(t_o, r_o);
+  d_o = r_o - src_o;
+  expect(std::sqrt(norm2(d_o) / norm2(src_o)) < 1e-13, "ZMobius MooeeInvDag MooeeDag == 1",
+         std::sqrt(norm2(d_o) / norm2(src_o)));
+  sol = Zero();
+  SchurSolver(Dz, src, sol);
+  Dz.M(sol, tmp);
+  tmp = tmp - src;
+  expect(std::sqrt(norm2(tmp) / norm2(src)) < 1e-9, "ZMobius Schur solve |M x - b| / |b|",
+         std::sqrt(norm2(tmp) / norm2(src)));
 
   // ---- errors come back as exceptions ----
   bool threw = false;
