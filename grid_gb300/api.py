@@ -126,6 +126,11 @@ _proto("gb_host_free", [_vp])
 _proto("gb_stream_create", [C.POINTER(_vp)])
 _proto("gb_stream_destroy", [_vp])
 _proto("gb_Dminus", [_vp, _vp, _vp, _i])
+_proto("gb_insert_slice", [_vp, _vp, _i, _vp, _i])
+_proto("gb_extract_slice", [_vp, _vp, _i, _vp, _i])
+_proto("gb_P", [_vp, _vp, _vp, _i])
+_proto("gb_op_set_mass", [_vp, _d])
+_proto("gb_op_mass", [_vp, _dp])
 for _n in ("gb_import_physical_source", "gb_import_unphysical_fermion"):
     _proto(_n, [_vp, _vp, _i, _vp])
 for _n in ("gb_export_physical_solution", "gb_export_physical_source"):
@@ -317,6 +322,30 @@ def axpy_norm(z: FermionField, a: float, x: FermionField, y: FermionField):
     return out
 
 
+def InsertSlice(low, high: FermionField, slice_: int, orthog: int = 0):
+    """InsertSlice(lowDim, higherDim, slice, 0) (Lattice_transfer.h:999-1070) along the
+    fifth dimension: the 4D field `low` (canonical complex array, [site][spin][colour]
+    per right-hand side) becomes slice s of the full 5D field `high`."""
+    if orthog != 0:
+        raise GridError(8, "InsertSlice: only the fifth dimension (orthog = 0) is supported")
+    a = np.ascontiguousarray(low, dtype=np.complex128).reshape(-1)
+    op = high.op
+    if a.size != op.vol4 * 12 * op.nrhs:
+        raise GridError(1, "4D field has the wrong size")
+    _check(lib.gb_insert_slice(op.h, a.ctypes.data, 0, high.h, int(slice_)))
+
+
+def ExtractSlice(high: FermionField, slice_: int, orthog: int = 0):
+    """ExtractSlice(lowDim, higherDim, slice, 0): slice s of a full 5D field as a 4D
+    canonical complex array."""
+    if orthog != 0:
+        raise GridError(8, "ExtractSlice: only the fifth dimension (orthog = 0) is supported")
+    op = high.op
+    out = np.empty(op.vol4 * 12 * op.nrhs, dtype=np.complex128)
+    _check(lib.gb_extract_slice(op.h, high.h, int(slice_), out.ctypes.data, 0))
+    return out
+
+
 def pickCheckerboard(cb: int, half: FermionField, full: FermionField):
     half.checkerboard = cb
     _check(lib.gb_field_pick_checkerboard(half.h, full.h))
@@ -365,6 +394,12 @@ class _FermionOperator:
 
     def Mass(self):
         return self.mass
+
+    def SetMass(self, mass):
+        """CayleyFermion5D::SetMass (CayleyFermion5D.h:75-78): rebuilds the Cayley
+        coefficients; WilsonFermion: the mass term of M."""
+        _check(lib.gb_op_set_mass(self.h, float(mass)))
+        self.mass = float(mass)
 
     # FermionOperator interface
     def M(self, i, o): _check(lib.gb_M(self.h, i.h, o.h))
@@ -471,6 +506,10 @@ class MobiusFermion(_FermionOperator):
         out = np.empty(self.vol4 * 12 * self.nrhs, dtype=np.complex128)
         _check(fn(self.h, in5d.h, out.ctypes.data, 0))
         return out
+
+    # MADWF support (CayleyFermion5DImplementation.h:70-88)
+    def P(self, i, o): _check(lib.gb_P(self.h, i.h, o.h, 0))
+    def Pdag(self, i, o): _check(lib.gb_P(self.h, i.h, o.h, 1))
 
     def ImportPhysicalFermionSource(self, src4d, out5d):
         self._surface_in(lib.gb_import_physical_source, src4d, out5d)
@@ -695,6 +734,124 @@ class SchurRedBlackDiagMooeeSolve:
             s.IterationsToCleanup = r.cleanup_iterations
         self.unprec_residual = res
         return r
+
+
+class ZeroGuesser:
+    """ZeroGuesser (Grid/algorithms/iterative/Guesser.h): a zero initial guess, which is
+    what the Schur solve starts from."""
+
+    def __call__(self, src, guess):
+        guess.zero()
+
+
+class PauliVillarsSolverUnprec:
+    """PauliVillarsSolverUnprec(CG) (PauliVillarsInverters.h:32-52): solves M(m = 1) sol = src
+    by CG on Mdag M at mass 1, restoring the operator's mass after."""
+
+    def __init__(self, cg: ConjugateGradient):
+        self.CG = cg
+
+    def __call__(self, matrix, src, sol):
+        m = matrix.Mass()
+        A = matrix.FermionField()
+        matrix.SetMass(1.0)
+        try:
+            matrix.Mdag(src, A)
+            self.CG(MdagMLinearOperator(matrix), A, sol)
+        finally:
+            matrix.SetMass(m)
+
+
+class PauliVillarsSolverRBprec:
+    """PauliVillarsSolverRBprec(SchurSolver) (PauliVillarsInverters.h:54-72): the
+    red-black Schur solve at mass 1."""
+
+    def __init__(self, schur: "SchurRedBlackDiagMooeeSolve"):
+        self.SchurSolver = schur
+
+    def __call__(self, matrix, src, sol):
+        m = matrix.Mass()
+        matrix.SetMass(1.0)
+        try:
+            self.SchurSolver(matrix, src, sol)
+        finally:
+            matrix.SetMass(m)
+
+
+class MADWFinnerIterCallbackBase:
+    """Called with the outer residual at the end of every MADWF iteration."""
+
+    def __call__(self, current_resid: float):
+        pass
+
+
+class MADWF:
+    """MADWF(Mato, Mati, PauliVillarsSolvero, SchurSolveri, Guesseri, resid, maxiter,
+    callback) (Grid/qcd/action/fermion/MADWF.h:47-209): solves the outer (Moebius) system
+    by defect correction, each step a Pauli-Villars solve of the outer operator and a Schur
+    solve of the cheaper inner (e.g. ZMobius with smaller Ls) operator joined through the
+    s = 0 slice of the P-rotated fields.  `src` is a 4D field (canonical complex array,
+    imported with ImportPhysicalFermionSource) or a full 5D field of the outer operator;
+    `sol5` receives the outer 5D solution.  Raises GridError (status NOT_CONVERGED) after
+    maxiter steps, where Grid asserts."""
+
+    def __init__(self, Mato, Mati, PauliVillarsSolvero, SchurSolveri, Guesseri, resid, maxiter, callback=None):
+        self.Mato, self.Mati = Mato, Mati
+        self.PauliVillarsSolvero, self.SchurSolveri, self.Guesseri = PauliVillarsSolvero, SchurSolveri, Guesseri
+        self.target_resid, self.maxiter, self.callback = float(resid), int(maxiter), callback
+        self.iterations = 0
+        self.residuals = []
+
+    def __call__(self, src, sol5):
+        Mo, Mi = self.Mato, self.Mati
+        A, B, b, c, defect = (Mo.FermionField() for _ in range(5))
+        ci, yi, xi, srci, Ai = (Mi.FermionField() for _ in range(5))
+        m = Mi.Mass()
+        if isinstance(src, FermionField):
+            b.copy_from(src)
+        else:
+            Mo.ImportPhysicalFermionSource(src, b)
+        nb = float(np.sum(b.norm2()))
+        defect.copy_from(b)
+        sol5.zero()
+        self.residuals = []
+        for i in range(self.maxiter):
+            # c0 from the current defect: the s = 0 slice of Pdag PV^-1 defect
+            self.PauliVillarsSolvero(Mo, defect, A)
+            Mo.Pdag(A, c)
+            c0 = ExtractSlice(c, 0)
+            # the inner system with surface term c0: Dwm P y = D(1) P (c0, 0, ..., 0)^T
+            ci.zero()
+            InsertSlice(c0, ci, 0)
+            Mi.P(ci, Ai)
+            Mi.SetMass(1.0)
+            try:
+                Mi.M(Ai, srci)
+            finally:
+                Mi.SetMass(m)
+            self.Guesseri(srci, xi)
+            self.SchurSolveri(Mi, srci, xi)
+            Mi.Pdag(xi, yi)
+            y0 = ExtractSlice(yi, 0)
+            # the bulk of the outer solution: Pdag PV^-1 Dm P (-y0, c_1, ..., c_{Ls-1})
+            InsertSlice(-y0, c, 0)
+            Mo.P(c, B)
+            Mo.M(B, A)
+            self.PauliVillarsSolvero(Mo, A, B)
+            Mo.Pdag(B, A)
+            InsertSlice(y0, A, 0)  # the surface solution back in
+            Mo.P(A, B)
+            axpy(sol5, 1.0, B, sol5)  # sol5 += M^-1 defect
+            Mo.M(sol5, A)
+            axpby(defect, 1.0, -1.0, b, A)  # defect = b - M sol5
+            resid = float(np.sqrt(np.sum(defect.norm2()) / nb))
+            self.residuals.append(resid)
+            self.iterations = i + 1
+            if self.callback is not None:
+                self.callback(resid)
+            if resid < self.target_resid:
+                return
+        raise GridError(5, f"MADWF: not converged in {self.maxiter} iterations (residual {self.residuals[-1]:.3e})")
 
 
 # ---- propagator-solve service ---------------------------------------------------------

@@ -40,6 +40,11 @@ static int check_op(const Op* op) {
   if (!op->gauge_loaded) { set_error("operator has no gauge field: call gb_op_import_gauge"); return GB_ERR_BAD_ARG; }
   return GB_OK;
 }
+// for calls that use only the geometry (and coefficients) of the operator, not its links
+static int check_op_geometry(const Op* op) {
+  if (!op) { set_error("null operator"); return GB_ERR_BAD_ARG; }
+  return GB_OK;
+}
 static int check_conf(const Field* a, const Field* b) {
   if (!a || !b) { set_error("null field"); return GB_ERR_BAD_ARG; }
   if (!ops_conformable(a->op, b->op) || a->n5 != b->n5) { set_error("fields are not conformable"); return GB_ERR_BAD_ARG; }
@@ -1075,6 +1080,79 @@ int gb_export_physical_solution(gb_op_t op, gb_field_t sol5d, double* out4d, int
 }
 int gb_export_physical_source(gb_op_t op, gb_field_t src5d, double* out4d, int on_device) {
   return export_surface(op, src5d, out4d, on_device, 0);
+}
+
+// InsertSlice / ExtractSlice along the fifth dimension (Lattice_transfer.h:999-1070)
+static int slice_checks(gb_op_t op, gb_field_t f, const double* p4, int s) {
+  GB_TRY(check_op_geometry(op));
+  if (!f || !p4) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (!ops_conformable(f->op, op)) { set_error("field is not conformable to the operator"); return GB_ERR_BAD_ARG; }
+  if (!f->full()) { set_error("slices: a full 5D field expected"); return GB_ERR_BAD_PARITY; }
+  if (s < 0 || s >= op->Ls) { set_error("slice %d outside [0, %d)", s, op->Ls); return GB_ERR_BAD_ARG; }
+  return GB_OK;
+}
+int gb_insert_slice(gb_op_t op, const double* src4d, int on_device, gb_field_t f5d, int s) {
+  GB_TRY(slice_checks(op, f5d, src4d, s));
+  const double* d = src4d;
+  if (!on_device) {
+    GB_TRY(ensure_stage(op, surface_bytes(op)));
+    GB_CHECK_CUDA(cudaMemcpyAsync(op->d_stage, src4d, surface_bytes(op), cudaMemcpyHostToDevice, op->stream));
+    d = op->d_stage;
+  }
+  GB_TRY(launch_slice(op, const_cast<double*>(d), half_view(f5d, 0), half_view(f5d, 1), s, 1));
+  if (!on_device) GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  return GB_OK;
+}
+int gb_extract_slice(gb_op_t op, gb_field_t f5d, int s, double* out4d, int on_device) {
+  GB_TRY(slice_checks(op, f5d, out4d, s));
+  double* d = out4d;
+  if (!on_device) {
+    GB_TRY(ensure_stage(op, surface_bytes(op)));
+    d = op->d_stage;
+  }
+  GB_TRY(launch_slice(op, d, half_view(f5d, 0), half_view(f5d, 1), s, 0));
+  if (!on_device) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(out4d, d, surface_bytes(op), cudaMemcpyDeviceToHost, op->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  }
+  return GB_OK;
+}
+
+// CayleyFermion5D::P / Pdag (CayleyFermion5DImplementation.h:70-88)
+int gb_P(gb_op_t op, gb_field_t in, gb_field_t out, int dag) {
+  GB_TRY(check_op_geometry(op));
+  if (!in || !out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (op->kind != 1) { set_error("P: Moebius operators only"); return GB_ERR_UNSUPPORTED; }
+  if (in == out || in->data == out->data) { set_error("P: in and out must be distinct fields"); return GB_ERR_BAD_ARG; }
+  GB_TRY(check_conf(in, out));
+  if (!ops_conformable(in->op, op)) { set_error("field is not conformable to the operator"); return GB_ERR_BAD_ARG; }
+  if (in->subset != out->subset) { set_error("P: in and out on different checkerboards"); return GB_ERR_BAD_PARITY; }
+  if (in->full()) {
+    for (int p = 0; p < 2; p++) GB_TRY(launch_chiral_shift(op, half_view(in, p), half_view(out, p), dag));
+  } else {
+    GB_TRY(launch_chiral_shift(op, half_view(in, in->subset), half_view(out, out->subset), dag));
+  }
+  return GB_OK;
+}
+
+// CayleyFermion5D::SetMass / Mass (CayleyFermion5D.h:71-83): the Cayley coefficients are
+// rebuilt on the host; kernels take them by value at each launch, so the change applies to
+// every operator call issued after this one
+int gb_op_set_mass(gb_op_t op, double mass) {
+  GB_TRY(check_op_geometry(op));
+  op->mass = mass;
+  op->diag_mass = 4.0 + mass;
+  if (op->kind == 1) {
+    if (op->zmobius) zcayley_setup(op);
+    else cayley_setup(op);
+  }
+  return GB_OK;
+}
+int gb_op_mass(gb_op_t op, double* mass) {
+  GB_TRY(check_op_geometry(op));
+  if (!mass) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  *mass = op->mass;
+  return GB_OK;
 }
 
 }  // extern "C"

@@ -539,17 +539,23 @@ int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon
 }
 
 // ---------------------------------------------------------------------------------------
-// 4D <-> 5D surface fields of a Moebius operator (CayleyFermion5DImplementation.h:57-129).
-// One thread per (rhs, 4D site) of a canonical 4D field c4[rhs][site][12].  INSERT writes
-// spins 0,1 (P+) of the 4D spinor at s = 0 and spins 2,3 (P-) at s = Ls-1, zeros in the
-// other halves of those two sites, and leaves every other s untouched (the caller zeroes
-// the field first).  EXTRACT reads the 4D spinor back: with `solution` spins 0,1 come from
-// s = Ls-1 and spins 2,3 from s = 0 (ExportPhysicalFermionSolution), otherwise the
-// reverse (ExportPhysicalFermionSource).
+// 4D <-> 5D surface fields of a Moebius operator (CayleyFermion5DImplementation.h:57-129)
+// and 4D slices of a 5D field (InsertSlice / ExtractSlice along the fifth dimension,
+// Grid/lattice/Lattice_transfer.h:999-1070).  One thread per (rhs, 4D site) of a canonical
+// 4D field c4[rhs][site][12].
+//   SURF_INSERT   spins 0,1 (P+) of the 4D spinor at s = 0 and spins 2,3 (P-) at s = Ls-1,
+//                 zeros in the other halves of those two sites; every other s untouched
+//                 (the caller zeroes the field first)
+//   SURF_EXTRACT  the 4D spinor back: with arg != 0 spins 0,1 come from s = Ls-1 and spins
+//                 2,3 from s = 0 (ExportPhysicalFermionSolution), otherwise the reverse
+//                 (ExportPhysicalFermionSource)
+//   SLICE_INSERT / SLICE_EXTRACT  the whole spinor at s = arg
 // ---------------------------------------------------------------------------------------
-template <class T, bool INSERT>
+enum { SURF_INSERT = 0, SURF_EXTRACT = 1, SLICE_INSERT = 2, SLICE_EXTRACT = 3 };
+
+template <class T, int MODE>
 __global__ void __launch_bounds__(256) surface_kernel(const GeoParams g, double* c4, void* even, float* even_n,
-                                                      void* odd, float* odd_n, int solution) {
+                                                      void* odd, float* odd_n, int arg) {
   using R = typename Arith<T>::type;
   const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= size_t(g.vol4) * g.nrhs_user) return;
@@ -568,7 +574,7 @@ __global__ void __launch_bounds__(256) surface_kernel(const GeoParams g, double*
   const size_t i1 = i0 + g.Ls - 1;                                   // s = Ls-1
   double2* c = reinterpret_cast<double2*>(c4) + (size_t(rhs) * g.vol4 + site) * 12;
   Spinor<R> a, b;
-  if (INSERT) {
+  if (MODE == SURF_INSERT) {
 #pragma unroll
     for (int k = 0; k < 12; k++) {
       const double2 v = c[k];
@@ -578,34 +584,86 @@ __global__ void __launch_bounds__(256) surface_kernel(const GeoParams g, double*
     }
     SpinorIO<T>::store(base, nrm, n5, i0, a);
     SpinorIO<T>::store(base, nrm, n5, i1, b);
-  } else {
+  } else if (MODE == SURF_EXTRACT) {
     SpinorIO<T>::load(base, nrm, n5, i0, a);
     SpinorIO<T>::load(base, nrm, n5, i1, b);
 #pragma unroll
     for (int k = 0; k < 12; k++) {
-      const bool from_last = (k < 6) == (solution != 0);
+      const bool from_last = (k < 6) == (arg != 0);
       c[k] = from_last ? make_double2(double(b.re[k]), double(b.im[k])) : make_double2(double(a.re[k]), double(a.im[k]));
     }
+  } else if (MODE == SLICE_INSERT) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const double2 v = c[k];
+      a.re[k] = R(v.x); a.im[k] = R(v.y);
+    }
+    SpinorIO<T>::store(base, nrm, n5, i0 + arg, a);
+  } else {
+    SpinorIO<T>::load(base, nrm, n5, i0 + arg, a);
+#pragma unroll
+    for (int k = 0; k < 12; k++) c[k] = make_double2(double(a.re[k]), double(a.im[k]));
   }
 }
 
-template <bool INSERT>
-static int surface_p(Op* op, double* c4, HalfView even, HalfView odd, int solution) {
+template <int MODE>
+static int surface_p(Op* op, double* c4, HalfView even, HalfView odd, int arg) {
   const GeoParams g = geo(op);
   const size_t n = size_t(op->vol4) * op->nrhs_user;
   switch (even.prec) {
-    case GB_F64: surface_kernel<double, INSERT><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, solution); break;
-    case GB_F32: surface_kernel<float, INSERT><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, solution); break;
-    case GB_F16: surface_kernel<__half, INSERT><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, solution); break;
+    case GB_F64: surface_kernel<double, MODE><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, arg); break;
+    case GB_F32: surface_kernel<float, MODE><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, arg); break;
+    case GB_F16: surface_kernel<__half, MODE><<<nblk(n), 256, 0, op->stream>>>(g, c4, even.data, even.norms, odd.data, odd.norms, arg); break;
   }
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
 int launch_surface_insert(Op* op, const double* c4, HalfView even, HalfView odd) {
-  return surface_p<true>(op, const_cast<double*>(c4), even, odd, 0);
+  return surface_p<SURF_INSERT>(op, const_cast<double*>(c4), even, odd, 0);
 }
 int launch_surface_extract(Op* op, HalfView even, HalfView odd, double* c4, int solution) {
-  return surface_p<false>(op, c4, even, odd, solution);
+  return surface_p<SURF_EXTRACT>(op, c4, even, odd, solution);
+}
+int launch_slice(Op* op, double* c4, HalfView even, HalfView odd, int s, int insert) {
+  if (s < 0 || s >= op->Ls) { set_error("slice %d outside [0, %d)", s, op->Ls); return GB_ERR_BAD_ARG; }
+  return insert ? surface_p<SLICE_INSERT>(op, c4, even, odd, s) : surface_p<SLICE_EXTRACT>(op, c4, even, odd, s);
+}
+
+// ---------------------------------------------------------------------------------------
+// CayleyFermion5D::P / Pdag (CayleyFermion5DImplementation.h:70-88): chi_s = P- psi_s +
+// P+ psi_{s+1} (P) or P+ psi_{s-1} (Pdag), s cyclic within each right-hand side's block of
+// Ls.  One thread per output 5D site of one checkerboard half; in and out are distinct.
+// ---------------------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) chiral_shift_kernel(const GeoParams g, const void* in, const float* in_n,
+                                                           void* out, float* out_n, int dag) {
+  using R = typename Arith<T>::type;
+  const size_t n5 = size_t(g.half4) * g.L5;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  const int s5 = int(i % g.L5);
+  const int s = s5 % g.Ls;
+  const int sp = dag ? (s + g.Ls - 1) % g.Ls : (s + 1) % g.Ls;
+  const size_t j = i - s + sp;
+  Spinor<R> a, b;
+  SpinorIO<T>::load(in, in_n, n5, i, a);
+  SpinorIO<T>::load(in, in_n, n5, j, b);
+#pragma unroll
+  for (int k = 0; k < 6; k++) { a.re[k] = b.re[k]; a.im[k] = b.im[k]; }
+  SpinorIO<T>::store(out, out_n, n5, i, a);
+}
+
+int launch_chiral_shift(Op* op, HalfView in, HalfView out, int dag) {
+  if (in.prec != out.prec) { set_error("P: mixed field precisions"); return GB_ERR_BAD_ARG; }
+  const GeoParams g = geo(op);
+  const size_t n = op->n5();
+  switch (in.prec) {
+    case GB_F64: chiral_shift_kernel<double><<<nblk(n), 256, 0, op->stream>>>(g, in.data, in.norms, out.data, out.norms, dag); break;
+    case GB_F32: chiral_shift_kernel<float><<<nblk(n), 256, 0, op->stream>>>(g, in.data, in.norms, out.data, out.norms, dag); break;
+    case GB_F16: chiral_shift_kernel<__half><<<nblk(n), 256, 0, op->stream>>>(g, in.data, in.norms, out.data, out.norms, dag); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
 }
 
 // ---------------------------------------------------------------------------------------

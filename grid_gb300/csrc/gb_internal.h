@@ -213,6 +213,10 @@ int launch_double_store(Op* op, const double* U_canon, int parity);
 // 4D <-> 5D surface fields (Moebius): canonical FP64 4D field in device memory
 int launch_surface_insert(Op* op, const double* c4, HalfView even, HalfView odd);
 int launch_surface_extract(Op* op, HalfView even, HalfView odd, double* c4, int solution);
+// 4D slice s of a full 5D field <-> canonical 4D field (device)
+int launch_slice(Op* op, double* c4, HalfView even, HalfView odd, int s, int insert);
+// CayleyFermion5D::P (dag = 0) / Pdag (dag = 1) on one checkerboard half
+int launch_chiral_shift(Op* op, HalfView in, HalfView out, int dag);
 int build_neighbours(Op* op);
 
 // CG kernels (gb_blas.cu)

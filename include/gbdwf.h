@@ -189,6 +189,23 @@ int gb_import_unphysical_fermion(gb_op_t op, const double* src4d, int on_device,
 int gb_export_physical_solution(gb_op_t op, gb_field_t sol5d, double* out4d, int on_device);
 int gb_export_physical_source(gb_op_t op, gb_field_t src5d, double* out4d, int on_device);
 
+/* InsertSlice(lowDim, higherDim, s, 0) / ExtractSlice(lowDim, higherDim, s, 0)
+ * (Grid/lattice/Lattice_transfer.h:999-1070) along the fifth dimension: the whole 4D
+ * spinor field at slice s (0 <= s < Ls) of a full 5D field; 4D layout as for the surface
+ * functions above.  Insert leaves every other slice untouched. */
+int gb_insert_slice(gb_op_t op, const double* src4d, int on_device, gb_field_t f5d, int s);
+int gb_extract_slice(gb_op_t op, gb_field_t f5d, int s, double* out4d, int on_device);
+
+/* CayleyFermion5D::P / Pdag (CayleyFermion5DImplementation.h:70-88), the chiral
+ * permutation of the MADWF method: chi_s = P- psi_s + P+ psi_{s+1} (dag = 0) or
+ * P+ psi_{s-1} (dag = 1), s cyclic.  Full or half fields; in and out distinct. */
+int gb_P(gb_op_t op, gb_field_t in, gb_field_t out, int dag);
+
+/* CayleyFermion5D::SetMass / Mass (CayleyFermion5D.h:71-83); WilsonFermion's mass for
+ * Wilson operators.  The Cayley coefficients are rebuilt at once; later calls use them. */
+int gb_op_set_mass(gb_op_t op, double mass);
+int gb_op_mass(gb_op_t op, double* mass);
+
 /* ---- solvers ------------------------------------------------------------------- */
 typedef struct {
   double tolerance;      /* ConjugateGradient::Tolerance                                  */

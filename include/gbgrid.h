@@ -3,9 +3,10 @@
  * Code written against Grid's fermion-operator path compiles against these classes
  * unchanged for that path: grids from SpaceTimeGrid, LatticeFermion / LatticeGaugeField,
  * WilsonFermion / MobiusFermion (FermionOperator interface), MdagMLinearOperator,
- * SchurDiagMooeeOperator, ConjugateGradient, ConjugateGradientReliableUpdate and
- * SchurRedBlackDiagMooeeSolve, plus norm2 / innerProduct / axpy / axpby / axpy_norm /
- * pickCheckerboard / setCheckerboard / precisionChange.  Every call forwards to the C ABI;
+ * SchurDiagMooeeOperator, ConjugateGradient, ConjugateGradientReliableUpdate,
+ * ConjugateGradientMultiShift, SchurRedBlackDiagMooeeSolve, ZMobiusFermion, MADWF with the
+ * Pauli-Villars solvers, plus norm2 / innerProduct / axpy / axpby / axpy_norm /
+ * pickCheckerboard / setCheckerboard / precisionChange / InsertSlice / ExtractSlice.  Every call forwards to the C ABI;
  * the fields live in device memory.  Reference interfaces:
  *   Grid/qcd/action/fermion/FermionOperator.h:40-192, MobiusFermion.h:45-56,
  *   WilsonFermion.h:139-142, Grid/algorithms/LinearOperator.h:44-105,286-349,590-616,
@@ -36,6 +37,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -313,6 +315,35 @@ template <class v> Lattice<v> operator*(RealD s, const Lattice<v>& a) {
   axpby(r, s, 0.0, a, a);
   return r;
 }
+template <class v> Lattice<v> operator-(const Lattice<v>& a) { return -1.0 * a; }
+
+// InsertSlice / ExtractSlice along the fifth dimension (Grid/lattice/Lattice_transfer.h:
+// 999-1070; orthog = 0 is s on Grid's 5D grids): lowDim on a full 4D grid, higherDim on a
+// full 5D grid with the same 4D extents
+namespace gbdetail {
+inline void check_slice_grids(const GridBase* low, const GridBase* high, int orthog, const char* what) {
+  if (orthog != 0) throw GridError(GB_ERR_UNSUPPORTED, std::string(what) + ": only orthog = 0 (the fifth dimension)");
+  if (low->Ls != 1 || low->_isCheckerBoarded || high->Ls < 2 || high->_isCheckerBoarded || low->dims4 != high->dims4)
+    throw GridError(GB_ERR_BAD_ARG, std::string(what) + ": a full 4D and a full 5D field of the same extents expected");
+}
+}  // namespace gbdetail
+template <class v> void InsertSlice(const Lattice<v>& lowDim, Lattice<v>& higherDim, int slice, int orthog) {
+  gbdetail::check_slice_grids(lowDim.Grid(), higherDim.Grid(), orthog, "InsertSlice");
+  const std::vector<ComplexD> h = lowDim.ExportHost();
+  gbdetail::check(gb_insert_slice(higherDim.Grid()->context(), reinterpret_cast<const double*>(h.data()), 0,
+                                  higherDim.handle(), slice),
+                  "InsertSlice");
+}
+template <class v> void ExtractSlice(Lattice<v>& lowDim, const Lattice<v>& higherDim, int slice, int orthog) {
+  gbdetail::check_slice_grids(lowDim.Grid(), higherDim.Grid(), orthog, "ExtractSlice");
+  std::vector<ComplexD> h(lowDim.HostSize());
+  gbdetail::check(gb_extract_slice(higherDim.Grid()->context(), higherDim.handle(), slice,
+                                   reinterpret_cast<double*>(h.data()), 0),
+                  "ExtractSlice");
+  lowDim.ImportHost(h);
+}
+// MADWF.h:33-42: a copy that changes precision when the field types differ
+template <class vi, class vo> void convert(const Lattice<vi>& from, Lattice<vo>& to) { precisionChange(to, from); }
 
 // ---- seeded synthetic inputs (GridParallelRNG + gaussian + SU3 configurations) --------
 class GridParallelRNG {
@@ -491,6 +522,15 @@ template <class Impl> class MobiusFermion : public FermionOperator<Impl> {
   }
   void Dminus(const FermionField& in, FermionField& out) {
     Base::run(gb_Dminus(this->op_, in.handle(), out.handle(), 0), "Dminus");
+  }
+  // MADWF support (CayleyFermion5D.h:71-85, CayleyFermion5DImplementation.h:70-88)
+  void SetMass(RealD mass) {
+    Base::run(gb_op_set_mass(this->op_, mass), "SetMass");
+    this->mass_ = mass;
+  }
+  void P(const FermionField& psi, FermionField& chi) { Base::run(gb_P(this->op_, psi.handle(), chi.handle(), 0), "P"); }
+  void Pdag(const FermionField& psi, FermionField& chi) {
+    Base::run(gb_P(this->op_, psi.handle(), chi.handle(), 1), "Pdag");
   }
   void DminusDag(const FermionField& in, FermionField& out) {
     Base::run(gb_Dminus(this->op_, in.handle(), out.handle(), 1), "DminusDag");
@@ -829,6 +869,12 @@ template <class Field> class SchurRedBlackDiagMooeeSolve {
   explicit SchurRedBlackDiagMooeeSolve(OperatorFunction<Field>& HermitianRBSolver, bool = false, bool = false)
       : solver_(HermitianRBSolver) {}
   template <class Matrix> void operator()(Matrix& _Matrix, const Field& in, Field& out) { solve(_Matrix, nullptr, in, out); }
+  // with an initial-guess functor (SchurRedBlack.h:189-233); the library solve starts from
+  // zero, so only ZeroGuesser is accepted
+  template <class Matrix, class Guesser, typename std::enable_if<Guesser::is_zero_guesser, int>::type = 0>
+  void operator()(Matrix& _Matrix, const Field& in, Field& out, Guesser&) {
+    solve(_Matrix, nullptr, in, out);
+  }
   template <class Matrix, class MatrixLo>
   void operator()(Matrix& _Matrix, MatrixLo& lower_precision, const Field& in, Field& out) {
     solve(_Matrix, lower_precision.handle(), in, out);
@@ -846,6 +892,137 @@ template <class Field> class SchurRedBlackDiagMooeeSolve {
     TrueResidual = cg->TrueResidual = r.true_residual;
     UnpreconditionedResidual = unprec;
     gbdetail::check(rc, "SchurRedBlackDiagMooeeSolve");
+  }
+};
+
+// ---- MADWF (Grid/qcd/action/fermion/MADWF.h, PauliVillarsInverters.h) ----------------
+// ZeroGuesser (Grid/algorithms/iterative/Guesser.h)
+template <class Field> struct ZeroGuesser {
+  static constexpr bool is_zero_guesser = true;
+  void operator()(const Field&, Field& guess) { guess = Zero(); }
+};
+
+// PauliVillarsSolverUnprec (PauliVillarsInverters.h:32-52): M(1) sol = src by CG on Mdag M
+template <class Field> class PauliVillarsSolverUnprec {
+ public:
+  ConjugateGradient<Field>& CG;
+  explicit PauliVillarsSolverUnprec(ConjugateGradient<Field>& cg) : CG(cg) {}
+  template <class Matrix> void operator()(Matrix& _Matrix, const Field& src, Field& sol) {
+    const RealD m = _Matrix.Mass();
+    Field A(_Matrix.FermionGrid());
+    MdagMLinearOperator<Matrix, Field> HermOp(_Matrix);
+    _Matrix.SetMass(1.0);
+    try {
+      _Matrix.Mdag(src, A);
+      CG(HermOp, A, sol);
+    } catch (...) {
+      _Matrix.SetMass(m);
+      throw;
+    }
+    _Matrix.SetMass(m);
+  }
+};
+
+// PauliVillarsSolverRBprec (PauliVillarsInverters.h:54-72): the Schur solve at mass 1
+template <class Field, class SchurSolverType> class PauliVillarsSolverRBprec {
+ public:
+  SchurSolverType& SchurSolver;
+  explicit PauliVillarsSolverRBprec(SchurSolverType& s) : SchurSolver(s) {}
+  template <class Matrix> void operator()(Matrix& _Matrix, const Field& src, Field& sol) {
+    const RealD m = _Matrix.Mass();
+    _Matrix.SetMass(1.0);
+    try {
+      SchurSolver(_Matrix, src, sol);
+    } catch (...) {
+      _Matrix.SetMass(m);
+      throw;
+    }
+    _Matrix.SetMass(m);
+  }
+};
+
+struct MADWFinnerIterCallbackBase {
+  virtual void operator()(const RealD) {}
+  virtual ~MADWFinnerIterCallbackBase() {}
+};
+
+// MADWF (MADWF.h:47-209): the outer (Moebius) system solved by defect correction; each step
+// is a Pauli-Villars solve of the outer operator and a Schur solve of the cheaper inner one,
+// joined through the s = 0 slice of the P-rotated fields.  src is a 4D field (imported with
+// ImportPhysicalFermionSource) or a 5D field of the outer operator.  Throws GridError
+// (GB_ERR_NOT_CONVERGED) after maxiter steps, where Grid asserts.
+template <class Matrixo, class Matrixi, class PVinverter, class SchurSolver, class Guesser> class MADWF {
+  typedef typename Matrixo::FermionField FermionFieldo;
+  typedef typename Matrixi::FermionField FermionFieldi;
+  Matrixo& Mato;
+  Matrixi& Mati;
+  PVinverter& PauliVillarsSolvero;
+  SchurSolver& SchurSolveri;
+  Guesser& Guesseri;
+  RealD target_resid;
+  int maxiter;
+  MADWFinnerIterCallbackBase* callback;
+
+ public:
+  int IterationsToComplete = 0;
+  RealD FinalResidual = 0;
+  MADWF(Matrixo& _Mato, Matrixi& _Mati, PVinverter& _PV, SchurSolver& _SchurSolveri, Guesser& _Guesseri, RealD resid,
+        int _maxiter, MADWFinnerIterCallbackBase* _callback = nullptr)
+      : Mato(_Mato), Mati(_Mati), PauliVillarsSolvero(_PV), SchurSolveri(_SchurSolveri), Guesseri(_Guesseri),
+        target_resid(resid), maxiter(_maxiter), callback(_callback) {}
+
+  void operator()(const FermionFieldo& src, FermionFieldo& sol5) {
+    FermionFieldi c0i(Mati.GaugeGrid()), y0i(Mati.GaugeGrid());
+    FermionFieldo c0(Mato.GaugeGrid()), y0(Mato.GaugeGrid());
+    FermionFieldo A(Mato.FermionGrid()), B(Mato.FermionGrid()), b(Mato.FermionGrid());
+    FermionFieldo c(Mato.FermionGrid()), defect(Mato.FermionGrid());
+    FermionFieldi ci(Mati.FermionGrid()), yi(Mati.FermionGrid()), xi(Mati.FermionGrid());
+    FermionFieldi srci(Mati.FermionGrid()), Ai(Mati.FermionGrid());
+    const RealD m = Mati.Mass();
+
+    if (src.Grid() == Mato.GaugeGrid()) Mato.ImportPhysicalFermionSource(src, b);
+    else if (src.Grid() == Mato.FermionGrid()) b = src;
+    else throw GridError(GB_ERR_BAD_ARG, "MADWF: source on neither the gauge nor the fermion grid of the outer operator");
+    const RealD nb = norm2(b);
+    defect = b;
+    sol5 = Zero();
+    for (int i = 0; i < maxiter; i++) {
+      // c0: the s = 0 slice of Pdag PV^-1 defect
+      PauliVillarsSolvero(Mato, defect, A);
+      Mato.Pdag(A, c);
+      ExtractSlice(c0, c, 0, 0);
+      // the inner system with surface term c0: Dwm P y = D(1) P (c0, 0, ..., 0)^T
+      ci = Zero();
+      convert(c0, c0i);
+      InsertSlice(c0i, ci, 0, 0);
+      Mati.P(ci, Ai);
+      Mati.SetMass(1.0);
+      Mati.M(Ai, srci);
+      Mati.SetMass(m);
+      SchurSolveri(Mati, srci, xi, Guesseri);
+      Mati.Pdag(xi, yi);
+      ExtractSlice(y0i, yi, 0, 0);
+      convert(y0i, y0);
+      // the bulk of the outer solution: Pdag PV^-1 Dm P (-y0, c_1, ..., c_{Ls-1}), then the
+      // surface solution back in and P back to x
+      c0 = -y0;
+      InsertSlice(c0, c, 0, 0);
+      Mato.P(c, B);
+      Mato.M(B, A);
+      PauliVillarsSolvero(Mato, A, B);
+      Mato.Pdag(B, A);
+      InsertSlice(y0, A, 0, 0);
+      Mato.P(A, B);
+      sol5 = sol5 + B;  // sol5 += M^-1 defect
+      Mato.M(sol5, A);
+      defect = b - A;
+      const RealD resid = std::sqrt(norm2(defect) / nb);
+      IterationsToComplete = i + 1;
+      FinalResidual = resid;
+      if (callback) (*callback)(resid);
+      if (resid < target_resid) return;
+    }
+    throw GridError(GB_ERR_NOT_CONVERGED, "MADWF: exceeded maxiter");
   }
 };
 

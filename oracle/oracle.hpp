@@ -330,9 +330,10 @@ inline cplx<double> cj(const cplx<double>& x) { return std::conj(x); }
 template <class C> struct CayleyT {
   int Ls = 0;
   double mf = 0, M5 = 0, b = 0, c = 0;
-  std::vector<C> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
-  void setup(int Ls_, double mf_, double M5_, double b_, double c_, const std::vector<C>& omega) {
+  std::vector<C> omega, bs, cs, bee, cee, dee, lee, leem, uee, ueem;
+  void setup(int Ls_, double mf_, double M5_, double b_, double c_, const std::vector<C>& omega_) {
     Ls = Ls_; mf = mf_; M5 = M5_; b = b_; c = c_;
+    omega = omega_;
     bs.assign(Ls, C(0)); cs.assign(Ls, C(0)); bee.assign(Ls, C(0)); cee.assign(Ls, C(0));
     dee.assign(Ls, C(0)); lee.assign(Ls, C(0)); leem.assign(Ls, C(0)); uee.assign(Ls, C(0)); ueem.assign(Ls, C(0));
     for (int i = 0; i < Ls; i++) {
@@ -419,6 +420,8 @@ template <class R> struct Op {
   virtual void MooeeDag(const Field<R>& in, Field<R>& out) = 0;
   virtual void MooeeInv(const Field<R>& in, Field<R>& out) = 0;
   virtual void MooeeInvDag(const Field<R>& in, Field<R>& out) = 0;
+  // SetMass (CayleyFermion5D.h:75-78: the Cayley coefficients are rebuilt)
+  virtual void set_mass(double m) = 0;
 
   void MdagM(const Field<R>& in, Field<R>& out) {
     Field<R> t; M(in, t); Mdag(t, out);
@@ -450,6 +453,7 @@ template <class R> struct Op {
 template <class R> struct Wilson : Op<R> {
   double mass, diag_mass;
   Wilson(const int* dims, int L5, double m) : Op<R>(dims, L5), mass(m), diag_mass(4.0 + m) {}
+  void set_mass(double m) override { mass = m; diag_mass = 4.0 + m; }
   void M(const Field<R>& in, Field<R>& out) override {
     this->Dhop(in, out, 0); axpy<R>(out, R(diag_mass), in, out);
   }
@@ -481,6 +485,7 @@ template <class R> struct CayleyBase : Op<R> {
   virtual void ImportUnphysical(const Field<R>& in4, Field<R>& out5) const = 0;
   virtual void ImportPhysicalSource(const Field<R>& in4, Field<R>& out5) = 0;
   virtual void ExportPhysical(const Field<R>& in5, Field<R>& out4, bool solution) const = 0;
+  virtual void P(const Field<R>& psi, Field<R>& chi, int dag) const = 0;
 };
 
 template <class R, class C = double> struct Mobius : CayleyBase<R> {
@@ -495,6 +500,22 @@ template <class R, class C = double> struct Mobius : CayleyBase<R> {
     cf.setup(Ls_, mf, M5, b, c, gamma);
   }
   int64_t n4(const Field<R>& f) const { return int64_t(f.size() / (size_t(Ls) * Nsc)); }
+  void set_mass(double m) override {
+    const std::vector<C> om = cf.omega;
+    cf.setup(Ls, m, cf.M5, cf.b, cf.c, om);
+  }
+  // P / Pdag (CayleyFermion5DImplementation.h:70-88): chi_s = P- psi_s + P+ psi_{s+1} (P)
+  // or P+ psi_{s-1} (Pdag), s cyclic; P+ keeps spins 0,1 (components k < 6)
+  void P(const Field<R>& psi, Field<R>& chi, int dag) const override {
+    const int64_t n = n4(psi);
+    chi.resize(psi.size());
+    for (int64_t x = 0; x < n; x++)
+      for (int s = 0; s < Ls; s++) {
+        const int sp = dag ? (s + Ls - 1) % Ls : (s + 1) % Ls;
+        for (int k = 0; k < Nsc; k++)
+          chi[(size_t(x) * Ls + s) * Nsc + k] = psi[(size_t(x) * Ls + (k < 6 ? sp : s)) * Nsc + k];
+      }
+  }
 
   void DW(const Field<R>& in, Field<R>& out, int dag) {
     this->Dhop(in, out, dag); axpy<R>(out, R(4.0 - cf.M5), in, out);

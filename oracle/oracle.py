@@ -20,6 +20,7 @@ OP_MEOOE, OP_MEOOE_DAG, OP_MOOEE, OP_MOOEE_DAG = 4, 5, 6, 7
 OP_MOOEE_INV, OP_MOOEE_INV_DAG, OP_MPC, OP_MPC_DAG = 8, 9, 10, 11
 OP_MPCDAGMPC, OP_MDAGM, OP_MEOOE5D, OP_MEOOE_DAG5D = 12, 13, 14, 15
 OP_DMINUS, OP_DMINUS_DAG = 16, 17
+OP_P, OP_PDAG = 18, 19  # CayleyFermion5D::P / Pdag
 # orc_physical modes (CayleyFermion5DImplementation.h:57-129)
 IMPORT_PHYSICAL_SOURCE, IMPORT_UNPHYSICAL, EXPORT_PHYSICAL_SOLUTION, EXPORT_PHYSICAL_SOURCE = 0, 1, 2, 3
 
@@ -44,6 +45,7 @@ def lib():
         L.orc_create.argtypes = [i, i, ip, i, dp, dp, dp]
         L.orc_create.restype = vp
         L.orc_free.argtypes = [vp]
+        L.orc_set_mass.argtypes = [vp, C.c_double]
         L.orc_apply.argtypes = [vp, i, dp, dp, i]
         L.orc_dhop_cb.argtypes = [vp, dp, dp, i, i]
         L.orc_doubled_links.argtypes = [vp, dp]
@@ -104,6 +106,10 @@ class OracleOp:
 
     def half_len(self):
         return self.vol // 2 * self.L5 * 12
+
+    def set_mass(self, mass):
+        """SetMass (CayleyFermion5D.h:75-78)."""
+        assert lib().orc_set_mass(self.h, float(mass)) == 0
 
     def apply(self, opcode, x, parity=1):
         x = np.ascontiguousarray(x, dtype=np.complex128)

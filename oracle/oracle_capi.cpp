@@ -34,13 +34,14 @@ enum Opcode {
   OP_M = 0, OP_MDAG = 1, OP_DHOP = 2, OP_DHOP_DAG = 3, OP_MEOOE = 4, OP_MEOOE_DAG = 5, OP_MOOEE = 6,
   OP_MOOEE_DAG = 7, OP_MOOEE_INV = 8, OP_MOOEE_INV_DAG = 9, OP_MPC = 10, OP_MPC_DAG = 11,
   OP_MPCDAGMPC = 12, OP_MDAGM = 13, OP_MEOOE5D = 14, OP_MEOOE_DAG5D = 15, OP_DMINUS = 16,
-  OP_DMINUS_DAG = 17
+  OP_DMINUS_DAG = 17, OP_P = 18, OP_PDAG = 19
 };
 
 // returns the input length (in complex numbers) that the opcode expects
 template <class R> size_t in_len(Op<R>* op, int opcode) {
   switch (opcode) {
     case OP_M: case OP_MDAG: case OP_DHOP: case OP_DHOP_DAG: case OP_MDAGM: case OP_DMINUS: case OP_DMINUS_DAG:
+    case OP_P: case OP_PDAG:
       return op->full_len();
     default: return op->half_len();
   }
@@ -75,6 +76,12 @@ template <class R> int apply(Op<R>* op, int kind, int opcode, const double* in, 
     case OP_DMINUS_DAG: {
       if (kind == 0) return 1;
       static_cast<CayleyBase<R>*>(op)->Dminus(a, b, opcode == OP_DMINUS_DAG);
+      break;
+    }
+    case OP_P:
+    case OP_PDAG: {
+      if (kind == 0) return 1;
+      static_cast<CayleyBase<R>*>(op)->P(a, b, opcode == OP_PDAG);
       break;
     }
     default: return 1;
@@ -126,6 +133,14 @@ void* orc_create(int kind, int prec, const int* dims, int L5, const double* par,
   return h;
 }
 void orc_free(void* p) { delete static_cast<Handle*>(p); }
+
+// SetMass: the operator's mass (and, for Cayley operators, its coefficients) changes
+int orc_set_mass(void* p, double mass) {
+  Handle* h = static_cast<Handle*>(p);
+  if (h->prec == 0) h->d->set_mass(mass);
+  else h->f->set_mass(mass);
+  return 0;
+}
 
 // parity = parity of the input field for the half-checkerboard opcodes
 int orc_apply(void* p, int opcode, const double* in, double* out, int parity) {

@@ -2,7 +2,7 @@
 // tests/core/Test_mobius_even_odd.cc, the Schur red-black solve, the mixed-precision
 // reliable-update CG of tests/Test_dwf_mixedcg_prec.cc, the multishift CG, the unpreconditioned Wilson CG of
 // tests/solver/Test_wilson_cg_unprec.cc, a user-defined linear operator through the
-// host-driven CG, the 4D <-> 5D surface fields and the ZMobius even-odd identities.  Exit status 0 when every check holds.
+// host-driven CG, the 4D <-> 5D surface fields, MADWF and the ZMobius even-odd identities.  Exit status 0 when every check holds.
 #include <cstdio>
 #include <cstdlib>
 
@@ -184,6 +184,34 @@ int main() {
   Ddwf.ExportPhysicalFermionSolution(prop5, prop4);
   expect(norm2(prop4) > 0 && SchurSolver.UnpreconditionedResidual < 1e-9, "physical propagator solve",
          SchurSolver.UnpreconditionedResidual);
+
+  // ---- MADWF: outer Ls = 8, inner Ls = 4 (tests/solver/Test_zMADWF_prec.cc pattern) ----
+  {
+    GridCartesian* FGrid4 = SpaceTimeGrid::makeFiveDimGrid(4, UGrid);
+    GridRedBlackCartesian* FrbGrid4 = SpaceTimeGrid::makeFiveDimRedBlackGrid(4, UGrid);
+    MobiusFermionD Dinner(Umu, *FGrid4, *FrbGrid4, *UGrid, *UrbGrid, mass, M5, b, c, params);
+    ConjugateGradient<LatticeFermion> CGpv(1e-12, 10000), CGin(1e-12, 10000, false);
+    SchurRedBlackDiagMooeeSolve<LatticeFermion> SchurPV(CGpv), SchurIn(CGin);
+    typedef PauliVillarsSolverRBprec<LatticeFermion, SchurRedBlackDiagMooeeSolve<LatticeFermion>> PVtype;
+    PVtype PV(SchurPV);
+    ZeroGuesser<LatticeFermion> Guess;
+    struct Count : MADWFinnerIterCallbackBase {
+      int calls = 0;
+      void operator()(const RealD) override { calls++; }
+    } count;
+    MADWF<MobiusFermionD, MobiusFermionD, PVtype, SchurRedBlackDiagMooeeSolve<LatticeFermion>,
+          ZeroGuesser<LatticeFermion>>
+        madwf(Ddwf, Dinner, PV, SchurIn, Guess, 1e-9, 30, &count);
+    LatticeFermion madwf_sol(FGrid);
+    madwf(eta, madwf_sol);
+    LatticeFermion dm = madwf_sol - prop5;
+    const RealD rd = std::sqrt(norm2(dm) / norm2(prop5));
+    std::printf("MADWF: %d outer iterations, residual %.3e\n", madwf.IterationsToComplete, madwf.FinalResidual);
+    expect(rd < 1e-7 && count.calls == madwf.IterationsToComplete && Ddwf.Mass() == mass && Dinner.Mass() == mass,
+           "MADWF solution == direct Schur solve", rd);
+    delete FGrid4;
+    delete FrbGrid4;
+  }
 
   // ---- ZMobius, complex omega (tests/core/Test_zmobius_even_odd.cc pattern) ----
   const std::vector<ComplexD> omega = {1.45806438985048, 1.18231318389348, 0.830951166685955, 0.542352409156791,

@@ -337,3 +337,53 @@ def test_zmobius_dminus_adjoint():
     lhs = np.vdot(a, op.apply(o.OP_DMINUS, b)).conj()
     rhs = np.vdot(b, op.apply(o.OP_DMINUS_DAG, a))
     assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+
+
+# ---- MADWF pieces (CayleyFermion5DImplementation.h:70-88, MADWF.h) ----------------------
+def test_p_is_a_chiral_shift_and_pdag_its_inverse():
+    op, _ = _mobius(Ls=6)
+    x = fermion(VOL, 6, 21)
+    y = op.apply(o.OP_P, x).reshape(VOL, 6, 12)
+    xr = x.reshape(VOL, 6, 12)
+    assert np.array_equal(y[:, :, 6:], xr[:, :, 6:])                      # P- psi_s
+    assert np.array_equal(y[:, :, :6], np.roll(xr[:, :, :6], -1, axis=1))  # P+ psi_{s+1}
+    assert np.array_equal(op.apply(o.OP_PDAG, y.reshape(-1)), x)
+    # Pdag is the adjoint of P
+    z = fermion(VOL, 6, 22)
+    assert abs(np.vdot(z, op.apply(o.OP_P, x)) - np.vdot(op.apply(o.OP_PDAG, z), x)) < 1e-12 * VOL
+
+
+def test_set_mass_equals_a_fresh_operator():
+    op, U = _mobius(Ls=6, mf=0.1)
+    fresh = o.OracleOp(1, 0, DIMS, 6, [1.0, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t())
+    x = fermion(VOL, 6, 23)
+    op.set_mass(1.0)
+    assert np.array_equal(op.apply(o.OP_M, x), fresh.apply(o.OP_M, x))
+    xh = fermion(VOL // 2, 6, 24)
+    assert np.array_equal(op.apply(o.OP_MOOEE_INV, xh), fresh.apply(o.OP_MOOEE_INV, xh))
+
+
+def test_madwf_with_inner_equal_outer_converges_in_one_step():
+    """With the inner operator equal to the outer one the defect correction of MADWF.h is
+    exact: one step reaches the solver tolerance, and the result is the direct solution."""
+    from oracle import madwf as mw
+    outer, U = _mobius(Ls=8, mf=0.05, eps=0.3, seed=5)
+    inner = o.OracleOp(1, 0, DIMS, 8, [0.05, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t())
+    b = outer.physical(o.IMPORT_PHYSICAL_SOURCE, fermion(VOL, 1, 4))
+    sol, hist = mw.madwf(outer, 8, 0.05, inner, 8, 0.05, b, 1e-12, 1e-12, 1e-9, 3)
+    assert len(hist) == 1 and hist[0] < 1e-10
+    ref, _, _, _ = outer.schur_solve(b, 1e-11, 10000)
+    assert o.rel_l2(sol, ref) < 1e-9
+
+
+def test_madwf_with_smaller_ls_inner_converges_to_the_outer_solution():
+    """Test_zMADWF_prec.cc's check: the MADWF solution equals the direct outer solve; the
+    defect falls geometrically with an Ls = 4 inner operator."""
+    from oracle import madwf as mw
+    outer, U = _mobius(Ls=8, mf=0.05, eps=0.3, seed=5)
+    inner = o.OracleOp(1, 0, DIMS, 4, [0.05, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t())
+    b = outer.physical(o.IMPORT_PHYSICAL_SOURCE, fermion(VOL, 1, 4))
+    sol, hist = mw.madwf(outer, 8, 0.05, inner, 4, 0.05, b, 1e-12, 1e-12, 1e-7, 20)
+    assert hist[-1] < 1e-7 and all(b_ < 0.2 * a for a, b_ in zip(hist, hist[1:]))
+    ref, _, _, _ = outer.schur_solve(b, 1e-11, 10000)
+    assert o.rel_l2(sol, ref) < 1e-6
