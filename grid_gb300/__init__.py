@@ -12,7 +12,7 @@ from .api import (  # noqa: F401
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
     NerscHeader, nersc_read_header, nersc_read, nersc_write, gauge_stats,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
-    antiperiodic_t, periodic, set_device, PinnedArray, Stream, norm2, innerProduct, axpy, axpby, axpy_norm,
+    antiperiodic_t, periodic, set_device, PinnedArray, Stream, TransferQueue, norm2, innerProduct, axpy, axpby, axpy_norm,
     pickCheckerboard, setCheckerboard, InsertSlice, ExtractSlice, ZeroGuesser, PauliVillarsSolverUnprec,
     PauliVillarsSolverRBprec, MADWF, MADWFinnerIterCallbackBase, Server, Request, make_request, request_bytes,
 )

@@ -92,6 +92,13 @@ _proto("gb_field_import", [_vp, _dp])
 _proto("gb_field_export", [_vp, _dp])
 _proto("gb_field_import_device", [_vp, _vp])
 _proto("gb_field_export_device", [_vp, _vp])
+_proto("gb_field_import_f32", [_vp, _vp])
+_proto("gb_field_export_f32", [_vp, _vp])
+_proto("gb_xfer_create", [_vp, C.POINTER(_vp)])
+_proto("gb_xfer_destroy", [_vp])
+_proto("gb_xfer_import", [_vp, _vp, _vp, _i])
+_proto("gb_xfer_export", [_vp, _vp, _vp, _i])
+_proto("gb_xfer_wait", [_vp])
 _proto("gb_field_zero", [_vp])
 _proto("gb_field_copy", [_vp, _vp])
 _proto("gb_field_norm2", [_vp, _dp])
@@ -144,14 +151,16 @@ def set_device(d: int):
 
 
 class PinnedArray:
-    """Page-locked host buffer viewed as a numpy complex128 array."""
+    """Page-locked host buffer viewed as a numpy complex128 (or, with dtype=np.complex64,
+    complex64) array."""
 
-    def __init__(self, n_complex: int):
+    def __init__(self, n_complex: int, dtype=np.complex128):
+        dtype = np.dtype(dtype)
         p = _vp()
-        _check(lib.gb_host_alloc(int(n_complex) * 16, C.byref(p)))
+        _check(lib.gb_host_alloc(int(n_complex) * dtype.itemsize, C.byref(p)))
         self.ptr = p
-        buf = (C.c_double * (2 * int(n_complex))).from_address(p.value)
-        self.array = np.frombuffer(buf, dtype=np.complex128)
+        buf = (C.c_char * (int(n_complex) * dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype)
 
     def __del__(self):
         if getattr(self, "ptr", None):
@@ -281,6 +290,19 @@ class FermionField:
         _check(lib.gb_field_export(self.h, _dptr(a)))
         return a
 
+    def import_f32(self, a: np.ndarray) -> "FermionField":
+        """The canonical form in single precision (complex64)."""
+        a = np.ascontiguousarray(a, dtype=np.complex64).reshape(-1)
+        if a.size != self.host_len():
+            raise GridError(1, f"host array has {a.size} complex numbers, field needs {self.host_len()}")
+        _check(lib.gb_field_import_f32(self.h, a.ctypes.data))
+        return self
+
+    def export_f32(self) -> np.ndarray:
+        a = np.empty(self.host_len(), dtype=np.complex64)
+        _check(lib.gb_field_export_f32(self.h, a.ctypes.data))
+        return a
+
     def zero(self):
         _check(lib.gb_field_zero(self.h))
         return self
@@ -298,6 +320,50 @@ class FermionField:
         out = np.empty(2 * self.op.nrhs, dtype=np.float64)
         _check(lib.gb_field_inner(self.h, other.h, _dptr(out)))
         return out[0::2] + 1j * out[1::2]
+
+
+class TransferQueue:
+    """gb_xfer_*: host fields in and out without blocking; the copy of the next input and of
+    the last result overlap each other and the operator's kernels.  Arrays (complex128 or
+    complex64, page-locked for overlap, e.g. PinnedArray) must stay alive and untouched
+    until wait() returns."""
+
+    def __init__(self, op: "_FermionOperator"):
+        self.op = op
+        h = _vp()
+        _check(lib.gb_xfer_create(op.h, C.byref(h)))
+        self.h = h
+        self._held = []
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib.gb_xfer_destroy(h)
+            self.h = None
+
+    @staticmethod
+    def _prec(a: np.ndarray) -> int:
+        if a.dtype == np.complex128:
+            return F64
+        if a.dtype == np.complex64:
+            return F32
+        raise GridError(1, "host arrays must be complex128 or complex64")
+
+    def import_(self, field: FermionField, a: np.ndarray):
+        if not a.flags.c_contiguous or a.size != field.host_len():
+            raise GridError(1, "host array must be contiguous with the field's canonical length")
+        self._held.append(a)
+        _check(lib.gb_xfer_import(self.h, field.h, a.ctypes.data, self._prec(a)))
+
+    def export(self, field: FermionField, a: np.ndarray):
+        if not a.flags.c_contiguous or a.size != field.host_len():
+            raise GridError(1, "host array must be contiguous with the field's canonical length")
+        self._held.append(a)
+        _check(lib.gb_xfer_export(self.h, field.h, a.ctypes.data, self._prec(a)))
+
+    def wait(self):
+        _check(lib.gb_xfer_wait(self.h))
+        self._held = []
 
 
 def norm2(f: FermionField):

@@ -693,19 +693,19 @@ size_t field_host_doubles(const Field* f) {
   return n4 * op->Ls * op->nrhs_user * 24;
 }
 
-int field_import_dev(Field* f, const double* dev) {
+int field_import_dev(Field* f, const void* dev, int canon_prec) {
   if (f->full()) {
-    for (int p = 0; p < 2; p++) GB_TRY(launch_import_half(f->op, dev, half_view(f, p), p, 1));
+    for (int p = 0; p < 2; p++) GB_TRY(launch_import_half(f->op, dev, canon_prec, half_view(f, p), p, 1));
   } else {
-    GB_TRY(launch_import_half(f->op, dev, half_view(f, 0), f->subset, 0));
+    GB_TRY(launch_import_half(f->op, dev, canon_prec, half_view(f, 0), f->subset, 0));
   }
   return GB_OK;
 }
-int field_export_dev(Field* f, double* dev) {
+int field_export_dev(Field* f, void* dev, int canon_prec) {
   if (f->full()) {
-    for (int p = 0; p < 2; p++) GB_TRY(launch_export_half(f->op, half_view(f, p), dev, p, 1));
+    for (int p = 0; p < 2; p++) GB_TRY(launch_export_half(f->op, half_view(f, p), dev, canon_prec, p, 1));
   } else {
-    GB_TRY(launch_export_half(f->op, half_view(f, 0), dev, f->subset, 0));
+    GB_TRY(launch_export_half(f->op, half_view(f, 0), dev, canon_prec, f->subset, 0));
   }
   return GB_OK;
 }
@@ -847,33 +847,149 @@ int gb_field_host_len(gb_field_t f, size_t* n) {
   *n = field_host_doubles(f);
   return GB_OK;
 }
-int gb_field_import(gb_field_t f, const double* host) {
+static int host_import(gb_field_t f, const void* host, int host_prec) {
   if (!f || !host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
   Op* op = f->op;
-  const size_t bytes = field_host_doubles(f) * sizeof(double);
+  const size_t bytes = field_host_doubles(f) * (host_prec == GB_F32 ? sizeof(float) : sizeof(double));
   GB_TRY(ensure_stage(op, bytes));
   GB_CHECK_CUDA(cudaMemcpyAsync(op->d_stage, host, bytes, cudaMemcpyHostToDevice, op->stream));
-  GB_TRY(field_import_dev(f, op->d_stage));
+  GB_TRY(field_import_dev(f, op->d_stage, host_prec));
   GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
   return GB_OK;
 }
-int gb_field_export(gb_field_t f, double* host) {
+static int host_export(gb_field_t f, void* host, int host_prec) {
   if (!f || !host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
   Op* op = f->op;
-  const size_t bytes = field_host_doubles(f) * sizeof(double);
+  const size_t bytes = field_host_doubles(f) * (host_prec == GB_F32 ? sizeof(float) : sizeof(double));
   GB_TRY(ensure_stage(op, bytes));
-  GB_TRY(field_export_dev(f, op->d_stage));
+  GB_TRY(field_export_dev(f, op->d_stage, host_prec));
   GB_CHECK_CUDA(cudaMemcpyAsync(host, op->d_stage, bytes, cudaMemcpyDeviceToHost, op->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
   return GB_OK;
 }
+int gb_field_import(gb_field_t f, const double* host) { return host_import(f, host, GB_F64); }
+int gb_field_export(gb_field_t f, double* host) { return host_export(f, host, GB_F64); }
+int gb_field_import_f32(gb_field_t f, const float* host) { return host_import(f, host, GB_F32); }
+int gb_field_export_f32(gb_field_t f, float* host) { return host_export(f, host, GB_F32); }
 int gb_field_import_device(gb_field_t f, const double* dev) {
   if (!f || !dev) { set_error("null argument"); return GB_ERR_BAD_ARG; }
-  return field_import_dev(f, dev);
+  return field_import_dev(f, dev, GB_F64);
 }
 int gb_field_export_device(gb_field_t f, double* dev) {
   if (!f || !dev) { set_error("null argument"); return GB_ERR_BAD_ARG; }
-  return field_export_dev(f, dev);
+  return field_export_dev(f, dev, GB_F64);
+}
+
+// ---- transfer queue: double-buffered staging, H2D and D2H on copy streams of their own ----
+}  // extern "C"
+
+struct gb_xfer_s {
+  Op* op = nullptr;
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  struct Slot {
+    void* buf = nullptr;
+    size_t cap = 0;
+    cudaEvent_t filled = nullptr, free = nullptr;
+  };
+  Slot in[2], out[2];
+  int in_next = 0, out_next = 0;
+};
+
+static int xfer_slot_ensure(gb_xfer_s::Slot& s, size_t bytes) {
+  if (s.cap >= bytes) return GB_OK;
+  if (s.buf) {
+    // the slot's last user is ordered before its free event
+    GB_CHECK_CUDA(cudaEventSynchronize(s.free));
+    cudaFree(s.buf);
+    s.buf = nullptr;
+    s.cap = 0;
+  }
+  GB_CHECK_CUDA(cudaMalloc(&s.buf, bytes));
+  s.cap = bytes;
+  return GB_OK;
+}
+
+static void xfer_release(gb_xfer_s* x) {
+  if (x->h2d) cudaStreamSynchronize(x->h2d);
+  if (x->d2h) cudaStreamSynchronize(x->d2h);
+  if (x->op) cudaStreamSynchronize(x->op->stream);
+  for (auto* set : {x->in, x->out})
+    for (int k = 0; k < 2; k++) {
+      cudaFree(set[k].buf);
+      if (set[k].filled) cudaEventDestroy(set[k].filled);
+      if (set[k].free) cudaEventDestroy(set[k].free);
+    }
+  if (x->h2d) cudaStreamDestroy(x->h2d);
+  if (x->d2h) cudaStreamDestroy(x->d2h);
+  delete x;
+}
+
+extern "C" {
+
+int gb_xfer_create(gb_op_t op, gb_xfer_t* out) {
+  if (!op || !out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  gb_xfer_s* x = new (std::nothrow) gb_xfer_s;
+  if (!x) { set_error("host allocation failed"); return GB_ERR_OOM; }
+  x->op = op;
+  cudaError_t e = cudaStreamCreateWithFlags(&x->h2d, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&x->d2h, cudaStreamNonBlocking);
+  for (auto* set : {x->in, x->out})
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+      e = cudaEventCreateWithFlags(&set[k].filled, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&set[k].free, cudaEventDisableTiming);
+    }
+  if (e != cudaSuccess) {
+    set_error("transfer queue: %s", cudaGetErrorString(e));
+    xfer_release(x);
+    return GB_ERR_CUDA;
+  }
+  *out = x;
+  return GB_OK;
+}
+int gb_xfer_destroy(gb_xfer_t x) {
+  if (x) xfer_release(x);
+  return GB_OK;
+}
+int gb_xfer_import(gb_xfer_t x, gb_field_t f, const void* host, int host_prec) {
+  if (!x || !f || !host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (host_prec != GB_F64 && host_prec != GB_F32) { set_error("host precision must be GB_F64 or GB_F32"); return GB_ERR_BAD_ARG; }
+  if (!ops_conformable(f->op, x->op)) { set_error("field is not conformable to the queue's operator"); return GB_ERR_BAD_ARG; }
+  Op* op = x->op;
+  gb_xfer_s::Slot& s = x->in[x->in_next];
+  const size_t bytes = field_host_doubles(f) * (host_prec == GB_F32 ? sizeof(float) : sizeof(double));
+  GB_TRY(xfer_slot_ensure(s, bytes));
+  x->in_next ^= 1;
+  GB_CHECK_CUDA(cudaStreamWaitEvent(x->h2d, s.free, 0));  // the slot's previous layout kernel is done
+  GB_CHECK_CUDA(cudaMemcpyAsync(s.buf, host, bytes, cudaMemcpyHostToDevice, x->h2d));
+  GB_CHECK_CUDA(cudaEventRecord(s.filled, x->h2d));
+  GB_CHECK_CUDA(cudaStreamWaitEvent(op->stream, s.filled, 0));
+  GB_TRY(field_import_dev(f, s.buf, host_prec));
+  GB_CHECK_CUDA(cudaEventRecord(s.free, op->stream));
+  return GB_OK;
+}
+int gb_xfer_export(gb_xfer_t x, gb_field_t f, void* host, int host_prec) {
+  if (!x || !f || !host) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (host_prec != GB_F64 && host_prec != GB_F32) { set_error("host precision must be GB_F64 or GB_F32"); return GB_ERR_BAD_ARG; }
+  if (!ops_conformable(f->op, x->op)) { set_error("field is not conformable to the queue's operator"); return GB_ERR_BAD_ARG; }
+  Op* op = x->op;
+  gb_xfer_s::Slot& s = x->out[x->out_next];
+  const size_t bytes = field_host_doubles(f) * (host_prec == GB_F32 ? sizeof(float) : sizeof(double));
+  GB_TRY(xfer_slot_ensure(s, bytes));
+  x->out_next ^= 1;
+  GB_CHECK_CUDA(cudaStreamWaitEvent(op->stream, s.free, 0));  // the slot's previous copy-out is done
+  GB_TRY(field_export_dev(f, s.buf, host_prec));
+  GB_CHECK_CUDA(cudaEventRecord(s.filled, op->stream));
+  GB_CHECK_CUDA(cudaStreamWaitEvent(x->d2h, s.filled, 0));
+  GB_CHECK_CUDA(cudaMemcpyAsync(host, s.buf, bytes, cudaMemcpyDeviceToHost, x->d2h));
+  GB_CHECK_CUDA(cudaEventRecord(s.free, x->d2h));
+  return GB_OK;
+}
+int gb_xfer_wait(gb_xfer_t x) {
+  if (!x) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  GB_CHECK_CUDA(cudaStreamSynchronize(x->h2d));
+  GB_CHECK_CUDA(cudaStreamSynchronize(x->op->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(x->d2h));
+  return GB_OK;
 }
 
 int gb_field_zero(gb_field_t f) {

@@ -470,10 +470,17 @@ __device__ __forceinline__ int64_t cb_to_site(int64_t xcb, int parity, const Geo
   return row * g.L[0] + x;
 }
 
-template <class T, bool IMPORT>
-__global__ void __launch_bounds__(256) layout_kernel(const GeoParams g, double* canon, void* dev, float* devn, int parity,
+// canonical host layout <-> device layout; CR is the canonical real type (double or float:
+// Grid's LatticeFermionD / LatticeFermionF host data)
+template <class CR> struct Canon2;
+template <> struct Canon2<double> { using type = double2; };
+template <> struct Canon2<float> { using type = float2; };
+
+template <class T, class CR, bool IMPORT>
+__global__ void __launch_bounds__(256) layout_kernel(const GeoParams g, CR* canon, void* dev, float* devn, int parity,
                                                      int canon_full) {
   using R = typename Arith<T>::type;
+  using C2 = typename Canon2<CR>::type;
   const size_t n5 = size_t(g.half4) * g.L5;
   const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n5) return;
@@ -491,18 +498,23 @@ __global__ void __launch_bounds__(256) layout_kernel(const GeoParams g, double* 
   }
   const int64_t c4 = canon_full ? cb_to_site(xcb, parity, g) : xcb;
   const int64_t n4c = canon_full ? g.vol4 : g.half4;
-  double2* c = reinterpret_cast<double2*>(canon) + ((size_t(rhs) * n4c + c4) * g.Ls + s) * 12;
+  C2* c = reinterpret_cast<C2*>(canon) + ((size_t(rhs) * n4c + c4) * g.Ls + s) * 12;
   if (IMPORT) {
 #pragma unroll
     for (int k = 0; k < 12; k++) {
-      const double2 v = c[k];
+      const C2 v = c[k];
       f.re[k] = R(v.x); f.im[k] = R(v.y);
     }
     SpinorIO<T>::store(dev, devn, n5, i, f);
   } else {
     SpinorIO<T>::load(dev, devn, n5, i, f);
 #pragma unroll
-    for (int k = 0; k < 12; k++) c[k] = make_double2(double(f.re[k]), double(f.im[k]));
+    for (int k = 0; k < 12; k++) {
+      C2 v;
+      v.x = CR(f.re[k]);
+      v.y = CR(f.im[k]);
+      c[k] = v;
+    }
   }
 }
 
@@ -518,24 +530,27 @@ static GeoParams geo(const Op* op) {
   return g;
 }
 
-template <bool IMPORT>
-static int layout_p(Op* op, double* canon, HalfView v, int parity, int canon_full) {
+template <class CR, bool IMPORT>
+static int layout_p(Op* op, CR* canon, HalfView v, int parity, int canon_full) {
   GeoParams g = geo(op);
   const size_t n5 = op->n5();
   switch (v.prec) {
-    case GB_F64: layout_kernel<double, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
-    case GB_F32: layout_kernel<float, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
-    case GB_F16: layout_kernel<__half, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
+    case GB_F64: layout_kernel<double, CR, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
+    case GB_F32: layout_kernel<float, CR, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
+    case GB_F16: layout_kernel<__half, CR, IMPORT><<<nblk(n5), 256, 0, op->stream>>>(g, canon, v.data, v.norms, parity, canon_full); break;
   }
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
 
-int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full) {
-  return layout_p<true>(op, const_cast<double*>(canon), out, parity, canon_is_full);
+int launch_import_half(Op* op, const void* canon, int canon_prec, HalfView out, int parity, int canon_is_full) {
+  if (canon_prec == GB_F32)
+    return layout_p<float, true>(op, static_cast<float*>(const_cast<void*>(canon)), out, parity, canon_is_full);
+  return layout_p<double, true>(op, static_cast<double*>(const_cast<void*>(canon)), out, parity, canon_is_full);
 }
-int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon_is_full) {
-  return layout_p<false>(op, canon, in, parity, canon_is_full);
+int launch_export_half(Op* op, HalfView in, void* canon, int canon_prec, int parity, int canon_is_full) {
+  if (canon_prec == GB_F32) return layout_p<float, false>(op, static_cast<float*>(canon), in, parity, canon_is_full);
+  return layout_p<double, false>(op, static_cast<double*>(canon), in, parity, canon_is_full);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -207,8 +207,10 @@ int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfVi
                const ColCoefsHost& h);
 
 // layout conversion between canonical FP64 (device) and the device layout
-int launch_import_half(Op* op, const double* canon, HalfView out, int parity, int canon_is_full);
-int launch_export_half(Op* op, HalfView in, double* canon, int parity, int canon_is_full);
+// canonical host layout (complex double or, with canon_prec = GB_F32, complex float) <->
+// device layout of one checkerboard half
+int launch_import_half(Op* op, const void* canon, int canon_prec, HalfView out, int parity, int canon_is_full);
+int launch_export_half(Op* op, HalfView in, void* canon, int canon_prec, int parity, int canon_is_full);
 int launch_double_store(Op* op, const double* U_canon, int parity);
 // 4D <-> 5D surface fields (Moebius): canonical FP64 4D field in device memory
 int launch_surface_insert(Op* op, const double* c4, HalfView even, HalfView odd);

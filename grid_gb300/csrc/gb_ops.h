@@ -32,8 +32,8 @@ int field_scale(Field* z, double a, Field* x);
 int field_copy(Field* dst, Field* src);
 int field_zero(Field* z);
 size_t field_host_doubles(const Field* f);
-int field_import_dev(Field* f, const double* dev);
-int field_export_dev(Field* f, double* dev);
+int field_import_dev(Field* f, const void* dev, int canon_prec);
+int field_export_dev(Field* f, void* dev, int canon_prec);
 int ensure_stage(Op* op, size_t bytes);
 int check_device_error(Op* op);
 

@@ -108,6 +108,26 @@ int gb_field_import(gb_field_t f, const double* host);
 int gb_field_export(gb_field_t f, double* host);
 int gb_field_import_device(gb_field_t f, const double* dev); /* canonical FP64 in device memory */
 int gb_field_export_device(gb_field_t f, double* dev);
+/* the canonical host form in single precision: complex<float> in the same order (Grid's
+ * LatticeFermionF host data); n_doubles of gb_field_host_len floats */
+int gb_field_import_f32(gb_field_t f, const float* host);
+int gb_field_export_f32(gb_field_t f, float* host);
+
+/* Transfer queue of an operator: host fields in and out without blocking the caller.
+ * Each import is a host->device copy on the queue's own copy stream into one of two
+ * staging buffers, then the layout kernel on the operator's stream, so operator calls
+ * issued after gb_xfer_import see the field; each export is the layout kernel on the
+ * operator's stream (after every call issued before it), then a device->host copy on a
+ * second copy stream.  The copy of the next input and of the last result therefore
+ * overlap each other and the operator's kernels.  Host buffers: canonical form in FP64
+ * (host_prec GB_F64) or FP32 (GB_F32), page-locked for the copies to overlap, left
+ * untouched (imports) or unread (exports) by the caller until gb_xfer_wait returns. */
+typedef struct gb_xfer_s* gb_xfer_t;
+int gb_xfer_create(gb_op_t op, gb_xfer_t* out);
+int gb_xfer_destroy(gb_xfer_t x);
+int gb_xfer_import(gb_xfer_t x, gb_field_t f, const void* host, int host_prec);
+int gb_xfer_export(gb_xfer_t x, gb_field_t f, void* host, int host_prec);
+int gb_xfer_wait(gb_xfer_t x); /* every queued import and export has completed */
 
 /* ---- field linear algebra (Grid/lattice/Lattice_arith.h, Lattice_reduction.h) ----
  * Reductions return one value per right-hand side (arrays of length nrhs), in FP64.
