@@ -11,6 +11,7 @@ from .api import (  # noqa: F401
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
     NerscHeader, nersc_read_header, nersc_read, nersc_write, gauge_stats,
+    IldgHeader, ildg_read_header, ildg_read, ildg_write,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
     antiperiodic_t, periodic, set_device, PinnedArray, Stream, TransferQueue, norm2, innerProduct, axpy, axpby, axpy_norm,
     pickCheckerboard, setCheckerboard, InsertSlice, ExtractSlice, ZeroGuesser, PauliVillarsSolverUnprec,

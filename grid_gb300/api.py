@@ -1050,6 +1050,42 @@ def nersc_write(path, U, dims, two_row=False, bits=64, big_endian=True, ensemble
                               int(sequence_number)))
 
 
+class IldgHeader(C.Structure):
+    _fields_ = [("dims", C.c_int * 4), ("precision", C.c_int), ("field", C.c_char * 32), ("lfn", C.c_char * 256),
+                ("has_checksum", C.c_int), ("scidac_suma", C.c_uint32), ("scidac_sumb", C.c_uint32),
+                ("scidac_suma_computed", C.c_uint32), ("scidac_sumb_computed", C.c_uint32),
+                ("has_plaquette", C.c_int), ("plaquette", C.c_double), ("link_trace", C.c_double),
+                ("plaquette_computed", C.c_double), ("link_trace_computed", C.c_double),
+                ("data_offset", C.c_int64), ("data_bytes", C.c_int64)]
+
+
+_proto("gb_ildg_read_header", [C.c_char_p, C.POINTER(IldgHeader)])
+_proto("gb_ildg_read", [C.c_char_p, _vp, _i, C.POINTER(IldgHeader), _i])
+_proto("gb_ildg_write", [C.c_char_p, _vp, _i, _ip, _i, C.c_char_p])
+
+
+def ildg_read_header(path) -> IldgHeader:
+    """The records of an ILDG file (no device work)."""
+    h = IldgHeader()
+    _check(lib.gb_ildg_read_header(str(path).encode(), C.byref(h)))
+    return h
+
+
+def ildg_read(path, check=True):
+    """IldgReader::readConfiguration: (canonical FP64 gauge field, header); the SciDAC
+    checksum, plaquette and link trace are verified when `check` (GridError otherwise)."""
+    h = ildg_read_header(path)
+    U = np.empty(int(np.prod(list(h.dims))) * 36, dtype=np.complex128)
+    _check(lib.gb_ildg_read(str(path).encode(), U.ctypes.data, 0, C.byref(h), int(bool(check))))
+    return U, h
+
+
+def ildg_write(path, U, dims, precision=64, lfn=""):
+    """IldgWriter::writeConfiguration of a canonical FP64 gauge field."""
+    U = np.ascontiguousarray(U, dtype=np.complex128)
+    _check(lib.gb_ildg_write(str(path).encode(), U.ctypes.data, 0, _dims(dims), int(precision), lfn.encode()))
+
+
 def gauge_stats(dims, U):
     """(avgPlaquette, linkTrace) of a canonical gauge field, computed on the device."""
     U = np.ascontiguousarray(U, dtype=np.complex128)

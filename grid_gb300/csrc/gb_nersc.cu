@@ -263,6 +263,11 @@ int parse_header(const char* path, gb_nersc_header* h) {
 }
 
 }  // namespace
+
+int gauge_stats_device(const int dims[4], const double* Ud, cudaStream_t s, double* plaq, double* trace) {
+  return gauge_stats_dev(dims, Ud, s, plaq, trace);
+}
+
 }  // namespace gb
 
 using namespace gb;

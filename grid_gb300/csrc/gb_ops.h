@@ -32,6 +32,8 @@ int field_scale(Field* z, double a, Field* x);
 int field_copy(Field* dst, Field* src);
 int field_zero(Field* z);
 size_t field_host_doubles(const Field* f);
+// WilsonLoops::avgPlaquette / linkTrace of a canonical FP64 gauge field in device memory
+int gauge_stats_device(const int dims[4], const double* Ud, cudaStream_t s, double* plaq, double* trace);
 int field_import_dev(Field* f, const void* dev, int canon_prec);
 int field_export_dev(Field* f, void* dev, int canon_prec);
 int ensure_stage(Op* op, size_t bytes);

@@ -312,6 +312,33 @@ int gb_nersc_read(const char* path, double* U, int on_device, gb_nersc_header* h
 /* writeConfiguration: two_row selects 4D_SU3_GAUGE; bits 32/64; big_endian as IEEE*BIG */
 int gb_nersc_write(const char* path, const double* U, int on_device, const int dims[4], int two_row, int bits,
                    int big_endian, const char* ensemble_id, const char* ensemble_label, int sequence_number);
+/* ---- ILDG / SciDAC gauge files (Grid/parallelIO/IldgIO.h:611-950, IldgIOtypes.h) ----
+ * LIME records; binary data site-lexicographic (x fastest), per site [mu][row][col]
+ * complex, IEEE32BIG or IEEE64BIG; the SciDAC checksum (BinaryIO.h:139-192) is the XOR
+ * over sites of the CRC-32 of the site's bytes rotated left by site % 29 (suma) and
+ * site % 31 (sumb). */
+typedef struct {
+  int dims[4];                       /* lx ly lz lt of the ildg-format record      */
+  int precision;                     /* 32 or 64                                   */
+  char field[32];                    /* "su3gauge"                                 */
+  char lfn[256];                     /* ildg-data-lfn                              */
+  int has_checksum;                  /* a scidac-checksum record was found         */
+  uint32_t scidac_suma, scidac_sumb; /* from the record                            */
+  uint32_t scidac_suma_computed, scidac_sumb_computed; /* of the data (gb_ildg_read) */
+  int has_plaquette;                 /* usqcdInfo (or grid-format) carried them    */
+  double plaquette, link_trace;      /* from the file                              */
+  double plaquette_computed, link_trace_computed;
+  int64_t data_offset, data_bytes;   /* the ildg-binary-data record                */
+} gb_ildg_header;
+/* the records only (no GPU work) */
+int gb_ildg_read_header(const char* path, gb_ildg_header* h);
+/* IldgReader::readConfiguration into canonical U[site][mu][3][3] (host, or device memory
+ * with on_device); check != 0 returns GB_ERR_IO when the checksum record is missing or
+ * differs, or the plaquette / link trace differ from the file's by >= 1e-5 (Grid asserts) */
+int gb_ildg_read(const char* path, double* U, int on_device, gb_ildg_header* h, int check);
+/* IldgWriter::writeConfiguration: precision 32 or 64; lfn may be NULL */
+int gb_ildg_write(const char* path, const double* U, int on_device, const int dims[4], int precision, const char* lfn);
+
 /* WilsonLoops::avgPlaquette and linkTrace (Grid/qcd/utils/WilsonLoops.h:88-126,203-218) */
 int gb_gauge_stats(const int dims[4], const double* U, int on_device, double* plaquette, double* link_trace);
 
