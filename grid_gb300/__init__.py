@@ -7,7 +7,8 @@ raises if it has not been built: there is no CPU fallback.
 """
 from .api import (  # noqa: F401
     GridError, lib, LIB_PATH, F64, F32, F16, RECON12, EVEN, ODD, FULL, DaggerNo, DaggerYes,
-    FermionField, WilsonFermion, MobiusFermion, ZMobiusFermion, MdagMLinearOperator, SchurDiagMooeeOperator,
+    FermionField, WilsonFermion, MobiusFermion, ZMobiusFermion, MobiusZolotarevFermion, ShamirZolotarevFermion,
+    ScaledShamirFermion, zolotarev, higham, MdagMLinearOperator, SchurDiagMooeeOperator,
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
     NerscHeader, nersc_read_header, nersc_read, nersc_write, gauge_stats,

@@ -77,6 +77,7 @@ _proto("gb_version", [])
 _proto("gb_wilson_create", [_ip, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
 _proto("gb_mobius_create", [_ip, _i, _d, _d, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
 _proto("gb_zmobius_create", [_ip, _i, _d, _d, _dp, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
+_proto("gb_zolotarev", [_d, _i, _i, _dp, _dp])
 _proto("gb_op_destroy", [_vp])
 _proto("gb_op_import_gauge", [_vp, _dp])
 _proto("gb_op_import_gauge_device", [_vp, _vp])
@@ -606,6 +607,47 @@ class ZMobiusFermion(MobiusFermion):
         _check(lib.gb_zmobius_create(_dims(dims), len(self.gamma), float(mf), float(M5), _dptr(gm), float(b), float(c),
                                      _dptr(ph), int(precision), int(nrhs), _vp(stream or 0), int(flags), C.byref(h)))
         self._finish(h, U, stream)
+
+
+def zolotarev(epsilon, n, type=0):
+    """Approx::zolotarev (Zolotarev.cc:296-417): (gamma, Delta) -- the Cayley-form zeros of
+    the optimal rational approximation to sgn(x) on epsilon <= |x| <= 1 and its maximum
+    error."""
+    gamma = np.empty(int(n), dtype=np.float64)
+    delta = C.c_double()
+    _check(lib.gb_zolotarev(float(epsilon), int(n), int(type), _dptr(gamma), C.byref(delta)))
+    return gamma, delta.value
+
+
+def higham(epsilon, n):
+    """Approx::higham (Zolotarev.cc:429-531): the tanh approximation; its Cayley zeros are
+    all 1 (the Moebius operator)."""
+    return np.ones(int(n), dtype=np.float64)
+
+
+class MobiusZolotarevFermion(ZMobiusFermion):
+    """MobiusZolotarevFermion(U, ..., mf, M5, b, c, lo, hi) (MobiusZolotarevFermion.h:45-70):
+    the Cayley operator with omega_s = hi * gamma_s of zolotarev(lo / hi, Ls, 0)."""
+
+    def __init__(self, U, dims, Ls, mf, M5, b, c, lo, hi, phases=None, precision=F64, nrhs=1, stream=None, flags=0):
+        gamma, self.Delta = zolotarev(float(lo) / float(hi), Ls, 0)
+        super().__init__(U, dims, list(float(hi) * gamma), mf, M5, b, c, phases, precision, nrhs, stream, flags)
+
+
+class ShamirZolotarevFermion(MobiusZolotarevFermion):
+    """ShamirZolotarevFermion(U, ..., mf, M5, lo, hi) (ShamirZolotarevFermion.h): b = 1, c = 0."""
+
+    def __init__(self, U, dims, Ls, mf, M5, lo, hi, phases=None, precision=F64, nrhs=1, stream=None, flags=0):
+        super().__init__(U, dims, Ls, mf, M5, 1.0, 0.0, lo, hi, phases, precision, nrhs, stream, flags)
+
+
+class ScaledShamirFermion(MobiusFermion):
+    """ScaledShamirFermion(U, ..., mf, M5, scale) (ScaledShamirFermion.h): Moebius with
+    b + c = scale, b - c = 1."""
+
+    def __init__(self, U, dims, Ls, mf, M5, scale, phases=None, precision=F64, nrhs=1, stream=None, flags=0):
+        super().__init__(U, dims, Ls, mf, M5, 0.5 * (scale + 1.0), 0.5 * (scale - 1.0), phases, precision, nrhs, stream,
+                         flags)
 
 
 # ---- linear operators and solvers -----------------------------------------------------

@@ -73,6 +73,14 @@ int gb_wilson_create(const int dims[4], double mass, const double* phases, int p
                      unsigned flags, gb_op_t* out);
 int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,
                      int precision, int nrhs, void* stream, unsigned flags, gb_op_t* out);
+/* Approx::zolotarev(epsilon, n, type) (Grid/algorithms/approx/Zolotarev.cc:296-417): the
+ * Cayley-form zeros gamma[0..n-1] of Zolotarev's optimal approximation to sgn(x) on
+ * epsilon <= |x| <= 1 (type 0: R(0) = 0, type 1: R(0) = infinity) and its maximum error
+ * (delta may be NULL).  MobiusZolotarevFermion(mf, M5, b, c, lo, hi) is the Cayley operator
+ * with omega_s = hi * gamma_s of zolotarev(lo / hi, Ls, 0) (MobiusZolotarevFermion.h:45-70,
+ * CayleyFermion5DImplementation.h:411-445): gb_zmobius_create with that omega. */
+int gb_zolotarev(double epsilon, int n, int type, double* gamma, double* delta);
+
 /* ZMobiusFermion(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, gamma, b, c, ImplParams)
  * (Grid/qcd/action/fermion/ZMobiusFermion.h): complex omega_s = gamma[s] (Ls complex
  * numbers as re, im), hence complex Cayley coefficients.  FP64 or FP32; Ls even, 2..16,

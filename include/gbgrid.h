@@ -604,6 +604,89 @@ typedef MobiusFermion<WilsonImplD> MobiusFermionD;
 typedef MobiusFermion<WilsonImplF> MobiusFermionF;
 typedef MobiusFermion<WilsonImplH> MobiusFermionH;
 typedef MobiusFermionD MobiusFermionR;
+
+// ---- Approx::zolotarev / higham (Grid/algorithms/approx/Zolotarev.h): the fields the
+// Cayley operators use (gamma, n, Delta, epsilon, type) ----------------------------------
+namespace Approx {
+struct zolotarev_data {
+  double* gamma = nullptr;
+  double Delta = 0, epsilon = 0;
+  int n = 0, type = 0;
+};
+inline zolotarev_data* zolotarev(double epsilon, int n, int type) {
+  zolotarev_data* z = new zolotarev_data;
+  z->gamma = new double[n];
+  z->n = n;
+  z->type = type;
+  z->epsilon = epsilon;
+  const int rc = gb_zolotarev(epsilon, n, type, z->gamma, &z->Delta);
+  if (rc != GB_OK) {
+    delete[] z->gamma;
+    delete z;
+    gbdetail::check(rc, "Approx::zolotarev");
+  }
+  return z;
+}
+// the tanh approximation: every Cayley zero is 1 (Zolotarev.cc:429-531)
+inline zolotarev_data* higham(double epsilon, int n) {
+  zolotarev_data* z = new zolotarev_data;
+  z->gamma = new double[n];
+  for (int i = 0; i < n; i++) z->gamma[i] = 1.0;
+  z->n = n;
+  z->epsilon = epsilon;
+  return z;
+}
+inline void zolotarev_free(zolotarev_data* z) {
+  if (z) {
+    delete[] z->gamma;
+    delete z;
+  }
+}
+}  // namespace Approx
+// MobiusZolotarevFermion / ShamirZolotarevFermion (MobiusZolotarevFermion.h:45-70,
+// ShamirZolotarevFermion.h): omega_s = hi * gamma_s of Approx::zolotarev(lo / hi, Ls, 0)
+// (CayleyFermion5DImplementation.h:445-447), through the complex-coefficient operator
+namespace gbdetail {
+inline std::vector<ComplexD> zolotarev_omega(int Ls, RealD lo, RealD hi) {
+  Approx::zolotarev_data* z = Approx::zolotarev(lo / hi, Ls, 0);
+  std::vector<ComplexD> w(Ls);
+  for (int s = 0; s < Ls; s++) w[s] = ComplexD(hi * z->gamma[s], 0.0);
+  Approx::zolotarev_free(z);
+  return w;
+}
+}  // namespace gbdetail
+template <class Impl> class MobiusZolotarevFermion : public ZMobiusFermion<Impl> {
+ public:
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  MobiusZolotarevFermion(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                         GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
+                         RealD b_, RealD c_, RealD lo, RealD hi, const ImplParams& p = ImplParams())
+      : ZMobiusFermion<Impl>(U, FiveDimGrid, FiveDimRedBlackGrid, FourDimGrid, FourDimRedBlackGrid, mass, M5_,
+                             gbdetail::zolotarev_omega(FiveDimGrid.Ls, lo, hi), b_, c_, p) {}
+};
+template <class Impl> class ShamirZolotarevFermion : public MobiusZolotarevFermion<Impl> {
+ public:
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  ShamirZolotarevFermion(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                         GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
+                         RealD lo, RealD hi, const ImplParams& p = ImplParams())
+      : MobiusZolotarevFermion<Impl>(U, FiveDimGrid, FiveDimRedBlackGrid, FourDimGrid, FourDimRedBlackGrid, mass, M5_,
+                                     1.0, 0.0, lo, hi, p) {}
+};
+// ScaledShamirFermion (ScaledShamirFermion.h): Moebius with b + c = scale, b - c = 1
+template <class Impl> class ScaledShamirFermion : public MobiusFermion<Impl> {
+ public:
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  ScaledShamirFermion(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                      GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
+                      RealD scale, const ImplParams& p = ImplParams())
+      : MobiusFermion<Impl>(U, FiveDimGrid, FiveDimRedBlackGrid, FourDimGrid, FourDimRedBlackGrid, mass, M5_,
+                            0.5 * (scale + 1.0), 0.5 * (scale - 1.0), p) {}
+};
+
 // Grid's ZWilsonImpl carries the complex Cayley coefficients in the action; here the
 // operator does, so the implementation tags are the Wilson ones
 typedef WilsonImplD ZWilsonImplD;
@@ -611,6 +694,12 @@ typedef WilsonImplF ZWilsonImplF;
 typedef ZMobiusFermion<ZWilsonImplD> ZMobiusFermionD;
 typedef ZMobiusFermion<ZWilsonImplF> ZMobiusFermionF;
 typedef ZMobiusFermionD ZMobiusFermionR;
+typedef MobiusZolotarevFermion<WilsonImplD> MobiusZolotarevFermionD;
+typedef MobiusZolotarevFermion<WilsonImplF> MobiusZolotarevFermionF;
+typedef ShamirZolotarevFermion<WilsonImplD> ShamirZolotarevFermionD;
+typedef ShamirZolotarevFermion<WilsonImplF> ShamirZolotarevFermionF;
+typedef ScaledShamirFermion<WilsonImplD> ScaledShamirFermionD;
+typedef ScaledShamirFermion<WilsonImplF> ScaledShamirFermionF;
 
 // ---- linear operators (Grid/algorithms/LinearOperator.h:44-105,286-349) --------------
 template <class Field> class LinearOperatorBase {

@@ -242,6 +242,20 @@ int main() {
   expect(std::sqrt(norm2(tmp) / norm2(src)) < 1e-9, "ZMobius Schur solve |M x - b| / |b|",
          std::sqrt(norm2(tmp) / norm2(src)));
 
+  // ---- Zolotarev Cayley operator (MobiusZolotarevFermion.h) ----
+  {
+    Approx::zolotarev_data* z = Approx::zolotarev(0.1, Ls, 0);
+    const bool zok = z->n == Ls && z->Delta > 0 && z->Delta < 1e-2;
+    Approx::zolotarev_free(z);
+    MobiusZolotarevFermionD Dzolo(Umu, *FGrid, *FrbGrid, *UGrid, *UrbGrid, mass, M5, b, c, 0.1, 2.0, params);
+    sol = Zero();
+    SchurSolver(Dzolo, src, sol);
+    Dzolo.M(sol, tmp);
+    tmp = tmp - src;
+    const RealD rz = std::sqrt(norm2(tmp) / norm2(src));
+    expect(zok && rz < 1e-9, "MobiusZolotarev Schur solve |M x - b| / |b|", rz);
+  }
+
   // ---- errors come back as exceptions ----
   bool threw = false;
   try {

@@ -82,3 +82,26 @@ def test_zmobius_rejects_fp16(gpu_available):
     op, _ = pair(g.F64)
     with pytest.raises(g.GridError):
         op.cayley_coeffs()
+
+
+def test_zolotarev_and_scaled_shamir_operators(gpu_available):
+    """MobiusZolotarevFermion = the Cayley operator with omega_s = hi * gamma_s of
+    zolotarev(lo / hi, Ls, 0); ScaledShamirFermion = Moebius with b + c = scale, b - c = 1:
+    both against the oracle, and a Schur solve of the Zolotarev operator."""
+    U = g.random_gauge(DIMS, 0.5, 61)
+    Ls, lo, hi = 8, 0.1, 2.0
+    op = g.MobiusZolotarevFermion(U, DIMS, Ls, 0.05, M5, 1.5, 0.5, lo, hi)
+    gamma, _ = g.zolotarev(lo / hi, Ls)
+    ref = o.OracleOp(2, 0, DIMS, Ls, zparams(0.05, M5, 1.5, 0.5, list(hi * gamma)), U, g.antiperiodic_t())
+    x = fermion(VOL, Ls, 68)
+    fin, fout = op.FermionField().import_(x), op.FermionField()
+    for name, code in (("M", o.OP_M), ("Mdag", o.OP_MDAG)):
+        getattr(op, name)(fin, fout)
+        assert o.rel_l2(fout.export(), ref.apply(code, x)) < 1e-12, name
+    fx = op.FermionField().zero()
+    g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-10, 5000))(op, fin, fx)
+    assert o.rel_l2(ref.apply(o.OP_M, fx.export()), x) < 1e-9
+    sh = g.ScaledShamirFermion(U, DIMS, Ls, 0.05, M5, 2.0)
+    ref2 = o.OracleOp(1, 0, DIMS, Ls, [0.05, M5, 1.5, 0.5], U, g.antiperiodic_t())
+    sh.M(fin, fout)
+    assert o.rel_l2(fout.export(), ref2.apply(o.OP_M, x)) < 1e-13
