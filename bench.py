@@ -339,7 +339,8 @@ def run_gpu(args, ws, rank, local, dist):
     }
     if ws == 1 and not args.no_extras:
         extras = {}
-        for name, fn in (("cg_schur_24^4xLs12", lambda: extra_cg_schur(g)),
+        for name, fn in (("wilson_8^4_cg", lambda: extra_wilson_cg(g)),
+                         ("cg_schur_24^4xLs12", lambda: extra_cg_schur(g)),
                          ("multi_rhs_wilson_32^3x64", lambda: extra_multi_rhs(g)),
                          ("serving", lambda: extra_serving(g, max_requests=args.serve_requests,
                                                            seconds=args.serve_seconds))):
@@ -401,10 +402,76 @@ def extra_cg_schur(g, fp64_maxit=20000):
     from oracle import oracle as o
     m32["solution_rel_err_vs_fp64"] = o.rel_l2(x32, x64)
     m16["solution_rel_err_vs_fp64"] = o.rel_l2(x16, x64)
+    # bounded CPU baseline: one FP64 MpcDagMpc of the oracle on the host cores, times the
+    # FP64 iteration count
+    ref = o.OracleOp(1, 0, dims, Ls, [mf, M5, B, C], U, g.antiperiodic_t())
+    o.set_threads(os.cpu_count() or 1)
+    xh = g.random_gaussian(vol // 2 * Ls * 12, 79)
+    t0 = time.perf_counter()
+    ref.apply(o.OP_MPCDAGMPC, xh, 1)
+    per_it = time.perf_counter() - t0
+    out["cpu_oracle"] = {"seconds_per_iteration": per_it, "cores": os.cpu_count(),
+                         "solve_estimate_seconds": per_it * f64["iterations"],
+                         "sample": "one FP64 MpcDagMpc of the 24^4 x 12 operator, scaled by the FP64 CG iterations"}
     out.update({"mixed_fp32": m32, "mixed_fp16": m16, "mixed_fp32_batched4": mb, "fp64": f64,
                 "speedup_mixed_vs_fp64": m32["solves_per_s"] / f64["solves_per_s"],
                 "speedup_mixed_batched_vs_fp64": mb["solves_per_s"] / f64["solves_per_s"]})
     return out
+
+
+def extra_wilson_cg(g):
+    """Wilson 8^4 (antiperiodic t), FP64, m = 0.1, gauge eps = 0.3: one full Dhop and an
+    unpreconditioned CG on MdagM to 1e-8 -- on the GPU and, for the same field and source,
+    on the host cores with the oracle (the reference's CPU-runnable configuration)."""
+    from oracle import oracle as o
+    dims, mass = (8, 8, 8, 8), 0.1
+    vol = int(np.prod(dims))
+    U = g.random_gauge(dims, 0.3, 1001)
+    src = g.random_gaussian(vol * 12, 1002)
+    op = g.WilsonFermion(U, dims, mass, precision=g.F64)
+    fin, fout = op.FermionField().import_(src), op.FermionField()
+    for _ in range(20):
+        op.Dhop(fin, fout, 0)
+    reps = 500
+    op.sync()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        op.Dhop(fin, fout, 0)
+    op.sync()
+    gpu_dhop = (time.perf_counter() - t0) / reps
+    fx = op.FermionField()
+
+    def gpu_solve(graphs):
+        fx.zero()
+        cg = g.ConjugateGradient(1e-8, 10000, use_graphs=graphs)
+        op.sync()
+        t0 = time.perf_counter()
+        r = cg(g.MdagMLinearOperator(op), fin, fx)
+        op.sync()
+        return time.perf_counter() - t0, r
+
+    gpu_solve(0)  # the operator's first solve allocates its workspace fields
+    gpu_solve(1)
+    gpu_cg_plain, _ = gpu_solve(0)
+    gpu_cg, r = gpu_solve(1)
+    ref = o.OracleOp(0, 0, dims, 1, [mass], U, g.antiperiodic_t())
+    o.set_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    for _ in range(20):
+        ref.apply(o.OP_DHOP, src)
+    cpu_dhop = (time.perf_counter() - t0) / 20
+    t0 = time.perf_counter()
+    psi, cpu_it, cpu_res = ref.cg(0, src, 1e-8, 10000)
+    cpu_cg = time.perf_counter() - t0
+    return {"workload": "wilson_8^4_m0.1_fp64_dhop_and_unprec_cg_1e-8",
+            "gpu": {"dhop_us": gpu_dhop * 1e6, "cg_seconds": gpu_cg, "iterations": int(r.iterations),
+                    "true_residual": float(r.true_residual), "cg_seconds_without_graphs": gpu_cg_plain,
+                    "note": "warm operator; iteration chunks captured as CUDA graphs (use_graphs=1)"},
+            "cpu_oracle": {"dhop_us": cpu_dhop * 1e6, "cg_seconds": cpu_cg, "iterations": int(cpu_it),
+                           "true_residual": float(cpu_res), "cores": os.cpu_count()},
+            "solution_rel_diff_gpu_vs_cpu": float(o.rel_l2(fx.export(), psi)),
+            "cg_speedup_gpu_vs_cpu": cpu_cg / gpu_cg,
+            "note": "8^4 is 4096 sites: launch- and latency-bound on the GPU"}
 
 
 def extra_multi_rhs(g):
