@@ -361,7 +361,8 @@ def extra_cg_schur(g, fp64_maxit=20000):
     """Mixed-precision SchurRedBlack CG on Moebius DWF 24^4 x Ls=12, mf=0.005, gauge eps=0.6,
     to a true residual of 1e-10: FP32 inner, FP16-stored inner (FP32 norms/arithmetic), a
     4-RHS batched mixed solve, and the plain FP64 CG.  Reliable updates every 100
-    iterations or when |r|^2 drops by 1e-6 (|r| by 1e-3)."""
+    iterations or when |r|^2 drops by 1e-6 (|r| by 1e-3).  Every solve captures its
+    iteration chunks as CUDA graphs (use_graphs=1)."""
     dims, Ls, mf = (24, 24, 24, 24), 12, 0.005
     U = g.random_gauge(dims, 0.6, 3003)
     vol = int(np.prod(dims))
@@ -373,14 +374,14 @@ def extra_cg_schur(g, fp64_maxit=20000):
         fs = od.FermionField().import_(src)
         fx = od.FermionField().zero()
         if inner is None:
-            cg = g.ConjugateGradient(1e-10, fp64_maxit, err_on_no_conv=False, check_every=20)
+            cg = g.ConjugateGradient(1e-10, fp64_maxit, err_on_no_conv=False, check_every=20, use_graphs=1)
             solver = g.SchurRedBlackDiagMooeeSolve(cg)
             keep = None
         else:
             of = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=inner, nrhs=nrhs)
             cg = g.ConjugateGradientReliableUpdate(1e-10, 30000, 1e-6, g.SchurDiagMooeeOperator(of),
                                                    g.SchurDiagMooeeOperator(od), relup_every=100,
-                                                   err_on_no_conv=False, check_every=20)
+                                                   err_on_no_conv=False, check_every=20, use_graphs=1)
             solver = g.SchurRedBlackDiagMooeeSolve(cg)
             keep = of
         od.sync()
@@ -563,6 +564,25 @@ def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0):
             "budget_gb": budget_gb}
 
 
+def cg_profile(g, iters):
+    """For a profiler's launch list, not a measurement: the mixed FP32 Schur CG of the
+    24^4 x Ls12 workload stopped after `iters` inner iterations (one reliable update at
+    iteration 100 when iters > 100, no final cleanup)."""
+    dims, Ls, mf = (24, 24, 24, 24), 12, 0.005
+    U = g.random_gauge(dims, 0.6, 3003)
+    vol = int(np.prod(dims))
+    od = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=g.F64)
+    of = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=g.F32)
+    fs = od.FermionField().import_(g.random_gaussian(vol * Ls * 12, 77))
+    fx = od.FermionField().zero()
+    cg = g.ConjugateGradientReliableUpdate(1e-10, iters, 1e-6, g.SchurDiagMooeeOperator(of),
+                                           g.SchurDiagMooeeOperator(od), relup_every=100, err_on_no_conv=False,
+                                           final_cleanup=False, check_every=20)
+    r = g.SchurRedBlackDiagMooeeSolve(cg)(od, fs, fx)
+    od.sync()
+    print(json.dumps({"cg_profile": "mobius_dwf_24^4xLs12_mixed_fp32", "iterations": int(r.iterations)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -572,7 +592,13 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="only the headline DhopEO/DhopOE measurement")
     ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving stream to replay")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the seeded arrival stream")
+    ap.add_argument("--cg-profile", type=int, default=0, metavar="ITERS",
+                    help="run only ITERS iterations of the 24^4 x 12 mixed CG (for a profiler's launch list)")
     args = ap.parse_args()
+    if args.cg_profile:
+        import grid_gb300 as g
+        cg_profile(g, args.cg_profile)
+        return
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -25,7 +25,8 @@ namespace gb {
 
 // columns per CTA and the shared-memory slot of one column (an odd number of float4, so
 // the column reads of a quarter warp fall on distinct banks)
-template <int LS> __host__ __device__ constexpr int col_q() { return LS >= 16 ? 16 : 32; }
+// (with two input tiles 16 columns, so that several CTAs fit an SM's shared memory)
+template <int LS, int NIN = 1> __host__ __device__ constexpr int col_q() { return (LS >= 16 || NIN > 1) ? 16 : 32; }
 template <int LS> __host__ __device__ constexpr int col_stride() { return (LS / 2) % 2 == 0 ? LS / 2 + 1 : LS / 2; }
 
 template <int LS> struct ColCoef {
@@ -48,11 +49,11 @@ struct ColParams {
 
 // stage one input into the [12][Q][ST] float4 tile: FP32 copies the vectors, FP16 decodes
 // the two components of each vector with the norms of the pair's sites
-template <class T, int LS> struct ColIO;
-template <int LS> struct ColIO<float, LS> {
+template <class T, int LS, int Q> struct ColIO;
+template <int LS, int Q> struct ColIO<float, LS, Q> {
   static __device__ __forceinline__ void load(const void* src, const float*, float*, float4* tile, size_t np, size_t q0,
                                               int nv) {
-    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    constexpr int H = LS / 2, ST = col_stride<LS>();
     const float4* x = static_cast<const float4*>(src);
 #pragma unroll 4
     for (int e = threadIdx.x; e < 12 * Q * H; e += 12 * Q) {
@@ -64,7 +65,7 @@ template <int LS> struct ColIO<float, LS> {
     }
   }
   static __device__ __forceinline__ void store(void* dst, float*, float*, float4* tile, size_t np, size_t q0, int nv) {
-    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    constexpr int H = LS / 2, ST = col_stride<LS>();
     float4* o = static_cast<float4*>(dst);
 #pragma unroll 4
     for (int e = threadIdx.x; e < 12 * Q * H; e += 12 * Q) {
@@ -76,11 +77,11 @@ template <int LS> struct ColIO<float, LS> {
     }
   }
 };
-template <int LS> struct ColIO<__half, LS> {
+template <int LS, int Q> struct ColIO<__half, LS, Q> {
   // snorm: Q * LS floats of shared memory for the CTA's site norms
   static __device__ __forceinline__ void load(const void* src, const float* norms, float* snorm, float4* tile,
                                               size_t np, size_t q0, int nv) {
-    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    constexpr int H = LS / 2, ST = col_stride<LS>();
     for (int e = threadIdx.x; e < 2 * nv; e += 12 * Q) snorm[e] = __ldg(norms + q0 * LS + e);
     __syncthreads();
     const uint4* x = static_cast<const uint4*>(src);
@@ -101,7 +102,7 @@ template <int LS> struct ColIO<__half, LS> {
   }
   static __device__ __forceinline__ void store(void* dst, float* norms, float* snorm, float4* tile, size_t np,
                                                size_t q0, int nv) {
-    constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+    constexpr int H = LS / 2, ST = col_stride<LS>();
     // the norm of each 5D site: the largest |re|, |im| over its 12 components
     for (int e = threadIdx.x; e < 2 * nv; e += 12 * Q) {
       const int qq = e / LS, sl = e - qq * LS, m = sl >> 1, l = sl & 1;
@@ -195,8 +196,9 @@ __device__ __forceinline__ void col_read(const float4* slot, float (&r)[LS], flo
 }
 
 template <class T, int LS, bool DAG, int OPA, int OPB>
-__global__ void __launch_bounds__(12 * col_q<LS>()) col_kernel(const ColParams p, const ColCoef<LS> c) {
-  constexpr int Q = col_q<LS>(), H = LS / 2, ST = col_stride<LS>();
+__global__ void __launch_bounds__(12 * col_q<LS, OPB != COLB_NONE ? 2 : 1>()) col_kernel(const ColParams p,
+                                                                                        const ColCoef<LS> c) {
+  constexpr int Q = col_q<LS, OPB != COLB_NONE ? 2 : 1>(), H = LS / 2, ST = col_stride<LS>();
   extern __shared__ float4 col_tile[];  // [inputs][12][Q][ST], then Q * LS norms (FP16)
   float4* tx = col_tile;
   float4* ty = col_tile + 12 * Q * ST;
@@ -205,8 +207,8 @@ __global__ void __launch_bounds__(12 * col_q<LS>()) col_kernel(const ColParams p
   const size_t q0 = size_t(blockIdx.x) * Q;
   const int qn = p.nq - q0 < size_t(Q) ? int(p.nq - q0) : Q;
   const int nv = qn * H;  // vectors of one plane in this CTA
-  ColIO<T, LS>::load(p.x, p.xn, snorm, tx, p.np, q0, nv);
-  if (OPB != COLB_NONE) ColIO<T, LS>::load(p.y, p.yn, snorm, ty, p.np, q0, nv);
+  ColIO<T, LS, Q>::load(p.x, p.xn, snorm, tx, p.np, q0, nv);
+  if (OPB != COLB_NONE) ColIO<T, LS, Q>::load(p.y, p.yn, snorm, ty, p.np, q0, nv);
   __syncthreads();
   const int k = t / Q, qq = t - k * Q;
   if (qq < qn) {
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(12 * col_q<LS>()) col_kernel(const ColParams p
     for (int m = 0; m < H; m++) slot[m] = make_float4(orr[2 * m], orr[2 * m + 1], oi[2 * m], oi[2 * m + 1]);
   }
   __syncthreads();
-  ColIO<T, LS>::store(p.out, p.outn, snorm, tx, p.np, q0, nv);
+  ColIO<T, LS, Q>::store(p.out, p.outn, snorm, tx, p.np, q0, nv);
 }
 
 template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost& h, ColCoef<LS>& c) {
@@ -266,7 +268,7 @@ template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost
 
 template <class T, int LS, bool DAG, int OPA, int OPB>
 static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
-  constexpr int Q = col_q<LS>();
+  constexpr int Q = col_q<LS, OPB != COLB_NONE ? 2 : 1>();
   const size_t smem = size_t(OPB != COLB_NONE ? 2 : 1) * 12 * Q * col_stride<LS>() * sizeof(float4) +
                       (sizeof(T) == 2 ? size_t(Q) * LS * sizeof(float) : 0);
   static std::atomic<bool> configured{false};
