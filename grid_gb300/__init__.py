@@ -9,7 +9,8 @@ from .api import (  # noqa: F401
     GridError, lib, LIB_PATH, F64, F32, F16, RECON12, EVEN, ODD, FULL, DaggerNo, DaggerYes,
     FermionField, WilsonFermion, MobiusFermion, ZMobiusFermion, MobiusZolotarevFermion, ShamirZolotarevFermion,
     ScaledShamirFermion, zolotarev, higham, MdagMLinearOperator, SchurDiagMooeeOperator,
-    ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve,
+    ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve, MixedPrecisionConjugateGradient,
+    MixedPrecisionConjugateGradientBatched, MixedParams,
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
     NerscHeader, nersc_read_header, nersc_read, nersc_write, gauge_stats,
     IldgHeader, ildg_read_header, ildg_read, ildg_write,

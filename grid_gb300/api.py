@@ -754,6 +754,53 @@ class ConjugateGradientReliableUpdate(ConjugateGradient):
         return r
 
 
+class MixedParams(C.Structure):
+    _fields_ = [("inner_tolerance", C.c_double), ("max_inner_iterations", C.c_int), ("max_outer_iterations", C.c_int),
+                ("max_patchup_iterations", C.c_int), ("outer_loop_norm_mult", C.c_double)]
+
+
+_proto("gb_mixed_params_default", [C.POINTER(MixedParams)], None)
+_proto("gb_cg_mixed", [_vp, _vp, _i, _vp, _vp, C.POINTER(CGParams), C.POINTER(MixedParams), C.POINTER(CGResult)])
+
+
+class MixedPrecisionConjugateGradient:
+    """MixedPrecisionConjugateGradient(tol, maxinnerit, maxouterit, sp_grid, Linop_f, Linop_d)
+    (ConjugateGradientMixedPrec.h:34-166): restarted FP32 inner CGs on Linop_f, FP64 outer
+    residuals and a final FP64 patch-up CG on Linop_d.  With nrhs > 1 operators it is
+    MixedPrecisionConjugateGradientBatched (every right-hand side in one inner solve)."""
+
+    def __init__(self, tol, maxinnerit, maxouterit, sp_grid, linop_f, linop_d, maxpatchit=0, check_every=None,
+                 use_graphs=0):
+        self.Tolerance, self.InnerTolerance = float(tol), float(tol)
+        self.MaxInnerIterations, self.MaxOuterIterations = int(maxinnerit), int(maxouterit)
+        self.MaxPatchupIterations = int(maxpatchit)
+        self.OuterLoopNormMult = 100.0
+        self.linop_f, self.linop_d = linop_f, linop_d
+        self.check_every, self.use_graphs = check_every, int(use_graphs)
+        self.TotalInnerIterations = self.TotalOuterIterations = self.TotalFinalStepIterations = 0
+        self.TrueResidual = 0.0
+
+    def __call__(self, src, sol):
+        if self.linop_f.kind != self.linop_d.kind:
+            raise GridError(1, "Linop_f and Linop_d must be the same kind of operator")
+        p, r = _params(self.Tolerance, 1, True, check_every=self.check_every, use_graphs=self.use_graphs), CGResult()
+        m = MixedParams()
+        lib.gb_mixed_params_default(C.byref(m))
+        m.inner_tolerance = self.InnerTolerance
+        m.max_inner_iterations, m.max_outer_iterations = self.MaxInnerIterations, self.MaxOuterIterations
+        m.max_patchup_iterations = self.MaxPatchupIterations
+        m.outer_loop_norm_mult = self.OuterLoopNormMult
+        _check(lib.gb_cg_mixed(self.linop_d.op.h, self.linop_f.op.h, self.linop_d.kind, src.h, sol.h, C.byref(p),
+                               C.byref(m), C.byref(r)))
+        self.TotalInnerIterations, self.TotalOuterIterations = r.iterations, r.reliable_updates
+        self.TotalFinalStepIterations, self.TrueResidual = r.cleanup_iterations, r.true_residual
+        self.result = r
+        return r
+
+
+MixedPrecisionConjugateGradientBatched = MixedPrecisionConjugateGradient
+
+
 MAX_SHIFTS = 32
 
 

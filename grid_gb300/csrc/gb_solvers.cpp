@@ -417,6 +417,71 @@ static int solve_checks(gb_op_t op, gb_field_t a, gb_field_t b, const gb_cg_para
   return GB_OK;
 }
 
+// MixedPrecisionConjugateGradient (ConjugateGradientMixedPrec.h:68-166) and, with
+// nrhs > 1 operators, its batched form (ConjugateGradientMixedPrecBatched.h:37-209) with
+// all right-hand sides in one inner multi-RHS CG.  Outer loop: r = src - A psi in FP64;
+// stop when |r|^2 < outer_mult * tol^2 |src|^2 for every right-hand side; raise the inner
+// tolerance until |r|^2 t^2 >= tol^2 |src|^2; solve A e = r in FP32 from zero to t (the
+// smallest over right-hand sides); psi += e.  Then an FP64 CG from psi to tol.
+static int cg_mixed(Op* od, Op* of, int kind, Field* src, Field* psi, const gb_cg_params* P, const gb_mixed_params* M,
+             gb_cg_result* R) {
+  Timer tm;
+  const int n = od->nrhs_user;
+  if (of->nrhs != od->nrhs || of->n5() != od->n5()) { set_error("mixed CG: operators differ in shape"); return GB_ERR_BAD_ARG; }
+  cudaStream_t saved = of->stream;
+  of->stream = od->stream;
+  struct Restore { Op* o; cudaStream_t s; ~Restore() { o->stream = s; } } restore{of, saved};
+  Field *tmp_d, *res_d, *src_f, *sol_f;
+  GB_TRY(field_for(od, kind, GB_ODD, GB_F64, WS_CG_T, WS_FCG_T, &tmp_d));
+  GB_TRY(field_for(od, kind, GB_ODD, GB_F64, WS_CG_R, WS_FCG_R, &res_d));
+  GB_TRY(field_for(of, kind, GB_ODD, of->prec, WS_RU_RF, WS_FRU_RF, &src_f));
+  GB_TRY(field_for(of, kind, GB_ODD, of->prec, WS_RU_XF, WS_FRU_XF, &sol_f));
+  if (!src->full()) tmp_d->subset = res_d->subset = src_f->subset = sol_f->subset = src->subset;
+  const double tol = P->tolerance;
+  const double mult = M->outer_loop_norm_mult > 0 ? M->outer_loop_norm_mult : 100.0;
+  std::vector<double> stop(od->nrhs), nr(od->nrhs), t(n, M->inner_tolerance > 0 ? M->inner_tolerance : tol);
+  GB_TRY(field_norm2(src, stop.data()));
+  for (double& v : stop) v *= tol * tol;
+  int total_inner = 0, outer = 0;
+  for (; outer < M->max_outer_iterations; outer++) {
+    GB_TRY(op_hermop(od, kind, psi, tmp_d));
+    GB_TRY(field_axpby(res_d, 1.0, -1.0, src, tmp_d));
+    GB_TRY(field_norm2(res_d, nr.data()));
+    bool done = true;
+    for (int i = 0; i < n; i++) done = done && nr[i] < mult * stop[i];
+    if (done) break;
+    double inner = 1.0;
+    for (int i = 0; i < n; i++) {
+      while (nr[i] * t[i] * t[i] < stop[i]) t[i] *= 2;
+      inner = std::min(inner, t[i]);
+    }
+    GB_TRY(field_copy(src_f, res_d));
+    GB_TRY(field_zero(sol_f));
+    gb_cg_params Pi = *P;
+    Pi.tolerance = inner;
+    Pi.max_iterations = M->max_inner_iterations;
+    Pi.err_on_no_conv = 0;
+    gb_cg_result Ri;
+    const int rc = cg_solve(of, kind, src_f, sol_f, &Pi, &Ri);
+    if (rc != GB_OK && rc != GB_ERR_NOT_CONVERGED) return rc;
+    total_inner += Ri.iterations;
+    GB_TRY(field_copy(tmp_d, sol_f));
+    GB_TRY(field_axpby(psi, 1.0, 1.0, psi, tmp_d));
+  }
+  gb_cg_params Pd = *P;
+  Pd.max_iterations = M->max_patchup_iterations > 0 ? M->max_patchup_iterations : M->max_inner_iterations;
+  gb_cg_result Rd;
+  const int rc = cg_solve(od, kind, src, psi, &Pd, &Rd);
+  R->iterations = total_inner;
+  R->reliable_updates = outer;
+  R->cleanup_iterations = Rd.iterations;
+  R->true_residual = Rd.true_residual;
+  R->converged = Rd.converged;
+  R->seconds = tm.seconds();
+  R->flops = hermop_flops(od, kind) * (total_inner + Rd.iterations + outer);
+  return rc;
+}
+
 static int finish(int rc, const gb_cg_params* p) {
   if (rc == GB_ERR_NOT_CONVERGED && !p->err_on_no_conv) return GB_OK;
   return rc;
@@ -456,6 +521,30 @@ int gb_cg_reliable(gb_op_t op_d, gb_op_t op_lo, int kind, gb_field_t src, gb_fie
   if (kind == 1) psi->subset = GB_ODD;
   SolveStream ss(op_d, op_lo, src, psi, p->use_graphs != 0);
   return finish(cg_reliable(op_d, op_lo, kind, src, psi, p, res), p);
+}
+
+void gb_mixed_params_default(gb_mixed_params* m) {
+  if (!m) return;
+  m->inner_tolerance = 0.0;
+  m->max_inner_iterations = 10000;
+  m->max_outer_iterations = 100;
+  m->max_patchup_iterations = 0;
+  m->outer_loop_norm_mult = 100.0;
+}
+
+int gb_cg_mixed(gb_op_t op_d, gb_op_t op_f, int kind, gb_field_t src, gb_field_t psi, const gb_cg_params* p,
+                const gb_mixed_params* m, gb_cg_result* res) {
+  GB_TRY(solve_checks(op_d, src, psi, p, res));
+  if (!m) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (!op_f || op_d->prec != GB_F64 || op_f->prec != GB_F32) { set_error("mixed CG: need FP64 op_d and FP32 op_f"); return GB_ERR_BAD_ARG; }
+  if (!op_f->gauge_loaded) { set_error("op_f has no gauge field"); return GB_ERR_BAD_ARG; }
+  if (kind != 0 && kind != 1) { set_error("kind must be 0 (MdagM) or 1 (MpcDagMpc)"); return GB_ERR_BAD_ARG; }
+  if (kind == 0 && (!src->full() || !psi->full())) { set_error("mixed CG: full fields expected"); return GB_ERR_BAD_PARITY; }
+  if (kind == 1 && src->subset != GB_ODD) { set_error("mixed CG: odd source expected"); return GB_ERR_BAD_PARITY; }
+  if (m->max_inner_iterations < 1 || m->max_outer_iterations < 0) { set_error("mixed CG: bad iteration limits"); return GB_ERR_BAD_ARG; }
+  if (kind == 1) psi->subset = GB_ODD;
+  SolveStream ss(op_d, op_f, src, psi, p->use_graphs != 0);
+  return finish(cg_mixed(op_d, op_f, kind, src, psi, p, m, res), p);
 }
 
 int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, const gb_cg_params* p, gb_cg_result* res,

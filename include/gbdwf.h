@@ -258,6 +258,27 @@ typedef struct {
 
 void gb_cg_params_default(gb_cg_params* p);
 
+/* MixedPrecisionConjugateGradient (ConjugateGradientMixedPrec.h:34-166): defect correction
+ * with restarted FP32 inner CGs.  Outer loop: r = src - A psi in FP64; stop when |r|^2 <
+ * outer_loop_norm_mult * tol^2 |src|^2; double the inner tolerance while |r|^2 t^2 <
+ * tol^2 |src|^2; solve A e = r in FP32 from zero to t within max_inner_iterations; psi +=
+ * e.  Then the final FP64 "patch-up" CG from psi to tol.  With nrhs > 1 operators this is
+ * MixedPrecisionConjugateGradientBatched (ConjugateGradientMixedPrecBatched.h:37-209),
+ * every right-hand side in one inner multi-RHS CG.  gb_cg_result: iterations =
+ * TotalInnerIterations, reliable_updates = TotalOuterIterations, cleanup_iterations =
+ * TotalFinalStepIterations, true_residual = TrueResidual.  p: tolerance, err_on_no_conv,
+ * check_every, use_graphs (max_iterations is unused). */
+typedef struct {
+  double inner_tolerance;      /* InnerTolerance (0: the outer tolerance)             */
+  int max_inner_iterations;    /* MaxInnerIterations                                  */
+  int max_outer_iterations;    /* MaxOuterIterations                                  */
+  int max_patchup_iterations;  /* MaxPatchupIterations (0: MaxInnerIterations)        */
+  double outer_loop_norm_mult; /* OuterLoopNormMult (Grid: 100)                        */
+} gb_mixed_params;
+void gb_mixed_params_default(gb_mixed_params* m);
+int gb_cg_mixed(gb_op_t op_d, gb_op_t op_f, int kind, gb_field_t src, gb_field_t psi, const gb_cg_params* p,
+                const gb_mixed_params* m, gb_cg_result* res);
+
 /* ConjugateGradient<Field>(MdagMLinearOperator) on a full field (Test_wilson_cg_unprec.cc) */
 int gb_cg_mdagm(gb_op_t op, gb_field_t src, gb_field_t psi, const gb_cg_params* p, gb_cg_result* res);
 /* ConjugateGradient<Field>(SchurDiagMooeeOperator) on an odd half field */

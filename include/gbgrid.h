@@ -883,6 +883,72 @@ template <class FieldD, class FieldF> class ConjugateGradientReliableUpdate : pu
   }
 };
 
+// MixedPrecisionConjugateGradient (ConjugateGradientMixedPrec.h:34-166): restarted FP32
+// inner CGs with FP64 outer residuals and a final FP64 patch-up CG.  Errors throw
+// (Grid asserts); the patch-up honours ErrorOnNoConverge of Grid's inner solvers (off).
+template <class FieldD, class FieldF> class MixedPrecisionConjugateGradient : public LinearFunction<FieldD> {
+ public:
+  RealD Tolerance, InnerTolerance;
+  Integer MaxInnerIterations, MaxOuterIterations, MaxPatchupIterations = 0;
+  RealD OuterLoopNormMult = 100.;
+  Integer TotalInnerIterations = 0, TotalOuterIterations = 0, TotalFinalStepIterations = 0;
+  RealD TrueResidual = 0;
+  bool UseGraphs = false;
+  LinearOperatorBase<FieldF>& Linop_f;
+  LinearOperatorBase<FieldD>& Linop_d;
+
+  MixedPrecisionConjugateGradient(RealD tol, Integer maxinnerit, Integer maxouterit, GridBase*,
+                                  LinearOperatorBase<FieldF>& lf, LinearOperatorBase<FieldD>& ld)
+      : Tolerance(tol), InnerTolerance(tol), MaxInnerIterations(maxinnerit), MaxOuterIterations(maxouterit),
+        Linop_f(lf), Linop_d(ld) {}
+
+  void operator()(const FieldD& src, FieldD& psi) override {
+    gb_op_t od = Linop_d.library_op(), of = Linop_f.library_op();
+    if (!od || !of || Linop_d.library_kind() != Linop_f.library_kind())
+      throw GridError(GB_ERR_UNSUPPORTED, "MixedPrecisionConjugateGradient: library operators of one kind expected");
+    gb_cg_params p;
+    gb_cg_params_default(&p);
+    p.tolerance = Tolerance;
+    p.err_on_no_conv = 0;
+    p.use_graphs = UseGraphs ? 1 : 0;
+    gb_mixed_params m;
+    gb_mixed_params_default(&m);
+    m.inner_tolerance = InnerTolerance;
+    m.max_inner_iterations = MaxInnerIterations;
+    m.max_outer_iterations = MaxOuterIterations;
+    m.max_patchup_iterations = MaxPatchupIterations;
+    m.outer_loop_norm_mult = OuterLoopNormMult;
+    gb_cg_result r;
+    const int rc = gb_cg_mixed(od, of, Linop_d.library_kind(), src.handle(), psi.handle(), &p, &m, &r);
+    TotalInnerIterations = r.iterations;
+    TotalOuterIterations = r.reliable_updates;
+    TotalFinalStepIterations = r.cleanup_iterations;
+    TrueResidual = r.true_residual;
+    gbdetail::check(rc, "MixedPrecisionConjugateGradient");
+  }
+};
+
+// MixedPrecisionConjugateGradientBatched (ConjugateGradientMixedPrecBatched.h:37-209):
+// the right-hand sides of a multi-RHS operator pair are solved together by the solver
+// above; the vector form solves them one after the other, as Grid's does
+template <class FieldD, class FieldF> class MixedPrecisionConjugateGradientBatched
+    : public MixedPrecisionConjugateGradient<FieldD, FieldF> {
+  typedef MixedPrecisionConjugateGradient<FieldD, FieldF> Base;
+
+ public:
+  MixedPrecisionConjugateGradientBatched(RealD tol, Integer maxinnerit, Integer maxouterit, Integer maxpatchit,
+                                         GridBase* g, LinearOperatorBase<FieldF>& lf, LinearOperatorBase<FieldD>& ld,
+                                         bool = true)
+      : Base(tol, maxinnerit, maxouterit, g, lf, ld) {
+    this->MaxPatchupIterations = maxpatchit;
+  }
+  using Base::operator();
+  void operator()(const std::vector<FieldD>& src, std::vector<FieldD>& sol) {
+    if (src.size() != sol.size()) throw GridError(GB_ERR_BAD_ARG, "MixedPrecisionConjugateGradientBatched: sizes differ");
+    for (size_t i = 0; i < src.size(); i++) Base::operator()(src[i], sol[i]);
+  }
+};
+
 // MultiShiftFunction (Grid/algorithms/approx/MultiShiftFunction.h:34-64): a partial-fraction
 // rational function f(x) = norm + sum_i residues[i] / (x + poles[i]).  The Remez
 // construction of Grid's AlgRemez is not part of this library: fill the arrays directly.

@@ -117,6 +117,20 @@ int main() {
               mCG.ReliableUpdatesPerformed, CG.IterationsToComplete);
   expect(std::sqrt(norm2(dpsi) / norm2(psi_d)) < 1e-8, "ReliableUpdate CG == FP64 CG", std::sqrt(norm2(dpsi) / norm2(psi_d)));
 
+  // ---- MixedPrecisionConjugateGradient (restarted FP32 inner CGs) ----
+  {
+    MixedPrecisionConjugateGradient<LatticeFermion, LatticeFermionF> rCG(1e-10, 10000, 50, FrbGrid, HermOpEO_f, HermOpEO);
+    LatticeFermion psi_m(FrbGrid);
+    psi_m = Zero();
+    psi_m.Checkerboard() = Odd;
+    rCG(src_o, psi_m);
+    LatticeFermion dm = psi_m - psi_d;
+    std::printf("mixed-precision CG: %d inner iterations, %d restarts, %d patch-up\n", rCG.TotalInnerIterations,
+                rCG.TotalOuterIterations, rCG.TotalFinalStepIterations);
+    expect(std::sqrt(norm2(dm) / norm2(psi_d)) < 1e-8 && rCG.TotalOuterIterations >= 1,
+           "MixedPrecisionConjugateGradient == FP64 CG", std::sqrt(norm2(dm) / norm2(psi_d)));
+  }
+
   // ---- user-defined operator: host-driven CG on device fields ----
   ShiftedMdagM<MobiusFermionD, LatticeFermion> Shifted(Ddwf, 0.5);
   ConjugateGradient<LatticeFermion> CGu(1e-10, 2000);
