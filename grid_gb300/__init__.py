@@ -16,6 +16,7 @@ from .api import (  # noqa: F401
     IldgHeader, ildg_read_header, ildg_read, ildg_write,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
     antiperiodic_t, periodic, set_device, PinnedArray, Stream, TransferQueue, norm2, innerProduct, axpy, axpby, axpy_norm,
+    axpby_norm, innerProductNorm, rankInnerProduct,
     pickCheckerboard, setCheckerboard, InsertSlice, ExtractSlice, ZeroGuesser, PauliVillarsSolverUnprec,
     PauliVillarsSolverRBprec, MADWF, MADWFinnerIterCallbackBase, Server, Request, make_request, request_bytes,
 )

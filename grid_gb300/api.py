@@ -413,6 +413,30 @@ def ExtractSlice(high: FermionField, slice_: int, orthog: int = 0):
     return out
 
 
+_proto("gb_field_axpby_norm", [_vp, _d, _d, _vp, _vp, _dp])
+_proto("gb_field_inner_norm", [_vp, _vp, _dp, _dp])
+
+
+def axpby_norm(z: FermionField, a: float, b: float, x: FermionField, y: FermionField):
+    """axpby_norm: z = a x + b y; returns |z|^2 per right-hand side."""
+    out = np.empty(z.op.nrhs, dtype=np.float64)
+    _check(lib.gb_field_axpby_norm(z.h, float(a), float(b), x.h, y.h, _dptr(out)))
+    return out
+
+
+def innerProductNorm(a: FermionField, b: FermionField):
+    """innerProductNorm: (<a|b>, |a|^2) per right-hand side."""
+    ip = np.empty(2 * a.op.nrhs, dtype=np.float64)
+    nr = np.empty(a.op.nrhs, dtype=np.float64)
+    _check(lib.gb_field_inner_norm(a.h, b.h, _dptr(ip), _dptr(nr)))
+    return ip[0::2] + 1j * ip[1::2], nr
+
+
+def rankInnerProduct(a: FermionField, b: FermionField):
+    """One process, one GPU: the rank-local inner product is the global one."""
+    return innerProduct(a, b)
+
+
 def pickCheckerboard(cb: int, half: FermionField, full: FermionField):
     half.checkerboard = cb
     _check(lib.gb_field_pick_checkerboard(half.h, full.h))

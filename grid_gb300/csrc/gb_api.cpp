@@ -1044,6 +1044,29 @@ int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, doubl
   std::memcpy(norm_out, v.data(), op->nrhs_user * sizeof(double));
   return GB_OK;
 }
+// axpby_norm (Lattice_reduction.h:316-372): z = a x + b y and |z|^2 per rhs (here two
+// passes: the axpby, then the norm)
+int gb_field_axpby_norm(gb_field_t z, double a, double b, gb_field_t x, gb_field_t y, double* norm_out) {
+  if (!norm_out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  GB_TRY(gb_field_axpby(z, a, b, x, y));
+  std::vector<double> v(z->op->nrhs);
+  GB_TRY(field_norm2(z, v.data()));
+  std::memcpy(norm_out, v.data(), z->op->nrhs_user * sizeof(double));
+  return GB_OK;
+}
+// innerProductNorm (Lattice_reduction.h:374-410): <a|b> (re, im per rhs) and |a|^2 per rhs
+int gb_field_inner_norm(gb_field_t a, gb_field_t b, double* inner_out, double* norm_out) {
+  if (!inner_out || !norm_out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  GB_TRY(check_conf(a, b));
+  if (a->subset != b->subset) { set_error("innerProductNorm: checkerboard mismatch"); return GB_ERR_BAD_PARITY; }
+  Op* op = a->op;
+  std::vector<double> ip(size_t(op->nrhs) * 2), nr(op->nrhs);
+  GB_TRY(field_inner(a, b, ip.data()));
+  GB_TRY(field_norm2(a, nr.data()));
+  std::memcpy(inner_out, ip.data(), size_t(op->nrhs_user) * 2 * sizeof(double));
+  std::memcpy(norm_out, nr.data(), op->nrhs_user * sizeof(double));
+  return GB_OK;
+}
 int gb_field_pick_checkerboard(gb_field_t half, gb_field_t full) {
   GB_TRY(check_conf(half, full));
   if (half->full() || !full->full()) { set_error("pickCheckerboard: (half, full) expected"); return GB_ERR_BAD_PARITY; }

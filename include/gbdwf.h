@@ -147,6 +147,9 @@ int gb_field_inner(gb_field_t a, gb_field_t b, double* out); /* innerProduct <a|
 int gb_field_axpy(gb_field_t z, double a, gb_field_t x, gb_field_t y);               /* z = a x + y   */
 int gb_field_axpby(gb_field_t z, double a, double b, gb_field_t x, gb_field_t y);    /* z = a x + b y */
 int gb_field_axpy_norm(gb_field_t z, double a, gb_field_t x, gb_field_t y, double* norm_out);
+int gb_field_axpby_norm(gb_field_t z, double a, double b, gb_field_t x, gb_field_t y, double* norm_out);
+/* innerProductNorm: <a|b> (re, im per rhs) and |a|^2 per rhs */
+int gb_field_inner_norm(gb_field_t a, gb_field_t b, double* inner_out, double* norm_out);
 int gb_field_pick_checkerboard(gb_field_t half, gb_field_t full); /* half's subset picks */
 int gb_field_set_checkerboard(gb_field_t full, gb_field_t half);
 

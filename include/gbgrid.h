@@ -286,6 +286,20 @@ template <class v> RealD axpy_norm(Lattice<v>& ret, ComplexD a, const Lattice<v>
   gbdetail::check(gb_field_axpy_norm(ret.handle(), real_coeff(a), x.handle(), y.handle(), &n), "gb_field_axpy_norm");
   return n;
 }
+template <class v> RealD axpby_norm(Lattice<v>& ret, ComplexD a, ComplexD b, const Lattice<v>& x, const Lattice<v>& y) {
+  double n = 0;
+  gbdetail::check(gb_field_axpby_norm(ret.handle(), real_coeff(a), real_coeff(b), x.handle(), y.handle(), &n),
+                  "gb_field_axpby_norm");
+  return n;
+}
+template <class v> void innerProductNorm(ComplexD& ip, RealD& nrm, const Lattice<v>& left, const Lattice<v>& right) {
+  double r[2] = {0, 0}, n = 0;
+  gbdetail::check(gb_field_inner_norm(left.handle(), right.handle(), r, &n), "gb_field_inner_norm");
+  ip = ComplexD(r[0], r[1]);
+  nrm = n;
+}
+// one process, one GPU: the rank-local inner product is the global one
+template <class v> ComplexD rankInnerProduct(const Lattice<v>& a, const Lattice<v>& b) { return innerProduct(a, b); }
 template <class v> void pickCheckerboard(int cb, Lattice<v>& half, const Lattice<v>& full) {
   half.Checkerboard() = cb;
   gbdetail::check(gb_field_pick_checkerboard(half.handle(), full.handle()), "gb_field_pick_checkerboard");

@@ -85,6 +85,19 @@ int main() {
   const ComplexD pMs = innerProduct(phi_o, Mpc_src), Mdps = innerProduct(MpcDag_phi, src_o);
   expect(std::abs(pMs - Mdps) / std::abs(pMs) < 1e-12, "<phi|Mpc src> == <MpcDag phi|src>", std::abs(pMs - Mdps) / std::abs(pMs));
 
+  // ---- fused reductions (Lattice_reduction.h) ----
+  {
+    LatticeFermion z(FGrid);
+    const RealD nz = axpby_norm(z, 0.5, -2.0, src, phi);
+    ComplexD ip;
+    RealD nrm;
+    innerProductNorm(ip, nrm, src, phi);
+    const ComplexD ip2 = rankInnerProduct(src, phi);
+    expect(std::abs(nz - norm2(z)) < 1e-12 * nz && std::abs(nrm - norm2(src)) < 1e-12 * nrm &&
+               std::abs(ip - innerProduct(src, phi)) < 1e-12 * std::abs(ip) && ip2 == innerProduct(src, phi),
+           "axpby_norm / innerProductNorm / rankInnerProduct", std::abs(nz - norm2(z)) / nz);
+  }
+
   // ---- Schur red-black solve, FP64 and mixed precision ----
   ConjugateGradient<LatticeFermion> CG(1e-10, 10000);
   SchurRedBlackDiagMooeeSolve<LatticeFermion> SchurSolver(CG);

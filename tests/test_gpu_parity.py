@@ -417,3 +417,30 @@ def test_recon12_needs_real_phases(gpu_available):
     with pytest.raises(g.GridError) as e:
         g.WilsonFermion(g.random_gauge(dims, 0.3, 1), dims, 0.1, phases=ph, flags=g.RECON12)
     assert e.value.status == 8
+
+
+@pytest.mark.parametrize("prec", [g.F64, g.F32])
+def test_axpby_norm_and_inner_product_norm(gpu_available, prec):
+    """axpby_norm and innerProductNorm (Lattice_reduction.h:316-410) per right-hand side,
+    against numpy on the values the fields hold."""
+    dims, Ls, nrhs = (4, 4, 4, 4), 4, 2
+    op, _, _ = mobius_pair(dims, Ls, 0.1, prec, nrhs=nrhs)
+    vol = int(np.prod(dims))
+    fx = op.FermionField().import_(fermion(vol * nrhs, Ls, 101))
+    fy = op.FermionField().import_(fermion(vol * nrhs, Ls, 102))
+    x = fx.export().reshape(nrhs, -1)
+    y = fy.export().reshape(nrhs, -1)
+    fz = op.FermionField()
+    n = g.axpby_norm(fz, 0.5, -1.25, fx, fy)
+    z = fz.export().reshape(nrhs, -1)
+    tol = 1e-13 if prec == g.F64 else 1e-6
+    assert o.rel_l2(z, 0.5 * x - 1.25 * y) < tol
+    # FP32 fields: per-site products in FP32, sums in FP64
+    rt = 1e-12 if prec == g.F64 else 1e-6
+    for r in range(nrhs):
+        assert abs(n[r] - np.vdot(z[r], z[r]).real) < rt * n[r]
+    ip, nr = g.innerProductNorm(fx, fy)
+    for r in range(nrhs):
+        assert abs(ip[r] - np.vdot(x[r], y[r])) < rt * np.sqrt(nr[r] * np.vdot(y[r], y[r]).real)
+        assert abs(nr[r] - np.vdot(x[r], x[r]).real) < rt * nr[r]
+    assert np.allclose(g.rankInnerProduct(fx, fy), g.innerProduct(fx, fy))
