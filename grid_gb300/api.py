@@ -413,6 +413,7 @@ def ExtractSlice(high: FermionField, slice_: int, orthog: int = 0):
     return out
 
 
+_proto("gb_bounded_wait_test", [_vp, _i, C.c_longlong])
 _proto("gb_field_axpby_norm", [_vp, _d, _d, _vp, _vp, _dp])
 _proto("gb_field_inner_norm", [_vp, _vp, _dp, _dp])
 

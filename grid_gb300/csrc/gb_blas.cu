@@ -744,3 +744,42 @@ int launch_double_store(Op* op, const double* U_canon, int parity) {
 }
 
 }  // namespace gb
+
+// ---------------------------------------------------------------------------------------
+// The bounded-wait contract of every device wait, exercised on its own: one thread polls
+// a device flag with a poll budget and, when the budget runs out, records the failure in
+// a status word the host reads and returns -- no trap, the context stays usable.
+// ---------------------------------------------------------------------------------------
+namespace gb {
+namespace {
+__global__ void bounded_flag_wait_kernel(const volatile int* flag, int expect, long long max_polls, int* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  long long i = 0;
+  while (*flag != expect && i < max_polls) {
+    __nanosleep(1000);
+    i++;
+  }
+  *status = (*flag == expect) ? 0 : 1;
+}
+}  // namespace
+}  // namespace gb
+
+extern "C" int gb_bounded_wait_test(gb_op_t op, int set_flag, long long max_polls) {
+  using namespace gb;
+  if (!op || max_polls < 1 || max_polls > (1ll << 22)) { set_error("bounded wait test: 1 <= max_polls <= 2^22"); return GB_ERR_BAD_ARG; }
+  int* d = nullptr;  // d[0]: the flag, d[1]: the status
+  GB_CHECK_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), 2 * sizeof(int), op->stream));
+  struct Free { int* p; cudaStream_t s; ~Free() { cudaFreeAsync(p, s); } } guard{d, op->stream};
+  const int init[2] = {set_flag ? 1 : 0, -1};
+  GB_CHECK_CUDA(cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, op->stream));
+  bounded_flag_wait_kernel<<<1, 32, 0, op->stream>>>(d, 1, max_polls, d + 1);
+  GB_CHECK_CUDA(cudaGetLastError());
+  int status = -1;
+  GB_CHECK_CUDA(cudaMemcpyAsync(&status, d + 1, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  if (status != 0) {
+    set_error("device wait gave up after %lld polls (flag never set)", max_polls);
+    return GB_ERR_TIMEOUT;
+  }
+  return GB_OK;
+}

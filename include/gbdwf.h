@@ -374,6 +374,12 @@ int gb_ildg_write(const char* path, const double* U, int on_device, const int di
 /* WilsonLoops::avgPlaquette and linkTrace (Grid/qcd/utils/WilsonLoops.h:88-126,203-218) */
 int gb_gauge_stats(const int dims[4], const double* U, int on_device, double* plaquette, double* link_trace);
 
+/* The bounded-wait contract of the library's device waits, on its own: a kernel polls a
+ * device flag at most max_polls times (~1 us apart; max_polls <= 2^22).  set_flag != 0
+ * sets the flag first (returns GB_OK); otherwise nothing sets it and the call returns
+ * GB_ERR_TIMEOUT with the context still usable. */
+int gb_bounded_wait_test(gb_op_t op, int set_flag, long long max_polls);
+
 /* ---- seeded synthetic inputs (Grid: GridParallelRNG + SU3::HotConfiguration) ----
  * Counter-based generator keyed by (seed, site, element); independent of thread count.
  * gb_random_gauge: U = reunitarise(exp(i*eps*H)), H traceless Hermitian with Gaussian
