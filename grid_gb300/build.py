@@ -22,7 +22,7 @@ LIB = HERE / "libgbdwf.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
-    "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
+    "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-fvisibility=hidden",
     "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-I", str(CSRC),
 ]
 

@@ -22,6 +22,10 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+/* the library is built with hidden visibility: only these declarations are exported */
+#pragma GCC visibility push(default)
+#endif
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -463,6 +467,9 @@ int gb_bench_kernel(gb_op_t op, int which, gb_field_t* ins, gb_field_t* outs, in
 
 #ifdef __cplusplus
 }
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility pop
 #endif
 
 #endif /* GBDWF_H */
