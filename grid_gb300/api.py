@@ -78,6 +78,7 @@ _proto("gb_wilson_create", [_ip, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)]
 _proto("gb_mobius_create", [_ip, _i, _d, _d, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
 _proto("gb_zmobius_create", [_ip, _i, _d, _d, _dp, _d, _d, _dp, _i, _i, _vp, C.c_uint, C.POINTER(_vp)])
 _proto("gb_zolotarev", [_d, _i, _i, _dp, _dp])
+_proto("gb_zmobius_gamma", [_i, _d, _i, _d, _d, _dp, _dp])
 _proto("gb_op_destroy", [_vp])
 _proto("gb_op_import_gauge", [_vp, _dp])
 _proto("gb_op_import_gauge_device", [_vp, _vp])
@@ -642,6 +643,18 @@ def zolotarev(epsilon, n, type=0):
     delta = C.c_double()
     _check(lib.gb_zolotarev(float(epsilon), int(n), int(type), _dptr(gamma), C.byref(delta)))
     return gamma, delta.value
+
+
+def computeZmobiusGamma(mobius_param_out, Ls_out, mobius_param_in, Ls_in, lambda_bound):
+    """Approx::computeZmobiusGamma (ZMobius.cc:149-175): (gamma, max_error) -- the Ls_out
+    complex gamma_s of the ZMobius operator whose sign function best approximates, on
+    0 <= x <= lambda_bound, that of the Moebius operator with Ls_in slices and b + c =
+    mobius_param_in; gamma_s = mobius_param_out * omega_s."""
+    gm = np.empty(2 * int(Ls_out), dtype=np.float64)
+    err = C.c_double()
+    _check(lib.gb_zmobius_gamma(int(Ls_out), float(mobius_param_out), int(Ls_in), float(mobius_param_in),
+                                float(lambda_bound), _dptr(gm), C.byref(err)))
+    return gm[0::2] + 1j * gm[1::2], err.value
 
 
 def higham(epsilon, n):

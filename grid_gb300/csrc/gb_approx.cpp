@@ -113,3 +113,193 @@ int gb_zolotarev(double epsilon, int n, int type, double* gamma, double* delta) 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Approx::computeZmobiusGamma (Grid/algorithms/approx/ZMobius.cc:73-183): the ZMobius
+// omega_s of Ls_out slices that best approximate (in the minimax sense on 0 <= x <=
+// lambda) the Moebius sign function of Ls_in slices with b + c = bpc_in,
+//   eps_in(x) = (f(x) - f(-x)) / (f(x) + f(-x)),  f(x) = (1 / bpc_in + x)^Ls_in,
+// by R(x) = N(x) / D(x), N odd of degree Ls_out - 1, D even and monic of degree Ls_out.
+// Then f_out = D + N = prod_s (x + omega_s): the omegas are minus its roots, sorted by
+// (real, imaginary) part and placed largest-first alternately from the two ends of the
+// fifth dimension, and gamma_s = bpc_out * omega_s.
+// Our method: the rational Remez exchange in long double (the levelled equations
+// N(x_k) - eps(x_k) D(x_k) = (-1)^k E D(x_k), linearised in E by the previous D, then a
+// new alternating set of error extrema on a fine grid), and Aberth's simultaneous
+// iteration for the roots.
+// ---------------------------------------------------------------------------------------
+#include <algorithm>
+#include <complex>
+
+namespace {
+
+using LD = long double;
+
+LD eps_mobius(LD x, LD omega, int Ls) {
+  const LD r = std::pow((omega - x) / (omega + x), LD(Ls));
+  return (1 - r) / (1 + r);
+}
+
+// Gaussian elimination with partial pivoting; false when singular
+bool solve_dense(std::vector<LD>& A, std::vector<LD>& b, int n) {
+  for (int c = 0; c < n; c++) {
+    int piv = c;
+    for (int r = c + 1; r < n; r++)
+      if (std::fabs(A[size_t(r) * n + c]) > std::fabs(A[size_t(piv) * n + c])) piv = r;
+    if (A[size_t(piv) * n + c] == 0) return false;
+    if (piv != c) {
+      for (int k = 0; k < n; k++) std::swap(A[size_t(c) * n + k], A[size_t(piv) * n + k]);
+      std::swap(b[c], b[piv]);
+    }
+    for (int r = c + 1; r < n; r++) {
+      const LD f = A[size_t(r) * n + c] / A[size_t(c) * n + c];
+      if (f == 0) continue;
+      for (int k = c; k < n; k++) A[size_t(r) * n + k] -= f * A[size_t(c) * n + k];
+      b[r] -= f * b[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; r--) {
+    LD s = b[r];
+    for (int k = r + 1; k < n; k++) s -= A[size_t(r) * n + k] * b[k];
+    b[r] = s / A[size_t(r) * n + r];
+  }
+  return true;
+}
+
+struct Rational {  // N(x) = sum a[j] x^(2j+1), D(x) = x^L + sum d[j] x^(2j)
+  int L;
+  std::vector<LD> a, d;
+  LD num(LD x) const {
+    LD s = 0, p = x, x2 = x * x;
+    for (LD c : a) { s += c * p; p *= x2; }
+    return s;
+  }
+  LD den(LD x) const {
+    LD s = 0, p = 1, x2 = x * x;
+    for (LD c : d) { s += c * p; p *= x2; }
+    return s + p;  // p = x^L after L/2 steps
+  }
+  LD eval(LD x) const { return num(x) / den(x); }
+};
+
+}  // namespace
+
+extern "C" int gb_zmobius_gamma(int Ls_out, double bpc_out, int Ls_in, double bpc_in, double lambda_bound,
+                                double* gamma, double* max_error) {
+  using gb::set_error;
+  if (!gamma) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (Ls_out < 2 || (Ls_out & 1) || Ls_out > 32 || Ls_in < 1 || !(bpc_in > 0) || !(bpc_out > 0) || !(lambda_bound > 0)) {
+    set_error("computeZmobiusGamma: need even 2 <= Ls_out <= 32, Ls_in >= 1, b+c > 0, lambda > 0");
+    return GB_ERR_BAD_ARG;
+  }
+  const int L = Ls_out, h = L / 2, n = L + 1;  // unknowns: a[h], d[h], E
+  const LD omega = LD(1) / LD(bpc_in), lam = LD(lambda_bound);
+  auto target = [&](LD x) { return eps_mobius(x, omega, Ls_in); };
+  // error grid: dense near 0, where the sign function turns over
+  const int G = 20000;
+  std::vector<LD> xs(G);
+  for (int i = 0; i < G; i++) {
+    const LD t = LD(i + 1) / LD(G);
+    xs[i] = lam * (LD(0.5) * t * t + LD(0.5) * t);
+  }
+  std::vector<LD> pts(n);
+  for (int k = 0; k < n; k++) {
+    const LD t = std::sin(LD(M_PI) * LD(k + 1) / LD(2 * n));
+    pts[k] = lam * t * t;
+  }
+  Rational R{L, std::vector<LD>(h, 0), std::vector<LD>(h, 0)};
+  LD E = 0, maxerr = 0;
+  bool ok = false;
+  for (int iter = 0; iter < 200; iter++) {
+    // the levelled equations, E linearised by the previous denominator
+    for (int inner = 0; inner < 50; inner++) {
+      std::vector<LD> A(size_t(n) * n, 0), b(n, 0);
+      for (int k = 0; k < n; k++) {
+        const LD x = pts[k], x2 = x * x, ek = target(x), sk = (k & 1) ? -1 : 1;
+        const LD dold = inner == 0 && iter == 0 ? std::pow(x, LD(L)) + 1 : R.den(x);
+        LD p = x;
+        for (int j = 0; j < h; j++) { A[size_t(k) * n + j] = p; p *= x2; }
+        p = 1;
+        for (int j = 0; j < h; j++) { A[size_t(k) * n + h + j] = -ek * p; p *= x2; }
+        A[size_t(k) * n + L] = -sk * dold;
+        b[k] = ek * std::pow(x, LD(L));
+      }
+      if (!solve_dense(A, b, n)) { set_error("computeZmobiusGamma: singular Remez system"); return GB_ERR_UNSUPPORTED; }
+      for (int j = 0; j < h; j++) { R.a[j] = b[j]; R.d[j] = b[h + j]; }
+      const LD Enew = b[L];
+      const bool settled = std::fabs(Enew - E) <= LD(1e-12) * std::fabs(Enew);
+      E = Enew;
+      if (settled) break;
+    }
+    // the extrema of the error, one per run of constant sign, the largest L+1 kept in order
+    std::vector<int> ext;
+    std::vector<LD> err(G);
+    for (int i = 0; i < G; i++) err[i] = R.eval(xs[i]) - target(xs[i]);
+    int best = 0;
+    for (int i = 1; i <= G; i++) {
+      if (i == G || (err[i] > 0) != (err[best] > 0)) {
+        ext.push_back(best);
+        if (i < G) best = i;
+      } else if (std::fabs(err[i]) > std::fabs(err[best])) {
+        best = i;
+      }
+    }
+    while (int(ext.size()) > n) {  // drop the smaller end, keeping the alternation
+      if (std::fabs(err[ext.front()]) < std::fabs(err[ext.back()])) ext.erase(ext.begin());
+      else ext.pop_back();
+    }
+    maxerr = 0;
+    for (int i = 0; i < G; i++) maxerr = std::max(maxerr, std::fabs(err[i]));
+    if (int(ext.size()) < n) { set_error("computeZmobiusGamma: fewer than %d alternation points", n); return GB_ERR_UNSUPPORTED; }
+    LD mn = std::fabs(err[ext[0]]);
+    for (int k = 0; k < n; k++) { pts[k] = xs[ext[k]]; mn = std::min(mn, std::fabs(err[ext[k]])); }
+    if (maxerr - mn <= LD(1e-6) * maxerr) { ok = true; break; }
+  }
+  if (!ok) { set_error("computeZmobiusGamma: the Remez exchange did not settle"); return GB_ERR_NOT_CONVERGED; }
+  // roots of c(x) = D(x) + N(x) (monic, degree L) by Aberth's iteration
+  std::vector<LD> c(L + 1, 0);  // c[i] = coefficient of x^i
+  for (int j = 0; j < h; j++) { c[2 * j] = R.d[j]; c[2 * j + 1] = R.a[j]; }
+  c[L] = 1;
+  using CX = std::complex<LD>;
+  auto peval = [&](CX z, CX& dp) {
+    CX p = c[L];
+    dp = 0;
+    for (int i = L - 1; i >= 0; i--) { dp = dp * z + p; p = p * z + c[i]; }
+    return p;
+  };
+  LD radius = 0;
+  for (int i = 0; i < L; i++) radius = std::max(radius, std::pow(std::fabs(c[i]), LD(1) / LD(L - i)));
+  std::vector<CX> z(L);
+  for (int i = 0; i < L; i++) z[i] = std::polar(radius, LD(2 * M_PI) * (LD(i) + LD(0.25)) / LD(L));
+  for (int it = 0; it < 500; it++) {
+    LD move = 0;
+    for (int i = 0; i < L; i++) {
+      CX dp;
+      const CX p = peval(z[i], dp);
+      if (p == CX(0)) continue;
+      const CX w = p / dp;
+      CX s = 0;
+      for (int j = 0; j < L; j++)
+        if (j != i) s += LD(1) / (z[i] - z[j]);
+      const CX step = w / (LD(1) - w * s);
+      z[i] -= step;
+      move = std::max(move, std::abs(step) / std::max(LD(1e-300), std::abs(z[i])));
+    }
+    if (move < LD(1e-17)) break;
+  }
+  std::vector<CX> om(L);
+  for (int i = 0; i < L; i++) om[i] = -z[i];
+  std::sort(om.begin(), om.end(), [](const CX& a, const CX& b) {
+    return a.real() < b.real() || (a.real() == b.real() && a.imag() < b.imag());
+  });
+  // largest first, alternately from the two ends (ZMobius.cc:130-141)
+  std::vector<CX> placed(L);
+  int lo = 0, hi = L - 1, ss = 0;
+  for (int from = L - 1; from >= 0; from--, ss++) placed[(ss % 2 == 0) ? lo++ : hi--] = om[from];
+  for (int s = 0; s < L; s++) {
+    gamma[2 * s] = double(placed[s].real() * LD(bpc_out));
+    gamma[2 * s + 1] = double(placed[s].imag() * LD(bpc_out));
+  }
+  if (max_error) *max_error = double(maxerr);
+  return GB_OK;
+}

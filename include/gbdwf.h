@@ -84,6 +84,13 @@ int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, 
  * with omega_s = hi * gamma_s of zolotarev(lo / hi, Ls, 0) (MobiusZolotarevFermion.h:45-70,
  * CayleyFermion5DImplementation.h:411-445): gb_zmobius_create with that omega. */
 int gb_zolotarev(double epsilon, int n, int type, double* gamma, double* delta);
+/* Approx::computeZmobiusGamma(gamma, bpc_out, Ls_out, bpc_in, Ls_in, lambda)
+ * (Grid/algorithms/approx/ZMobius.cc:73-183): the Ls_out (even, <= 32) complex gamma_s of
+ * the ZMobius operator whose sign function best approximates, on 0 <= x <= lambda, that
+ * of the Moebius operator with Ls_in slices and b + c = bpc_in; gamma_s = bpc_out omega_s.
+ * gamma: 2 Ls_out doubles (re, im); max_error (may be NULL): the minimax error. */
+int gb_zmobius_gamma(int Ls_out, double bpc_out, int Ls_in, double bpc_in, double lambda_bound, double* gamma,
+                     double* max_error);
 
 /* ZMobiusFermion(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, gamma, b, c, ImplParams)
  * (Grid/qcd/action/fermion/ZMobiusFermion.h): complex omega_s = gamma[s] (Ls complex

@@ -650,6 +650,19 @@ inline zolotarev_data* higham(double epsilon, int n) {
   z->epsilon = epsilon;
   return z;
 }
+// Approx::computeZmobiusGamma (Grid/algorithms/approx/ZMobius.cc:149-175)
+inline void computeZmobiusGamma(std::vector<ComplexD>& gamma_out, RealD mobius_param_out, int Ls_out,
+                                RealD mobius_param_in, int Ls_in, RealD lambda_bound) {
+  std::vector<double> g(2 * size_t(Ls_out));
+  gbdetail::check(gb_zmobius_gamma(Ls_out, mobius_param_out, Ls_in, mobius_param_in, lambda_bound, g.data(), nullptr),
+                  "Approx::computeZmobiusGamma");
+  gamma_out.resize(Ls_out);
+  for (int s = 0; s < Ls_out; s++) gamma_out[s] = ComplexD(g[2 * s], g[2 * s + 1]);
+}
+inline void computeZmobiusGamma(std::vector<ComplexD>& gamma_out, int Ls_out, RealD mobius_param, int Ls_in,
+                                RealD lambda_bound) {
+  computeZmobiusGamma(gamma_out, mobius_param, Ls_out, mobius_param, Ls_in, lambda_bound);
+}
 inline void zolotarev_free(zolotarev_data* z) {
   if (z) {
     delete[] z->gamma;

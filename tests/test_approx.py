@@ -53,3 +53,51 @@ def test_zolotarev_rejects_bad_arguments():
 
 def test_higham_is_moebius():
     assert np.array_equal(g.higham(0.1, 6), np.ones(6))
+
+
+# ---- Approx::computeZmobiusGamma (ZMobius.cc) ------------------------------------------
+def zmobius_sign(gamma, bpc_out, x):
+    om = np.asarray(gamma) / bpc_out
+    fp = np.prod([x + w for w in om], axis=0)
+    fm = np.prod([-x + w for w in om], axis=0)
+    return ((fp - fm) / (fp + fm)).real
+
+
+def mobius_sign(Ls, bpc, x):
+    r = ((1.0 / bpc - x) / (1.0 / bpc + x)) ** Ls
+    return (1 - r) / (1 + r)
+
+
+@pytest.mark.parametrize("Lo,Li,bpc,lam", [(10, 24, 2.0, 1.42), (8, 16, 2.0, 1.42), (12, 24, 2.0, 1.42),
+                                           (6, 12, 1.0, 1.0)])
+def test_zmobius_gamma_is_the_minimax_approximation(Lo, Li, bpc, lam):
+    """The ZMobius sign function of the returned gammas approximates the Moebius one with
+    error reaching its maximum, with alternating signs, at Ls_out + 1 points of (0, lambda]
+    (the Chebyshev alternation that characterises the minimax rational approximation)."""
+    gamma, err = g.computeZmobiusGamma(bpc, Lo, bpc, Li, lam)
+    assert gamma.shape == (Lo,) and 0 < err < 1e-2
+    x = np.linspace(lam * 1e-6, lam, 400001)
+    e = zmobius_sign(gamma, bpc, x) - mobius_sign(Li, bpc, x)
+    assert abs(np.abs(e).max() - err) < 1e-3 * err
+    signs, prev = [], 0
+    for i in np.flatnonzero(np.abs(e) > 0.999 * err):
+        s = np.sign(e[i])
+        if s != prev:
+            signs.append(s)
+            prev = s
+    assert len(signs) >= Lo + 1
+    # real coefficients: the omegas are closed under conjugation
+    assert np.allclose(np.sort_complex(gamma), np.sort_complex(gamma.conj()), atol=1e-9)
+    # Grid's placement: the largest omegas at the two ends of the fifth dimension
+    re = gamma.real
+    assert re[0] == re.max() and re[-1] == np.sort(re)[-2]
+
+
+def test_zmobius_gamma_error_falls_with_ls_and_scales_with_bpc_out():
+    errs = [g.computeZmobiusGamma(2.0, Lo, 2.0, 24, 1.42)[1] for Lo in (6, 8, 10, 12)]
+    assert all(b < 0.3 * a for a, b in zip(errs, errs[1:]))
+    g1, _ = g.computeZmobiusGamma(2.0, 8, 2.0, 16, 1.42)
+    g2, _ = g.computeZmobiusGamma(3.0, 8, 2.0, 16, 1.42)
+    assert np.allclose(g2, 1.5 * g1, rtol=1e-12)
+    with pytest.raises(g.GridError):
+        g.computeZmobiusGamma(2.0, 7, 2.0, 16, 1.42)

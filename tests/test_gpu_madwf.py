@@ -175,3 +175,23 @@ def test_madwf_not_converged_raises(gpu_available):
     with pytest.raises(g.GridError):
         madwf(eta, outer.FermionField())
     assert outer.Mass() == MF and inner.Mass() == MF
+
+
+def test_madwf_with_computed_zmobius_gammas(gpu_available):
+    """Test_zMADWF_prec.cc's workflow end to end: the inner ZMobius gammas come from
+    Approx::computeZmobiusGamma(b+c = 1, Ls_in = 8, outer b+c = 2, Ls_out = 12, lambda =
+    1.42), the inner operator has b = 1, c = 0, and MADWF reproduces the outer solve."""
+    Lo, Li = 12, 8
+    U, outer, ref, eta = _outer_problem(Lo, 1.5, 0.5)
+    gamma, err = g.computeZmobiusGamma(1.0, Li, 2.0, Lo, 1.42)
+    assert err < 1e-2
+    inner = g.ZMobiusFermion(U, DIMS, list(gamma), MF, MOBIUS["M5"], 1.0, 0.0)
+    pv = g.PauliVillarsSolverRBprec(g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000)))
+    madwf = g.MADWF(outer, inner, pv, g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000, False)),
+                    g.ZeroGuesser(), 1e-9, 20)
+    sol = outer.FermionField()
+    madwf(eta, sol)
+    assert madwf.residuals[-1] < 1e-9 and madwf.iterations <= 10
+    b = ref.physical(o.IMPORT_PHYSICAL_SOURCE, eta)
+    direct, _, _, _ = ref.schur_solve(b, 1e-11, 10000)
+    assert o.rel_l2(sol.export(), direct) < 1e-8
