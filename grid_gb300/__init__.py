@@ -13,7 +13,7 @@ from .api import (  # noqa: F401
     MixedPrecisionConjugateGradientBatched, MixedParams,
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,
     NerscHeader, nersc_read_header, nersc_read, nersc_write, gauge_stats,
-    IldgHeader, ildg_read_header, ildg_read, ildg_write,
+    IldgHeader, ildg_read_header, ildg_read, ildg_write, openqcd_read,
     CGParams, random_gauge, unit_gauge, random_gaussian, random_z2, device_count,
     antiperiodic_t, periodic, set_device, PinnedArray, Stream, TransferQueue, norm2, innerProduct, axpy, axpby, axpy_norm,
     axpby_norm, innerProductNorm, rankInnerProduct,

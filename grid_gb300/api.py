@@ -1213,6 +1213,22 @@ def ildg_write(path, U, dims, precision=64, lfn=""):
     _check(lib.gb_ildg_write(str(path).encode(), U.ctypes.data, 0, _dims(dims), int(precision), lfn.encode()))
 
 
+_proto("gb_openqcd_read_header", [C.c_char_p, _ip, _dp])
+_proto("gb_openqcd_read", [C.c_char_p, _vp, _i, _ip, _dp, _dp, _i])
+
+
+def openqcd_read(path, check=True):
+    """OpenQcdIO::readConfiguration: (canonical FP64 gauge field, dims (x, y, z, t),
+    header plaquette, computed plaquette); the plaquettes must agree when `check`."""
+    d = (C.c_int * 4)()
+    p = C.c_double()
+    _check(lib.gb_openqcd_read_header(str(path).encode(), d, C.byref(p)))
+    U = np.empty(int(np.prod(list(d))) * 36, dtype=np.complex128)
+    pc = C.c_double()
+    _check(lib.gb_openqcd_read(str(path).encode(), U.ctypes.data, 0, d, C.byref(p), C.byref(pc), int(bool(check))))
+    return U, tuple(d), p.value, pc.value
+
+
 def gauge_stats(dims, U):
     """(avgPlaquette, linkTrace) of a canonical gauge field, computed on the device."""
     U = np.ascontiguousarray(U, dtype=np.complex128)

@@ -382,6 +382,15 @@ int gb_ildg_read(const char* path, double* U, int on_device, gb_ildg_header* h, 
 /* IldgWriter::writeConfiguration: precision 32 or 64; lfn may be NULL */
 int gb_ildg_write(const char* path, const double* U, int on_device, const int dims[4], int precision, const char* lfn);
 
+/* ---- openQCD gauge files (Grid/parallelIO/OpenQcdIO.h:43-170; read only, as in Grid) ----
+ * dims in Grid order (x, y, z, t); plaquette in Grid's normalisation (the header's / 3).
+ * gb_openqcd_read: canonical U[site][mu][3][3] (host, or device memory with on_device);
+ * check != 0 returns GB_ERR_IO when the field's plaquette differs from the header's by
+ * >= 2e-15 (Grid asserts). */
+int gb_openqcd_read_header(const char* path, int dims[4], double* plaquette);
+int gb_openqcd_read(const char* path, double* U, int on_device, int dims[4], double* plaquette,
+                    double* plaquette_computed, int check);
+
 /* WilsonLoops::avgPlaquette and linkTrace (Grid/qcd/utils/WilsonLoops.h:88-126,203-218) */
 int gb_gauge_stats(const int dims[4], const double* U, int on_device, double* plaquette, double* link_trace);
 

@@ -1,6 +1,7 @@
-"""ILDG / SciDAC files on the CPU: the oracle's restatement pinned (CRC-32 check value,
+"""Gauge-file formats on the CPU. ILDG / SciDAC: the oracle's restatement pinned (CRC-32 check value,
 checksum rotation, LIME framing, write/read round trip) and the library's host-side LIME
-and XML parsing (gb_ildg_read_header, no device work) on files the oracle writes."""
+and XML parsing (gb_ildg_read_header, no device work) on files the oracle writes.
+openQCD: the header parser (gb_openqcd_read_header)."""
 import zlib
 
 import numpy as np
@@ -62,3 +63,21 @@ def test_library_parses_oracle_records(tmp_path):
     for bad in ("short.lime", "junk.lime"):
         with pytest.raises(g.GridError):
             g.ildg_read_header(tmp_path / bad)
+
+
+def test_library_parses_openqcd_header(tmp_path):
+    """openQCD header (OpenQcdIO.h:43-75) on the host: int32 Nt Nx Ny Nz (Grid order back
+    to x y z t) and the plaquette divided by Nc; implausible extents are refused."""
+    import ctypes
+
+    from oracle import openqcd
+    dims = (4, 6, 4, 8)
+    U = g.random_gauge(dims, 0.5, 7)
+    path = tmp_path / "cfg.oq"
+    plaq = openqcd.write(path, U, dims)
+    d = (ctypes.c_int * 4)()
+    p = ctypes.c_double()
+    assert g.lib.gb_openqcd_read_header(str(path).encode(), d, ctypes.byref(p)) == 0
+    assert tuple(d) == dims and abs(p.value - plaq) < 1e-15
+    (tmp_path / "swapped.oq").write_bytes(path.read_bytes()[:4][::-1] + path.read_bytes()[4:])
+    assert g.lib.gb_openqcd_read_header(str(tmp_path / "swapped.oq").encode(), d, ctypes.byref(p)) != 0
