@@ -565,9 +565,11 @@ def serving_stream(seconds, rate=20.0, seed=5005):
     return reqs
 
 
-def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0):
+def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0, inner=None):
     """Replays the first `max_requests` requests of the seeded stream at their arrival
-    times into the service (HBM budget 150 GB, mixed-precision CG to 1e-10)."""
+    times into the service (HBM budget 150 GB, mixed-precision CG to 1e-10; inner solves
+    in FP32, or FP16 storage with `inner=g.F16`)."""
+    inner = g.F32 if inner is None else inner
     reqs = serving_stream(seconds)[:max_requests]
     srv = g.Server(int(budget_gb * (1 << 30)), slots=slots, flags=g.Server.GRAPHS)
     t0 = time.perf_counter()
@@ -575,7 +577,8 @@ def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0):
         delay = q["t"] - (time.perf_counter() - t0)
         if delay > 0:
             time.sleep(delay)
-        srv.submit(g.make_request(q["dims"], q["Ls"], q["mf"], q["eps"], q["gauge_seed"], q["nsrc"], q["src_seed"]))
+        srv.submit(g.make_request(q["dims"], q["Ls"], q["mf"], q["eps"], q["gauge_seed"], q["nsrc"], q["src_seed"],
+                                  inner=inner))
     ok = srv.wait(len(reqs), 1800)
     wall = time.perf_counter() - t0
     res = srv.results(len(reqs) + 8)
@@ -591,7 +594,7 @@ def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0):
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "max_true_residual": float(max((r.true_residual for r in good), default=0.0)),
             "max_running": int(st.max_running), "peak_hbm_gb": st.peak_used_bytes / (1 << 30), "slots": slots,
-            "budget_gb": budget_gb}
+            "budget_gb": budget_gb, "inner_precision": "fp16" if inner == g.F16 else "fp32"}
 
 
 def cg_profile(g, iters):
