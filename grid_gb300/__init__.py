@@ -8,7 +8,8 @@ raises if it has not been built: there is no CPU fallback.
 from .api import (  # noqa: F401
     GridError, lib, LIB_PATH, F64, F32, F16, RECON12, EVEN, ODD, FULL, DaggerNo, DaggerYes,
     FermionField, WilsonFermion, MobiusFermion, ZMobiusFermion, MobiusZolotarevFermion, ShamirZolotarevFermion,
-    ScaledShamirFermion, zolotarev, higham, computeZmobiusGamma, MdagMLinearOperator, SchurDiagMooeeOperator,
+    ScaledShamirFermion, zolotarev, higham, computeZmobiusGamma, WilsonTMFermion5D, FourierAcceleratedPV,
+    PauliVillarsSolverFourierAccel, dft_s, copy_slice5, chiral_scale, MdagMLinearOperator, SchurDiagMooeeOperator,
     ConjugateGradient, ConjugateGradientReliableUpdate, SchurRedBlackDiagMooeeSolve, MixedPrecisionConjugateGradient,
     MixedPrecisionConjugateGradientBatched, MixedParams,
     ConjugateGradientMultiShift, MultiShiftFunction, MultiShiftResult,

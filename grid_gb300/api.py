@@ -565,6 +565,140 @@ class WilsonFermion(_FermionOperator):
         self._finish(h, U, stream)
 
 
+_proto("gb_wilson_tm5d_create", [_ip, _i, _dp, _dp, _dp, _i, _vp, C.c_uint, C.POINTER(_vp)])
+_proto("gb_op_tm_update", [_vp, _dp, _dp])
+_proto("gb_field_dft_s", [_vp, _vp, _dp])
+_proto("gb_field_copy_slice5", [_vp, _i, _vp, _i])
+_proto("gb_field_chiral_scale", [_vp, _vp, _dp])
+
+
+class WilsonTMFermion5D(_FermionOperator):
+    """WilsonTMFermion5D(U, ..., mass, mu) (WilsonTMFermion5D.h:40-145): len(mass) slices
+    of the 4D Wilson hop with Mooee = (4 + m_s) + i mu_s gamma5.  Its fields hold the
+    slices as right-hand-side slots; its CG converges every slice."""
+
+    def __init__(self, U, dims, mass, mu, phases=None, precision=F64, stream=None, flags=0):
+        self.dims = tuple(int(x) for x in dims)
+        self.kind = 0
+        self.mass = 0.0
+        ph = antiperiodic_t() if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        u = np.ascontiguousarray(mu, dtype=np.float64)
+        if m.shape != u.shape:
+            raise GridError(1, "mass and mu differ in length")
+        h = _vp()
+        _check(lib.gb_wilson_tm5d_create(_dims(dims), int(m.size), _dptr(m), _dptr(u), _dptr(ph), int(precision),
+                                         _vp(stream or 0), int(flags), C.byref(h)))
+        self._finish(h, U, stream)
+        self.nslices = int(m.size)
+
+    def update(self, mass, mu):
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        u = np.ascontiguousarray(mu, dtype=np.float64)
+        if m.size != self.nslices or u.size != self.nslices:
+            raise GridError(1, "one mass and one mu per slice")
+        _check(lib.gb_op_tm_update(self.h, _dptr(m), _dptr(u)))
+
+
+def dft_s(src: FermionField, dst: FermionField, mat: np.ndarray):
+    """dst_k = sum_s mat[k, s] src_s along the fifth dimension (complex Ls x Ls)."""
+    m = np.ascontiguousarray(mat, dtype=np.complex128)
+    _check(lib.gb_field_dft_s(src.h, dst.h, m.ctypes.data_as(_dp)))
+
+
+def copy_slice5(dst: FermionField, t: int, src: FermionField, s: int):
+    """slot t of dst = slot s of src (fields of any Ls on the same 4D lattice and stream)."""
+    _check(lib.gb_field_copy_slice5(dst.h, int(t), src.h, int(s)))
+
+
+def chiral_scale(src: FermionField, dst: FermionField, up, down):
+    """dst = up[q] P+ src + down[q] P- src on every slot q (complex per slot)."""
+    c = np.empty((len(up), 4), dtype=np.float64)
+    c[:, 0], c[:, 1] = np.real(up), np.imag(up)
+    c[:, 2], c[:, 3] = np.real(down), np.imag(down)
+    _check(lib.gb_field_chiral_scale(src.h, dst.h, _dptr(np.ascontiguousarray(c.reshape(-1)))))
+
+
+class FourierAcceleratedPV:
+    """FourierAcceleratedPV(dwfPV, Umu, cg, group_in_s=2) (FourierAcceleratedPV.h:56-237):
+    pvInv(src, dst) solves the Pauli-Villars (mass 1) system of a Cayley operator with
+    constant real b, c.  A twisted DFT along s (e^{-i pi s / Ls}, then the Ls-point
+    transform) makes it block diagonal; modes s and Ls-1-s pair into a 5D twisted-mass
+    Wilson system with
+      mass = -(b^2 M5 + c (1 - cos p + c M5) + b (cos p - 1 + 2 c M5 cos p)) / den,
+      mu = (b + c) sin p / den,  den = b^2 + c^2 + 2 b c cos p,  p = pi (2 s + 1) / Ls,
+    mu of opposite sign on the partner; group_in_s pairs are solved together by the
+    red-black Schur CG, each solution recombined as (pA -+ pB gamma5) / (pA^2 - pB^2) with
+    pA = b + c cos p, pB = -i c sin p, and the inverse transform and twist give dst."""
+
+    def __init__(self, dwfPV, Umu, cg, group_in_s=2):
+        self.dwfPV, self.Umu, self.cg, self.group_in_s = dwfPV, Umu, cg, int(group_in_s)
+        Ls = dwfPV.Ls
+        if Ls % (2 * self.group_in_s) != 0:
+            raise GridError(1, "Ls must be a multiple of 2 * group_in_s")
+        if getattr(dwfPV, "nrhs", 1) != 1:
+            raise GridError(8, "FourierAcceleratedPV: one right-hand side")
+        if hasattr(dwfPV, "gamma") and not np.allclose(dwfPV.gamma, dwfPV.gamma[0]):
+            raise GridError(8, "FourierAcceleratedPV: constant real b, c expected (CayleyFermion with omega_s = 1)")
+
+    def _tm(self):
+        if not hasattr(self, "tm"):
+            n = 2 * self.group_in_s
+            self.tm = WilsonTMFermion5D(self.Umu, self.dwfPV.dims, np.zeros(n), np.zeros(n), self.dwfPV.phases,
+                                        self.dwfPV.precision)
+        return self.tm
+
+    def pvInv(self, src: FermionField, dst: FermionField):
+        op = self.dwfPV
+        Ls, b, c, M5 = op.Ls, op.b, op.c, op.M5
+        s_idx = np.arange(Ls)
+        F = np.exp(-2j * np.pi * np.outer(s_idx, s_idx) / Ls)
+        T = F * np.exp(-1j * np.pi * s_idx / Ls)[None, :]                       # rotatePV(., ., false)
+        Binv = (np.exp(1j * np.pi * s_idx / Ls)[:, None] * F.conj()) / Ls      # rotatePV(., ., true)
+        src_diag, dst_diag = op.FermionField(), op.FermionField().zero()
+        dft_s(src, src_diag, T)
+        tm = self._tm()
+        g = self.group_in_s
+        ts, tx, ty = tm.FermionField(), tm.FermionField(), tm.FermionField()
+        solver = SchurRedBlackDiagMooeeSolve(self.cg)
+        for sgroup in range(Ls // 2 // g):
+            vmass, vmu, up, down = np.zeros(2 * g), np.zeros(2 * g), np.zeros(2 * g, complex), np.zeros(2 * g, complex)
+            for sidx in range(g):
+                s = sgroup * g + sidx
+                p = np.pi / Ls * (2.0 * s + 1.0)
+                cp, sp = np.cos(p), np.sin(p)
+                den = b * b + c * c + 2.0 * b * c * cp
+                mass = -(b * b * M5 + c * (1.0 - cp + c * M5) + b * (-1.0 + cp + 2.0 * c * cp * M5)) / den
+                mu = (b + c) * sp / den
+                vmass[2 * sidx:2 * sidx + 2] = mass
+                vmu[2 * sidx], vmu[2 * sidx + 1] = mu, -mu
+                pA, pB = b + c * cp, -1j * c * sp
+                pden = pA * pA - pB * pB
+                up[2 * sidx], down[2 * sidx] = (pA - pB) / pden, (pA + pB) / pden          # (pA - pB g5) / den
+                up[2 * sidx + 1], down[2 * sidx + 1] = (pA + pB) / pden, (pA - pB) / pden  # (pA + pB g5) / den
+                copy_slice5(ts, 2 * sidx, src_diag, s)
+                copy_slice5(ts, 2 * sidx + 1, src_diag, Ls - s - 1)
+            tm.update(vmass, vmu)
+            tx.zero()
+            solver(tm, ts, tx)
+            chiral_scale(tx, ty, up, down)
+            for sidx in range(g):
+                s = sgroup * g + sidx
+                copy_slice5(dst_diag, s, ty, 2 * sidx)
+                copy_slice5(dst_diag, Ls - s - 1, ty, 2 * sidx + 1)
+        dft_s(dst_diag, dst, Binv)
+
+
+class PauliVillarsSolverFourierAccel:
+    """PauliVillarsSolverFourierAccel(Umu, CG) (PauliVillarsInverters.h:74-88)."""
+
+    def __init__(self, Umu, cg: ConjugateGradient, group_in_s=2):
+        self.Umu, self.CG, self.group_in_s = Umu, cg, group_in_s
+
+    def __call__(self, matrix, src, sol):
+        FourierAcceleratedPV(matrix, self.Umu, self.CG, self.group_in_s).pvInv(src, sol)
+
+
 class MobiusFermion(_FermionOperator):
     """MobiusFermion<WilsonImplD/F>(U, FGrid, FrbGrid, UGrid, UrbGrid, mf, M5, b, c)."""
 
@@ -574,6 +708,7 @@ class MobiusFermion(_FermionOperator):
         self.M5, self.b, self.c = float(M5), float(b), float(c)
         self.kind = 1
         ph = antiperiodic_t() if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        self.phases = ph
         h = _vp()
         _check(lib.gb_mobius_create(_dims(dims), int(Ls), float(mf), float(M5), float(b), float(c), _dptr(ph),
                                     int(precision), int(nrhs), _vp(stream or 0), int(flags), C.byref(h)))
@@ -628,6 +763,7 @@ class ZMobiusFermion(MobiusFermion):
         self.gamma = [complex(z) for z in gamma]
         self.kind = 1
         ph = antiperiodic_t() if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        self.phases = ph
         gm = np.ascontiguousarray([v for z in self.gamma for v in (z.real, z.imag)], dtype=np.float64)
         h = _vp()
         _check(lib.gb_zmobius_create(_dims(dims), len(self.gamma), float(mf), float(M5), _dptr(gm), float(b), float(c),

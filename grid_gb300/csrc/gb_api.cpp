@@ -357,9 +357,33 @@ int op_meooe(Op* op, Field* in, Field* out, int dag) {
   return op_meooe5d(op, t, out, 1);
 }
 
+// the per-slot chiral diagonal of a twisted-mass operator (WilsonTMFermion5D.h:82-135):
+// Mooee = (4 + m) + i mu gamma5, MooeeInv = ((4 + m) - i mu gamma5) / ((4 + m)^2 + mu^2);
+// the daggers conjugate
+static int tm_diag(Op* op, Field* in, Field* out, int dag, int inverse, Field* z, double zc) {
+  const int L5 = op->L5;
+  std::vector<double> ur(L5), ui(L5), dr(L5), di(L5);
+  for (int s = 0; s < L5; s++) {
+    const double m = 4.0 + op->tm_mass[s], mu = op->tm_mu[s];
+    double re = m, im = mu;  // P+ component of Mooee
+    if (inverse) { const double q = m * m + mu * mu; re = m / q; im = -mu / q; }
+    if (dag) im = -im;
+    ur[s] = re; ui[s] = im;  // spins 0,1: gamma5 = +1
+    dr[s] = re; di[s] = -im; // spins 2,3: gamma5 = -1
+  }
+  const int halves = in->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++) {
+    HalfView zv = z ? half_view(z, h) : HalfView{};
+    GB_TRY(launch_chiral_scale(op, half_view(in, h), z ? &zv : nullptr, zc, half_view(out, h), ur.data(), ui.data(),
+                               dr.data(), di.data()));
+  }
+  return GB_OK;
+}
+
 int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
   if (in->full() != out->full()) { set_error("Mooee: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
+  if (op->tm) return tm_diag(op, in, out, dag, 0, z, zc);
   if (op->kind == 0) {
     if (z) return field_axpby(out, op->diag_mass, zc, in, z);
     return field_scale(out, op->diag_mass, in);
@@ -377,6 +401,7 @@ int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
   if (in->full() != out->full()) { set_error("MooeeInv: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
+  if (op->tm) return tm_diag(op, in, out, dag, 1, nullptr, 0.0);
   if (op->kind == 0) return field_scale(out, 1.0 / op->diag_mass, in);
   if (op->zmobius) {
     ZCoefsHost h;
@@ -440,6 +465,7 @@ int op_m(Op* op, Field* in, Field* out, int dag) {
   if (!in->full() || !out->full()) { set_error("M: full fields expected"); return GB_ERR_BAD_PARITY; }
   if (op->kind == 0) {
     GB_TRY(op_dhop_full(op, in, out, dag));
+    if (op->tm) return tm_diag(op, in, out, dag, 0, out, 1.0);  // out = Mooee in + Dhop in
     return field_axpby(out, 1.0, op->diag_mass, out, in);
   }
   Field* Din;
@@ -1287,6 +1313,73 @@ int gb_op_set_mass(gb_op_t op, double mass) {
   }
   return GB_OK;
 }
+// WilsonTMFermion5D (WilsonTMFermion5D.h:40-145): a Wilson operator on nslices slots
+int gb_wilson_tm5d_create(const int dims[4], int nslices, const double* mass, const double* mu, const double* phases,
+                          int precision, void* stream, unsigned flags, gb_op_t* out) {
+  if (!mass || !mu || !out) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (nslices < 2 || (nslices & 1) || nslices > kMaxSlots) {
+    set_error("WilsonTMFermion5D: an even number of slices in [2, %d]", kMaxSlots);
+    return GB_ERR_BAD_ARG;
+  }
+  if (precision == GB_F16) { set_error("WilsonTMFermion5D: FP64 or FP32"); return GB_ERR_UNSUPPORTED; }
+  GB_TRY(op_create(0, dims, 1, 0.0, 0.0, 0.0, 0.0, phases, precision, nslices, stream, flags, out));
+  Op* op = *out;
+  op->tm = true;
+  op->tm_mass.assign(mass, mass + nslices);
+  op->tm_mu.assign(mu, mu + nslices);
+  return GB_OK;
+}
+int gb_op_tm_update(gb_op_t op, const double* mass, const double* mu) {
+  GB_TRY(check_op_geometry(op));
+  if (!op->tm || !mass || !mu) { set_error("tm update: a twisted-mass operator and both arrays"); return GB_ERR_BAD_ARG; }
+  op->tm_mass.assign(mass, mass + op->L5);
+  op->tm_mu.assign(mu, mu + op->L5);
+  return GB_OK;
+}
+
+// the fifth-dimension transforms of the Fourier-accelerated Pauli-Villars solve
+int gb_field_dft_s(gb_field_t in, gb_field_t out, const double* mat) {
+  GB_TRY(check_conf(in, out));
+  if (!mat || in == out) { set_error("DFT along s: a matrix and distinct fields"); return GB_ERR_BAD_ARG; }
+  if (in->full() != out->full()) { set_error("DFT along s: full/half mismatch"); return GB_ERR_BAD_PARITY; }
+  out->subset = in->subset;
+  const int halves = in->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++) GB_TRY(launch_dft_s(in->op, half_view(in, h), half_view(out, h), mat));
+  return GB_OK;
+}
+int gb_field_copy_slice5(gb_field_t dst, int t, gb_field_t src, int s) {
+  if (!dst || !src) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  Op *od = dst->op, *os = src->op;
+  for (int k = 0; k < 4; k++)
+    if (od->dims[k] != os->dims[k]) { set_error("slice copy: different 4D extents"); return GB_ERR_BAD_ARG; }
+  if (od->stream != os->stream) { set_error("slice copy: fields on different streams"); return GB_ERR_BAD_ARG; }
+  if (dst->full() != src->full() || (!dst->full() && dst->subset != src->subset)) {
+    set_error("slice copy: checkerboards differ");
+    return GB_ERR_BAD_PARITY;
+  }
+  if (s < 0 || s >= os->L5 || t < 0 || t >= od->L5) { set_error("slice copy: slot out of range"); return GB_ERR_BAD_ARG; }
+  const int halves = src->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_copy_slot(od, half_view(src, h), os->L5, s, half_view(dst, h), od->L5, t));
+  return GB_OK;
+}
+int gb_field_chiral_scale(gb_field_t in, gb_field_t out, const double* coef) {
+  GB_TRY(check_conf(in, out));
+  if (!coef) { set_error("null argument"); return GB_ERR_BAD_ARG; }
+  if (in->full() != out->full()) { set_error("chiral scale: full/half mismatch"); return GB_ERR_BAD_PARITY; }
+  Op* op = in->op;
+  const int L5 = op->L5;
+  if (L5 > kMaxSlots) { set_error("chiral scale: L5 = %d above %d", L5, kMaxSlots); return GB_ERR_UNSUPPORTED; }
+  std::vector<double> ur(L5), ui(L5), dr(L5), di(L5);
+  for (int q = 0; q < L5; q++) { ur[q] = coef[4 * q]; ui[q] = coef[4 * q + 1]; dr[q] = coef[4 * q + 2]; di[q] = coef[4 * q + 3]; }
+  out->subset = in->subset;
+  const int halves = in->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_chiral_scale(op, half_view(in, h), nullptr, 0.0, half_view(out, h), ur.data(), ui.data(), dr.data(),
+                               di.data()));
+  return GB_OK;
+}
+
 int gb_op_mass(gb_op_t op, double* mass) {
   GB_TRY(check_op_geometry(op));
   if (!mass) { set_error("null argument"); return GB_ERR_BAD_ARG; }

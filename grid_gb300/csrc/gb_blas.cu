@@ -783,3 +783,147 @@ extern "C" int gb_bounded_wait_test(gb_op_t op, int set_flag, long long max_poll
   }
   return GB_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Per-slot chiral complex scaling and the fifth-dimension transforms of the
+// Fourier-accelerated Pauli-Villars solve (FourierAcceleratedPV.h:56-237) and of the
+// twisted-mass 5D Wilson operator (WilsonTMFermion5D.h:82-135).
+// ---------------------------------------------------------------------------------------
+namespace gb {
+namespace {
+
+// out_i = d(slot, chirality) x_i + zc z_i, d = dr + i di per slot for spins 0,1 (P+) and
+// spins 2,3 (P-); slots are the L5 positions s5 of a 5D site index
+struct ChiralCoef {
+  double up_re[kMaxSlots], up_im[kMaxSlots], dn_re[kMaxSlots], dn_im[kMaxSlots];
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) chiral_scale_kernel(const GeoParams g, const void* x, const float* xn, const void* z,
+                                                           const float* zn, double zc, void* out, float* outn,
+                                                           const ChiralCoef c) {
+  using R = typename Arith<T>::type;
+  const size_t n5 = size_t(g.half4) * g.L5;
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  const int s5 = int(i % g.L5);
+  Spinor<R> a;
+  SpinorIO<T>::load(x, xn, n5, i, a);
+  Spinor<R> b;
+  if (z) SpinorIO<T>::load(z, zn, n5, i, b);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const R dr = R(k < 6 ? c.up_re[s5] : c.dn_re[s5]);
+    const R di = R(k < 6 ? c.up_im[s5] : c.dn_im[s5]);
+    R re = dr * a.re[k] - di * a.im[k];
+    R im = dr * a.im[k] + di * a.re[k];
+    if (z) { re += R(zc) * b.re[k]; im += R(zc) * b.im[k]; }
+    a.re[k] = re;
+    a.im[k] = im;
+  }
+  SpinorIO<T>::store(out, outn, n5, i, a);
+}
+
+// out_{r,k} = sum_s mat[k][s] in_{r,s} along each rhs block of Ls slots; one thread per
+// (half-site, rhs, output slot k)
+template <class T>
+__global__ void __launch_bounds__(256) dft_s_kernel(const GeoParams g, const void* in, const float* inn, void* out,
+                                                    float* outn, const double2* mat) {
+  using R = typename Arith<T>::type;
+  const size_t n5 = size_t(g.half4) * g.L5;
+  const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n5) return;
+  const size_t xcb = t / g.L5;
+  const int s5 = int(t - xcb * g.L5);
+  const int r = s5 / g.Ls, k = s5 - r * g.Ls;
+  const size_t base = xcb * g.L5 + size_t(r) * g.Ls;
+  R accr[12], acci[12];
+#pragma unroll
+  for (int q = 0; q < 12; q++) { accr[q] = R(0); acci[q] = R(0); }
+  for (int s = 0; s < g.Ls; s++) {
+    Spinor<R> a;
+    SpinorIO<T>::load(in, inn, n5, base + s, a);
+    const double2 m = mat[size_t(k) * g.Ls + s];
+    const R mr = R(m.x), mi = R(m.y);
+#pragma unroll
+    for (int q = 0; q < 12; q++) {
+      accr[q] += mr * a.re[q] - mi * a.im[q];
+      acci[q] += mr * a.im[q] + mi * a.re[q];
+    }
+  }
+  Spinor<R> o;
+#pragma unroll
+  for (int q = 0; q < 12; q++) { o.re[q] = accr[q]; o.im[q] = acci[q]; }
+  SpinorIO<T>::store(out, outn, n5, t, o);
+}
+
+// slot t of dst (L5 = L5d) = slot s of src (L5 = L5s), same 4D checkerboard half
+template <class T>
+__global__ void __launch_bounds__(256) copy_slot_kernel(int64_t half4, const void* src, const float* srcn, int L5s, int s,
+                                                        void* dst, float* dstn, int L5d, int tslot) {
+  using R = typename Arith<T>::type;
+  const int64_t x = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (x >= half4) return;
+  Spinor<R> a;
+  SpinorIO<T>::load(src, srcn, size_t(half4) * L5s, size_t(x) * L5s + s, a);
+  SpinorIO<T>::store(dst, dstn, size_t(half4) * L5d, size_t(x) * L5d + tslot, a);
+}
+
+}  // namespace
+
+int launch_chiral_scale(Op* op, HalfView x, const HalfView* z, double zc, HalfView out, const double* up_re,
+                        const double* up_im, const double* dn_re, const double* dn_im) {
+  if (op->L5 > kMaxSlots) { set_error("chiral scaling: L5 = %d above %d", op->L5, kMaxSlots); return GB_ERR_UNSUPPORTED; }
+  if (x.prec != out.prec || (z && z->prec != x.prec)) { set_error("chiral scaling: mixed precisions"); return GB_ERR_BAD_ARG; }
+  ChiralCoef c;
+  for (int s = 0; s < kMaxSlots; s++) {
+    const bool in = s < op->L5;
+    c.up_re[s] = in ? up_re[s] : 0; c.up_im[s] = in ? up_im[s] : 0;
+    c.dn_re[s] = in ? dn_re[s] : 0; c.dn_im[s] = in ? dn_im[s] : 0;
+  }
+  const GeoParams g = geo(op);
+  const size_t n = op->n5();
+  const void* zd = z ? z->data : nullptr;
+  const float* zn = z ? z->norms : nullptr;
+  switch (x.prec) {
+    case GB_F64: chiral_scale_kernel<double><<<nblk(n), 256, 0, op->stream>>>(g, x.data, x.norms, zd, zn, zc, out.data, out.norms, c); break;
+    case GB_F32: chiral_scale_kernel<float><<<nblk(n), 256, 0, op->stream>>>(g, x.data, x.norms, zd, zn, zc, out.data, out.norms, c); break;
+    case GB_F16: chiral_scale_kernel<__half><<<nblk(n), 256, 0, op->stream>>>(g, x.data, x.norms, zd, zn, zc, out.data, out.norms, c); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+int launch_dft_s(Op* op, HalfView in, HalfView out, const double* mat_host) {
+  if (in.prec != out.prec) { set_error("DFT along s: mixed precisions"); return GB_ERR_BAD_ARG; }
+  const int Ls = op->Ls;
+  double2* dmat = nullptr;
+  GB_CHECK_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dmat), size_t(Ls) * Ls * sizeof(double2), op->stream));
+  struct Free { double2* p; cudaStream_t s; ~Free() { cudaFreeAsync(p, s); } } guard{dmat, op->stream};
+  GB_CHECK_CUDA(cudaMemcpyAsync(dmat, mat_host, size_t(Ls) * Ls * sizeof(double2), cudaMemcpyHostToDevice, op->stream));
+  const GeoParams g = geo(op);
+  const size_t n = op->n5();
+  switch (in.prec) {
+    case GB_F64: dft_s_kernel<double><<<nblk(n), 256, 0, op->stream>>>(g, in.data, in.norms, out.data, out.norms, dmat); break;
+    case GB_F32: dft_s_kernel<float><<<nblk(n), 256, 0, op->stream>>>(g, in.data, in.norms, out.data, out.norms, dmat); break;
+    case GB_F16: dft_s_kernel<__half><<<nblk(n), 256, 0, op->stream>>>(g, in.data, in.norms, out.data, out.norms, dmat); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  // the host matrix must outlive the copy: wait before returning
+  GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+  return GB_OK;
+}
+
+int launch_copy_slot(Op* op, HalfView src, int L5s, int s, HalfView dst, int L5d, int t) {
+  if (src.prec != dst.prec) { set_error("slot copy: mixed precisions"); return GB_ERR_BAD_ARG; }
+  const size_t n = size_t(op->half4);
+  switch (src.prec) {
+    case GB_F64: copy_slot_kernel<double><<<nblk(n), 256, 0, op->stream>>>(op->half4, src.data, src.norms, L5s, s, dst.data, dst.norms, L5d, t); break;
+    case GB_F32: copy_slot_kernel<float><<<nblk(n), 256, 0, op->stream>>>(op->half4, src.data, src.norms, L5s, s, dst.data, dst.norms, L5d, t); break;
+    case GB_F16: copy_slot_kernel<__half><<<nblk(n), 256, 0, op->stream>>>(op->half4, src.data, src.norms, L5s, s, dst.data, dst.norms, L5d, t); break;
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+}  // namespace gb

@@ -29,6 +29,7 @@ namespace gb {
 
 constexpr int kMaxLs = 64;      // longest fifth dimension handled by the 5D kernels
 constexpr int kMaxL5 = 1024;    // Ls * nrhs upper bound
+constexpr int kMaxSlots = 64;   // L5 bound of the per-slot coefficient kernels
 constexpr int kRedBlocks = 1216;  // 8 blocks per SM on 152 SMs for reductions
 
 void set_error(const char* fmt, ...);
@@ -84,6 +85,10 @@ struct Op {
   // ZMobius: complex omega_s, so complex Cayley coefficients (the real arrays above are
   // then unused)
   bool zmobius = false;
+  // WilsonTMFermion5D (a Wilson operator, kind 0, whose L5 slots are the fifth dimension):
+  // Mooee = (4 + m_s) + i mu_s gamma5 per slot
+  bool tm = false;
+  std::vector<double> tm_mass, tm_mu;
   std::vector<std::complex<double>> zgamma, zbs, zcs, zbee, zcee, zdee, zlee, zleem, zuee, zueem;
 
   // reduction scratch
@@ -111,12 +116,21 @@ struct Op {
 // Fields created on one operator may be used with another of the same geometry (4D
 // extents, Ls, right-hand sides) on the same stream: the device layout is identical and
 // the work of both is ordered on that one stream.
+// A twisted-mass 5D operator keeps its slices in the slots where a Cayley operator keeps
+// s, so its fields and those of a 5D grid with Ls = its slice count (one right-hand side)
+// share one layout.
 inline bool ops_conformable(const Op* a, const Op* b) {
   if (a == b) return true;
   if (!a || !b) return false;
   for (int k = 0; k < 4; k++)
     if (a->dims[k] != b->dims[k]) return false;
-  return a->Ls == b->Ls && a->nrhs == b->nrhs && a->nrhs_user == b->nrhs_user && a->stream == b->stream;
+  if (a->stream != b->stream) return false;
+  if (a->tm != b->tm) {
+    const Op* t = a->tm ? a : b;
+    const Op* o = a->tm ? b : a;
+    return o->nrhs == 1 && o->L5 == t->L5;
+  }
+  return a->Ls == b->Ls && a->nrhs == b->nrhs && a->nrhs_user == b->nrhs_user;
 }
 
 struct Field {
@@ -219,6 +233,13 @@ int launch_surface_extract(Op* op, HalfView even, HalfView odd, double* c4, int 
 int launch_slice(Op* op, double* c4, HalfView even, HalfView odd, int s, int insert);
 // CayleyFermion5D::P (dag = 0) / Pdag (dag = 1) on one checkerboard half
 int launch_chiral_shift(Op* op, HalfView in, HalfView out, int dag);
+// out = d(slot, chirality) x [+ zc z] with per-slot complex d for spins 0,1 and 2,3
+int launch_chiral_scale(Op* op, HalfView x, const HalfView* z, double zc, HalfView out, const double* up_re,
+                        const double* up_im, const double* dn_re, const double* dn_im);
+// out_{r,k} = sum_s mat[k][s] in_{r,s} (complex Ls x Ls, row major) along each rhs block
+int launch_dft_s(Op* op, HalfView in, HalfView out, const double* mat_host);
+// slot t of dst (L5d slots) = slot s of src (L5s slots), one checkerboard half
+int launch_copy_slot(Op* op, HalfView src, int L5s, int s, HalfView dst, int L5d, int t);
 int build_neighbours(Op* op);
 
 // CG kernels (gb_blas.cu)

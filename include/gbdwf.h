@@ -243,6 +243,24 @@ int gb_extract_slice(gb_op_t op, gb_field_t f5d, int s, double* out4d, int on_de
  * P+ psi_{s-1} (dag = 1), s cyclic.  Full or half fields; in and out distinct. */
 int gb_P(gb_op_t op, gb_field_t in, gb_field_t out, int dag);
 
+/* WilsonTMFermion5D(U, FGrid, FrbGrid, UGrid, UrbGrid, mass, mu) (WilsonTMFermion5D.h:40-145):
+ * nslices (even, <= 64) independent slices of the 4D Wilson hop with Mooee = (4 + m_s) +
+ * i mu_s gamma5 per slice; the slices are the operator's right-hand-side slots, so its
+ * fields are nslices-right-hand-side 4D Wilson fields and its CG converges each slice to
+ * the tolerance.  FP64 or FP32.  gb_op_tm_update: TM update(mass, mu). */
+int gb_wilson_tm5d_create(const int dims[4], int nslices, const double* mass, const double* mu, const double* phases,
+                          int precision, void* stream, unsigned flags, gb_op_t* out);
+int gb_op_tm_update(gb_op_t op, const double* mass, const double* mu);
+
+/* Fifth-dimension transforms (FourierAcceleratedPV.h:56-237).  gb_field_dft_s: out_k =
+ * sum_s mat[k][s] in_s on each rhs block of Ls slots, mat Ls x Ls complex row major (re,
+ * im).  gb_field_copy_slice5: slot t of dst = slot s of src, fields of any Ls on the same
+ * 4D geometry and stream.  gb_field_chiral_scale: out = c gamma-chirally per slot,
+ * coef[4 q .. 4 q + 3] = (re, im) for spins 0,1 and (re, im) for spins 2,3 of slot q. */
+int gb_field_dft_s(gb_field_t in, gb_field_t out, const double* mat);
+int gb_field_copy_slice5(gb_field_t dst, int t, gb_field_t src, int s);
+int gb_field_chiral_scale(gb_field_t in, gb_field_t out, const double* coef);
+
 /* CayleyFermion5D::SetMass / Mass (CayleyFermion5D.h:71-83); WilsonFermion's mass for
  * Wilson operators.  The Cayley coefficients are rebuilt at once; later calls use them. */
 int gb_op_set_mass(gb_op_t op, double mass);
@@ -325,7 +343,8 @@ int gb_cg_multishift(gb_op_t op, int kind, gb_field_t src, int nshift, const dou
 
 /* SchurRedBlackDiagMooeeSolve(CG)(M, src, sol) (SchurRedBlack.h:236-291,373-436).
  * op_lo == NULL: plain CG in op's precision; else mixed precision (reliable update).
- * unprec_resid (may be NULL): |M sol - src| / |src| per right-hand side. */
+ * unprec_resid (may be NULL): |M sol - src| / |src| per right-hand side of op (an array
+ * of gb_op_info's nrhs doubles; the slices of a twisted-mass operator count as such). */
 int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, const gb_cg_params* p,
                    gb_cg_result* res, double* unprec_resid);
 

@@ -30,6 +30,7 @@
 #error "gbgrid.h is C++; C callers use gbdwf.h"
 #endif
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -523,11 +524,12 @@ template <class Impl> class MobiusFermion : public FermionOperator<Impl> {
   typedef typename Impl::ImplParams ImplParams;
   int Ls;
   RealD M5, b, c;
+  ImplParams params;
   MobiusFermion(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
                 GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid, RealD mass, RealD M5_,
                 RealD b_, RealD c_, const ImplParams& p = ImplParams())
       : Base(&FiveDimGrid, &FiveDimRedBlackGrid, &FourDimGrid, &FourDimRedBlackGrid, mass),
-        Ls(FiveDimGrid.Ls), M5(M5_), b(b_), c(c_) {
+        Ls(FiveDimGrid.Ls), M5(M5_), b(b_), c(c_), params(p) {
     const std::vector<double> ph = Base::phases(p);
     gbdetail::check(gb_mobius_create(FourDimGrid.dims4.data(), Ls, mass, M5_, b_, c_, ph.data(), Impl::precision, 1,
                                      gbdetail::stream(), 0, &this->op_),
@@ -602,6 +604,7 @@ template <class Impl> class ZMobiusFermion : public MobiusFermion<Impl> {
              M5_, b_, c_),
         omega(gamma) {
     if (int(gamma.size()) != this->Ls) throw GridError(GB_ERR_BAD_ARG, "ZMobiusFermion: gamma.size() != Ls");
+    this->params = p;
     const std::vector<double> ph = FermionOperator<Impl>::phases(p);
     gbdetail::check(gb_zmobius_create(FourDimGrid.dims4.data(), this->Ls, mass, M5_,
                                       reinterpret_cast<const double*>(gamma.data()), b_, c_, ph.data(),
@@ -712,6 +715,31 @@ template <class Impl> class ScaledShamirFermion : public MobiusFermion<Impl> {
                       RealD scale, const ImplParams& p = ImplParams())
       : MobiusFermion<Impl>(U, FiveDimGrid, FiveDimRedBlackGrid, FourDimGrid, FourDimRedBlackGrid, mass, M5_,
                             0.5 * (scale + 1.0), 0.5 * (scale - 1.0), p) {}
+};
+
+// WilsonTMFermion5D<Impl> (WilsonTMFermion5D.h:40-145): FiveDimGrid.Ls slices of the 4D
+// Wilson hop with Mooee = (4 + mass[s]) + i mu[s] gamma5
+template <class Impl> class WilsonTMFermion5D : public FermionOperator<Impl> {
+  typedef FermionOperator<Impl> Base;
+
+ public:
+  typedef typename Impl::GaugeField GaugeField;
+  typedef typename Impl::ImplParams ImplParams;
+  WilsonTMFermion5D(const GaugeField& U, GridCartesian& FiveDimGrid, GridRedBlackCartesian& FiveDimRedBlackGrid,
+                    GridCartesian& FourDimGrid, GridRedBlackCartesian& FourDimRedBlackGrid,
+                    const std::vector<RealD>& mass, const std::vector<RealD>& mu, const ImplParams& p = ImplParams())
+      : Base(&FiveDimGrid, &FiveDimRedBlackGrid, &FourDimGrid, &FourDimRedBlackGrid, 0.0) {
+    if (int(mass.size()) != FiveDimGrid.Ls || mu.size() != mass.size())
+      throw GridError(GB_ERR_BAD_ARG, "WilsonTMFermion5D: one mass and one mu per slice");
+    const std::vector<double> ph = Base::phases(p);
+    gbdetail::check(gb_wilson_tm5d_create(FourDimGrid.dims4.data(), FiveDimGrid.Ls, mass.data(), mu.data(), ph.data(),
+                                          Impl::precision, gbdetail::stream(), 0, &this->op_),
+                    "WilsonTMFermion5D");
+    this->ImportGauge(U);
+  }
+  void update(const std::vector<RealD>& mass, const std::vector<RealD>& mu) {
+    Base::run(gb_op_tm_update(this->op_, mass.data(), mu.data()), "WilsonTMFermion5D::update");
+  }
 };
 
 // Grid's ZWilsonImpl carries the complex Cayley coefficients in the action; here the
@@ -1068,8 +1096,14 @@ template <class Field> class SchurRedBlackDiagMooeeSolve {
     if (!cg) throw GridError(GB_ERR_UNSUPPORTED, "SchurRedBlackDiagMooeeSolve: a ConjugateGradient solver expected");
     const gb_cg_params p = cg->params();
     gb_cg_result r;
+    // one unpreconditioned residual per right-hand side (slot) of the operator
+    int ls = 0, nrhs = 1, prec = 0;
+    int64_t half4 = 0;
+    gbdetail::check(gb_op_info(M.handle(), &ls, &nrhs, &half4, &prec), "SchurRedBlackDiagMooeeSolve");
+    std::vector<double> unprec_v(size_t(nrhs > 0 ? nrhs : 1), 0.0);
+    const int rc = gb_schur_solve(M.handle(), lo, in.handle(), out.handle(), &p, &r, unprec_v.data());
     double unprec = 0;
-    const int rc = gb_schur_solve(M.handle(), lo, in.handle(), out.handle(), &p, &r, &unprec);
+    for (double v : unprec_v) unprec = std::max(unprec, v);
     IterationsToComplete = cg->IterationsToComplete = r.iterations;
     TrueResidual = cg->TrueResidual = r.true_residual;
     UnpreconditionedResidual = unprec;
@@ -1120,6 +1154,95 @@ template <class Field, class SchurSolverType> class PauliVillarsSolverRBprec {
       throw;
     }
     _Matrix.SetMass(m);
+  }
+};
+
+// FourierAcceleratedPV (FourierAcceleratedPV.h:56-237): the Pauli-Villars (mass 1) inverse of
+// a Cayley operator with constant real b, c.  A twisted DFT along s block-diagonalises it;
+// modes s and Ls-1-s pair into 5D twisted-mass Wilson systems (group_in_s pairs at a time)
+// solved by the red-black Schur CG, recombined with (pA -+ pB gamma5) / (pA^2 - pB^2), and
+// transformed back.
+template <class Field, class Matrix, class GaugeField> class FourierAcceleratedPV {
+  Matrix& dwfPV;
+  const GaugeField& Umu;
+  ConjugateGradient<Field>& cg;
+  int group_in_s;
+
+ public:
+  FourierAcceleratedPV(Matrix& m, const GaugeField& U, ConjugateGradient<Field>& c, int g = 2)
+      : dwfPV(m), Umu(U), cg(c), group_in_s(g) {
+    if (dwfPV.Ls % (2 * group_in_s) != 0) throw GridError(GB_ERR_BAD_ARG, "FourierAcceleratedPV: Ls % (2 group_in_s)");
+  }
+  void pvInv(const Field& src, Field& dst) const {
+    const int Ls = dwfPV.Ls, g = group_in_s;
+    const double b = dwfPV.b, c = dwfPV.c, M5 = dwfPV.M5, pi = 3.14159265358979323846;
+    std::vector<ComplexD> T(size_t(Ls) * Ls), B(size_t(Ls) * Ls);
+    for (int k = 0; k < Ls; k++)
+      for (int s = 0; s < Ls; s++) {
+        T[size_t(k) * Ls + s] = std::polar(1.0, -2 * pi * k * s / Ls - pi * s / Ls);
+        B[size_t(s) * Ls + k] = std::polar(1.0 / Ls, 2 * pi * k * s / Ls + pi * s / Ls);
+      }
+    GridBase* F = dwfPV.FermionGrid();
+    Field src_diag(F), dst_diag(F);
+    dst_diag = Zero();
+    gbdetail::check(gb_field_dft_s(src.handle(), src_diag.handle(), reinterpret_cast<const double*>(T.data())),
+                    "FourierAcceleratedPV");
+    GridCartesian* U4 = dynamic_cast<GridCartesian*>(dwfPV.GaugeGrid());
+    GridCartesian G5(U4->dims4, 2 * g);
+    GridRedBlackCartesian G5rb(&G5);
+    GridRedBlackCartesian U4rb(U4);
+    std::vector<RealD> vmass(2 * g, 0.0), vmu(2 * g, 0.0);
+    typedef WilsonImplT<typename Field::vector_object, vLorentzColourMatrixD> TMImpl;
+    WilsonTMFermion5D<TMImpl> tm(Umu, G5, G5rb, *U4, U4rb, vmass, vmu, dwfPV.params);
+    SchurRedBlackDiagMooeeSolve<Field> sol(cg);
+    Field ts(&G5), tx(&G5), ty(&G5);
+    std::vector<double> coef(size_t(8) * g);
+    for (int sgroup = 0; sgroup < Ls / 2 / g; sgroup++) {
+      for (int sidx = 0; sidx < g; sidx++) {
+        const int s = sgroup * g + sidx;
+        const double p = pi / Ls * (2.0 * s + 1.0), cp = std::cos(p), sp = std::sin(p);
+        const double den = b * b + c * c + 2.0 * b * c * cp;
+        const double mass = -(b * b * M5 + c * (1.0 - cp + c * M5) + b * (-1.0 + cp + 2.0 * c * cp * M5)) / den;
+        const double mu = (b + c) * sp / den;
+        vmass[2 * sidx] = vmass[2 * sidx + 1] = mass;
+        vmu[2 * sidx] = mu;
+        vmu[2 * sidx + 1] = -mu;
+        const ComplexD pA(b + c * cp, 0.0), pB(0.0, -c * sp), pden = pA * pA - pB * pB;
+        const ComplexD lo = (pA - pB) / pden, hi = (pA + pB) / pden;
+        const ComplexD cf[4] = {lo, hi, hi, lo};  // slot 2 sidx: (pA - pB g5); 2 sidx + 1: (pA + pB g5)
+        for (int q = 0; q < 4; q++) {
+          coef[size_t(8) * sidx + 2 * q] = cf[q].real();
+          coef[size_t(8) * sidx + 2 * q + 1] = cf[q].imag();
+        }
+        gbdetail::check(gb_field_copy_slice5(ts.handle(), 2 * sidx, src_diag.handle(), s), "FourierAcceleratedPV");
+        gbdetail::check(gb_field_copy_slice5(ts.handle(), 2 * sidx + 1, src_diag.handle(), Ls - s - 1),
+                        "FourierAcceleratedPV");
+      }
+      tm.update(vmass, vmu);
+      tx = Zero();
+      sol(tm, ts, tx);
+      gbdetail::check(gb_field_chiral_scale(tx.handle(), ty.handle(), coef.data()), "FourierAcceleratedPV");
+      for (int sidx = 0; sidx < g; sidx++) {
+        const int s = sgroup * g + sidx;
+        gbdetail::check(gb_field_copy_slice5(dst_diag.handle(), s, ty.handle(), 2 * sidx), "FourierAcceleratedPV");
+        gbdetail::check(gb_field_copy_slice5(dst_diag.handle(), Ls - s - 1, ty.handle(), 2 * sidx + 1),
+                        "FourierAcceleratedPV");
+      }
+    }
+    gbdetail::check(gb_field_dft_s(dst_diag.handle(), dst.handle(), reinterpret_cast<const double*>(B.data())),
+                    "FourierAcceleratedPV");
+  }
+};
+
+// PauliVillarsSolverFourierAccel (PauliVillarsInverters.h:74-88)
+template <class Field, class GaugeField> class PauliVillarsSolverFourierAccel {
+ public:
+  const GaugeField& Umu;
+  ConjugateGradient<Field>& CG;
+  PauliVillarsSolverFourierAccel(const GaugeField& U, ConjugateGradient<Field>& cg) : Umu(U), CG(cg) {}
+  template <class Matrix> void operator()(Matrix& _Matrix, const Field& src, Field& sol) {
+    FourierAcceleratedPV<Field, Matrix, GaugeField> faPV(_Matrix, Umu, CG);
+    faPV.pvInv(src, sol);
   }
 };
 

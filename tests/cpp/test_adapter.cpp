@@ -222,6 +222,19 @@ int main() {
     typedef PauliVillarsSolverRBprec<LatticeFermion, SchurRedBlackDiagMooeeSolve<LatticeFermion>> PVtype;
     PVtype PV(SchurPV);
     ZeroGuesser<LatticeFermion> Guess;
+    // the Fourier-accelerated Pauli-Villars inverse equals the red-black one
+    {
+      ConjugateGradient<LatticeFermion> CGfa(1e-12, 10000);
+      PauliVillarsSolverFourierAccel<LatticeFermion, LatticeGaugeField> PVfa(Umu, CGfa);
+      LatticeFermion pa(FGrid), pb(FGrid);
+      pa = Zero();
+      pb = Zero();
+      PVfa(Ddwf, src, pa);
+      PV(Ddwf, src, pb);
+      LatticeFermion dp = pa - pb;
+      expect(std::sqrt(norm2(dp) / norm2(pb)) < 1e-9 && Ddwf.Mass() == mass,
+             "PauliVillarsSolverFourierAccel == PauliVillarsSolverRBprec", std::sqrt(norm2(dp) / norm2(pb)));
+    }
     struct Count : MADWFinnerIterCallbackBase {
       int calls = 0;
       void operator()(const RealD) override { calls++; }
