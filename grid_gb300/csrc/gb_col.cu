@@ -195,6 +195,43 @@ __device__ __forceinline__ void col_read(const float4* slot, float (&r)[LS], flo
   }
 }
 
+// the program on one (component, column): slot (and yslot) hold its LS values as LS/2
+// float4 (re_s, re_s+1, im_s, im_s+1); the result replaces slot
+template <int LS, bool DAG, int OPA, int OPB>
+__device__ __forceinline__ void col_run(float4* slot, const float4* yslot, float zc, const ColCoef<LS>& c,
+                                        bool upper) {
+  constexpr int H = LS / 2;
+  const bool first = DAG ? !upper : upper;
+  float xr[LS], xi[LS], orr[LS], oi[LS];
+  col_read<LS>(slot, xr, xi);
+  if (OPA == COL_M5D) {
+    col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
+  } else if (OPA == COL_INV) {
+    col_inv<LS>(xr, xi, c, first);
+#pragma unroll
+    for (int s = 0; s < LS; s++) { orr[s] = xr[s]; oi[s] = xi[s]; }
+  } else if (OPA == COL_INV_M5D) {
+    col_inv<LS>(xr, xi, c, first);
+    col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
+  } else {  // COL_M5D_INV
+    col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
+    col_inv<LS>(orr, oi, c, first);
+  }
+  if (OPB != COLB_NONE) {
+    float yr[LS], yi[LS];
+    col_read<LS>(yslot, yr, yi);
+    if (OPB == COLB_M5D) {
+      col_m5d<LS, DAG>(yr, yi, xr, xi, c.d2, c.u2, c.l2, upper);
+#pragma unroll
+      for (int s = 0; s < LS; s++) { yr[s] = xr[s]; yi[s] = xi[s]; }
+    }
+#pragma unroll
+    for (int s = 0; s < LS; s++) { orr[s] = fmaf(zc, yr[s], orr[s]); oi[s] = fmaf(zc, yi[s], oi[s]); }
+  }
+#pragma unroll
+  for (int m = 0; m < H; m++) slot[m] = make_float4(orr[2 * m], orr[2 * m + 1], oi[2 * m], oi[2 * m + 1]);
+}
+
 template <class T, int LS, bool DAG, int OPA, int OPB>
 __global__ void __launch_bounds__(12 * col_q<LS, OPB != COLB_NONE ? 2 : 1>()) col_kernel(const ColParams p,
                                                                                         const ColCoef<LS> c) {
@@ -211,41 +248,80 @@ __global__ void __launch_bounds__(12 * col_q<LS, OPB != COLB_NONE ? 2 : 1>()) co
   if (OPB != COLB_NONE) ColIO<T, LS, Q>::load(p.y, p.yn, snorm, ty, p.np, q0, nv);
   __syncthreads();
   const int k = t / Q, qq = t - k * Q;
-  if (qq < qn) {
-    const bool upper = k < 6;
-    const bool first = DAG ? !upper : upper;
-    float4* slot = tx + (k * Q + qq) * ST;
-    float xr[LS], xi[LS], orr[LS], oi[LS];
-    col_read<LS>(slot, xr, xi);
-    if (OPA == COL_M5D) {
-      col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
-    } else if (OPA == COL_INV) {
-      col_inv<LS>(xr, xi, c, first);
-#pragma unroll
-      for (int s = 0; s < LS; s++) { orr[s] = xr[s]; oi[s] = xi[s]; }
-    } else if (OPA == COL_INV_M5D) {
-      col_inv<LS>(xr, xi, c, first);
-      col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
-    } else {  // COL_M5D_INV
-      col_m5d<LS, DAG>(xr, xi, orr, oi, c.d1, c.u1, c.l1, upper);
-      col_inv<LS>(orr, oi, c, first);
-    }
-    if (OPB != COLB_NONE) {
-      float yr[LS], yi[LS];
-      col_read<LS>(ty + (k * Q + qq) * ST, yr, yi);
-      if (OPB == COLB_M5D) {
-        col_m5d<LS, DAG>(yr, yi, xr, xi, c.d2, c.u2, c.l2, upper);
-#pragma unroll
-        for (int s = 0; s < LS; s++) { yr[s] = xr[s]; yi[s] = xi[s]; }
-      }
-#pragma unroll
-      for (int s = 0; s < LS; s++) { orr[s] = fmaf(p.zc, yr[s], orr[s]); oi[s] = fmaf(p.zc, yi[s], oi[s]); }
-    }
-#pragma unroll
-    for (int m = 0; m < H; m++) slot[m] = make_float4(orr[2 * m], orr[2 * m + 1], oi[2 * m], oi[2 * m + 1]);
-  }
+  if (qq < qn) col_run<LS, DAG, OPA, OPB>(tx + (k * Q + qq) * ST, ty + (k * Q + qq) * ST, p.zc, c, k < 6);
   __syncthreads();
   ColIO<T, LS, Q>::store(p.out, p.outn, snorm, tx, p.np, q0, nv);
+}
+
+// FP32 programs as a persistent kernel: each CTA walks its tiles of 16 columns with the
+// next tile's inputs arriving by cp.async (16-byte copies straight into the padded,
+// bank-conflict-free shared layout) in a second stage while the current one computes
+// and stores.  No wait spins: cp.async.wait_group waits on the thread's own copies.
+constexpr int kColPipeQ = 16;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// columns [q0, q0 + nv / H) of all 12 planes into a [12][Q][ST] tile
+template <int LS>
+__device__ __forceinline__ void col_issue(const float4* x, float4* tile, size_t np, size_t q0, int nv) {
+  constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>();
+#pragma unroll 4
+  for (int e = threadIdx.x; e < 12 * Q * H; e += 12 * Q) {
+    const int k = e / (Q * H), r = e - k * (Q * H);
+    if (r < nv) {
+      const int qq = r / H, m = r - qq * H;
+      cp_async16(tile + (k * Q + qq) * ST + m, x + size_t(k) * np + q0 * H + r);
+    }
+  }
+}
+
+template <int LS, bool DAG, int OPA, int OPB>
+__global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParams p, const ColCoef<LS> c) {
+  constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>(), NIN = OPB != COLB_NONE ? 2 : 1;
+  constexpr int TILE = 12 * Q * ST;   // float4 of one input tile
+  extern __shared__ float4 col_ring[];  // [2 stages][NIN][12][Q][ST]
+  const size_t ntiles = (p.nq + Q - 1) / Q;
+  const float4* xs = static_cast<const float4*>(p.x);
+  const float4* ys = static_cast<const float4*>(p.y);
+  float4* o = static_cast<float4*>(p.out);
+  const int t = threadIdx.x, k = t / Q, qq = t - k * Q;
+  auto vectors = [&](size_t tile) { return int(min(p.nq - tile * Q, size_t(Q))) * H; };
+  auto issue = [&](size_t tile, int st) {  // one commit group per stage fill, empty past the end
+    if (tile < ntiles) {
+      float4* base = col_ring + size_t(st) * NIN * TILE;
+      col_issue<LS>(xs, base, p.np, tile * Q, vectors(tile));
+      if (NIN == 2) col_issue<LS>(ys, base + TILE, p.np, tile * Q, vectors(tile));
+    }
+    cp_async_commit();
+  };
+  size_t tile = blockIdx.x;
+  issue(tile, 0);
+  issue(tile + gridDim.x, 1);
+  for (int st = 0; tile < ntiles; tile += gridDim.x, st ^= 1) {
+    cp_async_wait<1>();  // this stage's group has landed (the newer one may still fly)
+    __syncthreads();
+    float4* base = col_ring + size_t(st) * NIN * TILE;
+    const int nv = vectors(tile);
+    if (qq < nv / H) col_run<LS, DAG, OPA, OPB>(base + (k * Q + qq) * ST, base + TILE + (k * Q + qq) * ST, p.zc, c, k < 6);
+    __syncthreads();
+#pragma unroll 4
+    for (int e = t; e < 12 * Q * H; e += 12 * Q) {
+      const int kk = e / (Q * H), r = e - kk * (Q * H);
+      if (r < nv) {
+        const int q2 = r / H, m = r - q2 * H;
+        o[size_t(kk) * p.np + tile * Q * H + r] = base[(kk * Q + q2) * ST + m];
+      }
+    }
+    __syncthreads();  // the stage is read out before it is refilled
+    issue(tile + 2 * size_t(gridDim.x), st);
+  }
+  cp_async_wait<0>();
 }
 
 template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost& h, ColCoef<LS>& c) {
@@ -266,8 +342,38 @@ template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost
   }
 }
 
+#ifndef GB_COL_PIPE
+#define GB_COL_PIPE 1
+#endif
+
+template <int LS, bool DAG, int OPA, int OPB>
+static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
+  constexpr int NIN = OPB != COLB_NONE ? 2 : 1;
+  const size_t smem = size_t(2) * NIN * 12 * kColPipeQ * col_stride<LS>() * sizeof(float4);
+  static std::atomic<int> per_sm{0};
+  static std::atomic<int> sms{0};
+  if (per_sm.load() == 0) {
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_kernel<LS, DAG, OPA, OPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(smem)));
+    int n = 0, dev = 0, count = 0;
+    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_kernel<LS, DAG, OPA, OPB>,
+                                                                12 * kColPipeQ, smem));
+    GB_CHECK_CUDA(cudaGetDevice(&dev));
+    GB_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
+    sms.store(count);
+    per_sm.store(n > 0 ? n : 1);
+  }
+  const size_t ntiles = (p.nq + kColPipeQ - 1) / kColPipeQ;
+  const size_t slots = size_t(per_sm.load()) * size_t(sms.load());
+  const unsigned blocks = unsigned(ntiles < slots ? ntiles : slots);
+  col_pipe_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * kColPipeQ, smem, op->stream>>>(p, c);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 template <class T, int LS, bool DAG, int OPA, int OPB>
 static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
+  if (GB_COL_PIPE && sizeof(T) == 4) return col_pipe_go<LS, DAG, OPA, OPB>(op, p, c);
   constexpr int Q = col_q<LS, OPB != COLB_NONE ? 2 : 1>();
   const size_t smem = size_t(OPB != COLB_NONE ? 2 : 1) * 12 * Q * col_stride<LS>() * sizeof(float4) +
                       (sizeof(T) == 2 ? size_t(Q) * LS * sizeof(float) : 0);
