@@ -239,12 +239,18 @@ static int m5d_field(Op* op, Field* psi, Field* phi, Field* chi, const std::vect
 }
 
 // a fused s-column program on every checkerboard half of the fields (FP32 Moebius)
+// (dot: Re<dot|out> partial sums into op->d_partial, their count into *dot_parts; one
+// checkerboard half only)
 static int col_field(Op* op, int opa, int opb, int dag, Field* x, Field* y, Field* out, double zc,
-                     const ColCoefsHost& h) {
+                     const ColCoefsHost& h, Field* dot = nullptr, int* dot_parts = nullptr) {
   const int halves = out->full() ? 2 : 1;
+  if (dot_parts) *dot_parts = 0;
   for (int k = 0; k < halves; k++) {
     const HalfView yv = y ? half_view(y, k) : HalfView{nullptr, nullptr, x->prec};
-    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h));
+    const bool fuse = dot && halves == 1 && dot->prec == x->prec;
+    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h,
+                      fuse ? half_view(dot, k).data : nullptr, fuse ? op->d_partial : nullptr,
+                      fuse ? dot_parts : nullptr));
   }
   return GB_OK;
 }
@@ -415,8 +421,10 @@ int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
   return GB_OK;
 }
 
-// SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349)
-int op_mpc(Op* op, Field* in, Field* out, int dag) {
+// SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349).  With dot (MpcDag of
+// an FP32 Moebius operator) the last program also reduces Re<dot|out> (see col_field).
+int op_mpc(Op* op, Field* in, Field* out, int dag, Field* dot, int* dot_parts) {
+  if (dot_parts) *dot_parts = 0;
   if (in->subset != GB_ODD) { set_error("Mpc: odd checkerboard expected"); return GB_ERR_BAD_PARITY; }
   Field *te1, *te2, *to;
   GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E1, &te1));
@@ -444,7 +452,7 @@ int op_mpc(Op* op, Field* in, Field* out, int dag) {
     ColCoefsHost h;
     coeffs_mooee(op, 1, h.l1, h.d1, h.u1);
     h.l2 = meo.l1; h.d2 = meo.d1; h.u2 = meo.u1;
-    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h);
+    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h, dot, dot_parts);
   }
   GB_TRY(op_meooe(op, in, te1, dag));
   GB_TRY(op_mooee_inv(op, te1, te2, dag));
@@ -452,11 +460,11 @@ int op_mpc(Op* op, Field* in, Field* out, int dag) {
   return op_mooee(op, in, out, dag, to, -1.0);  // out = Mooee in - tmp
 }
 
-int op_mpcdagmpc(Op* op, Field* in, Field* out) {
+int op_mpcdagmpc(Op* op, Field* in, Field* out, int* dot_parts) {
   Field* t;
   GB_TRY(ws_get(op, GB_ODD, in->prec, WS_MPCDAGMPC, &t));
   GB_TRY(op_mpc(op, in, t, 0));
-  return op_mpc(op, t, out, 1);
+  return op_mpc(op, t, out, 1, dot_parts ? in : nullptr, dot_parts);
 }
 
 // M / Mdag on full fields (WilsonFermionImplementation.h:113-127,

@@ -217,8 +217,12 @@ struct ZCoefsHost {
 enum { ZPROG_M5D = 0, ZPROG_INV = 2, ZPROG_DIAG = 3 };
 bool zmobius_ls_supported(int Ls);
 int launch_zcol(Op* op, int prog, int dag, HalfView x, const HalfView* y, HalfView out, double zc, const ZCoefsHost& h);
+// With dotp (FP32, the program MooeeDag - M5Ddag z of MpcDag only) the kernel also
+// writes Re<dotp|out> as per-CTA partial sums [CTA][2] into dot_partial and their count
+// into *dot_parts (0 when it could not fuse; the caller then reduces separately).
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
-               const ColCoefsHost& h);
+               const ColCoefsHost& h, const void* dotp = nullptr, double* dot_partial = nullptr,
+               int* dot_parts = nullptr);
 
 // layout conversion between canonical FP64 (device) and the device layout
 // canonical host layout (complex double or, with canon_prec = GB_F32, complex float) <->

@@ -48,8 +48,11 @@ int op_dhop_full(Op* op, Field* in, Field* out, int dag);
 int op_meooe(Op* op, Field* in, Field* out, int dag);
 int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc);
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag);
-int op_mpc(Op* op, Field* in, Field* out, int dag);
-int op_mpcdagmpc(Op* op, Field* in, Field* out);
+int op_mpc(Op* op, Field* in, Field* out, int dag, Field* dot = nullptr, int* dot_parts = nullptr);
+// dot_parts: when non-null, the last kernel may also reduce Re<in|out> into op->d_partial
+// ([CTA][2], the layout of the inner-product partials) and sets *dot_parts to the number of
+// CTA sums written, or to 0 when it did not
+int op_mpcdagmpc(Op* op, Field* in, Field* out, int* dot_parts = nullptr);
 int op_m(Op* op, Field* in, Field* out, int dag);
 int op_mdagm(Op* op, Field* in, Field* out);
 int op_dminus(Op* op, Field* in, Field* out, int dag);
@@ -59,6 +62,11 @@ double hermop_flops(const Op* op, int kind);
 // kind 0: MdagM on full fields; kind 1: MpcDagMpc on odd half fields
 inline int op_hermop(Op* op, int kind, Field* in, Field* out) {
   return kind == 0 ? op_mdagm(op, in, out) : op_mpcdagmpc(op, in, out);
+}
+// the same, reducing Re<in|out> on the way where the operator's kernels allow it
+inline int op_hermop_dot(Op* op, int kind, Field* in, Field* out, int* dot_parts) {
+  *dot_parts = 0;
+  return kind == 0 ? op_mdagm(op, in, out) : op_mpcdagmpc(op, in, out, dot_parts);
 }
 
 }  // namespace gb

@@ -119,8 +119,11 @@ struct ChunkRunner {
   int launch(int m) {
     for (int j = 0; j < m; j++) {
       GB_TRY(cg_p_update(op, p, r));
-      GB_TRY(op_hermop(op, kind, p, mmp));
-      GB_TRY(cg_alpha(op, p, mmp));
+      // d = <p|mmp>: reduced by the HermOp's last kernel where it can, else by a pass of its own
+      int parts = 0;
+      GB_TRY(op_hermop_dot(op, kind, p, mmp, &parts));
+      if (parts > 0) GB_TRY(launch_cg_alpha(op, op->d_partial, parts));
+      else GB_TRY(cg_alpha(op, p, mmp));
       GB_TRY(cg_update(op, r, mmp, psi, p));
     }
     return GB_OK;
