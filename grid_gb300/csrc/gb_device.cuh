@@ -163,6 +163,10 @@ template <> struct PairIO<float> {
       f.im[k] = make_float2(r.v[k].z, r.v[k].w);
     }
   }
+  // the stored values and the per-lane factor that scales them to the field's values
+  // (a linear consumer may apply the factor late); FP32 stores the values themselves
+  static __device__ __forceinline__ void decode_unscaled(const Raw& r, Pair12& f) { decode(r, f); }
+  static __device__ __forceinline__ float2 scale(const Raw&) { return make_float2(1.f, 1.f); }
   // q = pair index (= i/2), np = pairs per plane
   static __device__ __forceinline__ void load(const void* base, const float2*, size_t np, size_t q, Pair12& f) {
     const float4* p = static_cast<const float4*>(base) + q;
@@ -211,6 +215,18 @@ template <> struct PairIO<__half> {
       f.im[2 * g + 1] = __fmul2_rn(__half22float2(h[3]), r.n);
     }
   }
+  // the halves as floats, without the per-site norms (scale() returns them)
+  static __device__ __forceinline__ void decode_unscaled(const Raw& r, Pair12& f) {
+#pragma unroll
+    for (int g = 0; g < 6; g++) {
+      const __half2* h = reinterpret_cast<const __half2*>(&r.v[g]);
+      f.re[2 * g] = __half22float2(h[0]);
+      f.im[2 * g] = __half22float2(h[1]);
+      f.re[2 * g + 1] = __half22float2(h[2]);
+      f.im[2 * g + 1] = __half22float2(h[3]);
+    }
+  }
+  static __device__ __forceinline__ float2 scale(const Raw& r) { return r.n; }
   static __device__ __forceinline__ void load(const void* base, const float2* norms, size_t np, size_t q, Pair12& f) {
     const uint4* p = static_cast<const uint4*>(base) + q;
     const float2 n = __ldg(norms + q);

@@ -304,43 +304,49 @@ __device__ __forceinline__ void project2(const Pair12& f, float2 (&hr)[6], float
   }
 }
 
-// acc (+)= reconstruction of u; FIRST assigns
+// acc (+)= n * reconstruction of u, n the per-lane factor of the neighbour's storage
+// (1 for FP32, whose adds are then exactly a + u and a - u); FIRST assigns
 template <int MU, int S, bool FIRST>
-__device__ __forceinline__ void reconstruct2(Pair12& r, const float2 (&ur)[6], const float2 (&ui)[6]) {
+__device__ __forceinline__ void reconstruct2(Pair12& r, const float2 (&ur)[6], const float2 (&ui)[6], float2 n) {
+  const float2 np = n, nn = make_float2(-n.x, -n.y);
+  // a + T n b, T = +-1
+  auto acc = [&](int T, float2 a, float2 b) { return __ffma2_rn(b, T > 0 ? np : nn, a); };
+  const int SP = S, SM = -S;
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     const float2 u0r = ur[c], u0i = ui[c], u1r = ur[3 + c], u1i = ui[3 + c];
     if (FIRST) {
-      r.re[c] = u0r; r.im[c] = u0i; r.re[3 + c] = u1r; r.im[3 + c] = u1i;
       const float2 zero = f2(0.f);
+      r.re[c] = acc(1, zero, u0r); r.im[c] = acc(1, zero, u0i);
+      r.re[3 + c] = acc(1, zero, u1r); r.im[3 + c] = acc(1, zero, u1i);
       if (MU == 0) {  // r2 = -S i u1, r3 = -S i u0
-        r.re[6 + c] = adds2<S>(zero, u1i); r.im[6 + c] = adds2<-S>(zero, u1r);
-        r.re[9 + c] = adds2<S>(zero, u0i); r.im[9 + c] = adds2<-S>(zero, u0r);
+        r.re[6 + c] = acc(SP, zero, u1i); r.im[6 + c] = acc(SM, zero, u1r);
+        r.re[9 + c] = acc(SP, zero, u0i); r.im[9 + c] = acc(SM, zero, u0r);
       } else if (MU == 1) {  // r2 = S u1, r3 = -S u0
-        r.re[6 + c] = adds2<S>(zero, u1r); r.im[6 + c] = adds2<S>(zero, u1i);
-        r.re[9 + c] = adds2<-S>(zero, u0r); r.im[9 + c] = adds2<-S>(zero, u0i);
+        r.re[6 + c] = acc(SP, zero, u1r); r.im[6 + c] = acc(SP, zero, u1i);
+        r.re[9 + c] = acc(SM, zero, u0r); r.im[9 + c] = acc(SM, zero, u0i);
       } else if (MU == 2) {  // r2 = -S i u0, r3 = S i u1
-        r.re[6 + c] = adds2<S>(zero, u0i); r.im[6 + c] = adds2<-S>(zero, u0r);
-        r.re[9 + c] = adds2<-S>(zero, u1i); r.im[9 + c] = adds2<S>(zero, u1r);
+        r.re[6 + c] = acc(SP, zero, u0i); r.im[6 + c] = acc(SM, zero, u0r);
+        r.re[9 + c] = acc(SM, zero, u1i); r.im[9 + c] = acc(SP, zero, u1r);
       } else {  // r2 = S u0, r3 = S u1
-        r.re[6 + c] = adds2<S>(zero, u0r); r.im[6 + c] = adds2<S>(zero, u0i);
-        r.re[9 + c] = adds2<S>(zero, u1r); r.im[9 + c] = adds2<S>(zero, u1i);
+        r.re[6 + c] = acc(SP, zero, u0r); r.im[6 + c] = acc(SP, zero, u0i);
+        r.re[9 + c] = acc(SP, zero, u1r); r.im[9 + c] = acc(SP, zero, u1i);
       }
     } else {
-      r.re[c] = add2(r.re[c], u0r); r.im[c] = add2(r.im[c], u0i);
-      r.re[3 + c] = add2(r.re[3 + c], u1r); r.im[3 + c] = add2(r.im[3 + c], u1i);
+      r.re[c] = acc(1, r.re[c], u0r); r.im[c] = acc(1, r.im[c], u0i);
+      r.re[3 + c] = acc(1, r.re[3 + c], u1r); r.im[3 + c] = acc(1, r.im[3 + c], u1i);
       if (MU == 0) {
-        r.re[6 + c] = adds2<S>(r.re[6 + c], u1i); r.im[6 + c] = adds2<-S>(r.im[6 + c], u1r);
-        r.re[9 + c] = adds2<S>(r.re[9 + c], u0i); r.im[9 + c] = adds2<-S>(r.im[9 + c], u0r);
+        r.re[6 + c] = acc(SP, r.re[6 + c], u1i); r.im[6 + c] = acc(SM, r.im[6 + c], u1r);
+        r.re[9 + c] = acc(SP, r.re[9 + c], u0i); r.im[9 + c] = acc(SM, r.im[9 + c], u0r);
       } else if (MU == 1) {
-        r.re[6 + c] = adds2<S>(r.re[6 + c], u1r); r.im[6 + c] = adds2<S>(r.im[6 + c], u1i);
-        r.re[9 + c] = adds2<-S>(r.re[9 + c], u0r); r.im[9 + c] = adds2<-S>(r.im[9 + c], u0i);
+        r.re[6 + c] = acc(SP, r.re[6 + c], u1r); r.im[6 + c] = acc(SP, r.im[6 + c], u1i);
+        r.re[9 + c] = acc(SM, r.re[9 + c], u0r); r.im[9 + c] = acc(SM, r.im[9 + c], u0i);
       } else if (MU == 2) {
-        r.re[6 + c] = adds2<S>(r.re[6 + c], u0i); r.im[6 + c] = adds2<-S>(r.im[6 + c], u0r);
-        r.re[9 + c] = adds2<-S>(r.re[9 + c], u1i); r.im[9 + c] = adds2<S>(r.im[9 + c], u1r);
+        r.re[6 + c] = acc(SP, r.re[6 + c], u0i); r.im[6 + c] = acc(SM, r.im[6 + c], u0r);
+        r.re[9 + c] = acc(SM, r.re[9 + c], u1i); r.im[9 + c] = acc(SP, r.im[9 + c], u1r);
       } else {
-        r.re[6 + c] = adds2<S>(r.re[6 + c], u0r); r.im[6 + c] = adds2<S>(r.im[6 + c], u0i);
-        r.re[9 + c] = adds2<S>(r.re[9 + c], u1r); r.im[9 + c] = adds2<S>(r.im[9 + c], u1i);
+        r.re[6 + c] = acc(SP, r.re[6 + c], u0r); r.im[6 + c] = acc(SP, r.im[6 + c], u0i);
+        r.re[9 + c] = acc(SP, r.re[9 + c], u1r); r.im[9 + c] = acc(SP, r.im[9 + c], u1i);
       }
     }
   }
@@ -400,12 +406,14 @@ __device__ __forceinline__ void dhop_pair_step(const DhopParams& p, const int (&
   if constexpr (I + PF < 8)
     PairIO<T>::load_raw(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[kLegOrder[I + PF]]) * hl + sp,
                         buf[(I + PF) % (PF + 1)]);
+  // the storage factor (FP16 site norms) is linear through projection and link: it is
+  // applied by the reconstruction's fused multiply-adds
   Pair12 f;
-  PairIO<T>::decode(buf[I % (PF + 1)], f);
+  PairIO<T>::decode_unscaled(buf[I % (PF + 1)], f);
   float2 hr[6], hi[6], ur[6], ui[6];
   project2<MU, S>(f, hr, hi);
   su3_mul2(U + LEG * 9, hr, hi, ur, ui);
-  reconstruct2<MU, S, I == 0>(acc, ur, ui);
+  reconstruct2<MU, S, I == 0>(acc, ur, ui, PairIO<T>::scale(buf[I % (PF + 1)]));
   if constexpr (I + 1 < 8) dhop_pair_step<T, DAG, PF, I + 1>(p, nb, sp, np, hl, U, buf, acc);
 }
 
