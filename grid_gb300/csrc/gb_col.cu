@@ -259,7 +259,14 @@ __global__ void __launch_bounds__(12 * col_q<LS, OPB != COLB_NONE ? 2 : 1>()) co
 // next tile's inputs arriving by cp.async (16-byte copies straight into the padded,
 // bank-conflict-free shared layout) in a second stage while the current one computes
 // and stores.  No wait spins: cp.async.wait_group waits on the thread's own copies.
-constexpr int kColPipeQ = 16;
+#ifndef GB_COL_PIPE_Q
+#define GB_COL_PIPE_Q 16
+#endif
+#ifndef GB_COL_STAGES
+#define GB_COL_STAGES 2
+#endif
+constexpr int kColPipeQ = GB_COL_PIPE_Q;     // columns per tile
+constexpr int kColStages = GB_COL_STAGES;    // tiles in flight per CTA
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -287,7 +294,7 @@ template <int LS, bool DAG, int OPA, int OPB, bool DOT>
 __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParams p, const ColCoef<LS> c) {
   constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>(), NIN = OPB != COLB_NONE ? 2 : 1;
   constexpr int TILE = 12 * Q * ST;   // float4 of one input tile
-  extern __shared__ float4 col_ring[];  // [2 stages][NIN][12][Q][ST]
+  extern __shared__ float4 col_ring[];  // [kColStages][NIN][12][Q][ST]
   const size_t ntiles = (p.nq + Q - 1) / Q;
   const float4* xs = static_cast<const float4*>(p.x);
   const float4* ys = static_cast<const float4*>(p.y);
@@ -304,10 +311,12 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
   };
   size_t tile = blockIdx.x;
   double dot = 0.0;  // DOT: this thread's share of Re<dotp|out>, FP32 per tile, FP64 across tiles
-  issue(tile, 0);
-  issue(tile + gridDim.x, 1);
-  for (int st = 0; tile < ntiles; tile += gridDim.x, st ^= 1) {
-    cp_async_wait<1>();  // this stage's group has landed (the newer one may still fly)
+  for (int k0 = 0; k0 < kColStages - 1; k0++) issue(tile + size_t(k0) * gridDim.x, k0);
+  for (int st = 0; tile < ntiles; tile += gridDim.x, st = st + 1 == kColStages ? 0 : st + 1) {
+    // refill the stage computed last (stored out before the last barrier), then wait for
+    // this stage's group: all but the newest kColStages - 1 groups have landed
+    issue(tile + size_t(kColStages - 1) * gridDim.x, st == 0 ? kColStages - 1 : st - 1);
+    cp_async_wait<kColStages - 1>();
     __syncthreads();
     float4* base = col_ring + size_t(st) * NIN * TILE;
     const int nv = vectors(tile);
@@ -330,7 +339,6 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     }
     if (DOT) dot += double(dt);
     __syncthreads();  // the stage is read out before it is refilled
-    issue(tile + 2 * size_t(gridDim.x), st);
   }
   cp_async_wait<0>();
   if (DOT) {  // fixed-order CTA sum: warp shuffles, then the warps' sums in order
@@ -373,7 +381,7 @@ template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost
 template <int LS, bool DAG, int OPA, int OPB, bool DOT = false>
 static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* dot_parts = nullptr) {
   constexpr int NIN = OPB != COLB_NONE ? 2 : 1;
-  const size_t smem = size_t(2) * NIN * 12 * kColPipeQ * col_stride<LS>() * sizeof(float4);
+  const size_t smem = size_t(kColStages) * NIN * 12 * kColPipeQ * col_stride<LS>() * sizeof(float4);
   static std::atomic<int> per_sm{0};
   static std::atomic<int> sms{0};
   if (per_sm.load() == 0) {
