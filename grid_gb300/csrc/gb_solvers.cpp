@@ -268,9 +268,21 @@ int cg_reliable(Op* od, Op* of, int kind, Field* src, Field* psi, const gb_cg_pa
   double* d_ssq = of->d_result + 2 * n;
   double* d_cp = of->d_result + 3 * n;
   double* d_cpt = od->d_result + 4 * n;
-  // r = src - A psi (always, as Grid does), cp = |r|^2
-  GB_TRY(op_hermop(od, kind, psi, mmp_d));
-  GB_TRY(field_axpby(r_d, 1.0, -1.0, src, mmp_d));
+  // r = src - A psi as Grid does, cp = |r|^2; for a zero initial guess A psi = 0 and
+  // r = src exactly, so the FP64 operator is not applied
+  std::vector<double> guess(n);
+  GB_TRY(field_norm2(psi, guess.data()));
+  bool zero_guess = true;
+  for (double g : guess) {
+    if (std::isnan(g)) { set_error("reliable-update CG: NaN in the initial guess"); return GB_ERR_BAD_ARG; }
+    if (g != 0.0) zero_guess = false;
+  }
+  if (zero_guess) {
+    GB_TRY(field_copy(r_d, src));
+  } else {
+    GB_TRY(op_hermop(od, kind, psi, mmp_d));
+    GB_TRY(field_axpby(r_d, 1.0, -1.0, src, mmp_d));
+  }
   GB_TRY(field_norm2_dev(src, od->d_result + 5 * n));
   GB_TRY(field_norm2_dev(r_d, d_cpt));
   GB_CHECK_CUDA(cudaMemcpyAsync(d_ssq, od->d_result + 5 * n, n * sizeof(double), cudaMemcpyDeviceToDevice, od->stream));
