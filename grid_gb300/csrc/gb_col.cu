@@ -356,6 +356,88 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
   }
 }
 
+// FP16 programs on the same ring: each stage holds a tile's raw vectors (6 planes of
+// 16-byte vectors, two components of a site pair each, in their global order) and its
+// per-site norms, fetched by cp.async; after they land the CTA decodes them into the
+// float tile, runs the program and stores through the FP16 encoder (fresh norms).
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+template <int LS>
+__device__ __forceinline__ void col_issue_half(const uint4* x, const float* xn, uint4* raw, float* rnorm, size_t np,
+                                               size_t q0, int nv) {
+  constexpr int Q = kColPipeQ, H = LS / 2;
+  for (int e = threadIdx.x; e < 6 * Q * H; e += 12 * Q) {
+    const int g = e / (Q * H), r = e - g * (Q * H);
+    if (r < nv) cp_async16(raw + g * (Q * H) + r, x + size_t(g) * np + q0 * H + r);
+  }
+  for (int e = threadIdx.x; e < 2 * nv; e += 12 * Q) cp_async4(rnorm + e, xn + q0 * LS + e);
+}
+
+template <int LS>
+__device__ __forceinline__ void col_decode_half(const uint4* raw, const float* rnorm, float4* tile, int nv) {
+  constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>();
+  for (int e = threadIdx.x; e < 6 * Q * H; e += 12 * Q) {
+    const int g = e / (Q * H), r = e - g * (Q * H);
+    if (r < nv) {
+      const int qq = r / H, m = r - qq * H;
+      const uint4 v = raw[g * (Q * H) + r];
+      const __half2* h = reinterpret_cast<const __half2*>(&v);
+      const float n0 = rnorm[qq * LS + 2 * m], n1 = rnorm[qq * LS + 2 * m + 1];
+      const float2 a = __half22float2(h[0]), b = __half22float2(h[1]), c = __half22float2(h[2]),
+                   d = __half22float2(h[3]);
+      tile[((2 * g) * Q + qq) * ST + m] = make_float4(a.x * n0, a.y * n1, b.x * n0, b.y * n1);
+      tile[((2 * g + 1) * Q + qq) * ST + m] = make_float4(c.x * n0, c.y * n1, d.x * n0, d.y * n1);
+    }
+  }
+}
+
+template <int LS, bool DAG, int OPA, int OPB>
+__global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_half_kernel(const ColParams p, const ColCoef<LS> c) {
+  constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>(), NIN = OPB != COLB_NONE ? 2 : 1;
+  constexpr int RAW = 6 * Q * H;      // uint4 of one input's raw tile
+  constexpr int TILE = 12 * Q * ST;   // float4 of one input's decoded tile
+  // [NIN float tiles][kColStages][NIN][raw tile][Q * LS norms], then Q * LS floats of scratch
+  extern __shared__ float4 col_half_smem[];
+  float4* ftile = col_half_smem;
+  uint4* ring = reinterpret_cast<uint4*>(col_half_smem + NIN * TILE);
+  constexpr int SLOT = RAW + Q * LS / 4;  // uint4 per input per stage (norms packed 4 per uint4)
+  float* snorm = reinterpret_cast<float*>(ring + size_t(kColStages) * NIN * SLOT);
+  const size_t ntiles = (p.nq + Q - 1) / Q;
+  const uint4* xs = static_cast<const uint4*>(p.x);
+  const uint4* ys = static_cast<const uint4*>(p.y);
+  const int t = threadIdx.x, k = t / Q, qq = t - k * Q;
+  auto vectors = [&](size_t tile) { return int(min(p.nq - tile * Q, size_t(Q))) * H; };
+  auto slot = [&](int st, int j) { return ring + (size_t(st) * NIN + j) * SLOT; };
+  auto issue = [&](size_t tile, int st) {
+    if (tile < ntiles) {
+      col_issue_half<LS>(xs, p.xn, slot(st, 0), reinterpret_cast<float*>(slot(st, 0) + RAW), p.np, tile * Q,
+                         vectors(tile));
+      if (NIN == 2)
+        col_issue_half<LS>(ys, p.yn, slot(st, 1), reinterpret_cast<float*>(slot(st, 1) + RAW), p.np, tile * Q,
+                           vectors(tile));
+    }
+    cp_async_commit();
+  };
+  size_t tile = blockIdx.x;
+  for (int k0 = 0; k0 < kColStages - 1; k0++) issue(tile + size_t(k0) * gridDim.x, k0);
+  for (int st = 0; tile < ntiles; tile += gridDim.x, st = st + 1 == kColStages ? 0 : st + 1) {
+    issue(tile + size_t(kColStages - 1) * gridDim.x, st == 0 ? kColStages - 1 : st - 1);
+    cp_async_wait<kColStages - 1>();
+    __syncthreads();
+    const int nv = vectors(tile);
+    for (int j = 0; j < NIN; j++)
+      col_decode_half<LS>(slot(st, j), reinterpret_cast<const float*>(slot(st, j) + RAW), ftile + j * TILE, nv);
+    __syncthreads();
+    if (qq < nv / H) col_run<LS, DAG, OPA, OPB>(ftile + (k * Q + qq) * ST, ftile + TILE + (k * Q + qq) * ST, p.zc, c, k < 6);
+    __syncthreads();
+    ColIO<__half, LS, Q>::store(p.out, p.outn, snorm, ftile, p.np, tile * Q, nv);
+    __syncthreads();  // the float tile and this stage are read out before they are reused
+  }
+  cp_async_wait<0>();
+}
+
 template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost& h, ColCoef<LS>& c) {
   const std::vector<double>& lee = dag ? op->uee : op->lee;
   const std::vector<double>& leem = dag ? op->ueem : op->leem;
@@ -405,9 +487,37 @@ static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* do
   return GB_OK;
 }
 
+template <int LS, bool DAG, int OPA, int OPB>
+static int col_pipe_half_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
+  constexpr int Q = kColPipeQ, NIN = OPB != COLB_NONE ? 2 : 1;
+  constexpr size_t RAW = size_t(6) * Q * (LS / 2), SLOT = RAW + Q * LS / 4;
+  const size_t smem = size_t(NIN) * 12 * Q * col_stride<LS>() * sizeof(float4) +
+                      size_t(kColStages) * NIN * SLOT * sizeof(uint4) + size_t(Q) * LS * sizeof(float);
+  static std::atomic<int> per_sm{0};
+  static std::atomic<int> sms{0};
+  if (per_sm.load() == 0) {
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_half_kernel<LS, DAG, OPA, OPB>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int n = 0, dev = 0, count = 0;
+    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_half_kernel<LS, DAG, OPA, OPB>, 12 * Q,
+                                                                smem));
+    GB_CHECK_CUDA(cudaGetDevice(&dev));
+    GB_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
+    sms.store(count);
+    per_sm.store(n > 0 ? n : 1);
+  }
+  const size_t ntiles = (p.nq + Q - 1) / Q;
+  const size_t slots = size_t(per_sm.load()) * size_t(sms.load());
+  const unsigned blocks = unsigned(ntiles < slots ? ntiles : slots);
+  col_pipe_half_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * Q, smem, op->stream>>>(p, c);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 template <class T, int LS, bool DAG, int OPA, int OPB>
 static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
   if (GB_COL_PIPE && sizeof(T) == 4) return col_pipe_go<LS, DAG, OPA, OPB>(op, p, c);
+  if (GB_COL_PIPE && sizeof(T) == 2) return col_pipe_half_go<LS, DAG, OPA, OPB>(op, p, c);
   constexpr int Q = col_q<LS, OPB != COLB_NONE ? 2 : 1>();
   const size_t smem = size_t(OPB != COLB_NONE ? 2 : 1) * 12 * Q * col_stride<LS>() * sizeof(float4) +
                       (sizeof(T) == 2 ? size_t(Q) * LS * sizeof(float) : 0);
