@@ -34,6 +34,7 @@ struct DhopParams {
   int64_t n4h;
   size_t n5;
   int L5;
+  int L5a;  // slots that hold right-hand sides (below L5 when an odd count is padded)
   int L5c;  // slots per CTA (L5 split over gridDim.y when above 256)
   int k4;
   int* err;
@@ -209,9 +210,11 @@ __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
     mbar_expect_tx(&bar, bytes);
     bulk_g2s(RECON ? sraw : sU, static_cast<const R*>(p.links) + x0 * per_site, bytes, &bar);
   }
+  // threads cover the right-hand-side slots only; the zero padding slot of an odd
+  // right-hand-side count is written as zero by the site's slot-0 thread
   const int j = t / p.L5c;
   const int s = int(blockIdx.y) * p.L5c + (t - j * p.L5c);
-  const bool active = j < nsite && s < p.L5;
+  const bool active = j < nsite && s < p.L5a;
   int nb[8];
   if (active) {
     const int4* q = reinterpret_cast<const int4*>(p.nbr + (x0 + j) * 8);
@@ -239,25 +242,32 @@ __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
   dhop_leg<T, DAG, 6>(p, nb, s, U, acc);
   dhop_leg<T, DAG, 7>(p, nb, s, U, acc);
   SpinorIO<T>::store(p.out, p.out_norms, p.n5, size_t(x0 + j) * p.L5 + s, acc);
+  if (s == 0 && p.L5a < p.L5) {
+    Spinor<R> zero;
+#pragma unroll
+    for (int k = 0; k < 12; k++) { zero.re[k] = R(0); zero.im[k] = R(0); }
+    for (int z = p.L5a; z < p.L5; z++) SpinorIO<T>::store(p.out, p.out_norms, p.n5, size_t(x0 + j) * p.L5 + z, zero);
+  }
 }
 
-// 4D sites per CTA: L5 * k4 threads, a multiple of 32 where possible, about 256, and at
-// most 40 KB of staged links
+// 4D sites per CTA: L5 * k4 threads, about 256, at most 40 KB of staged links, and a
+// multiple of 32 threads where possible
 static int pick_k4(int L5, size_t link_bytes_per_site) {
   if (L5 >= 128) return 1;
   int k4 = 256 / L5;
-  while (k4 > 1 && (L5 * k4) % 32 != 0) k4--;
-  if ((L5 * k4) % 32 != 0) k4 = 256 / L5;
   const int kmax = int((40 * 1024) / link_bytes_per_site);
   if (k4 > kmax) k4 = kmax;
-  return k4 < 1 ? 1 : k4;
+  if (k4 < 1) k4 = 1;
+  int w = k4;
+  while (w > 1 && (L5 * w) % 32 != 0) w--;
+  return (L5 * w) % 32 == 0 ? w : k4;
 }
 
 template <class T, bool DAG, bool RECON> static int launch_dhop_t(Op* op, const DhopParams& p) {
   using R = typename Arith<T>::type;
   const int threads = p.L5c * p.k4;
   const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
-  const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
+  const unsigned ychunks = unsigned((p.L5a + p.L5c - 1) / p.L5c);
   const size_t smem = size_t(p.k4) * (RECON ? 240 : 144) * sizeof(R);
   static std::atomic<bool> configured{false};
   if (!configured.load()) {
@@ -540,7 +550,9 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
   p.n4h = op->half4;
   p.n5 = op->n5();
   p.L5 = op->L5;
-  p.L5c = op->L5 > 256 ? 256 : op->L5;
+  // FP64 works per 5D site and skips the padding slot; the site-pair kernels keep it
+  p.L5a = op->prec == GB_F64 ? op->Ls * op->nrhs_user : op->L5;
+  p.L5c = p.L5a > 256 ? 256 : p.L5a;
   p.k4 = pick_k4(p.L5c, (op->prec == GB_F64 ? 1152 : 576) * (op->recon12 ? 5 : 3) / 3);  // links + 12-real staging
   p.err = op->d_err;
   for (int k = 0; k < 4; k++) {
