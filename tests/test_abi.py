@@ -50,3 +50,28 @@ def test_bad_arguments_are_rejected_before_any_device_call():
     assert g.lib.gb_mobius_create(dims, 16, 0.1, 1.8, 1.5, 0.5, None, 0, 100, None, 0, C.byref(h)) == 8  # L5 too big
     # the fifth dimension must be even (site pairs of the FP32/FP16 layout)
     assert g.lib.gb_mobius_create(dims, 5, 0.1, 1.8, 1.5, 0.5, None, 0, 1, None, 0, C.byref(h)) == 8
+
+
+def test_header_is_c99_and_a_c_program_links_and_calls(tmp_path):
+    """The boundary is a C ABI: the header compiles as strict C99 and a C program links
+    the library and calls it (what a ctypes / cgo / JNI binding relies on)."""
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_abi.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "gbdwf.h"\n'
+        'int main(void) {\n'
+        '  printf("%d %s %s\\n", gb_version(), gb_status_string(0), gb_status_string(5));\n'
+        '  return 0;\n}\n')
+    exe = tmp_path / "use_abi"
+    lib_dir = Path(g.LIB_PATH).parent
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                    "-o", str(exe), f"-L{lib_dir}", "-lgbdwf", f"-Wl,-rpath,{lib_dir}"], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split(" ", 1)
+    assert int(out[0]) == g.lib.gb_version()
+    assert out[1].strip() == "ok not converged"
