@@ -749,7 +749,8 @@ int check_device_error(Op* op) {
   GB_CHECK_CUDA(cudaMemcpyAsync(&h, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
   if (h) {
-    set_error("a bounded device wait timed out");
+    op->poisoned = true;
+    set_error("a bounded device wait timed out: this operator's results are untrusted; recreate it");
     cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream);
     return GB_ERR_TIMEOUT;
   }

@@ -473,7 +473,9 @@ __global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kerne
     nb[0] = a.x; nb[1] = a.y; nb[2] = a.z; nb[3] = a.w;
     nb[4] = b.x; nb[5] = b.y; nb[6] = b.z; nb[7] = b.w;
   }
-  // every thread waits for the links, so none leaves while the copy is in flight
+  // every thread waits for the links before it leaves.  If the bounded wait gives up,
+  // the copy may still be in flight when the CTA exits: the error flag is raised and the
+  // host then refuses further Dhops on this operator (Op::poisoned)
   const bool ok = mbar_wait_bounded(&bar, 0);
   if (!ok) atomicExch(p.err, 1);
   if (RECON) {
@@ -533,6 +535,10 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
   if (op->L5 > kMaxL5) {
     set_error("Dhop: L5 = %d exceeds %d", op->L5, kMaxL5);
     return GB_ERR_UNSUPPORTED;
+  }
+  if (op->poisoned) {
+    set_error("Dhop: an earlier device wait of this operator timed out; its results are untrusted, recreate it");
+    return GB_ERR_TIMEOUT;
   }
   DhopParams p;
   p.in = in.data;

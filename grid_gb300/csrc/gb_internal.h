@@ -79,6 +79,11 @@ struct Op {
   void* links[2] = {nullptr, nullptr};  // per output parity
   int* nbr[2] = {nullptr, nullptr};
   int* d_err = nullptr;                 // device error flag of bounded waits
+  // Set when the host finds d_err raised.  A Dhop CTA whose bounded wait for its TMA copy
+  // gave up returns while that copy may still be writing into shared memory that the
+  // next CTA on the SM receives, so no later result of this operator can be trusted:
+  // every further Dhop on it returns GB_ERR_TIMEOUT until the operator is recreated.
+  bool poisoned = false;
 
   // Cayley coefficients (Moebius) -- host copies
   std::vector<double> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
