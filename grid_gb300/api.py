@@ -27,7 +27,6 @@ LIB_PATH = Path(__file__).resolve().with_name("libgbdwf.so")
 
 F64, F32, F16 = 0, 1, 2
 RECON12 = 1  # gb_*_create flag GB_FLAG_RECON12: 12-real links
-DHOP_STREAM = 2  # gb_*_create flag GB_FLAG_DHOP_STREAM: the t-stream FP32 Dhop kernel
 EVEN, ODD, FULL = 0, 1, 2
 DaggerNo, DaggerYes = 0, 1
 
@@ -127,7 +126,6 @@ _proto("gb_random_gaussian", [_sz, _u64, _dp])
 _proto("gb_random_z2", [_sz, _u64, _dp])
 _proto("gb_unit_gauge", [_ip, _dp])
 _proto("gb_bench_kernel", [_vp, _i, C.POINTER(_vp), C.POINTER(_vp), _i, _i, _dp])
-_proto("gb_op_dhop_config", [_vp, C.POINTER(_i)])
 _proto("gb_set_device", [_i])
 _proto("gb_op_sync", [_vp])
 _proto("gb_op_event_record", [_vp, _i])
@@ -551,13 +549,6 @@ class _FermionOperator:
         ms = C.c_double()
         _check(lib.gb_bench_kernel(self.h, which, a, b, n, reps, C.byref(ms)))
         return ms.value
-
-    def dhop_config(self) -> dict:
-        """The launch shape of this operator's last FP32 Dhop (gb_op_dhop_config)."""
-        v = (C.c_int * 8)()
-        _check(lib.gb_op_dhop_config(self.h, v))
-        return dict(kernel="stream" if v[0] == 1 else "gather", ctas=v[1], ctas_per_sm=v[2], threads=v[3],
-                    smem=v[4], rows=v[5], chunks=v[6])
 
 
 class WilsonFermion(_FermionOperator):

@@ -51,11 +51,6 @@ int gb_set_device(int device) {
   GB_CHECK_CUDA(cudaSetDevice(device));
   return GB_OK;
 }
-int gb_op_dhop_config(gb_op_t op, int out[8]) {
-  if (!op || !out) return GB_ERR_BAD_ARG;
-  for (int q = 0; q < 8; q++) out[q] = op->dhop_cfg[q];
-  return GB_OK;
-}
 int gb_op_sync(gb_op_t op) {
   if (!op) return GB_ERR_BAD_ARG;
   GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));

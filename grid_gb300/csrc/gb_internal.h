@@ -84,10 +84,6 @@ struct Op {
   // next CTA on the SM receives, so no later result of this operator can be trusted:
   // every further Dhop on it returns GB_ERR_TIMEOUT until the operator is recreated.
   bool poisoned = false;
-  // the last FP32 Dhop launch: {kernel (1 t-stream, 0 per-site gather), CTAs, resident
-  // CTAs per SM (t-stream), threads per CTA, dynamic shared memory bytes, x-rows per CTA,
-  // chunks of the fifth dimension, 0}
-  int dhop_cfg[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
   // Cayley coefficients (Moebius) -- host copies
   std::vector<double> bs, cs, bee, cee, dee, lee, leem, uee, ueem;
@@ -172,9 +168,6 @@ struct HalfView {
 inline HalfView half_view(const Field* f, int parity) { return HalfView{f->half_ptr(parity), f->half_norms(parity), f->prec}; }
 
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag);
-// FP32 t-stream Dhop (gb_dhop_stream.cu) over nside checkerboards: GB_ERR_UNSUPPORTED
-// (nothing launched) when the operator or shape has no stream layout
-int launch_dhop_stream(Op* op, const HalfView* in, const HalfView* out, const int* parity, int nside, int dag);
 int launch_dhop_full(Op* op, HalfView in_odd, HalfView out_even, HalfView in_even, HalfView out_odd, int dag);
 // force term of the output parity's sites into mat (FP64 canonical gauge layout, indexed
 // by x_cb when half_out, else by the lexicographic site); A has the output parity

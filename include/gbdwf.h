@@ -70,14 +70,9 @@ int gb_device_count(int* n);
  * stream: a cudaStream_t (NULL = the default stream).
  * flags: GB_FLAG_RECON12 = store the doubled links as 12 reals (rows 0, 1) and rebuild
  * row 2 in the Dhop kernel (the optional 12-real reconstruction); needs real boundary
- * phases (+1 / -1), else GB_ERR_UNSUPPORTED.  GB_FLAG_DHOP_STREAM = run the FP32 Dhop
- * as the t-stream kernel (a CTA walks t over whole x-rows, with its own rows staged in
- * shared memory) instead of the per-site gather kernel, where the shape allows; the two
- * differ only in the order of the eight leg sums (Grid's choice of WilsonKernels
- * implementation, WilsonKernels::Opt, WilsonKernels.h:41-43).
+ * phases (+1 / -1), else GB_ERR_UNSUPPORTED.
  */
 #define GB_FLAG_RECON12 1u
-#define GB_FLAG_DHOP_STREAM 2u
 int gb_wilson_create(const int dims[4], double mass, const double* phases, int precision, int nrhs, void* stream,
                      unsigned flags, gb_op_t* out);
 int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,
@@ -504,11 +499,6 @@ int gb_host_free(void* ptr);
  * returns the average device milliseconds per application.
  * which: 0 DhopEO, 1 DhopOE, 2 Mooee, 3 MooeeInv, 4 Meooe5D, 5 MpcDagMpc, 6 Dhop(full) */
 int gb_bench_kernel(gb_op_t op, int which, gb_field_t* ins, gb_field_t* outs, int n_pairs, int reps, double* ms);
-/* The launch shape of the operator's last FP32 Dhop: {kernel (1 t-stream, 0 per-site
- * gather), CTAs, resident CTAs per SM (t-stream), threads per CTA, dynamic shared memory
- * bytes, x-rows per CTA (t-stream), chunks of the fifth dimension, 0}.  Grid has no
- * counterpart (its kernel choice is WilsonKernels::Opt, a static setting). */
-int gb_op_dhop_config(gb_op_t op, int out[8]);
 
 #ifdef __cplusplus
 }

@@ -56,45 +56,6 @@ def test_dhop_eo_oe(gpu_available, prec, dag, case):
         assert o.rel_l2(fout.export(), ref.dhop_cb(x, in_cb, dag)) < TOL[prec]
 
 
-@pytest.mark.parametrize("dag", [0, 1])
-@pytest.mark.parametrize("case", ["stream_chunks", "stream_rows", "stream_small", "stream_wilson"])
-def test_dhop_fp32_stream_kernel(gpu_available, dag, case):
-    """The t-stream FP32 Dhop kernel (GB_FLAG_DHOP_STREAM) against the oracle: DhopEO,
-    DhopOE and the full Dhop.  "stream_chunks" splits the fifth dimension over CTAs (24 site
-    pairs per 4D site: 4 right-hand sides of Ls = 12), "stream_rows" has CTAs of several
-    x-rows whose y legs partly stay inside the CTA, "stream_small" CTAs of one partial
-    warp, "stream_wilson" a 4D Wilson operator.  Every slot of the fifth dimension hops
-    alike, so the oracle runs it as one Ls = L5 operator."""
-    dims, Ls, nrhs = {"stream_chunks": ((16, 4, 4, 4), 12, 4), "stream_rows": ((8, 8, 4, 6), 16, 1),
-                      "stream_small": ((4, 4, 2, 4), 4, 1), "stream_wilson": ((6, 4, 2, 10), 1, 2)}[case]
-    U = g.random_gauge(dims, 0.5, 7)
-    if case == "stream_wilson":
-        op = g.WilsonFermion(U, dims, 0.1, precision=g.F32, nrhs=nrhs, flags=g.DHOP_STREAM)
-    else:
-        op = g.MobiusFermion(U, dims, Ls, 0.01, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], precision=g.F32, nrhs=nrhs,
-                             flags=g.DHOP_STREAM)
-    L5 = Ls * nrhs
-    ref = o.OracleOp(1, 0, dims, L5, [0.01, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"]], U, g.antiperiodic_t())
-    nh = int(np.prod(dims)) // 2
-
-    def host(x, n):  # oracle layout [site][rhs*Ls + s] -> host fields, one right-hand side after another
-        return x.reshape(n, nrhs, Ls, 12).transpose(1, 0, 2, 3).reshape(-1)
-
-    def oracle_layout(y, n):
-        return y.reshape(nrhs, n, Ls, 12).transpose(1, 0, 2, 3).reshape(-1)
-
-    for in_cb in (1, 0):
-        x = fermion(nh, L5, 60 + in_cb)
-        fout = op.FermionRedBlackField(1 - in_cb)
-        (op.DhopEO if in_cb == 1 else op.DhopOE)(half(op, in_cb, host(x, nh)), fout, dag)
-        assert op.dhop_config()["kernel"] == "stream"
-        assert o.rel_l2(oracle_layout(fout.export(), nh), ref.dhop_cb(x, in_cb, dag)) < TOL[g.F32]
-    x = fermion(2 * nh, L5, 62)
-    fout = op.FermionField()
-    op.Dhop(op.FermionField().import_(host(x, 2 * nh)), fout, dag)
-    assert o.rel_l2(oracle_layout(fout.export(), 2 * nh), ref.apply(o.OP_DHOP_DAG if dag else o.OP_DHOP, x)) < TOL[g.F32]
-
-
 @pytest.mark.parametrize("prec", [g.F64, g.F32])
 def test_full_dhop_and_M(gpu_available, prec):
     dims = (4, 4, 4, 6)
