@@ -150,52 +150,49 @@ def dist_barrier(dist):
 
 
 # ---------------------------------------------------------------------------------------
-def cpu_baseline_oracle(U, x_odd, x_even, budget_s=12.0):
-    """The oracle (OpenMP C++ restatement of Grid's site loop) on the host cores, on a
-    bounded sample: as many DhopEO+DhopOE pairs of the full workload as fit in budget_s."""
+ANTIPERIODIC_T = [1.0, 0.0, 1.0, 0.0, 1.0, 0.0, -1.0, 0.0]
+CPU_KERNEL = ("Grid's CPU hopping-term algorithm (half-spinor projection, SU(3) x two-spinor, "
+              "reconstruction; OpenMP over 4D sites, Ls vectorised), FP32, oracle/cpu_dhop.cpp")
+
+
+def cpu_dhop_steps(budget_s: float, max_steps: int, seed_gauge=1234):
+    """DhopEO + DhopOE steps of the full 16^4 x 16 workload on the host cores with the
+    oracle's half-spinor CPU Dhop, inputs from the oracle's restatement of the seeded
+    generator (the CUDA library is not loaded): as many steps as fit in budget_s, at most
+    max_steps.  Returns (GB/s on the workload's algorithmic bytes, steps, seconds, threads)."""
     from oracle import oracle as o
     threads = o.max_threads()
-    op = o.OracleOp(1, 1, DIMS, LS, [MF, M5, B, C], U, np.array([1, 0, 1, 0, 1, 0, -1, 0], float))
-    op.dhop_cb(x_odd, 1)  # warm
+    U = o.random_gauge(DIMS, EPS, seed_gauge)
+    nh = int(np.prod(DIMS)) // 2 * LS
+    h = o.HalfSpinorDhop(DIMS, LS, U, ANTIPERIODIC_T)
+    h.set(1, o.random_gaussian(nh * 12, 1))
+    h.set(0, o.random_gaussian(nh * 12, 2))
+    h.dhop(0)  # warm
+    h.dhop(1)
     n, t0 = 0, time.perf_counter()
-    while True:
-        op.dhop_cb(x_odd, 1)
-        op.dhop_cb(x_even, 0)
+    while n < max_steps:
+        h.dhop(0)
+        h.dhop(1)
         n += 1
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    sites = x_odd.size // 12
-    gbs = 2 * n * sites * bytes_per_site(1, LS) / dt / 1e9
+    return 2 * n * nh * bytes_per_site(1, LS) / dt / 1e9, n, dt, threads
+
+
+def cpu_baseline_oracle(budget_s=12.0):
+    gbs, n, dt, threads = cpu_dhop_steps(budget_s, 1 << 30)
     return {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} DhopEO+DhopOE pairs of the full 16^4x16 FP32 workload in {dt:.1f} s (oracle, OpenMP)"}
+            "sample": f"{n} DhopEO+DhopOE pairs of the full 16^4x16 FP32 workload in {dt:.1f} s: {CPU_KERNEL}"}
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: the oracle's CPU implementation on the same config and metric."""
+    """--impl reference: Grid's CPU algorithm for the path (the oracle's half-spinor Dhop;
+    Grid itself cannot be built here) on the same config and metric.  Imports only oracle/."""
     if rank != 0:
         return
-    import grid_gb300 as g
-    U = g.random_gauge(DIMS, EPS, 1234)
-    nh = int(np.prod(DIMS)) // 2 * LS
-    xo = g.random_gaussian(nh * 12, 1)
-    xe = g.random_gaussian(nh * 12, 2)
-    from oracle import oracle as o
-    threads = o.max_threads()
-    op = o.OracleOp(1, 1, DIMS, LS, [MF, M5, B, C], U, g.antiperiodic_t())
-    t0 = time.perf_counter()
-    for _ in range(max(1, min(args.warmup, 1))):
-        op.dhop_cb(xo, 1)
-        op.dhop_cb(xe, 0)
-    t_step = time.perf_counter() - t0
-    # a bounded sample: at most ~120 s of timed CPU work whatever --steps asks for
-    n = max(1, min(args.steps, int(120.0 / max(t_step, 1e-6))))
-    t0 = time.perf_counter()
-    for _ in range(n):
-        op.dhop_cb(xo, 1)
-        op.dhop_cb(xe, 0)
-    dt = time.perf_counter() - t0
-    gbs = 2 * n * nh * bytes_per_site(1, LS) / dt / 1e9
+    # a bounded sample: at most ~60 s of timed CPU work whatever --steps asks for
+    gbs, n, dt, threads = cpu_dhop_steps(60.0, max(1, args.steps))
     line = {"metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / n * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -204,7 +201,7 @@ def run_reference(args, ws, rank):
                        "b": B, "c": C, "M5": M5, "mf": MF, "eps": EPS},
             "cpu_baseline": {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{n} of {args.steps} DhopEO+DhopOE steps of the full workload timed "
-                                       "(oracle, OpenMP; at most ~120 s of CPU work)"},
+                                       f"(at most ~60 s of CPU work): {CPU_KERNEL}"},
             "e2e": {"value": gbs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -308,7 +305,7 @@ def run_gpu(args, ws, rank, local, dist):
     peak, peak_kind = measured_peaks()
     achieved = step_bytes / (full_ms / 1e3) / 1e9
     traffic = profile_traffic("dhop_full_dwf16_fp32.txt")
-    cpu = cpu_baseline_oracle(U, g.random_gaussian(nh * 12, 10), g.random_gaussian(nh * 12, 20)) if ws == 1 else None
+    cpu = cpu_baseline_oracle() if ws == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

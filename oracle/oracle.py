@@ -59,6 +59,14 @@ def lib():
         L.orc_deriv.argtypes = [vp, i, dp, dp, i, i, dp]
         L.orc_set_threads.argtypes = [i]
         L.orc_max_threads.restype = i
+        L.orc_random_gauge.argtypes = [ip, d, C.c_uint64, dp]
+        L.orc_random_gaussian.argtypes = [C.c_int64, C.c_uint64, dp]
+        L.orc_hs_create.argtypes = [ip, i, dp, dp]
+        L.orc_hs_create.restype = vp
+        L.orc_hs_free.argtypes = [vp]
+        L.orc_hs_set.argtypes = [vp, i, dp]
+        L.orc_hs_get.argtypes = [vp, i, dp]
+        L.orc_hs_dhop.argtypes = [vp, i, i]
         _lib = L
     return _lib
 
@@ -226,3 +234,50 @@ def rel_l2(a, b):
     b = np.asarray(b).reshape(-1)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+# ---- the reference arm's inputs and CPU Dhop (cpu_dhop.cpp) ----
+def random_gauge(dims, eps: float, seed: int) -> np.ndarray:
+    """The seeded gauge field of the CUDA library's generator, restated (bit for bit):
+    canonical U[site][mu][3][3] complex128."""
+    vol = int(np.prod(dims))
+    U = np.empty(vol * 4 * 9, dtype=np.complex128)
+    lib().orc_random_gauge(_dims(dims), float(eps), int(seed), _p(U))
+    return U
+
+
+def random_gaussian(n: int, seed: int) -> np.ndarray:
+    """n complex numbers with N(0,1) parts, the library generator's stream, restated."""
+    out = np.empty(int(n), dtype=np.complex128)
+    lib().orc_random_gaussian(int(n), int(seed), _p(out))
+    return out
+
+
+class HalfSpinorDhop:
+    """Grid's CPU hopping-term algorithm on one checkerboard in FP32 (half-spinor
+    projection, SU(3) x two-spinor, reconstruction; OpenMP over 4D sites, the fifth
+    dimension vectorised).  set()/get() convert a canonical half field outside the timed
+    dhop() call."""
+
+    def __init__(self, dims, L5: int, U: np.ndarray, phases):
+        ph = np.ascontiguousarray(np.asarray(phases, dtype=np.float64))
+        self.h = lib().orc_hs_create(_dims(dims), int(L5), _p(np.ascontiguousarray(U)), _p(ph))
+        if not self.h:
+            raise ValueError("L5 must be in [1, 64]")
+        self.n = int(np.prod(dims)) // 2 * int(L5) * 12
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_hs_free(self.h)
+
+    def set(self, parity: int, x: np.ndarray):
+        assert x.size == self.n
+        lib().orc_hs_set(self.h, int(parity), _p(np.ascontiguousarray(x)))
+
+    def get(self, parity: int) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.complex128)
+        lib().orc_hs_get(self.h, int(parity), _p(out))
+        return out
+
+    def dhop(self, out_parity: int, dag: int = 0):
+        lib().orc_hs_dhop(self.h, int(out_parity), int(dag))

@@ -1,7 +1,8 @@
 """The reference arm of bench.py on the CPU: `--impl reference` times the oracle's
-DhopEO + DhopOE on the host cores and prints one JSON line on the same metric, unit and
-workload as the GPU arm, with its own cpu_baseline and an end-to-end figure that moves
-no bytes over the host link."""
+half-spinor DhopEO + DhopOE on the host cores and prints one JSON line on the same
+metric, unit and workload as the GPU arm, with its own cpu_baseline and an end-to-end
+figure that moves no bytes over the host link.  The arm loads no part of the CUDA
+library."""
 import json
 import subprocess
 import sys
@@ -27,6 +28,19 @@ def test_reference_arm_json_line():
     assert d["value"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert "half-spinor" in cb["sample"]
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_loads_no_product_library():
+    """The arm's process maps only the oracle's library, never libgbdwf.so."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '1'];"
+            "runpy.run_path('bench.py', run_name='__main__');"
+            "maps = open('/proc/self/maps').read();"
+            "assert 'libgbdwf' not in maps, 'product library loaded';"
+            "assert 'liboracle' in maps; print('clean')")
+    run = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert run.returncode == 0, run.stderr[-2000:]
+    assert "clean" in run.stdout

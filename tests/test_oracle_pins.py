@@ -387,3 +387,23 @@ def test_madwf_with_smaller_ls_inner_converges_to_the_outer_solution():
     assert hist[-1] < 1e-7 and all(b_ < 0.2 * a for a, b_ in zip(hist, hist[1:]))
     ref, _, _, _ = outer.schur_solve(b, 1e-11, 10000)
     assert o.rel_l2(sol, ref) < 1e-6
+
+
+def test_reference_arm_generator_and_half_spinor_dhop():
+    """The reference arm builds its inputs with the oracle's restatement of the library's
+    seeded generator (equal bit for bit) and times the half-spinor CPU Dhop, which must
+    equal the oracle's site-loop Dhop (FP32 arithmetic: relative L2 below 1e-6) for both
+    checkerboards and both dagger signs."""
+    dims, L5 = (4, 4, 4, 8), 8
+    U = o.random_gauge(dims, 0.5, 1234)
+    assert np.array_equal(U, g.random_gauge(dims, 0.5, 1234))
+    assert np.array_equal(o.random_gaussian(999, 7), g.random_gaussian(999, 7))
+    nh = int(np.prod(dims)) // 2
+    ref = o.OracleOp(1, 0, dims, L5, [0.01, 1.8, 1.5, 0.5], U, g.antiperiodic_t())
+    h = o.HalfSpinorDhop(dims, L5, U, g.antiperiodic_t())
+    for in_cb in (1, 0):
+        for dag in (0, 1):
+            x = o.random_gaussian(nh * L5 * 12, 10 + in_cb)
+            h.set(in_cb, x)
+            h.dhop(1 - in_cb, dag)
+            assert o.rel_l2(h.get(1 - in_cb), ref.dhop_cb(x, in_cb, dag)) < 1e-6
