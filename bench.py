@@ -613,6 +613,34 @@ def cg_profile(g, iters):
     print(json.dumps({"cg_profile": "mobius_dwf_24^4xLs12_mixed_fp32", "iterations": int(r.iterations)}))
 
 
+DHOP_PROFILE_CASES = {
+    # name: (kind, dims, Ls, nrhs, precision); every input half field is above the 129 MB L2
+    "wilson16rhs_fp32": ("wilson", (24, 24, 24, 32), 1, 16, "F32"),
+    "dwf_fp16": ("mobius", (32, 32, 32, 32), 12, 1, "F16"),
+    "dwf_fp64": ("mobius", (16, 16, 16, 16), 16, 2, "F64"),
+    "dwf_fp32": ("mobius", (16, 16, 16, 16), 16, 1, "F32"),
+}
+
+
+def dhop_profile(g, case, launches=3):
+    """For a profiler's capture, not a measurement: `launches` DhopEO launches of a small
+    case of each Dhop kernel (DHOP_PROFILE_CASES)."""
+    kind, dims, Ls, nrhs, prec = DHOP_PROFILE_CASES[case]
+    prec = getattr(g, prec)
+    U = g.random_gauge(dims, EPS, 1234)
+    if kind == "wilson":
+        op = g.WilsonFermion(U, dims, 0.02, precision=prec, nrhs=nrhs)
+    else:
+        op = g.MobiusFermion(U, dims, Ls, MF, M5, B, C, precision=prec, nrhs=nrhs)
+    n = op.half_sites4 * Ls * nrhs * 12
+    fin = op.FermionRedBlackField(g.ODD).import_(g.random_gaussian(n, 7))
+    fout = op.FermionRedBlackField(g.EVEN)
+    for _ in range(launches):
+        op.DhopEO(fin, fout, 0)
+    op.sync()
+    print(json.dumps({"dhop_profile": case, "dims": list(dims), "Ls": Ls, "nrhs": nrhs, "launches": launches}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -624,7 +652,13 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the seeded arrival stream")
     ap.add_argument("--cg-profile", type=int, default=0, metavar="ITERS",
                     help="run only ITERS iterations of the 24^4 x 12 mixed CG (for a profiler's launch list)")
+    ap.add_argument("--dhop-profile", choices=sorted(DHOP_PROFILE_CASES), default=None,
+                    help="run three DhopEO launches of a small case of one Dhop kernel (for a profiler's capture)")
     args = ap.parse_args()
+    if args.dhop_profile:
+        import grid_gb300 as g
+        dhop_profile(g, args.dhop_profile)
+        return
     if args.cg_profile:
         import grid_gb300 as g
         cg_profile(g, args.cg_profile)

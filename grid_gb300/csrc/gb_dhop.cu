@@ -510,6 +510,10 @@ static int pick_k4_pair(int hc) {
 
 template <class T, bool DAG, bool RECON> static int launch_dhop_pair_t(Op* op, DhopParams p) {
   p.L5c = p.L5 > 256 ? 256 : p.L5;  // even
+  // A fifth dimension of several 8-pair groups (multi-RHS operators) is split into CTAs of
+  // 8 pairs: a warp then covers 4 sites x 8 pairs, whole 128-byte lines of every plane,
+  // where 48 slots (3 x 128 B per site) in one CTA would straddle lines
+  if (p.L5 > 16 && p.L5 % 16 == 0) p.L5c = 16;
   p.k4 = pick_k4_pair(p.L5c / 2);
   const int threads = (p.L5c / 2) * p.k4;
   const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;

@@ -238,8 +238,16 @@ int orc_cg(void* p, int kind, const double* src, double* psi, double tol, int ma
 
 // SchurRedBlackDiagMooeeSolve with CG (SchurRedBlack.h:236-291,373-436) in double.
 // src, sol: full fields.  resid[0] = CG true residual, resid[1] = unpreconditioned
-// true residual |M sol - src| / |src|.
+// true residual |M sol - src| / |src|.  guess (full field, or NULL for zero): the odd
+// checkerboard's starting vector of the CG, as Grid's solver takes the incoming solution's
+// odd sites (SchurRedBlack.h:261-265); it changes the work, not what the CG converges to.
+int orc_schur_solve_guess(void* p, const double* src, const double* guess, double* sol, double tol, int maxit,
+                          int* info, double* resid);
 int orc_schur_solve(void* p, const double* src, double* sol, double tol, int maxit, int* info, double* resid) {
+  return orc_schur_solve_guess(p, src, nullptr, sol, tol, maxit, info, resid);
+}
+int orc_schur_solve_guess(void* p, const double* src, const double* guess, double* sol, double tol, int maxit,
+                          int* info, double* resid) {
   Handle* h = static_cast<Handle*>(p);
   if (h->prec != 0) return 1;
   Op<double>* op = h->d;
@@ -251,6 +259,7 @@ int orc_schur_solve(void* p, const double* src, double* sol, double tol, int max
   for (size_t i = 0; i < Mtmp.size(); i++) tmp[i] = src_o[i] - Mtmp[i];
   op->MpcDag(tmp, src_o);
   sol_o.assign(src_o.size(), cplx<double>(0));
+  if (guess) pick_cb<double>(op->g, op->L5, 1, load<double>(guess, op->full_len()), sol_o);
   CGResult r = cg<double>([&](const Field<double>& a, Field<double>& b) { op->MpcDagMpc(a, b); }, src_o, sol_o, tol, maxit);
   op->Meooe(sol_o, tmp, 1);
   for (size_t i = 0; i < tmp.size(); i++) t2.push_back(src_e[i] - tmp[i]);

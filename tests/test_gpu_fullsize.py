@@ -111,3 +111,39 @@ def test_wilson_32x64_16rhs_dhop(gpu_available):
     for r in range(nrhs):
         want = single.dhop_cb(x[r * per:(r + 1) * per].astype(np.complex128), 1)
         assert o.rel_l2(got[r * per:(r + 1) * per].astype(np.complex128), want) < TOL[g.F32], r
+
+
+@pytest.mark.parametrize("inner", [g.F32, g.F16])
+def test_mixed_schur_solution_vs_oracle_fp64_12x12(gpu_available, inner):
+    """The config of the mixed-precision benchmark (Moebius, Ls = 12, mf = 0.005, gauge
+    eps = 0.6, reliable updates every 100 iterations or when |r| drops by 1e-3) at 12^4,
+    the largest lattice whose FP64 oracle solve fits the test's time: the mixed solve
+    reaches a Schur-system true residual of 1e-10, and its error against the oracle's
+    FP64 solution is stated.  The oracle's red-black CG starts from the GPU's solution and
+    runs to 1e-12 (the start changes its work, not what it converges to), so the
+    difference is the GPU solution's error to within the oracle's own 1e-12 residual.
+    Measured on GB300: 5.0e-9 (FP32 inner) and 4.6e-9 (FP16 inner); a 1e-10 residual on
+    this operator allows errors of that size (the oracle's own 1e-10 and 1e-12 solutions
+    at 8^4 differ by 3.2e-9).  The bound is 2e-8."""
+    dims, Ls, mf = (12, 12, 12, 12), 12, 0.005
+    U = g.random_gauge(dims, 0.6, 311)
+    params = (mf, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"])
+    od = g.MobiusFermion(U, dims, Ls, *params, precision=g.F64)
+    of = g.MobiusFermion(U, dims, Ls, *params, precision=inner)
+    ref = o.OracleOp(1, 0, dims, Ls, list(params), U, g.antiperiodic_t())
+    src = fermion(int(np.prod(dims)), Ls, 312)
+    fs = od.FermionField().import_(src)
+    fx = od.FermionField().zero()
+    cg = g.ConjugateGradientReliableUpdate(1e-10, 30000, 1e-6, g.SchurDiagMooeeOperator(of),
+                                           g.SchurDiagMooeeOperator(od), relup_every=100)
+    solver = g.SchurRedBlackDiagMooeeSolve(cg)
+    solver(od, fs, fx)
+    x = fx.export()
+    assert cg.TrueResidual < 1e-10
+    xr, it, r_cg, r_un = ref.schur_solve(src, 1e-12, 5000, guess=x)
+    assert r_cg < 1e-12
+    err = o.rel_l2(x, xr)
+    print(f"12^4x12 mixed ({'fp32' if inner == g.F32 else 'fp16'} inner): {cg.IterationsToComplete} iterations, "
+          f"Schur residual {cg.TrueResidual:.2e}, unpreconditioned {solver.unprec_residual[0]:.2e}, "
+          f"error vs the oracle FP64 solution {err:.2e} (oracle: {it} more iterations from the GPU solution)")
+    assert err < 2e-8

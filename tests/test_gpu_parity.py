@@ -1,6 +1,8 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle on the same seeded
-inputs.  Tolerances (relative L2): FP64 1e-13, FP32 1e-6 for the operators; solvers are
-checked by the true residual |A x - b| / |b| measured with the oracle's FP64 operator."""
+inputs.  Tolerances (relative L2): FP64 1e-13, FP32 1e-6 for every operator, the
+composites (M, MdagM, Mooee, MooeeInv, Mpc, MpcDagMpc) included (FP32 measures 1.3e-7 at
+most); solvers are checked by the true residual |A x - b| / |b| measured with the
+oracle's FP64 operator."""
 import numpy as np
 import pytest
 
@@ -65,7 +67,7 @@ def test_full_dhop_and_M(gpu_available, prec):
     fout = op.FermionField()
     for name, code in (("M", o.OP_M), ("Mdag", o.OP_MDAG), ("MdagM", o.OP_MDAGM)):
         getattr(op, name)(fin, fout)
-        assert o.rel_l2(fout.export(), ref.apply(code, x)) < TOL[prec] * 10, name
+        assert o.rel_l2(fout.export(), ref.apply(code, x)) < TOL[prec], name
     for dag, code in ((0, o.OP_DHOP), (1, o.OP_DHOP_DAG)):
         op.Dhop(fin, fout, dag)
         assert o.rel_l2(fout.export(), ref.apply(code, x)) < TOL[prec]
@@ -86,7 +88,7 @@ def test_mobius_half_ops(gpu_available, prec, Ls):
         fin = half(op, cb, x)
         fout = op.FermionRedBlackField(cb)
         getattr(op, name)(fin, fout)
-        assert o.rel_l2(fout.export(), ref.apply(code, x, cb)) < TOL[prec] * 10, (name, cb)
+        assert o.rel_l2(fout.export(), ref.apply(code, x, cb)) < TOL[prec], (name, cb)
 
 
 def test_fp16_storage_operators(gpu_available):
@@ -123,7 +125,7 @@ def test_wilson_half_ops(gpu_available, prec):
         fin = half(op, 1, x)
         fout = op.FermionRedBlackField(1)
         getattr(op, name)(fin, fout)
-        assert o.rel_l2(fout.export(), ref.apply(code, x, 1)) < TOL[prec] * 10, name
+        assert o.rel_l2(fout.export(), ref.apply(code, x, 1)) < TOL[prec], name
 
 
 @pytest.mark.parametrize("prec", [g.F64, g.F32])
