@@ -541,6 +541,28 @@ def extra_multi_rhs(g):
     out.update({"batched_solve_seconds": dt, "solves_per_s": nrhs / dt, "iterations": int(r.iterations),
                 "reliable_updates": int(r.reliable_updates), "true_residual": float(r.true_residual),
                 "unprec_residual": float(max(solver.unprec_residual)), "converged": int(r.converged)})
+    del od, of, fs, fx
+    # the same solver on one right-hand side at a time (a point source and a Z2 source),
+    # for the batch's solves/s against single solves
+    of1 = g.WilsonFermion(U, dims, mass, precision=g.F32)
+    od1 = g.WilsonFermion(U, dims, mass, precision=g.F64)
+    single = []
+    for k in (0, 12):
+        fs1 = od1.FermionField().import_(srcs[k])
+        fx1 = od1.FermionField().zero()
+        cg1 = g.ConjugateGradientReliableUpdate(1e-10, 20000, 1e-6, g.SchurDiagMooeeOperator(of1),
+                                                g.SchurDiagMooeeOperator(od1), relup_every=100, err_on_no_conv=False)
+        s1 = g.SchurRedBlackDiagMooeeSolve(cg1)
+        od1.sync()
+        t0 = time.perf_counter()
+        r1 = s1(od1, fs1, fx1)
+        od1.sync()
+        single.append({"source": "point (spin 0, colour 0)" if k == 0 else "Z2 noise", "seconds": time.perf_counter() - t0,
+                       "iterations": int(r1.iterations), "true_residual": float(r1.true_residual)})
+    t1 = sum(x["seconds"] for x in single) / len(single)
+    out["single_rhs"] = single
+    out["single_rhs_solves_per_s"] = 1.0 / t1
+    out["batch_vs_single_solves_per_s"] = (nrhs / dt) * t1
     return out
 
 
