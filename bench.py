@@ -340,7 +340,7 @@ def run_gpu(args, ws, rank, local, dist):
                          ("cg_schur_24^4xLs12", lambda: extra_cg_schur(g)),
                          ("multi_rhs_wilson_32^3x64", lambda: extra_multi_rhs(g)),
                          ("serving", lambda: extra_serving(g, max_requests=args.serve_requests,
-                                                           seconds=args.serve_seconds))):
+                                                           seconds=args.serve_seconds, drain=args.serve_drain))):
             t0 = time.perf_counter()
             try:
                 extras[name] = fn()
@@ -584,13 +584,22 @@ def serving_stream(seconds, rate=20.0, seed=5005):
     return reqs
 
 
-def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0, inner=None):
-    """Replays the first `max_requests` requests of the seeded stream at their arrival
-    times into the service (HBM budget 150 GB, mixed-precision CG to 1e-10; inner solves
-    in FP32, or FP16 storage with `inner=g.F16`)."""
+def extra_serving(g, max_requests=None, seconds=60.0, drain=30.0, slots=6, budget_gb=150.0, inner=None,
+                  age_limit=10.0):
+    """Replays the seeded stream (Poisson 20/s over `seconds`: ~1200 requests) at its
+    arrival times into the service: HBM budget 150 GB, mixed-precision CG to 1e-10 (FP32
+    inner, or FP16 storage with `inner=g.F16`), admission of the first queued request
+    that fits with an age bound.  Arrivals stop at `seconds`; at `seconds + drain` every
+    request still queued is shed and those running complete.  Reports completed solves/s
+    over the wall time, p50/p99 latency of the completed requests, the queue depth over
+    time, shed and rejected counts, and the concurrency of the requests' device work on
+    the GPU's clock."""
     inner = g.F32 if inner is None else inner
-    reqs = serving_stream(seconds)[:max_requests]
+    reqs = serving_stream(seconds)
+    if max_requests:
+        reqs = reqs[:max_requests]
     srv = g.Server(int(budget_gb * (1 << 30)), slots=slots, flags=g.Server.GRAPHS)
+    srv.set_age_limit(age_limit)
     t0 = time.perf_counter()
     for q in reqs:
         delay = q["t"] - (time.perf_counter() - t0)
@@ -598,22 +607,53 @@ def extra_serving(g, max_requests=24, seconds=60.0, slots=6, budget_gb=150.0, in
             time.sleep(delay)
         srv.submit(g.make_request(q["dims"], q["Ls"], q["mf"], q["eps"], q["gauge_seed"], q["nsrc"], q["src_seed"],
                                   inner=inner))
-    ok = srv.wait(len(reqs), 1800)
+    t_arrivals = time.perf_counter() - t0
+    while time.perf_counter() - t0 < seconds + drain and srv.stats().finished < len(reqs):
+        time.sleep(0.25)
+    shed = srv.cancel_queued()
+    t_shed = time.perf_counter() - t0
+    all_done = srv.wait(len(reqs), 1800)
     wall = time.perf_counter() - t0
     res = srv.results(len(reqs) + 8)
     st = srv.stats()
+    tr_t, tr_q, tr_r = srv.trace()
     srv.close()
-    lat = np.array([r.t_end - r.t_submit for r in res])
     good = [r for r in res if r.status == 0]
+    lat = np.array([r.t_end - r.t_submit for r in good])
     nsol = sum(r.nsrc for r in good)
-    return {"workload": f"serving: first {len(reqs)} requests of the seeded Poisson(20/s) stream",
-            "completed": len(good), "failed": len(res) - len(good), "all_done": bool(ok), "wall_s": wall,
+    # time-weighted queue depth and device concurrency
+    qd = {}
+    if len(tr_t) > 1:
+        dt = np.diff(tr_t)
+        qd = {"max": int(tr_q.max()), "mean_time_weighted": float((tr_q[:-1] * dt).sum() / max(dt.sum(), 1e-9)),
+              "at_10s": [int(tr_q[max(0, np.searchsorted(tr_t, x) - 1)]) for x in np.arange(10.0, tr_t[-1], 10.0)]}
+    ev = sorted([(r.dev_start, 1) for r in good if r.dev_start >= 0] + [(r.dev_end, -1) for r in good if r.dev_start >= 0])
+    conc, busy, multi, peak = 0, 0.0, 0.0, 0
+    for k in range(len(ev) - 1):
+        conc += ev[k][1]
+        peak = max(peak, conc)
+        span = ev[k + 1][0] - ev[k][0]
+        if conc >= 1:
+            busy += span
+        if conc >= 2:
+            multi += span
+    return {"workload": f"serving: the seeded Poisson(20/s) stream over {seconds:.0f} s, {len(reqs)} requests, "
+                        f"drain limit {drain:.0f} s after the last arrival window",
+            "arrivals": len(reqs), "completed": len(good), "shed": int(shed), "rejected": int(st.rejected),
+            "failed": len(res) - len(good) - int(shed) - int(st.rejected), "all_done": bool(all_done),
+            "wall_s": wall, "arrival_window_s": t_arrivals, "shed_at_s": t_shed,
             "solves_per_s": nsol / wall, "requests_per_s": len(good) / wall,
+            "completed_solves": nsol,
             "latency_p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "latency_p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "max_true_residual": float(max((r.true_residual for r in good), default=0.0)),
             "max_running": int(st.max_running), "peak_hbm_gb": st.peak_used_bytes / (1 << 30), "slots": slots,
-            "budget_gb": budget_gb, "inner_precision": "fp16" if inner == g.F16 else "fp32"}
+            "budget_gb": budget_gb, "inner_precision": "fp16" if inner == g.F16 else "fp32",
+            "admission": f"first queued request that fits, in arrival order; none may pass a request older than {age_limit:.0f} s",
+            "queue_depth": qd,
+            "device_concurrency": {"max_requests_in_flight": int(peak), "busy_s": busy,
+                                   "fraction_of_busy_time_with_2_or_more": multi / busy if busy > 0 else 0.0,
+                                   "source": "CUDA events bracketing each request's device work on its slot's stream"}}
 
 
 def cg_profile(g, iters):
@@ -670,7 +710,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="only the headline DhopEO/DhopOE measurement")
-    ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving stream to replay")
+    ap.add_argument("--serve-requests", type=int, default=0, help="replay only the first N requests of the stream (0: all)")
+    ap.add_argument("--serve-drain", type=float, default=30.0,
+                    help="seconds after the arrival window at which still-queued requests are shed")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the seeded arrival stream")
     ap.add_argument("--cg-profile", type=int, default=0, metavar="ITERS",
                     help="run only ITERS iterations of the 24^4 x 12 mixed CG (for a profiler's launch list)")

@@ -1197,13 +1197,14 @@ class RequestResult(C.Structure):
                 ("iterations", C.c_int), ("reliable_updates", C.c_int), ("cleanup_iterations", C.c_int),
                 ("true_residual", C.c_double), ("unprec_residual", C.c_double), ("solution_norm2", C.c_double),
                 ("t_submit", C.c_double),
-                ("t_start", C.c_double), ("t_end", C.c_double)]
+                ("t_start", C.c_double), ("t_end", C.c_double), ("dev_start", C.c_double), ("dev_end", C.c_double)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("budget_bytes", C.c_size_t), ("used_bytes", C.c_size_t), ("peak_used_bytes", C.c_size_t),
                 ("running", C.c_int), ("max_running", C.c_int), ("queued", C.c_int), ("submitted", C.c_int64),
-                ("finished", C.c_int64), ("now", C.c_double)]
+                ("finished", C.c_int64), ("now", C.c_double), ("cancelled", C.c_int64), ("rejected", C.c_int64),
+                ("max_queued", C.c_int)]
 
 
 _proto("gb_server_create", [C.c_size_t, _i, C.c_uint, C.POINTER(_vp)])
@@ -1213,6 +1214,9 @@ _proto("gb_server_results", [_vp, C.POINTER(RequestResult), _i, _ip])
 _proto("gb_server_stats", [_vp, C.POINTER(ServerStats)])
 _proto("gb_server_destroy", [_vp])
 _proto("gb_request_bytes", [C.POINTER(Request), C.POINTER(C.c_size_t)])
+_proto("gb_server_set_age_limit", [_vp, _d])
+_proto("gb_server_cancel_queued", [_vp, C.POINTER(C.c_int64)])
+_proto("gb_server_trace", [_vp, _dp, _ip, _ip, _i, _ip])
 
 
 def make_request(dims, Ls, mf, eps, gauge_seed, nsrc, src_seed, M5=1.8, b=1.5, c=0.5, tol=1e-10, maxit=20000,
@@ -1234,9 +1238,12 @@ def request_bytes(r: Request) -> int:
 
 
 class Server:
-    """Continuous-batching propagator-solve service (gb_server_*)."""
+    """Continuous-batching propagator-solve service (gb_server_*).  Admission: the first
+    queued request that fits what is left of the HBM budget, in arrival order (or least
+    work first with SHORTEST_FIRST); once the oldest has waited age_limit seconds nothing
+    passes it (FIFO: only the oldest is ever admitted)."""
 
-    DRY_RUN, GRAPHS = 1, 2
+    DRY_RUN, GRAPHS, FIFO, SHORTEST_FIRST = 1, 2, 4, 8
 
     def __init__(self, hbm_budget_bytes: int, slots: int = 4, flags: int = 0):
         h = _vp()
@@ -1263,6 +1270,25 @@ class Server:
         s = ServerStats()
         _check(lib.gb_server_stats(self.h, C.byref(s)))
         return s
+
+    def set_age_limit(self, seconds: float):
+        _check(lib.gb_server_set_age_limit(self.h, float(seconds)))
+
+    def cancel_queued(self) -> int:
+        """Shed every request not yet admitted (they finish with GB_ERR_CANCELLED)."""
+        n = C.c_int64()
+        _check(lib.gb_server_cancel_queued(self.h, C.byref(n)))
+        return n.value
+
+    def trace(self, max_n: int = 1 << 16):
+        """(t, queued, running) samples at every submission, admission and completion."""
+        t = np.empty(max_n, dtype=np.float64)
+        q = np.empty(max_n, dtype=np.int32)
+        r = np.empty(max_n, dtype=np.int32)
+        n = C.c_int()
+        _check(lib.gb_server_trace(self.h, t.ctypes.data_as(_dp), q.ctypes.data_as(_ip), r.ctypes.data_as(_ip),
+                                   int(max_n), C.byref(n)))
+        return t[:n.value], q[:n.value], r[:n.value]
 
     def close(self):
         if getattr(self, "h", None):

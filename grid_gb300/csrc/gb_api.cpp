@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 
@@ -58,6 +59,70 @@ static int check_subset(const Field* f, int subset, const char* what) {
   return GB_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// Allocation.  Device memory of operators and fields comes from the stream-ordered
+// allocator on the operator's stream (cudaMallocAsync / cudaFreeAsync), and the device's
+// default memory pool keeps freed blocks for reuse: creating or destroying an operator
+// then neither synchronises the device nor calls into the driver's allocator once the
+// pool holds enough, so one stream's set-up does not stall another stream's kernels (the
+// propagator service creates operators per request while other requests run).  Small
+// page-locked host buffers come from a process-wide pool for the same reason:
+// cudaFreeHost synchronises the device.
+// ---------------------------------------------------------------------------------------
+static void keep_pool_memory(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  for (int d : done)
+    if (d == device) return;
+  done.push_back(device);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = ~uint64_t(0);  // never trim at synchronisation points
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+}
+static cudaError_t dev_alloc(void** p, size_t n, cudaStream_t s) { return cudaMallocAsync(p, n, s); }
+static void dev_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+namespace {
+struct PinnedPool {
+  std::mutex mu;
+  std::multimap<size_t, void*> free_blocks;  // size class -> block
+  std::map<void*, size_t> sizes;
+};
+PinnedPool& pinned_pool() {
+  static PinnedPool* pp = new PinnedPool;  // process lifetime: blocks stay page-locked until exit
+  return *pp;
+}
+}  // namespace
+static void* pinned_get(size_t bytes) {
+  const size_t cls = (bytes + 255) & ~size_t(255);
+  PinnedPool& pp = pinned_pool();
+  {
+    std::lock_guard<std::mutex> lk(pp.mu);
+    auto it = pp.free_blocks.find(cls);
+    if (it != pp.free_blocks.end()) {
+      void* p = it->second;
+      pp.free_blocks.erase(it);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, cls) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(pp.mu);
+  pp.sizes[p] = cls;
+  return p;
+}
+static void pinned_put(void* p) {
+  if (!p) return;
+  PinnedPool& pp = pinned_pool();
+  std::lock_guard<std::mutex> lk(pp.mu);
+  pp.free_blocks.emplace(pp.sizes[p], p);
+}
+
 int field_alloc(Op* op, int subset, int prec, Field** out) {
   Field* f = new (std::nothrow) gb_field_s;
   if (!f) { set_error("host allocation failed"); return GB_ERR_OOM; }
@@ -66,10 +131,10 @@ int field_alloc(Op* op, int subset, int prec, Field** out) {
   f->prec = prec;
   f->n5 = op->n5();
   const size_t halves = subset == GB_FULL ? 2 : 1;
-  cudaError_t e = cudaMalloc(&f->data, halves * f->half_bytes());
+  cudaError_t e = dev_alloc(&f->data, halves * f->half_bytes(), op->stream);
   if (e != cudaSuccess) {
     delete static_cast<gb_field_s*>(f);
-    set_error("cudaMalloc of %zu bytes failed: %s", halves * f->n5 * spinor_bytes(prec), cudaGetErrorString(e));
+    set_error("device allocation of %zu bytes failed: %s", halves * f->n5 * spinor_bytes(prec), cudaGetErrorString(e));
     return GB_ERR_OOM;
   }
   // zero on the operator's stream: a non-blocking stream does not wait for work on the
@@ -77,11 +142,11 @@ int field_alloc(Op* op, int subset, int prec, Field** out) {
   // have written the (lazily allocated) field
   cudaMemsetAsync(f->data, 0, halves * f->half_bytes(), op->stream);
   if (prec == GB_F16) {
-    e = cudaMalloc(&f->norms, halves * f->n5 * sizeof(float));
+    e = dev_alloc(reinterpret_cast<void**>(&f->norms), halves * f->n5 * sizeof(float), op->stream);
     if (e != cudaSuccess) {
-      cudaFree(f->data);
+      dev_free(f->data, op->stream);
       delete static_cast<gb_field_s*>(f);
-      set_error("cudaMalloc of norms failed: %s", cudaGetErrorString(e));
+      set_error("device allocation of norms failed: %s", cudaGetErrorString(e));
       return GB_ERR_OOM;
     }
     cudaMemsetAsync(f->norms, 0, halves * f->n5 * sizeof(float), op->stream);
@@ -93,8 +158,8 @@ int field_alloc(Op* op, int subset, int prec, Field** out) {
 void field_free(Field* f) {
   if (!f) return;
   if (f->owned) {
-    cudaFree(f->data);
-    if (f->norms) cudaFree(f->norms);
+    dev_free(f->data, f->op->stream);
+    dev_free(f->norms, f->op->stream);
   }
   delete static_cast<gb_field_s*>(f);
 }
@@ -617,17 +682,17 @@ static void op_release(Op* op) {
   for (Field* f : op->ws) field_free(f);
   op->ws.clear();
   for (int p = 0; p < 2; p++) {
-    cudaFree(op->links[p]);
-    cudaFree(op->nbr[p]);
+    dev_free(op->links[p], op->stream);
+    dev_free(op->nbr[p], op->stream);
   }
-  cudaFree(op->d_err);
-  cudaFree(op->d_partial);
-  cudaFree(op->d_result);
-  cudaFreeHost(op->h_result);
-  cudaFree(op->d_stage);
-  cudaFree(op->d_cg);
-  cudaFreeHost(op->h_cg);
-  cudaFree(op->d_all_done);
+  dev_free(op->d_err, op->stream);
+  dev_free(op->d_partial, op->stream);
+  dev_free(op->d_result, op->stream);
+  pinned_put(op->h_result);
+  dev_free(op->d_stage, op->stream);
+  dev_free(op->d_cg, op->stream);
+  pinned_put(op->h_cg);
+  dev_free(op->d_all_done, op->stream);
 }
 
 static int op_create(int kind, const int dims[4], int Ls, double mass, double M5, double b, double c,
@@ -675,10 +740,11 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
     return GB_ERR_UNSUPPORTED;
   }
   if (kind == 1) cayley_setup(op);
+  keep_pool_memory(op->device);
   int rc = GB_OK;
   auto alloc = [&](void** p, size_t n) {
     if (rc != GB_OK) return;
-    if (cudaMalloc(p, n) != cudaSuccess) { set_error("cudaMalloc of %zu bytes failed", n); rc = GB_ERR_OOM; }
+    if (dev_alloc(p, n, op->stream) != cudaSuccess) { set_error("device allocation of %zu bytes failed", n); rc = GB_ERR_OOM; }
   };
   for (int p = 0; p < 2; p++) {
     alloc(&op->links[p], op->link_bytes_per_parity());
@@ -689,8 +755,8 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
   alloc(reinterpret_cast<void**>(&op->d_result), size_t(nrhs) * 8 * sizeof(double));
   alloc(reinterpret_cast<void**>(&op->d_cg), size_t(nrhs) * sizeof(CGScalars));
   alloc(reinterpret_cast<void**>(&op->d_all_done), 4 * sizeof(int));
-  if (rc == GB_OK && cudaMallocHost(reinterpret_cast<void**>(&op->h_result), size_t(nrhs) * 8 * sizeof(double)) != cudaSuccess) rc = GB_ERR_OOM;
-  if (rc == GB_OK && cudaMallocHost(reinterpret_cast<void**>(&op->h_cg), size_t(nrhs) * sizeof(CGScalars) + 64) != cudaSuccess) rc = GB_ERR_OOM;
+  if (rc == GB_OK && !(op->h_result = static_cast<double*>(pinned_get(size_t(nrhs) * 8 * sizeof(double))))) rc = GB_ERR_OOM;
+  if (rc == GB_OK && !(op->h_cg = static_cast<CGScalars*>(pinned_get(size_t(nrhs) * sizeof(CGScalars) + 64)))) rc = GB_ERR_OOM;
   if (rc == GB_OK && cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream) != cudaSuccess) rc = GB_ERR_CUDA;
   if (rc == GB_OK) rc = build_neighbours(op);
   if (rc != GB_OK) {
@@ -713,10 +779,13 @@ int op_import_gauge_dev(Op* op, const double* U_dev) {
 
 int ensure_stage(Op* op, size_t bytes) {
   if (op->stage_bytes >= bytes) return GB_OK;
-  cudaFree(op->d_stage);
+  dev_free(op->d_stage, op->stream);
   op->d_stage = nullptr;
   op->stage_bytes = 0;
-  if (cudaMalloc(&op->d_stage, bytes) != cudaSuccess) { set_error("cudaMalloc of %zu staging bytes failed", bytes); return GB_ERR_OOM; }
+  if (dev_alloc(reinterpret_cast<void**>(&op->d_stage), bytes, op->stream) != cudaSuccess) {
+    set_error("device allocation of %zu staging bytes failed", bytes);
+    return GB_ERR_OOM;
+  }
   op->stage_bytes = bytes;
   return GB_OK;
 }
@@ -780,6 +849,7 @@ const char* gb_status_string(int s) {
     case GB_ERR_NO_DEVICE: return "no CUDA device";
     case GB_ERR_UNSUPPORTED: return "unsupported";
     case GB_ERR_IO: return "file I/O or format error";
+    case GB_ERR_CANCELLED: return "cancelled";
   }
   return "unknown status";
 }

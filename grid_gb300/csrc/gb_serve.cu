@@ -1,15 +1,20 @@
 // gb_serve.cu -- a continuous-batching propagator-solve service on one GPU.
 //
 // Requests (Moebius DWF: geometry, Ls, mass, a seeded gauge field, nsrc Gaussian
-// sources) enter a FIFO queue.  `slots` worker threads each own a CUDA stream; a worker
-// admits the head request as soon as its device-memory estimate fits the remaining HBM
-// budget, builds an FP64 and an inner-precision operator with nrhs = number of sources
+// sources) enter a queue.  `slots` worker threads each own a CUDA stream; a worker admits
+// a queued request as soon as its device-memory estimate fits what is left of the HBM
+// budget (arrival order, or least work first, with an age bound after which the oldest
+// request may not be passed), builds an FP64 and an inner-precision operator with nrhs = number of sources
 // (so one multi-RHS Dslash launch reads each link once for all of the request's sources),
 // generates the gauge field and the sources on the device, and runs the mixed-precision
 // SchurRedBlackDiagMooeeSolve.  Requests that arrive while others run are admitted as
 // slots and memory free up; their kernels overlap on the device through the streams.
 // A request whose sources do not fit the budget together is solved in chunks of
-// sources; one that does not fit with a single source is rejected (GB_ERR_OOM).
+// sources; one that does not fit with a single source is rejected at submission
+// (GB_ERR_OOM).  The worker path allocates through the library's stream-ordered
+// allocator, so no slot synchronises the device while the others run.  Each request's
+// device work is bracketed by CUDA events on its slot's stream, which places it on the
+// GPU's own timeline.
 //
 // Dry-run mode (flags bit 0) replaces the device work by a sleep of the request's
 // dry_seconds, so the admission logic can be exercised without a GPU.
@@ -149,16 +154,28 @@ struct gb_server_s {
   unsigned flags = 0;
   int use_graphs = 0;
   int device = 0;
+  double age_limit = 10.0;  // seconds the oldest request waits before nothing may pass it
   std::mutex mu;
   std::condition_variable cv, cv_done;
   std::deque<std::pair<int64_t, gb_request>> queue;
   std::vector<gb_request_result> done;
   std::vector<std::thread> workers;
-  int running = 0, max_running = 0;
-  int64_t next_id = 0, submitted = 0, finished = 0;
+  int running = 0, max_running = 0, max_queued = 0;
+  int64_t next_id = 0, submitted = 0, finished = 0, cancelled = 0, rejected = 0;
   bool stop = false;
+  struct Sample {
+    double t;
+    int queued, running;
+  };
+  std::vector<Sample> trace;
+  cudaEvent_t origin = nullptr;  // the device timeline's zero, recorded at creation
+  double origin_host = 0.0;      // host seconds since t0 when origin completed
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+  void sample() {  // under mu
+    max_queued = std::max(max_queued, int(queue.size()));
+    trace.push_back(Sample{now(), int(queue.size()), running});
+  }
 };
 
 namespace {
@@ -172,6 +189,44 @@ size_t request_bytes(const gb_request& r, int nsrc) {
   const size_t lo = r.inner_precision == GB_F16 ? 52 : 96;
   const size_t per_site4 = 1152 + 576 + 64 + 576;  // FP64 + FP32 links, neighbours, FP64 gauge staging
   return size_t(vol) * per_site4 + size_t(n5) * (26 * 192 + 12 * lo);
+}
+
+// work of one CG iteration (the shortest-first key): 4D volume x Ls x sources
+double request_work(const gb_request& r) {
+  double v = 1;
+  for (int k = 0; k < 4; k++) v *= r.dims[k];
+  return v * r.Ls * r.nsrc;
+}
+// largest chunk of a request's sources that fits the whole budget (0: none does)
+int fitting_chunk(const gb_server_s* S, const gb_request& r) {
+  int chunk = r.nsrc;
+  while (chunk > 0 && request_bytes(r, chunk) > S->budget) chunk--;
+  return chunk;
+}
+// The queue position to admit now, or -1 (under mu).  Default: the first in arrival order
+// that fits what is left of the budget; FIFO (flags bit 2), or once the oldest has waited
+// age_limit: only the oldest; shortest first (bit 3): the least work among those allowed.
+int pick(gb_server_s* S, size_t* need, int* chunk) {
+  const int n = int(S->queue.size());
+  if (n == 0) return -1;
+  const bool only_head = (S->flags & 4) || S->now() - S->queue.front().second.t_submit >= S->age_limit;
+  int best = -1;
+  double best_work = 0;
+  for (int i = 0; i < (only_head ? 1 : n); i++) {
+    const gb_request& r = S->queue[i].second;
+    const int c = fitting_chunk(S, r);
+    const size_t nb = request_bytes(r, c);
+    if (S->used + nb > S->budget) continue;
+    const double w = request_work(r);
+    if (best < 0 || ((S->flags & 8) && w < best_work)) {
+      best = i;
+      best_work = w;
+      *need = nb;
+      *chunk = c;
+      if (!(S->flags & 8)) break;
+    }
+  }
+  return best;
 }
 
 int solve_request(gb_server_s* S, const gb_request& rq, int nsrc, uint64_t src_seed_offset, cudaStream_t st,
@@ -188,16 +243,16 @@ int solve_request(gb_server_s* S, const gb_request& rq, int nsrc, uint64_t src_s
   do {
     if ((rc = gb_mobius_create(rq.dims, rq.Ls, rq.mf, rq.M5, rq.b, rq.c, ph, GB_F64, nsrc, st, 0, &od))) break;
     if ((rc = gb_mobius_create(rq.dims, rq.Ls, rq.mf, rq.M5, rq.b, rq.c, ph, rq.inner_precision, nsrc, st, 0, &of))) break;
-    if (cudaMalloc(&dU, size_t(vol) * 36 * 16) != cudaSuccess) { rc = GB_ERR_OOM; break; }
+    if (cudaMallocAsync(reinterpret_cast<void**>(&dU), size_t(vol) * 36 * 16, st) != cudaSuccess) { rc = GB_ERR_OOM; break; }
     const int64_t nl = vol * 4;
     random_gauge_kernel<<<unsigned((nl + 127) / 128), 128, 0, st>>>(nl, rq.eps, rq.gauge_seed, reinterpret_cast<double2*>(dU));
     if ((rc = gb_op_import_gauge_device(od, dU))) break;
     if ((rc = gb_op_import_gauge_device(of, dU))) break;
-    cudaFree(dU);
+    cudaFreeAsync(dU, st);
     dU = nullptr;
     if ((rc = gb_field_create(od, GB_FULL, GB_F64, &src))) break;
     if ((rc = gb_field_create(od, GB_FULL, GB_F64, &sol))) break;
-    if (cudaMalloc(&dS, ncomplex * 16) != cudaSuccess) { rc = GB_ERR_OOM; break; }
+    if (cudaMallocAsync(reinterpret_cast<void**>(&dS), ncomplex * 16, st) != cudaSuccess) { rc = GB_ERR_OOM; break; }
     random_gaussian_kernel<<<unsigned((ncomplex + 255) / 256), 256, 0, st>>>(
         ncomplex, rq.src_seed + src_seed_offset, reinterpret_cast<double2*>(dS));
     if ((rc = gb_field_import_device(src, dS))) break;
@@ -225,8 +280,8 @@ int solve_request(gb_server_s* S, const gb_request& rq, int nsrc, uint64_t src_s
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) rc = GB_ERR_CUDA;
   } while (false);
-  if (dU) cudaFree(dU);
-  if (dS) cudaFree(dS);
+  if (dU) cudaFreeAsync(dU, st);
+  if (dS) cudaFreeAsync(dS, st);
   gb_field_destroy(src);
   gb_field_destroy(sol);
   gb_op_destroy(of);
@@ -234,40 +289,49 @@ int solve_request(gb_server_s* S, const gb_request& rq, int nsrc, uint64_t src_s
   return rc;
 }
 
+// device seconds of event e on the server's device timeline (-1 when unavailable)
+double device_time(gb_server_s* S, cudaEvent_t e) {
+  float ms = 0.f;
+  if (!S->origin || cudaEventElapsedTime(&ms, S->origin, e) != cudaSuccess) return -1.0;
+  return S->origin_host + ms * 1e-3;
+}
+
 void worker(gb_server_s* S) {
-  if (!(S->flags & 1)) cudaSetDevice(S->device);
+  const bool dry = S->flags & 1;
+  if (!dry) cudaSetDevice(S->device);
   cudaStream_t st = nullptr;
-  if (!(S->flags & 1)) cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (!dry) {
+    cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+  }
   for (;;) {
     std::pair<int64_t, gb_request> item;
     size_t need = 0;
     int chunk = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
+      int at = -1;
       for (;;) {
         if (S->stop && S->queue.empty()) {
           lk.unlock();
+          if (e0) cudaEventDestroy(e0);
+          if (e1) cudaEventDestroy(e1);
           if (st) cudaStreamDestroy(st);
           return;
         }
-        if (!S->queue.empty()) {
-          const gb_request& h = S->queue.front().second;
-          // largest chunk of the head request's sources that fits the whole budget
-          chunk = h.nsrc;
-          while (chunk > 1 && request_bytes(h, chunk) > S->budget) chunk--;
-          need = request_bytes(h, chunk);
-          if (need > S->budget || S->used + need <= S->budget) break;  // reject, or admit
-        }
-        S->cv.wait(lk);
+        if ((at = pick(S, &need, &chunk)) >= 0) break;
+        // wake at least when the oldest request reaches its age bound
+        S->cv.wait_for(lk, std::chrono::milliseconds(50));
       }
-      item = S->queue.front();
-      S->queue.pop_front();
-      if (need <= S->budget) {
-        S->used += need;
-        S->peak_used = std::max(S->peak_used, S->used);
-        S->running++;
-        S->max_running = std::max(S->max_running, S->running);
-      }
+      item = S->queue[at];
+      S->queue.erase(S->queue.begin() + at);
+      S->used += need;
+      S->peak_used = std::max(S->peak_used, S->used);
+      S->running++;
+      S->max_running = std::max(S->max_running, S->running);
+      S->sample();
     }
     const gb_request& rq = item.second;
     gb_request_result res;
@@ -277,12 +341,12 @@ void worker(gb_server_s* S) {
     res.t_start = S->now();
     res.nsrc = rq.nsrc;
     res.chunk = chunk;
-    if (need > S->budget) {
-      res.status = GB_ERR_OOM;
-    } else if (S->flags & 1) {
+    res.dev_start = res.dev_end = -1.0;
+    if (dry) {
       std::this_thread::sleep_for(std::chrono::duration<double>(rq.dry_seconds));
       res.status = GB_OK;
     } else {
+      cudaEventRecord(e0, st);
       int rc = GB_OK;
       for (int first = 0; first < rq.nsrc && rc == GB_OK; first += chunk) {
         const int n = std::min(chunk, rq.nsrc - first);
@@ -291,17 +355,21 @@ void worker(gb_server_s* S) {
         rc = solve_request(S, rq, n, uint64_t(first) * 0x100000001ull, st, &res, rq.solution,
                            size_t(first) * size_t(vol) * rq.Ls * 24);
       }
+      cudaEventRecord(e1, st);
+      if (cudaEventSynchronize(e1) == cudaSuccess) {
+        res.dev_start = device_time(S, e0);
+        res.dev_end = device_time(S, e1);
+      }
       res.status = rc;
     }
     res.t_end = S->now();
     {
       std::lock_guard<std::mutex> lk(S->mu);
-      if (need <= S->budget) {
-        S->used -= need;
-        S->running--;
-      }
+      S->used -= need;
+      S->running--;
       S->done.push_back(res);
       S->finished++;
+      S->sample();
     }
     S->cv.notify_all();
     S->cv_done.notify_all();
@@ -342,6 +410,14 @@ int gb_server_create(size_t hbm_budget_bytes, int slots, unsigned flags, gb_serv
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { delete S; set_error("no CUDA device"); return GB_ERR_NO_DEVICE; }
     cudaGetDevice(&S->device);
+    // the device timeline's origin: an event that has completed at a known host time
+    if (cudaEventCreate(&S->origin) == cudaSuccess) {
+      cudaEventRecord(S->origin, nullptr);
+      cudaEventSynchronize(S->origin);
+      S->origin_host = S->now();
+    } else {
+      S->origin = nullptr;
+    }
   }
   for (int i = 0; i < slots; i++) S->workers.emplace_back(worker, S);
   *out = S;
@@ -361,11 +437,75 @@ int gb_server_submit(gb_server_t S, const gb_request* r, int64_t* id) {
     gb_request q = *r;
     q.t_submit = S->now();
     const int64_t i = S->next_id++;
-    S->queue.emplace_back(i, q);
     S->submitted++;
     if (id) *id = i;
+    if (fitting_chunk(S, q) == 0) {  // not even one source fits the whole budget
+      gb_request_result res;
+      std::memset(&res, 0, sizeof(res));
+      res.id = i;
+      res.status = GB_ERR_OOM;
+      res.nsrc = q.nsrc;
+      res.t_submit = res.t_start = res.t_end = q.t_submit;
+      res.dev_start = res.dev_end = -1.0;
+      S->done.push_back(res);
+      S->finished++;
+      S->rejected++;
+    } else {
+      S->queue.emplace_back(i, q);
+    }
+    S->sample();
   }
   S->cv.notify_all();
+  S->cv_done.notify_all();
+  return GB_OK;
+}
+
+int gb_server_set_age_limit(gb_server_t S, double seconds) {
+  if (!S || !(seconds >= 0)) return GB_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->age_limit = seconds;
+  return GB_OK;
+}
+
+int gb_server_cancel_queued(gb_server_t S, int64_t* n) {
+  if (!S) return GB_ERR_BAD_ARG;
+  int64_t k = 0;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    const double t = S->now();
+    for (auto& it : S->queue) {
+      gb_request_result res;
+      std::memset(&res, 0, sizeof(res));
+      res.id = it.first;
+      res.status = GB_ERR_CANCELLED;
+      res.nsrc = it.second.nsrc;
+      res.t_submit = it.second.t_submit;
+      res.t_start = res.t_end = t;
+      res.dev_start = res.dev_end = -1.0;
+      S->done.push_back(res);
+      k++;
+    }
+    S->queue.clear();
+    S->finished += k;
+    S->cancelled += k;
+    S->sample();
+  }
+  if (n) *n = k;
+  S->cv.notify_all();
+  S->cv_done.notify_all();
+  return GB_OK;
+}
+
+int gb_server_trace(gb_server_t S, double* t, int* queued, int* running, int max, int* n) {
+  if (!S || !n || max < 0) return GB_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  const int k = std::min<int>(max, int(S->trace.size()));
+  for (int i = 0; i < k; i++) {
+    if (t) t[i] = S->trace[i].t;
+    if (queued) queued[i] = S->trace[i].queued;
+    if (running) running[i] = S->trace[i].running;
+  }
+  *n = k;
   return GB_OK;
 }
 
@@ -399,6 +539,9 @@ int gb_server_stats(gb_server_t S, gb_server_stats_t* st) {
   st->submitted = S->submitted;
   st->finished = S->finished;
   st->now = S->now();
+  st->cancelled = S->cancelled;
+  st->rejected = S->rejected;
+  st->max_queued = S->max_queued;
   return GB_OK;
 }
 
@@ -410,6 +553,7 @@ int gb_server_destroy(gb_server_t S) {
   }
   S->cv.notify_all();
   for (auto& t : S->workers) t.join();
+  if (S->origin) cudaEventDestroy(S->origin);
   delete S;
   return GB_OK;
 }

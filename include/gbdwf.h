@@ -41,7 +41,8 @@ enum {
   GB_ERR_TIMEOUT = 6,       /* a bounded device wait gave up                         */
   GB_ERR_NO_DEVICE = 7,     /* no CUDA device visible                                */
   GB_ERR_UNSUPPORTED = 8,
-  GB_ERR_IO = 9             /* file I/O, format, or a checksum / plaquette mismatch (NerscIO.h asserts) */
+  GB_ERR_IO = 9,            /* file I/O, format, or a checksum / plaquette mismatch (NerscIO.h asserts) */
+  GB_ERR_CANCELLED = 10     /* a queued service request shed by gb_server_cancel_queued  */
 };
 
 /* ---- precisions and subsets ---- */
@@ -437,10 +438,19 @@ int gb_unit_gauge(const int dims[4], double* U);
  * No single Grid interface corresponds: a service loop in front of
  * SchurRedBlackDiagMooeeSolve(ConjugateGradientReliableUpdate) on MobiusFermion.
  * A request solves M x = b for nsrc Gaussian 5D sources on a seeded gauge field; its
- * sources share one multi-RHS operator.  Workers (slots) admit the queue head when its
- * memory estimate fits the budget; solves of different requests overlap on the device.
+ * sources share one multi-RHS operator.  Workers (slots) admit queued requests whose
+ * memory estimate fits what the budget has left; solves of different requests overlap on
+ * the device (each slot has its own stream, and the library's allocations are
+ * stream-ordered, so a slot's set-up does not synchronise the device).
+ * Admission (default): the first queued request, in arrival order, that fits; once the
+ * oldest request has waited age_limit seconds (gb_server_set_age_limit, default 10 s)
+ * nothing may pass it, so a large request is not starved.  A request that cannot fit the
+ * whole budget even with one source is rejected at submission (status GB_ERR_OOM).
  * flags: bit 0 = dry run (no device work: each request sleeps dry_seconds),
- *        bit 1 = capture the CG iteration chunks in CUDA graphs. */
+ *        bit 1 = capture the CG iteration chunks in CUDA graphs,
+ *        bit 2 = strict FIFO admission (only the oldest request may be admitted),
+ *        bit 3 = shortest first: among the requests that may be admitted, the one with
+ *                the least work per CG iteration (volume x Ls x sources). */
 typedef struct {
   int dims[4];
   int Ls;
@@ -466,6 +476,9 @@ typedef struct {
   double unprec_residual; /* max over sources of |M x - b| / |b| */
   double solution_norm2;
   double t_submit, t_start, t_end; /* seconds since the server was created */
+  double dev_start, dev_end;      /* the request's device work on the GPU's clock (CUDA events
+                                     on its slot's stream), seconds since the server was
+                                     created; -1 without device work */
 } gb_request_result;
 
 typedef struct {
@@ -473,6 +486,8 @@ typedef struct {
   int running, max_running, queued;
   int64_t submitted, finished;
   double now;
+  int64_t cancelled, rejected; /* shed by gb_server_cancel_queued; rejected at submission */
+  int max_queued;
 } gb_server_stats_t;
 
 typedef struct gb_server_s* gb_server_t;
@@ -483,6 +498,13 @@ int gb_server_results(gb_server_t s, gb_request_result* out, int max, int* n);
 int gb_server_stats(gb_server_t s, gb_server_stats_t* st);
 int gb_server_destroy(gb_server_t s);
 int gb_request_bytes(const gb_request* r, size_t* bytes); /* the admission estimate */
+int gb_server_set_age_limit(gb_server_t s, double seconds);
+/* Sheds every request still queued (not admitted): each finishes with GB_ERR_CANCELLED;
+ * *n = how many.  Requests already running complete. */
+int gb_server_cancel_queued(gb_server_t s, int64_t* n);
+/* The queue depth over time: one sample (t, queued, running) at every submission,
+ * admission and completion, oldest first; *n = samples copied (at most max). */
+int gb_server_trace(gb_server_t s, double* t, int* queued, int* running, int max, int* n);
 
 /* ---- device, stream and host-buffer utilities ------------------------------------ */
 int gb_set_device(int device);                       /* cudaSetDevice for this thread        */

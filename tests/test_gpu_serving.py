@@ -1,7 +1,8 @@
 """The propagator-solve service on the GPU: a request's result is the same alone and in
 a mix of concurrent requests (tolerance: relative L2 1e-12; every solve reaches the true
 residual 1e-10), agrees with the oracle's FP64 Schur solve of the same seeded inputs, and
-CUDA-graph capture of the CG chunks does not change it."""
+CUDA-graph capture of the CG chunks does not change it.  The concurrent requests' device
+work overlaps on the GPU's own clock (CUDA events on each slot's stream)."""
 import numpy as np
 import pytest
 
@@ -41,7 +42,13 @@ def test_same_alone_and_in_the_mix(gpu_available):
     s.close()
     assert all(x.status == 0 for x in res)
     assert all(x.true_residual < 1e-10 and x.unprec_residual < 1e-9 for x in res)
-    assert st.max_running >= 2  # the solves overlapped on the device
+    assert st.max_running >= 2
+    # the device intervals of different requests overlap on the GPU timeline
+    iv = [(x.dev_start, x.dev_end) for x in res]
+    assert all(0 <= a < b for a, b in iv)
+    overlaps = [(i, j) for i in range(len(iv)) for j in range(i + 1, len(iv))
+                if min(iv[i][1], iv[j][1]) - max(iv[i][0], iv[j][0]) > 0]
+    assert overlaps, iv
     assert o.rel_l2(mixed, alone) < 1e-12
     assert res[2].iterations == r0.iterations
 

@@ -1,9 +1,13 @@
 """Host logic of the propagator-solve service, in dry-run mode (no device work: each
 request holds its memory for dry_seconds).  Checks continuous batching: requests that
 arrive while others run are admitted as slots and memory free up, the HBM budget is never
-exceeded, admission is first-come first-served, oversized requests are solved in chunks
-of sources or rejected."""
+exceeded, admission goes in arrival order but lets a request that fits pass one that
+does not (until the oldest reaches its age bound), oversized requests are solved in
+chunks of sources or rejected at submission, queued requests can be shed, and the queue
+depth is traced."""
 import time
+
+import numpy as np
 
 import grid_gb300 as g
 
@@ -67,7 +71,8 @@ def test_oversized_request_is_chunked_or_rejected():
     tiny.submit(req(dims=(24, 24, 24, 24), Ls=16, nsrc=1, dry=0.01))
     assert tiny.wait(1, 10)
     (r,) = tiny.results()
-    assert r.status == 3  # GB_ERR_OOM: does not fit even one source
+    assert r.status == 3  # GB_ERR_OOM: does not fit even one source, rejected at submission
+    assert tiny.stats().rejected == 1
     tiny.close()
 
 
@@ -77,3 +82,72 @@ def test_request_bytes_scale_with_sources_and_volume():
     c = g.request_bytes(req(dims=(16, 8, 8, 8), Ls=8, nsrc=4))
     assert a < b < c
     assert abs(c / b - 2) < 0.01
+
+
+def test_skip_ahead_then_age_bound():
+    """A large request that does not fit what is left of the budget is passed by a small
+    one that does; once the large one has waited age_limit nothing passes it."""
+    small = g.request_bytes(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1))
+    large = g.request_bytes(req(dims=(16, 16, 16, 16), Ls=16, nsrc=4))
+    budget = large + small // 2  # the large one fits only when nothing else runs
+    s = g.Server(budget, slots=4, flags=g.Server.DRY_RUN)
+    s.set_age_limit(0.25)
+    hold = s.submit(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1, dry=0.6))  # runs, blocking the large one
+    time.sleep(0.05)
+    big = s.submit(req(dims=(16, 16, 16, 16), Ls=16, nsrc=4, dry=0.05))
+    time.sleep(0.02)
+    passer = s.submit(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1, dry=0.05))  # fits beside `hold`
+    time.sleep(0.4)  # the large request is now older than the age bound
+    late = s.submit(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1, dry=0.05))
+    assert s.wait(4, 10)
+    res = {x.id: x for x in s.results()}
+    assert res[passer].t_start < res[big].t_start  # passed the large request
+    assert res[big].t_start < res[late].t_start  # the age bound held the late one back
+    assert res[big].t_start >= res[hold].t_end - 1e-3
+    assert s.stats().peak_used_bytes <= budget
+    s.close()
+
+
+def test_fifo_and_shortest_first_policies():
+    small = g.request_bytes(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1))
+    large = g.request_bytes(req(dims=(16, 16, 16, 16), Ls=16, nsrc=4))
+    # FIFO: the small request waits behind the large one that does not fit yet
+    s = g.Server(large + small // 2, slots=4, flags=g.Server.DRY_RUN | g.Server.FIFO)
+    hold = s.submit(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1, dry=0.3))
+    time.sleep(0.05)
+    big = s.submit(req(dims=(16, 16, 16, 16), Ls=16, nsrc=4, dry=0.05))
+    small_id = s.submit(req(dims=(8, 8, 8, 8), Ls=8, nsrc=1, dry=0.05))
+    assert s.wait(3, 10)
+    res = {x.id: x for x in s.results()}
+    assert res[big].t_start <= res[small_id].t_start
+    assert res[big].t_start >= res[hold].t_end - 1e-3
+    s.close()
+    # shortest first: with one slot busy, the queued requests start smallest first
+    s = g.Server(64 * GB, slots=1, flags=g.Server.DRY_RUN | g.Server.SHORTEST_FIRST)
+    s.set_age_limit(60.0)
+    s.submit(req(dry=0.2))
+    time.sleep(0.05)
+    ids = [s.submit(req(dims=d, Ls=8, nsrc=1, dry=0.02)) for d in ((16, 16, 16, 16), (8, 8, 8, 8), (12, 12, 12, 12))]
+    assert s.wait(4, 10)
+    res = {x.id: x for x in s.results()}
+    order = sorted(ids, key=lambda i: res[i].t_start)
+    assert order == [ids[1], ids[2], ids[0]]
+    s.close()
+
+
+def test_cancel_queued_and_trace():
+    s = g.Server(64 * GB, slots=1, flags=g.Server.DRY_RUN)
+    run = s.submit(req(dry=0.3))
+    time.sleep(0.05)
+    queued = [s.submit(req(dry=0.01)) for _ in range(5)]
+    assert s.cancel_queued() == 5
+    assert s.wait(6, 10)
+    res = {x.id: x for x in s.results()}
+    assert res[run].status == 0
+    assert all(res[i].status == 10 for i in queued)  # GB_ERR_CANCELLED
+    st = s.stats()
+    assert st.cancelled == 5 and st.max_queued == 5
+    t, q, r = s.trace()
+    assert len(t) >= 8 and all(np.diff(t) >= 0)
+    assert q.max() == 5 and q[-1] == 0 and r.max() == 1
+    s.close()
