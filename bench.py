@@ -365,20 +365,20 @@ def extra_cg_schur(g, fp64_maxit=20000):
     vol = int(np.prod(dims))
     out = {"workload": "mobius_dwf_24^4xLs12_mf0.005_schur_cg_1e-10"}
 
-    def solve(inner, nrhs, seed):
+    def solve(inner, nrhs, seed, graphs=1):
         od = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=g.F64, nrhs=nrhs)
         src = g.random_gaussian(vol * Ls * 12 * nrhs, seed)
         fs = od.FermionField().import_(src)
         fx = od.FermionField().zero()
         if inner is None:
-            cg = g.ConjugateGradient(1e-10, fp64_maxit, err_on_no_conv=False, check_every=20, use_graphs=1)
+            cg = g.ConjugateGradient(1e-10, fp64_maxit, err_on_no_conv=False, check_every=20, use_graphs=graphs)
             solver = g.SchurRedBlackDiagMooeeSolve(cg)
             keep = None
         else:
             of = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=inner, nrhs=nrhs)
             cg = g.ConjugateGradientReliableUpdate(1e-10, 30000, 1e-6, g.SchurDiagMooeeOperator(of),
                                                    g.SchurDiagMooeeOperator(od), relup_every=100,
-                                                   err_on_no_conv=False, check_every=20, use_graphs=1)
+                                                   err_on_no_conv=False, check_every=20, use_graphs=graphs)
             solver = g.SchurRedBlackDiagMooeeSolve(cg)
             keep = of
         od.sync()
@@ -423,6 +423,7 @@ def extra_cg_schur(g, fp64_maxit=20000):
                 "note": "the odd-checkerboard Schur system (MpcDagMpc) only; the red-black source and solution steps are not timed"}
 
     m32, x32 = solve(g.F32, 1, 77)
+    m32_loop, _ = solve(g.F32, 1, 77, graphs=2)  # the CG loop on the device (conditional graph node)
     m16, x16 = solve(g.F16, 1, 77)
     mb, _ = solve(g.F32, 4, 78)
     f64, x64 = solve(None, 1, 77)
@@ -441,7 +442,7 @@ def extra_cg_schur(g, fp64_maxit=20000):
                          "solve_estimate_seconds": per_it * f64["iterations"],
                          "sample": "one FP64 MpcDagMpc of the 24^4 x 12 operator, scaled by the FP64 CG iterations"}
     out["mixed_fp32_restarted"] = solve_restart(77)
-    out.update({"mixed_fp32": m32, "mixed_fp16": m16, "mixed_fp32_batched4": mb, "fp64": f64,
+    out.update({"mixed_fp32": m32, "mixed_fp32_device_loop": m32_loop, "mixed_fp16": m16, "mixed_fp32_batched4": mb, "fp64": f64,
                 "speedup_mixed_vs_fp64": m32["solves_per_s"] / f64["solves_per_s"],
                 "speedup_mixed_batched_vs_fp64": mb["solves_per_s"] / f64["solves_per_s"]})
     return out

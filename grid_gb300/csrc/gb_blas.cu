@@ -410,6 +410,30 @@ int launch_cg_alpha(Op* op, const double* partial_inner, int nparts) {
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
+// The device-resident CG loop (a CUDA graph whose conditional WHILE node repeats a
+// captured chunk of iterations).  flags = op->d_all_done: [0] every right-hand side has
+// converged, [1] right-hand sides that want a reliable update (both written by
+// cg_beta_kernel each iteration), [2] chunks run in this launch, [3] the most chunks one
+// launch may run.  arm sets [2], [3] before a launch; check decides after every chunk.
+__global__ void cg_loop_arm_kernel(int* flags, int max_chunks) {
+  flags[2] = 0;
+  flags[3] = max_chunks;
+}
+__global__ void cg_loop_check_kernel(cudaGraphConditionalHandle h, int* flags) {
+  const int n = ++flags[2];
+  cudaGraphSetConditional(h, (!flags[0] && !flags[1] && n < flags[3]) ? 1u : 0u);
+}
+int launch_cg_loop_arm(Op* op, int max_chunks) {
+  cg_loop_arm_kernel<<<1, 1, 0, op->stream>>>(op->d_all_done, max_chunks);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+int launch_cg_loop_check(Op* op, cudaGraphConditionalHandle h) {
+  cg_loop_check_kernel<<<1, 1, 0, op->stream>>>(h, op->d_all_done);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
 int launch_cg_beta(Op* op, const double* partial_norm, int nparts) {
   cg_beta_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial_norm, nparts, op->nrhs, op->d_all_done);
   GB_CHECK_CUDA(cudaGetLastError());

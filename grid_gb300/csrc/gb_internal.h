@@ -262,6 +262,10 @@ int launch_cg_beta(Op* op, const double* partial_norm, int nparts);
 int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5);
 // after a reliable update: cp = c = maxres = cp_true ; b = cp_true / cprev
 int launch_cg_relup_reset(Op* op, const double* d_cp_true);
+// the device-resident CG loop's condition: arm before a graph launch (at most max_chunks
+// chunks), check after every chunk inside the WHILE body (gb_blas.cu)
+int launch_cg_loop_arm(Op* op, int max_chunks);
+int launch_cg_loop_check(Op* op, cudaGraphConditionalHandle h);
 
 }  // namespace gb
 

@@ -405,7 +405,7 @@ int gb_server_create(size_t hbm_budget_bytes, int slots, unsigned flags, gb_serv
   S->budget = hbm_budget_bytes;
   S->slots = slots;
   S->flags = flags;
-  S->use_graphs = (flags & 2) ? 1 : 0;
+  S->use_graphs = (flags & 2) ? 2 : 0;  // the device-resident CG loop
   if (!(flags & 1)) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { delete S; set_error("no CUDA device"); return GB_ERR_NO_DEVICE; }

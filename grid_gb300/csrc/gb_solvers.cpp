@@ -59,14 +59,15 @@ int cg_p_update(Op* op, Field* p, Field* r) {
   return GB_OK;
 }
 
+// flags[0..3] = op->d_all_done (converged, reliable update wanted, chunks the last device
+// loop ran, its cap)
 int fetch_scalars(Op* op, int* flags) {
   GB_CHECK_CUDA(cudaMemcpyAsync(op->h_cg, op->d_cg, size_t(op->nrhs) * sizeof(CGScalars), cudaMemcpyDeviceToHost,
                                 op->stream));
   int* hf = reinterpret_cast<int*>(reinterpret_cast<char*>(op->h_cg) + size_t(op->nrhs) * sizeof(CGScalars));
-  GB_CHECK_CUDA(cudaMemcpyAsync(hf, op->d_all_done, 2 * sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+  GB_CHECK_CUDA(cudaMemcpyAsync(hf, op->d_all_done, 4 * sizeof(int), cudaMemcpyDeviceToHost, op->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(op->stream));
-  flags[0] = hf[0];
-  flags[1] = hf[1];
+  for (int i = 0; i < 4; i++) flags[i] = hf[i];
   return GB_OK;
 }
 
@@ -112,9 +113,47 @@ struct ChunkRunner {
   int runs = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // use_graphs == 2: the loop graph, WHILE (condition) { chunk iterations; check }
+  cudaGraph_t lgraph = nullptr;
+  cudaGraphExec_t lexec = nullptr;
   ~ChunkRunner() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    if (lexec) cudaGraphExecDestroy(lexec);
+    if (lgraph) cudaGraphDestroy(lgraph);
+  }
+  // whether the device-resident loop can run now: a non-legacy stream, and a first chunk
+  // already run directly (the workspace it allocates cannot be allocated inside the loop)
+  bool loop_ready() const { return op->stream != nullptr && runs > 0; }
+  // up to max_chunks chunks of `chunk` iterations on the device, stopping after the chunk in
+  // which every right-hand side converged or a reliable update became due
+  int loop(int max_chunks) {
+    if (!lexec) {
+      GB_CHECK_CUDA(cudaGraphCreate(&lgraph, 0));
+      cudaGraphConditionalHandle h;
+      GB_CHECK_CUDA(cudaGraphConditionalHandleCreate(&h, lgraph, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams np = {};
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = h;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      GB_CHECK_CUDA(cudaGraphAddNode(&node, lgraph, nullptr, nullptr, 0, &np));
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      GB_CHECK_CUDA(cudaStreamBeginCaptureToGraph(op->stream, body, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal));
+      int rc = launch(chunk);
+      if (rc == GB_OK) rc = launch_cg_loop_check(op, h);
+      cudaGraph_t got = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(op->stream, &got);
+      if (rc != GB_OK) return rc;
+      if (e != cudaSuccess) { set_error("CG loop capture: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
+      GB_CHECK_CUDA(cudaGraphInstantiate(&lexec, lgraph, 0));
+    }
+    GB_TRY(launch_cg_loop_arm(op, max_chunks));
+    GB_CHECK_CUDA(cudaGraphLaunch(lexec, op->stream));
+    runs++;
+    return GB_OK;
   }
   int launch(int m) {
     for (int j = 0; j < m; j++) {
@@ -207,15 +246,22 @@ int cg_solve(Op* op, int kind, Field* src, Field* psi, const gb_cg_params* P, gb
   GB_TRY(field_norm2_dev(r, d_cp));
   GB_TRY(launch_cg_init(op, d_ssq, d_cp, P->tolerance, 0.0));
   const int chunk = P->check_every > 0 ? P->check_every : 8;
-  int flags[2] = {0, 0};
+  int flags[4] = {0, 0, 0, 0};
   GB_TRY(fetch_scalars(op, flags));
   int k = 0;
   ChunkRunner runner{op, kind, p, mmp, r, psi, chunk, P->use_graphs != 0};
   while (!flags[0] && k < P->max_iterations) {
-    const int m = std::min(chunk, P->max_iterations - k);
-    GB_TRY(runner.iterate(m));
-    k += m;
-    GB_TRY(fetch_scalars(op, flags));
+    const int full_chunks = (P->max_iterations - k) / chunk;
+    if (P->use_graphs == 2 && runner.loop_ready() && full_chunks > 0) {
+      GB_TRY(runner.loop(full_chunks));
+      GB_TRY(fetch_scalars(op, flags));
+      k += flags[2] * chunk;
+    } else {
+      const int m = std::min(chunk, P->max_iterations - k);
+      GB_TRY(runner.iterate(m));
+      k += m;
+      GB_TRY(fetch_scalars(op, flags));
+    }
     GB_TRY(check_device_error(op));
   }
   std::vector<double> res(n);
@@ -293,7 +339,7 @@ int cg_reliable(Op* od, Op* of, int kind, Field* src, Field* psi, const gb_cg_pa
   GB_TRY(field_zero(x_f));
   GB_TRY(launch_cg_init(of, d_ssq, d_cp, P->tolerance, P->delta > 0 ? P->delta : 0.0));
   const int chunk = P->check_every > 0 ? P->check_every : 8;
-  int flags[2] = {0, 0};
+  int flags[4] = {0, 0, 0, 0};
   GB_TRY(fetch_scalars(of, flags));
   int k = 0, l = 0, since = 0;
   auto promote = [&]() -> int {  // psi += (double) x_f
@@ -302,11 +348,20 @@ int cg_reliable(Op* od, Op* of, int kind, Field* src, Field* psi, const gb_cg_pa
   };
   ChunkRunner runner{of, kind, p_f, mmp_f, r_f, x_f, chunk, P->use_graphs != 0};
   while (!flags[0] && k < P->max_iterations) {
-    const int m = std::min(chunk, P->max_iterations - k);
-    GB_TRY(runner.iterate(m));
-    k += m;
-    since += m;
-    GB_TRY(fetch_scalars(of, flags));
+    int full_chunks = (P->max_iterations - k) / chunk;
+    if (P->relup_every > 0) full_chunks = std::min(full_chunks, (P->relup_every - since + chunk - 1) / chunk);
+    if (P->use_graphs == 2 && runner.loop_ready() && full_chunks > 0) {
+      GB_TRY(runner.loop(full_chunks));
+      GB_TRY(fetch_scalars(of, flags));
+      k += flags[2] * chunk;
+      since += flags[2] * chunk;
+    } else {
+      const int m = std::min(chunk, P->max_iterations - k);
+      GB_TRY(runner.iterate(m));
+      k += m;
+      since += m;
+      GB_TRY(fetch_scalars(of, flags));
+    }
     GB_TRY(check_device_error(of));
     if (flags[0]) break;
     if (flags[1] > 0 || (P->relup_every > 0 && since >= P->relup_every)) {

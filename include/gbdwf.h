@@ -276,7 +276,11 @@ typedef struct {
   int relup_every;       /* ... or at least every relup_every inner iterations (0 = off)  */
   int final_cleanup;     /* ConjugateGradientReliableUpdate::DoFinalCleanup               */
   int check_every;       /* host convergence poll interval in iterations (0 = default)    */
-  int use_graphs;        /* capture the iteration chunk in a CUDA graph                   */
+  int use_graphs;        /* 1: capture the iteration chunk in a CUDA graph; 2: the CG loop
+                            itself on the device -- one graph whose conditional WHILE node
+                            repeats the captured chunk until every right-hand side has
+                            converged, a reliable update is due or the iteration cap is
+                            reached, so the host steps in only at those points            */
 } gb_cg_params;
 
 typedef struct {
@@ -447,7 +451,7 @@ int gb_unit_gauge(const int dims[4], double* U);
  * nothing may pass it, so a large request is not starved.  A request that cannot fit the
  * whole budget even with one source is rejected at submission (status GB_ERR_OOM).
  * flags: bit 0 = dry run (no device work: each request sleeps dry_seconds),
- *        bit 1 = capture the CG iteration chunks in CUDA graphs,
+ *        bit 1 = run each solve's CG loop on the device (gb_cg_params use_graphs = 2),
  *        bit 2 = strict FIFO admission (only the oldest request may be admitted),
  *        bit 3 = shortest first: among the requests that may be admitted, the one with
  *                the least work per CG iteration (volume x Ls x sources). */

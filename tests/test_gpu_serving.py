@@ -97,3 +97,32 @@ def test_cg_with_graphs_matches_direct(gpu_available):
         out.append((cg.IterationsToComplete, fx.export()))
     assert out[0][0] == out[1][0]
     assert o.rel_l2(out[0][1], out[1][1]) < 1e-14
+
+
+@pytest.mark.parametrize("solver", ["plain_fp64", "reliable_fp32"])
+def test_device_resident_cg_loop_matches_host_loop(gpu_available, solver):
+    """use_graphs = 2 runs the CG loop on the device (a graph's conditional WHILE node
+    repeats the captured chunk until convergence or a reliable update is due): the same
+    kernels in the same order as the host-driven loop, so the same iterations and the same
+    solution to rounding."""
+    dims, Ls = (8, 8, 8, 8), 8
+    U = g.random_gauge(dims, 0.5, 17)
+    od = g.MobiusFermion(U, dims, Ls, 0.02, 1.8, 1.5, 0.5, precision=g.F64)
+    of = g.MobiusFermion(U, dims, Ls, 0.02, 1.8, 1.5, 0.5, precision=g.F32)
+    src = g.random_gaussian(int(np.prod(dims)) * Ls * 12, 18)
+    out = []
+    for graphs in (0, 2):
+        fs = od.FermionField().import_(src)
+        fx = od.FermionField().zero()
+        if solver == "plain_fp64":
+            cg = g.ConjugateGradient(1e-10, 5000, check_every=10, use_graphs=graphs)
+        else:
+            cg = g.ConjugateGradientReliableUpdate(1e-10, 20000, 1e-6, g.SchurDiagMooeeOperator(of),
+                                                   g.SchurDiagMooeeOperator(od), relup_every=100, check_every=10,
+                                                   use_graphs=graphs)
+        solver_ = g.SchurRedBlackDiagMooeeSolve(cg)
+        r = solver_(od, fs, fx)
+        out.append((int(r.iterations), float(r.true_residual), fx.export()))
+    assert out[0][0] == out[1][0]
+    assert out[1][1] < 1e-10
+    assert o.rel_l2(out[0][2], out[1][2]) < 1e-13
