@@ -255,11 +255,18 @@ class FermionField:
         self.h = h
         self.precision = op.precision if precision is None else precision
 
+    @classmethod
+    def _view(cls, op: "_FermionOperator", h) -> "FermionField":
+        """A field object over a handle the library owns (never destroyed through it)."""
+        f = cls.__new__(cls)
+        f.op, f.h, f.precision, f._borrowed = op, _vp(h), op.precision, True
+        return f
+
     def __del__(self):
         h = getattr(self, "h", None)
-        if h:
+        if h and not getattr(self, "_borrowed", False):
             lib.gb_field_destroy(h)
-            self.h = None
+        self.h = None
 
     @property
     def _as_parameter_(self):
@@ -619,84 +626,77 @@ def chiral_scale(src: FermionField, dst: FermionField, up, down):
     _check(lib.gb_field_chiral_scale(src.h, dst.h, _dptr(np.ascontiguousarray(c.reshape(-1)))))
 
 
+class CGSolver(C.Structure):
+    """gb_cg_solver: the state of the library's CG-based solver functions."""
+    _fields_ = [("cg", CGParams), ("op_lo", _vp), ("result", CGResult), ("unprec_residual", C.c_double)]
+
+
+_SOLVER_FN = C.CFUNCTYPE(C.c_int, _vp, _vp, _vp, _vp)
+_MADWF_CB = C.CFUNCTYPE(C.c_int, _vp, C.c_int, C.c_double)
+for _n in ("gb_solver_schur", "gb_solver_pv_unprec", "gb_solver_pv_rbprec", "gb_solver_pv_fourier"):
+    _proto(_n, [_vp, _vp, _vp, _vp])
+_proto("gb_pv_fourier_create", [_dp, C.POINTER(CGParams), _i, C.POINTER(_vp)])
+_proto("gb_pv_fourier_destroy", [_vp])
+_proto("gb_pv_fourier_set_params", [_vp, C.POINTER(CGParams)])
+_proto("gb_pv_fourier_result", [_vp, C.POINTER(CGResult)])
+_proto("gb_madwf", [_vp, _vp, _SOLVER_FN, _vp, _SOLVER_FN, _vp, _vp, _vp, _d, _i, _MADWF_CB, _vp, _ip, _dp])
+
+
+class _PVFourierHandle:
+    """gb_pv_fourier_t: the library's Fourier-accelerated Pauli-Villars inverse, which keeps
+    its twisted-mass operator between calls.  Holds the gauge array for the handle's life."""
+
+    def __init__(self, Umu, cg, group_in_s):
+        self.U = np.ascontiguousarray(Umu, dtype=np.complex128)
+        self.cg = cg
+        h = _vp()
+        _check(lib.gb_pv_fourier_create(_dptr(self.U), C.byref(cg.params()), int(group_in_s), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib.gb_pv_fourier_destroy(self.h)
+            self.h = None
+
+    def __call__(self, op, src, dst):
+        _check(lib.gb_pv_fourier_set_params(self.h, C.byref(self.cg.params())))
+        rc = lib.gb_solver_pv_fourier(self.h, op.h, src.h, dst.h)
+        r = CGResult()
+        lib.gb_pv_fourier_result(self.h, C.byref(r))
+        self.cg.result, self.cg.IterationsToComplete, self.cg.TrueResidual = r, r.iterations, r.true_residual
+        _check(rc)
+
+
 class FourierAcceleratedPV:
     """FourierAcceleratedPV(dwfPV, Umu, cg, group_in_s=2) (FourierAcceleratedPV.h:56-237):
-    pvInv(src, dst) solves the Pauli-Villars (mass 1) system of a Cayley operator with
-    constant real b, c.  A twisted DFT along s (e^{-i pi s / Ls}, then the Ls-point
-    transform) makes it block diagonal; modes s and Ls-1-s pair into a 5D twisted-mass
-    Wilson system with
-      mass = -(b^2 M5 + c (1 - cos p + c M5) + b (cos p - 1 + 2 c M5 cos p)) / den,
-      mu = (b + c) sin p / den,  den = b^2 + c^2 + 2 b c cos p,  p = pi (2 s + 1) / Ls,
-    mu of opposite sign on the partner; group_in_s pairs are solved together by the
-    red-black Schur CG, each solution recombined as (pA -+ pB gamma5) / (pA^2 - pB^2) with
-    pA = b + c cos p, pB = -i c sin p, and the inverse transform and twist give dst."""
+    pvInv(src, dst) solves the Pauli-Villars (mass 1) system of a Moebius operator with
+    constant real b, c by the library's gb_solver_pv_fourier: a twisted DFT along s makes
+    it block diagonal, modes s and Ls-1-s pair into 5D twisted-mass Wilson systems solved
+    group_in_s pairs at a time by the red-black Schur CG, and the recombined solutions are
+    transformed back.  cg's IterationsToComplete is the sum over the pair solves."""
 
     def __init__(self, dwfPV, Umu, cg, group_in_s=2):
         self.dwfPV, self.Umu, self.cg, self.group_in_s = dwfPV, Umu, cg, int(group_in_s)
-        Ls = dwfPV.Ls
-        if Ls % (2 * self.group_in_s) != 0:
+        if dwfPV.Ls % (2 * self.group_in_s) != 0:
             raise GridError(1, "Ls must be a multiple of 2 * group_in_s")
-        if getattr(dwfPV, "nrhs", 1) != 1:
-            raise GridError(8, "FourierAcceleratedPV: one right-hand side")
-        if hasattr(dwfPV, "gamma") and not np.allclose(dwfPV.gamma, dwfPV.gamma[0]):
-            raise GridError(8, "FourierAcceleratedPV: constant real b, c expected (CayleyFermion with omega_s = 1)")
-
-    def _tm(self):
-        if not hasattr(self, "tm"):
-            n = 2 * self.group_in_s
-            self.tm = WilsonTMFermion5D(self.Umu, self.dwfPV.dims, np.zeros(n), np.zeros(n), self.dwfPV.phases,
-                                        self.dwfPV.precision)
-        return self.tm
+        self._pv = _PVFourierHandle(Umu, cg, self.group_in_s)
 
     def pvInv(self, src: FermionField, dst: FermionField):
-        op = self.dwfPV
-        Ls, b, c, M5 = op.Ls, op.b, op.c, op.M5
-        s_idx = np.arange(Ls)
-        F = np.exp(-2j * np.pi * np.outer(s_idx, s_idx) / Ls)
-        T = F * np.exp(-1j * np.pi * s_idx / Ls)[None, :]                       # rotatePV(., ., false)
-        Binv = (np.exp(1j * np.pi * s_idx / Ls)[:, None] * F.conj()) / Ls      # rotatePV(., ., true)
-        src_diag, dst_diag = op.FermionField(), op.FermionField().zero()
-        dft_s(src, src_diag, T)
-        tm = self._tm()
-        g = self.group_in_s
-        ts, tx, ty = tm.FermionField(), tm.FermionField(), tm.FermionField()
-        solver = SchurRedBlackDiagMooeeSolve(self.cg)
-        for sgroup in range(Ls // 2 // g):
-            vmass, vmu, up, down = np.zeros(2 * g), np.zeros(2 * g), np.zeros(2 * g, complex), np.zeros(2 * g, complex)
-            for sidx in range(g):
-                s = sgroup * g + sidx
-                p = np.pi / Ls * (2.0 * s + 1.0)
-                cp, sp = np.cos(p), np.sin(p)
-                den = b * b + c * c + 2.0 * b * c * cp
-                mass = -(b * b * M5 + c * (1.0 - cp + c * M5) + b * (-1.0 + cp + 2.0 * c * cp * M5)) / den
-                mu = (b + c) * sp / den
-                vmass[2 * sidx:2 * sidx + 2] = mass
-                vmu[2 * sidx], vmu[2 * sidx + 1] = mu, -mu
-                pA, pB = b + c * cp, -1j * c * sp
-                pden = pA * pA - pB * pB
-                up[2 * sidx], down[2 * sidx] = (pA - pB) / pden, (pA + pB) / pden          # (pA - pB g5) / den
-                up[2 * sidx + 1], down[2 * sidx + 1] = (pA + pB) / pden, (pA - pB) / pden  # (pA + pB g5) / den
-                copy_slice5(ts, 2 * sidx, src_diag, s)
-                copy_slice5(ts, 2 * sidx + 1, src_diag, Ls - s - 1)
-            tm.update(vmass, vmu)
-            tx.zero()
-            solver(tm, ts, tx)
-            chiral_scale(tx, ty, up, down)
-            for sidx in range(g):
-                s = sgroup * g + sidx
-                copy_slice5(dst_diag, s, ty, 2 * sidx)
-                copy_slice5(dst_diag, Ls - s - 1, ty, 2 * sidx + 1)
-        dft_s(dst_diag, dst, Binv)
+        self._pv(self.dwfPV, src, dst)
 
 
 class PauliVillarsSolverFourierAccel:
-    """PauliVillarsSolverFourierAccel(Umu, CG) (PauliVillarsInverters.h:74-88)."""
+    """PauliVillarsSolverFourierAccel(Umu, CG) (PauliVillarsInverters.h:74-88): the
+    Fourier-accelerated inverse of whatever Moebius operator it is called with."""
 
-    def __init__(self, Umu, cg: ConjugateGradient, group_in_s=2):
-        self.Umu, self.CG, self.group_in_s = Umu, cg, group_in_s
+    def __init__(self, Umu, cg, group_in_s=2):
+        self.Umu, self.CG, self.group_in_s = Umu, cg, int(group_in_s)
+        self._pv = _PVFourierHandle(Umu, cg, self.group_in_s)
 
     def __call__(self, matrix, src, sol):
-        FourierAcceleratedPV(matrix, self.Umu, self.CG, self.group_in_s).pvInv(src, sol)
+        if matrix.Ls % (2 * self.group_in_s) != 0:
+            raise GridError(1, "Ls must be a multiple of 2 * group_in_s")
+        self._pv(matrix, src, sol)
 
 
 class MobiusFermion(_FermionOperator):
@@ -1053,16 +1053,30 @@ class SchurRedBlackDiagMooeeSolve:
 
     def __call__(self, op, src, sol):
         s = self.solver
-        lo = s.linop_f.op.h if isinstance(s, ConjugateGradientReliableUpdate) else None
         p, r = s.params(), CGResult()
         res = np.zeros(op.nrhs, dtype=np.float64)
-        _check(lib.gb_schur_solve(op.h, lo, src.h, sol.h, C.byref(p), C.byref(r), _dptr(res)))
+        _check(lib.gb_schur_solve(op.h, self._op_lo(), src.h, sol.h, C.byref(p), C.byref(r), _dptr(res)))
+        self._take(r, op)
+        self.unprec_residual = res
+        return r
+
+    def _op_lo(self):
+        s = self.solver
+        return s.linop_f.op.h if isinstance(s, ConjugateGradientReliableUpdate) else None
+
+    def _state(self) -> CGSolver:
+        """the gb_cg_solver of the library's solver functions for this solve"""
+        st = CGSolver()
+        st.cg = self.solver.params()
+        st.op_lo = self._op_lo()
+        return st
+
+    def _take(self, r: CGResult, op):
+        s = self.solver
         s._store(r, op)
         if isinstance(s, ConjugateGradientReliableUpdate):
             s.ReliableUpdatesPerformed = r.reliable_updates
             s.IterationsToCleanup = r.cleanup_iterations
-        self.unprec_residual = res
-        return r
 
 
 class ZeroGuesser:
@@ -1074,37 +1088,32 @@ class ZeroGuesser:
 
 
 class PauliVillarsSolverUnprec:
-    """PauliVillarsSolverUnprec(CG) (PauliVillarsInverters.h:32-52): solves M(m = 1) sol = src
-    by CG on Mdag M at mass 1, restoring the operator's mass after."""
+    """PauliVillarsSolverUnprec(CG) (PauliVillarsInverters.h:32-52): M(m = 1) sol = src by
+    CG on Mdag M at mass 1 (the library's gb_solver_pv_unprec, which restores the mass)."""
 
     def __init__(self, cg: ConjugateGradient):
         self.CG = cg
 
     def __call__(self, matrix, src, sol):
-        m = matrix.Mass()
-        A = matrix.FermionField()
-        matrix.SetMass(1.0)
-        try:
-            matrix.Mdag(src, A)
-            self.CG(MdagMLinearOperator(matrix), A, sol)
-        finally:
-            matrix.SetMass(m)
+        st = CGSolver()
+        st.cg = self.CG.params()
+        rc = lib.gb_solver_pv_unprec(C.byref(st), matrix.h, src.h, sol.h)
+        self.CG._store(st.result, matrix)
+        _check(rc)
 
 
 class PauliVillarsSolverRBprec:
-    """PauliVillarsSolverRBprec(SchurSolver) (PauliVillarsInverters.h:54-72): the
-    red-black Schur solve at mass 1."""
+    """PauliVillarsSolverRBprec(SchurSolver) (PauliVillarsInverters.h:54-72): the red-black
+    Schur solve at mass 1 (the library's gb_solver_pv_rbprec)."""
 
     def __init__(self, schur: "SchurRedBlackDiagMooeeSolve"):
         self.SchurSolver = schur
 
     def __call__(self, matrix, src, sol):
-        m = matrix.Mass()
-        matrix.SetMass(1.0)
-        try:
-            self.SchurSolver(matrix, src, sol)
-        finally:
-            matrix.SetMass(m)
+        st = self.SchurSolver._state()
+        rc = lib.gb_solver_pv_rbprec(C.byref(st), matrix.h, src.h, sol.h)
+        self.SchurSolver._take(st.result, matrix)
+        _check(rc)
 
 
 class MADWFinnerIterCallbackBase:
@@ -1116,71 +1125,72 @@ class MADWFinnerIterCallbackBase:
 
 class MADWF:
     """MADWF(Mato, Mati, PauliVillarsSolvero, SchurSolveri, Guesseri, resid, maxiter,
-    callback) (Grid/qcd/action/fermion/MADWF.h:47-209): solves the outer (Moebius) system
-    by defect correction, each step a Pauli-Villars solve of the outer operator and a Schur
-    solve of the cheaper inner (e.g. ZMobius with smaller Ls) operator joined through the
-    s = 0 slice of the P-rotated fields.  `src` is a 4D field (canonical complex array,
-    imported with ImportPhysicalFermionSource) or a full 5D field of the outer operator;
-    `sol5` receives the outer 5D solution.  Raises GridError (status NOT_CONVERGED) after
-    maxiter steps, where Grid asserts."""
+    callback) (Grid/qcd/action/fermion/MADWF.h:47-209): the library's gb_madwf solves the
+    outer (Moebius) system by defect correction, each step a Pauli-Villars solve of the
+    outer operator and a Schur solve of the cheaper inner (e.g. ZMobius with smaller Ls)
+    operator joined through the s = 0 slice of the P-rotated fields.  The two solvers (any
+    callables solver(matrix, src, sol)) and the guesser are called back from it.  `src` is a
+    4D field (canonical complex array, imported with ImportPhysicalFermionSource) or a full
+    5D field of the outer operator; `sol5` receives the outer 5D solution.  Raises
+    GridError (status NOT_CONVERGED) after maxiter steps, where Grid asserts."""
 
     def __init__(self, Mato, Mati, PauliVillarsSolvero, SchurSolveri, Guesseri, resid, maxiter, callback=None):
         self.Mato, self.Mati = Mato, Mati
         self.PauliVillarsSolvero, self.SchurSolveri, self.Guesseri = PauliVillarsSolvero, SchurSolveri, Guesseri
         self.target_resid, self.maxiter, self.callback = float(resid), int(maxiter), callback
-        self.iterations = 0
+        self.iterations = self.IterationsToComplete = 0
+        self.FinalResidual = 0.0
         self.residuals = []
 
     def __call__(self, src, sol5):
         Mo, Mi = self.Mato, self.Mati
-        A, B, b, c, defect = (Mo.FermionField() for _ in range(5))
-        ci, yi, xi, srci, Ai = (Mi.FermionField() for _ in range(5))
-        m = Mi.Mass()
         if isinstance(src, FermionField):
-            b.copy_from(src)
+            b = src
         else:
+            b = Mo.FermionField()
             Mo.ImportPhysicalFermionSource(src, b)
-        nb = float(np.sum(b.norm2()))
-        defect.copy_from(b)
-        sol5.zero()
-        self.residuals = []
-        for i in range(self.maxiter):
-            # c0 from the current defect: the s = 0 slice of Pdag PV^-1 defect
-            self.PauliVillarsSolvero(Mo, defect, A)
-            Mo.Pdag(A, c)
-            c0 = ExtractSlice(c, 0)
-            # the inner system with surface term c0: Dwm P y = D(1) P (c0, 0, ..., 0)^T
-            ci.zero()
-            InsertSlice(c0, ci, 0)
-            Mi.P(ci, Ai)
-            Mi.SetMass(1.0)
-            try:
-                Mi.M(Ai, srci)
-            finally:
-                Mi.SetMass(m)
-            self.Guesseri(srci, xi)
-            self.SchurSolveri(Mi, srci, xi)
-            Mi.Pdag(xi, yi)
-            y0 = ExtractSlice(yi, 0)
-            # the bulk of the outer solution: Pdag PV^-1 Dm P (-y0, c_1, ..., c_{Ls-1})
-            InsertSlice(-y0, c, 0)
-            Mo.P(c, B)
-            Mo.M(B, A)
-            self.PauliVillarsSolvero(Mo, A, B)
-            Mo.Pdag(B, A)
-            InsertSlice(y0, A, 0)  # the surface solution back in
-            Mo.P(A, B)
-            axpy(sol5, 1.0, B, sol5)  # sol5 += M^-1 defect
-            Mo.M(sol5, A)
-            axpby(defect, 1.0, -1.0, b, A)  # defect = b - M sol5
-            resid = float(np.sqrt(np.sum(defect.norm2()) / nb))
+        errors = []
+
+        def guarded(body):
+            # a Python exception cannot cross the C frames: keep it, end the solve, raise it
+            def trampoline(*args):
+                try:
+                    body(*args)
+                    return 0
+                except GridError as e:
+                    errors.append(e)
+                    return e.status or 1
+                except BaseException as e:  # noqa: BLE001 -- re-raised below
+                    errors.append(e)
+                    return 1
+            return trampoline
+
+        def pv(user, op, s, x):
+            self.PauliVillarsSolvero(Mo, FermionField._view(Mo, s), FermionField._view(Mo, x))
+
+        def inner(user, op, s, x):
+            fs, fx = FermionField._view(Mi, s), FermionField._view(Mi, x)
+            self.Guesseri(fs, fx)
+            self.SchurSolveri(Mi, fs, fx)
+
+        def step(user, it, resid):
             self.residuals.append(resid)
-            self.iterations = i + 1
+            self.iterations = self.IterationsToComplete = it
+            self.FinalResidual = resid
             if self.callback is not None:
                 self.callback(resid)
-            if resid < self.target_resid:
-                return
-        raise GridError(5, f"MADWF: not converged in {self.maxiter} iterations (residual {self.residuals[-1]:.3e})")
+
+        self.residuals = []
+        self.iterations = self.IterationsToComplete = 0
+        pv_fn, inner_fn, cb_fn = _SOLVER_FN(guarded(pv)), _SOLVER_FN(guarded(inner)), _MADWF_CB(guarded(step))
+        it, fr = C.c_int(), C.c_double()
+        rc = lib.gb_madwf(Mo.h, Mi.h, pv_fn, None, inner_fn, None, b.h, sol5.h, self.target_resid, self.maxiter,
+                          cb_fn, None, C.byref(it), C.byref(fr))
+        self.iterations = self.IterationsToComplete = it.value
+        self.FinalResidual = fr.value
+        if errors:
+            raise errors[0]
+        _check(rc)
 
 
 # ---- propagator-solve service ---------------------------------------------------------

@@ -353,6 +353,70 @@ int gb_cg_multishift(gb_op_t op, int kind, gb_field_t src, int nshift, const dou
 int gb_schur_solve(gb_op_t op, gb_op_t op_lo, gb_field_t src, gb_field_t sol, const gb_cg_params* p,
                    gb_cg_result* res, double* unprec_resid);
 
+/* ---- MADWF and its Pauli-Villars inverters ------------------------------------------
+ * A solver: solve op sol = src for full 5D fields of op; sol's contents on entry are the
+ * initial guess where the solver takes one.  Returns a status; GB_OK to go on.  The
+ * Grid template parameters PVinverter and SchurSolver of MADWF become a function and its
+ * user pointer, so a caller may pass its own solver or one of those below. */
+typedef int (*gb_solver_fn)(void* user, gb_op_t op, gb_field_t src, gb_field_t sol);
+
+/* The state of the library's CG-based solvers (user pointer of the functions below): the
+ * CG parameters, op_lo (NULL: plain CG in op's precision; else the mixed-precision inner
+ * operator of a reliable-update CG, whose mass follows op's), and the results of the last
+ * call (iterations summed over the CG solves it made; the largest true residual). */
+typedef struct {
+  gb_cg_params cg;
+  gb_op_t op_lo;
+  gb_cg_result result;
+  double unprec_residual; /* gb_solver_schur: max over right-hand sides of |M sol - src|/|src| */
+} gb_cg_solver;
+
+/* SchurRedBlackDiagMooeeSolve(CG)(op, src, sol) (SchurRedBlack.h:236-291) with a zero
+ * initial guess (ZeroGuesser, Guesser.h). */
+int gb_solver_schur(void* user /* gb_cg_solver* */, gb_op_t op, gb_field_t src, gb_field_t sol);
+/* PauliVillarsSolverUnprec(CG) (PauliVillarsInverters.h:32-52): M(mass 1) sol = src by CG
+ * on Mdag M from sol's contents; op's mass is restored on every return. */
+int gb_solver_pv_unprec(void* user /* gb_cg_solver*, op_lo NULL */, gb_op_t op, gb_field_t src, gb_field_t sol);
+/* PauliVillarsSolverRBprec(SchurSolver) (PauliVillarsInverters.h:54-72): the red-black
+ * Schur solve at mass 1 (op's and op_lo's masses restored on every return). */
+int gb_solver_pv_rbprec(void* user /* gb_cg_solver* */, gb_op_t op, gb_field_t src, gb_field_t sol);
+
+/* PauliVillarsSolverFourierAccel(Umu, CG) (PauliVillarsInverters.h:74-88) running
+ * FourierAcceleratedPV::pvInv (FourierAcceleratedPV.h:56-237): the mass-1 inverse of a
+ * Moebius operator with constant real b, c, one right-hand side, FP64 or FP32.  A twisted
+ * DFT along s block-diagonalises it; modes s and Ls-1-s pair into 5D twisted-mass Wilson
+ * systems (group_in_s pairs per red-black Schur CG) whose solutions are recombined with
+ * (pA -+ pB gamma5) / (pA^2 - pB^2) and transformed back.  U: the canonical FP64 gauge
+ * field in host memory, borrowed (it must stay valid while the handle is used) and read at
+ * every call; the twisted-mass operator is built at the first call and kept while the
+ * geometry, precision, stream and boundary phases stay the same.  Ls % (2 group_in_s)
+ * must be 0. */
+typedef struct gb_pv_fourier_s* gb_pv_fourier_t;
+int gb_pv_fourier_create(const double* U, const gb_cg_params* cg, int group_in_s, gb_pv_fourier_t* out);
+int gb_pv_fourier_destroy(gb_pv_fourier_t pv);
+int gb_pv_fourier_set_params(gb_pv_fourier_t pv, const gb_cg_params* cg);
+int gb_pv_fourier_result(gb_pv_fourier_t pv, gb_cg_result* res);
+int gb_solver_pv_fourier(void* user /* gb_pv_fourier_t */, gb_op_t op, gb_field_t src, gb_field_t sol);
+
+/* MADWF(Mato, Mati, PauliVillarsSolvero, SchurSolveri, Guesseri, resid, maxiter, callback)
+ * (Grid/qcd/action/fermion/MADWF.h:47-209): solves outer sol5 = src5 (full 5D fields of
+ * the Moebius or ZMobius outer operator; a 4D source goes in by gb_import_physical_source)
+ * by defect correction.  Each step: c = Pdag PV^-1 defect; the inner system Dwm P y =
+ * D(1) P (c_0, 0, ..., 0) solved by inner_solve from a zero guess; the bulk Pdag PV^-1 Dm
+ * P (-y_0, c_1, ...) with y_0 put back at s = 0; sol5 += P of that; defect = src5 - M sol5.
+ * pv solves the outer operator at its own mass (the Pauli-Villars solvers set mass 1),
+ * inner_solve the inner operator at its mass.  After each step callback (may be NULL)
+ * gets the step number (1-based) and |defect| / |src5| (sums over right-hand sides); a
+ * non-zero return ends the solve with that status.  Stops when that residual is below
+ * resid, else returns GB_ERR_NOT_CONVERGED after maxiter steps (where Grid asserts).  The
+ * operators share the 4D lattice and the number of right-hand sides; the inner mass is
+ * restored on every return.  iterations / final_resid (may be NULL): IterationsToComplete
+ * and the last residual. */
+typedef int (*gb_madwf_callback)(void* user, int iteration, double resid);
+int gb_madwf(gb_op_t outer, gb_op_t inner, gb_solver_fn pv, void* pv_user, gb_solver_fn inner_solve,
+             void* inner_user, gb_field_t src5, gb_field_t sol5, double resid, int maxiter, gb_madwf_callback callback,
+             void* callback_user, int* iterations, double* final_resid);
+
 /* ---- NERSC gauge configurations (Grid/parallelIO/NerscIO.h:62-300) ---------------
  * Canonical FP64 gauge fields U[site][mu][3][3] to and from NERSC files: DATATYPE
  * 4D_SU3_GAUGE (two rows stored, the third rebuilt) or 4D_SU3_GAUGE_3x3; FLOATING_POINT

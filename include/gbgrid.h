@@ -34,7 +34,9 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <exception>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -192,6 +194,8 @@ class CheckerboardRef {
 template <class vobj> class Lattice {
   GridBase* grid_ = nullptr;
   gb_field_t h_ = nullptr;
+  bool owned_ = true;
+  Lattice(GridBase* grid, gb_field_t h, bool owned) : grid_(grid), h_(h), owned_(owned) {}
 
  public:
   typedef vobj vector_object;
@@ -199,10 +203,13 @@ template <class vobj> class Lattice {
     gbdetail::check(gb_field_create(grid->context(), grid->_isCheckerBoarded ? GB_EVEN : GB_FULL, vobj::precision, &h_),
                     "gb_field_create");
   }
+  // a Lattice over a field that the library owns (the work fields MADWF hands to the
+  // solvers it calls back); it never destroys the field
+  static Lattice View(GridBase* grid, gb_field_t h) { return Lattice(grid, h, false); }
   Lattice(const Lattice& o) : Lattice(o.grid_) { *this = o; }
-  Lattice(Lattice&& o) noexcept : grid_(o.grid_), h_(o.h_) { o.h_ = nullptr; }
+  Lattice(Lattice&& o) noexcept : grid_(o.grid_), h_(o.h_), owned_(o.owned_) { o.h_ = nullptr; }
   ~Lattice() {
-    if (h_) gb_field_destroy(h_);
+    if (h_ && owned_) gb_field_destroy(h_);
   }
   Lattice& operator=(const Lattice& o) {
     if (this != &o) gbdetail::check(gb_field_copy(h_, o.h_), "gb_field_copy");
@@ -211,6 +218,7 @@ template <class vobj> class Lattice {
   Lattice& operator=(Lattice&& o) noexcept {
     std::swap(grid_, o.grid_);
     std::swap(h_, o.h_);
+    std::swap(owned_, o.owned_);
     return *this;
   }
   Lattice& operator=(const Zero&) {
@@ -1089,11 +1097,27 @@ template <class Field> class SchurRedBlackDiagMooeeSolve {
   void operator()(Matrix& _Matrix, MatrixLo& lower_precision, const Field& in, Field& out) {
     solve(_Matrix, lower_precision.handle(), in, out);
   }
+  // the gb_cg_solver of the library's solver functions (gb_solver_pv_rbprec, ...) for this
+  // solver, and the results of such a call taken back
+  gb_cg_solver solver_state(gb_op_t lo = nullptr) const {
+    gb_cg_solver st{};
+    st.cg = cg().params();
+    st.op_lo = lo;
+    return st;
+  }
+  void take_result(const gb_cg_solver& st) {
+    IterationsToComplete = cg().IterationsToComplete = st.result.iterations;
+    TrueResidual = cg().TrueResidual = st.result.true_residual;
+  }
 
  private:
-  template <class Matrix> void solve(Matrix& M, gb_op_t lo, const Field& in, Field& out) {
+  ConjugateGradient<Field>& cg() const {
     auto* cg = dynamic_cast<ConjugateGradient<Field>*>(&solver_);
     if (!cg) throw GridError(GB_ERR_UNSUPPORTED, "SchurRedBlackDiagMooeeSolve: a ConjugateGradient solver expected");
+    return *cg;
+  }
+  template <class Matrix> void solve(Matrix& M, gb_op_t lo, const Field& in, Field& out) {
+    ConjugateGradient<Field>* cg = &this->cg();
     const gb_cg_params p = cg->params();
     gb_cg_result r;
     // one unpreconditioned residual per right-hand side (slot) of the operator
@@ -1119,130 +1143,90 @@ template <class Field> struct ZeroGuesser {
 };
 
 // PauliVillarsSolverUnprec (PauliVillarsInverters.h:32-52): M(1) sol = src by CG on Mdag M
+// (the library's gb_solver_pv_unprec, which restores the mass)
 template <class Field> class PauliVillarsSolverUnprec {
  public:
   ConjugateGradient<Field>& CG;
   explicit PauliVillarsSolverUnprec(ConjugateGradient<Field>& cg) : CG(cg) {}
   template <class Matrix> void operator()(Matrix& _Matrix, const Field& src, Field& sol) {
-    const RealD m = _Matrix.Mass();
-    Field A(_Matrix.FermionGrid());
-    MdagMLinearOperator<Matrix, Field> HermOp(_Matrix);
-    _Matrix.SetMass(1.0);
-    try {
-      _Matrix.Mdag(src, A);
-      CG(HermOp, A, sol);
-    } catch (...) {
-      _Matrix.SetMass(m);
-      throw;
-    }
-    _Matrix.SetMass(m);
+    gb_cg_solver st{};
+    st.cg = CG.params();
+    const int rc = gb_solver_pv_unprec(&st, _Matrix.handle(), src.handle(), sol.handle());
+    CG.IterationsToComplete = st.result.iterations;
+    CG.TrueResidual = st.result.true_residual;
+    gbdetail::check(rc, "PauliVillarsSolverUnprec");
   }
 };
 
-// PauliVillarsSolverRBprec (PauliVillarsInverters.h:54-72): the Schur solve at mass 1
+// PauliVillarsSolverRBprec (PauliVillarsInverters.h:54-72): the Schur solve at mass 1 (the
+// library's gb_solver_pv_rbprec); SchurSolverType provides solver_state / take_result
 template <class Field, class SchurSolverType> class PauliVillarsSolverRBprec {
  public:
   SchurSolverType& SchurSolver;
   explicit PauliVillarsSolverRBprec(SchurSolverType& s) : SchurSolver(s) {}
   template <class Matrix> void operator()(Matrix& _Matrix, const Field& src, Field& sol) {
-    const RealD m = _Matrix.Mass();
-    _Matrix.SetMass(1.0);
-    try {
-      SchurSolver(_Matrix, src, sol);
-    } catch (...) {
-      _Matrix.SetMass(m);
-      throw;
-    }
-    _Matrix.SetMass(m);
+    gb_cg_solver st = SchurSolver.solver_state();
+    const int rc = gb_solver_pv_rbprec(&st, _Matrix.handle(), src.handle(), sol.handle());
+    SchurSolver.take_result(st);
+    gbdetail::check(rc, "PauliVillarsSolverRBprec");
   }
 };
 
+namespace gbdetail {
+// gb_pv_fourier_t owned by an adapter object
+class PVFourier {
+  gb_pv_fourier_t h_ = nullptr;
+
+ public:
+  PVFourier(const double* U, const gb_cg_params& p, int group_in_s) {
+    check(gb_pv_fourier_create(U, &p, group_in_s, &h_), "FourierAcceleratedPV");
+  }
+  PVFourier(const PVFourier&) = delete;
+  PVFourier& operator=(const PVFourier&) = delete;
+  ~PVFourier() { gb_pv_fourier_destroy(h_); }
+  template <class Field> void solve(gb_op_t op, ConjugateGradient<Field>& cg, const Field& src, Field& dst) const {
+    const gb_cg_params p = cg.params();
+    check(gb_pv_fourier_set_params(h_, &p), "FourierAcceleratedPV");
+    const int rc = gb_solver_pv_fourier(h_, op, src.handle(), dst.handle());
+    gb_cg_result r{};
+    gb_pv_fourier_result(h_, &r);
+    cg.IterationsToComplete = r.iterations;
+    cg.TrueResidual = r.true_residual;
+    check(rc, "FourierAcceleratedPV");
+  }
+};
+}  // namespace gbdetail
+
 // FourierAcceleratedPV (FourierAcceleratedPV.h:56-237): the Pauli-Villars (mass 1) inverse of
-// a Cayley operator with constant real b, c.  A twisted DFT along s block-diagonalises it;
-// modes s and Ls-1-s pair into 5D twisted-mass Wilson systems (group_in_s pairs at a time)
-// solved by the red-black Schur CG, recombined with (pA -+ pB gamma5) / (pA^2 - pB^2), and
-// transformed back.
+// a Moebius operator with constant real b, c by the library's gb_solver_pv_fourier: a
+// twisted DFT along s block-diagonalises it, modes s and Ls-1-s pair into 5D twisted-mass
+// Wilson systems (group_in_s pairs at a time) solved by the red-black Schur CG, and the
+// recombined solutions are transformed back.  Umu must outlive the object.
 template <class Field, class Matrix, class GaugeField> class FourierAcceleratedPV {
   Matrix& dwfPV;
-  const GaugeField& Umu;
   ConjugateGradient<Field>& cg;
-  int group_in_s;
+  gbdetail::PVFourier pv_;
 
  public:
   FourierAcceleratedPV(Matrix& m, const GaugeField& U, ConjugateGradient<Field>& c, int g = 2)
-      : dwfPV(m), Umu(U), cg(c), group_in_s(g) {
-    if (dwfPV.Ls % (2 * group_in_s) != 0) throw GridError(GB_ERR_BAD_ARG, "FourierAcceleratedPV: Ls % (2 group_in_s)");
+      : dwfPV(m), cg(c), pv_(reinterpret_cast<const double*>(U.data.data()), c.params(), g) {
+    if (dwfPV.Ls % (2 * g) != 0) throw GridError(GB_ERR_BAD_ARG, "FourierAcceleratedPV: Ls % (2 group_in_s)");
   }
-  void pvInv(const Field& src, Field& dst) const {
-    const int Ls = dwfPV.Ls, g = group_in_s;
-    const double b = dwfPV.b, c = dwfPV.c, M5 = dwfPV.M5, pi = 3.14159265358979323846;
-    std::vector<ComplexD> T(size_t(Ls) * Ls), B(size_t(Ls) * Ls);
-    for (int k = 0; k < Ls; k++)
-      for (int s = 0; s < Ls; s++) {
-        T[size_t(k) * Ls + s] = std::polar(1.0, -2 * pi * k * s / Ls - pi * s / Ls);
-        B[size_t(s) * Ls + k] = std::polar(1.0 / Ls, 2 * pi * k * s / Ls + pi * s / Ls);
-      }
-    GridBase* F = dwfPV.FermionGrid();
-    Field src_diag(F), dst_diag(F);
-    dst_diag = Zero();
-    gbdetail::check(gb_field_dft_s(src.handle(), src_diag.handle(), reinterpret_cast<const double*>(T.data())),
-                    "FourierAcceleratedPV");
-    GridCartesian* U4 = dynamic_cast<GridCartesian*>(dwfPV.GaugeGrid());
-    GridCartesian G5(U4->dims4, 2 * g);
-    GridRedBlackCartesian G5rb(&G5);
-    GridRedBlackCartesian U4rb(U4);
-    std::vector<RealD> vmass(2 * g, 0.0), vmu(2 * g, 0.0);
-    typedef WilsonImplT<typename Field::vector_object, vLorentzColourMatrixD> TMImpl;
-    WilsonTMFermion5D<TMImpl> tm(Umu, G5, G5rb, *U4, U4rb, vmass, vmu, dwfPV.params);
-    SchurRedBlackDiagMooeeSolve<Field> sol(cg);
-    Field ts(&G5), tx(&G5), ty(&G5);
-    std::vector<double> coef(size_t(8) * g);
-    for (int sgroup = 0; sgroup < Ls / 2 / g; sgroup++) {
-      for (int sidx = 0; sidx < g; sidx++) {
-        const int s = sgroup * g + sidx;
-        const double p = pi / Ls * (2.0 * s + 1.0), cp = std::cos(p), sp = std::sin(p);
-        const double den = b * b + c * c + 2.0 * b * c * cp;
-        const double mass = -(b * b * M5 + c * (1.0 - cp + c * M5) + b * (-1.0 + cp + 2.0 * c * cp * M5)) / den;
-        const double mu = (b + c) * sp / den;
-        vmass[2 * sidx] = vmass[2 * sidx + 1] = mass;
-        vmu[2 * sidx] = mu;
-        vmu[2 * sidx + 1] = -mu;
-        const ComplexD pA(b + c * cp, 0.0), pB(0.0, -c * sp), pden = pA * pA - pB * pB;
-        const ComplexD lo = (pA - pB) / pden, hi = (pA + pB) / pden;
-        const ComplexD cf[4] = {lo, hi, hi, lo};  // slot 2 sidx: (pA - pB g5); 2 sidx + 1: (pA + pB g5)
-        for (int q = 0; q < 4; q++) {
-          coef[size_t(8) * sidx + 2 * q] = cf[q].real();
-          coef[size_t(8) * sidx + 2 * q + 1] = cf[q].imag();
-        }
-        gbdetail::check(gb_field_copy_slice5(ts.handle(), 2 * sidx, src_diag.handle(), s), "FourierAcceleratedPV");
-        gbdetail::check(gb_field_copy_slice5(ts.handle(), 2 * sidx + 1, src_diag.handle(), Ls - s - 1),
-                        "FourierAcceleratedPV");
-      }
-      tm.update(vmass, vmu);
-      tx = Zero();
-      sol(tm, ts, tx);
-      gbdetail::check(gb_field_chiral_scale(tx.handle(), ty.handle(), coef.data()), "FourierAcceleratedPV");
-      for (int sidx = 0; sidx < g; sidx++) {
-        const int s = sgroup * g + sidx;
-        gbdetail::check(gb_field_copy_slice5(dst_diag.handle(), s, ty.handle(), 2 * sidx), "FourierAcceleratedPV");
-        gbdetail::check(gb_field_copy_slice5(dst_diag.handle(), Ls - s - 1, ty.handle(), 2 * sidx + 1),
-                        "FourierAcceleratedPV");
-      }
-    }
-    gbdetail::check(gb_field_dft_s(dst_diag.handle(), dst.handle(), reinterpret_cast<const double*>(B.data())),
-                    "FourierAcceleratedPV");
-  }
+  void pvInv(const Field& src, Field& dst) const { pv_.solve(dwfPV.handle(), cg, src, dst); }
 };
 
-// PauliVillarsSolverFourierAccel (PauliVillarsInverters.h:74-88)
+// PauliVillarsSolverFourierAccel (PauliVillarsInverters.h:74-88); the library keeps its
+// twisted-mass operator from one call to the next
 template <class Field, class GaugeField> class PauliVillarsSolverFourierAccel {
+  gbdetail::PVFourier pv_;
+
  public:
   const GaugeField& Umu;
   ConjugateGradient<Field>& CG;
-  PauliVillarsSolverFourierAccel(const GaugeField& U, ConjugateGradient<Field>& cg) : Umu(U), CG(cg) {}
+  PauliVillarsSolverFourierAccel(const GaugeField& U, ConjugateGradient<Field>& cg)
+      : pv_(reinterpret_cast<const double*>(U.data.data()), cg.params(), 2), Umu(U), CG(cg) {}
   template <class Matrix> void operator()(Matrix& _Matrix, const Field& src, Field& sol) {
-    FourierAcceleratedPV<Field, Matrix, GaugeField> faPV(_Matrix, Umu, CG);
-    faPV.pvInv(src, sol);
+    pv_.solve(_Matrix.handle(), CG, src, sol);
   }
 };
 
@@ -1251,11 +1235,13 @@ struct MADWFinnerIterCallbackBase {
   virtual ~MADWFinnerIterCallbackBase() {}
 };
 
-// MADWF (MADWF.h:47-209): the outer (Moebius) system solved by defect correction; each step
-// is a Pauli-Villars solve of the outer operator and a Schur solve of the cheaper inner one,
-// joined through the s = 0 slice of the P-rotated fields.  src is a 4D field (imported with
-// ImportPhysicalFermionSource) or a 5D field of the outer operator.  Throws GridError
-// (GB_ERR_NOT_CONVERGED) after maxiter steps, where Grid asserts.
+// MADWF (MADWF.h:47-209): the library's gb_madwf solves the outer (Moebius) system by
+// defect correction, each step a Pauli-Villars solve of the outer operator and a Schur
+// solve of the cheaper inner one, joined through the s = 0 slice of the P-rotated fields;
+// the solver objects, the guesser and the callback are called back from it.  src is a 4D
+// field (imported with ImportPhysicalFermionSource) or a 5D field of the outer operator.
+// Throws GridError (GB_ERR_NOT_CONVERGED) after maxiter steps, where Grid asserts; an
+// exception from a solver or the callback ends the solve and is rethrown.
 template <class Matrixo, class Matrixi, class PVinverter, class SchurSolver, class Guesser> class MADWF {
   typedef typename Matrixo::FermionField FermionFieldo;
   typedef typename Matrixi::FermionField FermionFieldi;
@@ -1267,6 +1253,42 @@ template <class Matrixo, class Matrixi, class PVinverter, class SchurSolver, cla
   RealD target_resid;
   int maxiter;
   MADWFinnerIterCallbackBase* callback;
+  std::exception_ptr error_;
+
+  template <class Body> int guarded(Body&& body) {
+    try {
+      body();
+      return GB_OK;
+    } catch (const GridError& e) {
+      if (!error_) error_ = std::current_exception();
+      return e.status != GB_OK ? e.status : GB_ERR_BAD_ARG;
+    } catch (...) {
+      if (!error_) error_ = std::current_exception();
+      return GB_ERR_BAD_ARG;
+    }
+  }
+  static int pv_call(void* user, gb_op_t, gb_field_t src, gb_field_t sol) {
+    MADWF* m = static_cast<MADWF*>(user);
+    return m->guarded([&] {
+      const FermionFieldo s = FermionFieldo::View(m->Mato.FermionGrid(), src);
+      FermionFieldo x = FermionFieldo::View(m->Mato.FermionGrid(), sol);
+      m->PauliVillarsSolvero(m->Mato, s, x);
+    });
+  }
+  static int inner_call(void* user, gb_op_t, gb_field_t src, gb_field_t sol) {
+    MADWF* m = static_cast<MADWF*>(user);
+    return m->guarded([&] {
+      const FermionFieldi s = FermionFieldi::View(m->Mati.FermionGrid(), src);
+      FermionFieldi x = FermionFieldi::View(m->Mati.FermionGrid(), sol);
+      m->SchurSolveri(m->Mati, s, x, m->Guesseri);
+    });
+  }
+  static int step_call(void* user, int, double resid) {
+    MADWF* m = static_cast<MADWF*>(user);
+    return m->guarded([&] {
+      if (m->callback) (*m->callback)(resid);
+    });
+  }
 
  public:
   int IterationsToComplete = 0;
@@ -1277,57 +1299,25 @@ template <class Matrixo, class Matrixi, class PVinverter, class SchurSolver, cla
         target_resid(resid), maxiter(_maxiter), callback(_callback) {}
 
   void operator()(const FermionFieldo& src, FermionFieldo& sol5) {
-    FermionFieldi c0i(Mati.GaugeGrid()), y0i(Mati.GaugeGrid());
-    FermionFieldo c0(Mato.GaugeGrid()), y0(Mato.GaugeGrid());
-    FermionFieldo A(Mato.FermionGrid()), B(Mato.FermionGrid()), b(Mato.FermionGrid());
-    FermionFieldo c(Mato.FermionGrid()), defect(Mato.FermionGrid());
-    FermionFieldi ci(Mati.FermionGrid()), yi(Mati.FermionGrid()), xi(Mati.FermionGrid());
-    FermionFieldi srci(Mati.FermionGrid()), Ai(Mati.FermionGrid());
-    const RealD m = Mati.Mass();
-
-    if (src.Grid() == Mato.GaugeGrid()) Mato.ImportPhysicalFermionSource(src, b);
-    else if (src.Grid() == Mato.FermionGrid()) b = src;
-    else throw GridError(GB_ERR_BAD_ARG, "MADWF: source on neither the gauge nor the fermion grid of the outer operator");
-    const RealD nb = norm2(b);
-    defect = b;
-    sol5 = Zero();
-    for (int i = 0; i < maxiter; i++) {
-      // c0: the s = 0 slice of Pdag PV^-1 defect
-      PauliVillarsSolvero(Mato, defect, A);
-      Mato.Pdag(A, c);
-      ExtractSlice(c0, c, 0, 0);
-      // the inner system with surface term c0: Dwm P y = D(1) P (c0, 0, ..., 0)^T
-      ci = Zero();
-      convert(c0, c0i);
-      InsertSlice(c0i, ci, 0, 0);
-      Mati.P(ci, Ai);
-      Mati.SetMass(1.0);
-      Mati.M(Ai, srci);
-      Mati.SetMass(m);
-      SchurSolveri(Mati, srci, xi, Guesseri);
-      Mati.Pdag(xi, yi);
-      ExtractSlice(y0i, yi, 0, 0);
-      convert(y0i, y0);
-      // the bulk of the outer solution: Pdag PV^-1 Dm P (-y0, c_1, ..., c_{Ls-1}), then the
-      // surface solution back in and P back to x
-      c0 = -y0;
-      InsertSlice(c0, c, 0, 0);
-      Mato.P(c, B);
-      Mato.M(B, A);
-      PauliVillarsSolvero(Mato, A, B);
-      Mato.Pdag(B, A);
-      InsertSlice(y0, A, 0, 0);
-      Mato.P(A, B);
-      sol5 = sol5 + B;  // sol5 += M^-1 defect
-      Mato.M(sol5, A);
-      defect = b - A;
-      const RealD resid = std::sqrt(norm2(defect) / nb);
-      IterationsToComplete = i + 1;
-      FinalResidual = resid;
-      if (callback) (*callback)(resid);
-      if (resid < target_resid) return;
+    std::unique_ptr<FermionFieldo> b;
+    gb_field_t src5 = src.handle();
+    if (src.Grid() == Mato.GaugeGrid()) {
+      b.reset(new FermionFieldo(Mato.FermionGrid()));
+      Mato.ImportPhysicalFermionSource(src, *b);
+      src5 = b->handle();
+    } else if (src.Grid() != Mato.FermionGrid()) {
+      throw GridError(GB_ERR_BAD_ARG, "MADWF: source on neither the gauge nor the fermion grid of the outer operator");
     }
-    throw GridError(GB_ERR_NOT_CONVERGED, "MADWF: exceeded maxiter");
+    error_ = nullptr;
+    int it = 0;
+    double fr = 0;
+    const int rc = gb_madwf(Mato.handle(), Mati.handle(), &MADWF::pv_call, this, &MADWF::inner_call, this, src5,
+                            sol5.handle(), target_resid, maxiter, &MADWF::step_call, this, &it, &fr);
+    IterationsToComplete = it;
+    FinalResidual = fr;
+    if (error_) std::rethrow_exception(error_);
+    if (rc == GB_ERR_NOT_CONVERGED) throw GridError(GB_ERR_NOT_CONVERGED, "MADWF: exceeded maxiter");
+    gbdetail::check(rc, "MADWF");
   }
 };
 

@@ -195,3 +195,83 @@ def test_madwf_with_computed_zmobius_gammas(gpu_available):
     b = ref.physical(o.IMPORT_PHYSICAL_SOURCE, eta)
     direct, _, _, _ = ref.schur_solve(b, 1e-11, 10000)
     assert o.rel_l2(sol.export(), direct) < 1e-8
+
+
+def _c_solver(name):
+    return g.api._SOLVER_FN((name, g.api.lib))
+
+
+def test_madwf_library_solvers_through_the_c_abi(gpu_available):
+    """gb_madwf driven with the library's own solver functions as C function pointers (no
+    host-language callback in the loop) gives the residual history of the MADWF class."""
+    Lo, Li = 8, 4
+    U, outer, ref, eta = _outer_problem(Lo)
+    inner = mobius(U, Li)
+    madwf = g.MADWF(outer, inner, g.PauliVillarsSolverRBprec(g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000))),
+                    g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000, False)), g.ZeroGuesser(), 1e-9, 20)
+    want = outer.FermionField()
+    madwf(eta, want)
+    b = outer.FermionField()
+    outer.ImportPhysicalFermionSource(eta, b)
+    pv_st, in_st = g.api.CGSolver(), g.api.CGSolver()
+    pv_st.cg = g.ConjugateGradient(1e-12, 10000).params()
+    in_st.cg = g.ConjugateGradient(1e-12, 10000, False).params()
+    seen = []
+    cb = g.api._MADWF_CB(lambda user, it, r: seen.append((it, r)) or 0)
+    sol = outer.FermionField()
+    it, fr = g.api.C.c_int(), g.api.C.c_double()
+    rc = g.api.lib.gb_madwf(outer.h, inner.h, _c_solver("gb_solver_pv_rbprec"), g.api.C.addressof(pv_st),
+                            _c_solver("gb_solver_schur"), g.api.C.addressof(in_st), b.h, sol.h, 1e-9, 20, cb, None,
+                            g.api.C.byref(it), g.api.C.byref(fr))
+    assert rc == 0
+    assert [r for _, r in seen] == madwf.residuals and it.value == madwf.iterations == len(seen)
+    assert fr.value == madwf.residuals[-1]
+    assert o.rel_l2(sol.export(), want.export()) < 1e-14
+    assert in_st.result.iterations > 0 and in_st.unprec_residual < 1e-9
+    assert outer.Mass() == MF and inner.Mass() == MF
+
+
+def test_madwf_solver_exception_propagates(gpu_available):
+    """An exception raised by a host-language solver ends the library's loop and is raised
+    again to the caller; both operators keep their masses."""
+    Lo, Li = 8, 4
+    U, outer, ref, eta = _outer_problem(Lo)
+    inner = mobius(U, Li)
+    pv = g.PauliVillarsSolverRBprec(g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000)))
+    calls = []
+
+    def failing_pv(matrix, src, sol):
+        calls.append(1)
+        if len(calls) == 3:
+            raise ValueError("planted")
+        pv(matrix, src, sol)
+
+    madwf = g.MADWF(outer, inner, failing_pv, g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000, False)),
+                    g.ZeroGuesser(), 1e-9, 20)
+    with pytest.raises(ValueError, match="planted"):
+        madwf(eta, outer.FermionField())
+    assert len(calls) == 3 and madwf.iterations == 1
+    assert outer.Mass() == MF and inner.Mass() == MF
+
+
+def test_madwf_operators_on_different_streams(gpu_available):
+    """Outer operator on its own stream, inner on the default stream: the surface slices
+    pass between the streams in order, and the result is the single-stream one."""
+    Lo, Li = 8, 4
+    U, outer, ref, eta = _outer_problem(Lo)
+    inner = mobius(U, Li)
+    st = g.Stream()
+    outer_s = g.MobiusFermion(U, DIMS, Lo, MF, MOBIUS["M5"], MOBIUS["b"], MOBIUS["c"], stream=st.ptr)
+
+    def run(o_op):
+        madwf = g.MADWF(o_op, inner, g.PauliVillarsSolverRBprec(g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000))),
+                        g.SchurRedBlackDiagMooeeSolve(g.ConjugateGradient(1e-12, 10000, False)), g.ZeroGuesser(), 1e-9, 20)
+        sol = o_op.FermionField()
+        madwf(eta, sol)
+        return madwf.residuals, sol.export()
+
+    h1, x1 = run(outer)
+    h2, x2 = run(outer_s)
+    del outer_s  # before its stream
+    assert h1 == h2
+    assert np.array_equal(x1, x2)
