@@ -91,7 +91,8 @@ static int launch_m5d_p(Op* op, const M5Params& p, const double* l, const double
 }
 
 int launch_m5d_z(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
-                 const double* upper, int dag, size_t n5, const HalfView* z, double zc) {
+                 const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts) {
+  if (norm_parts) *norm_parts = 0;
   if (op->Ls > kMaxLs) {
     set_error("M5D: Ls = %d exceeds %d", op->Ls, kMaxLs);
     return GB_ERR_UNSUPPORTED;
@@ -110,13 +111,13 @@ int launch_m5d_z(Op* op, HalfView psi, HalfView phi, HalfView chi, const double*
   p.L5 = op->L5;
   p.Ls = op->Ls;
   // FP32 / FP16 (site-pair layout, Ls even): one thread per pair of s slots
-  if (psi.prec != GB_F64) return launch_m5d_pair(op, psi, phi, chi, lower, diag, upper, dag, n5, z, zc);
+  if (psi.prec != GB_F64) return launch_m5d_pair(op, psi, phi, chi, lower, diag, upper, dag, n5, z, zc, norm_parts);
   return launch_m5d_p<double>(op, p, lower, diag, upper, dag);
 }
 
 int launch_m5d(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
                const double* upper, int dag, size_t n5) {
-  return launch_m5d_z(op, psi, phi, chi, lower, diag, upper, dag, n5, nullptr, 0.0);
+  return launch_m5d_z(op, psi, phi, chi, lower, diag, upper, dag, n5, nullptr, 0.0, nullptr);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -292,30 +292,28 @@ void coeffs_m5d_unit(const Op* op, std::vector<double>& l, std::vector<double>& 
   l[0] = op->mass;
 }
 
+// (norm_parts: |chi|^2 partial sums into op->d_partial where the kernel can, one
+// checkerboard half only; see launch_m5d_pair)
 static int m5d_field(Op* op, Field* psi, Field* phi, Field* chi, const std::vector<double>& l,
-                     const std::vector<double>& d, const std::vector<double>& u, int dag, Field* z, double zc) {
+                     const std::vector<double>& d, const std::vector<double>& u, int dag, Field* z, double zc,
+                     int* norm_parts = nullptr) {
   const int halves = chi->full() ? 2 : 1;
+  if (norm_parts) *norm_parts = 0;
   for (int h = 0; h < halves; h++) {
     HalfView zv = z ? half_view(z, h) : HalfView{nullptr, nullptr, chi->prec};
     GB_TRY(launch_m5d_z(op, half_view(psi, h), half_view(phi, h), half_view(chi, h), l.data(), d.data(), u.data(), dag,
-                        chi->n5, z ? &zv : nullptr, zc));
+                        chi->n5, z ? &zv : nullptr, zc, halves == 1 ? norm_parts : nullptr));
   }
   return GB_OK;
 }
 
 // a fused s-column program on every checkerboard half of the fields (FP32 Moebius)
-// (dot: Re<dot|out> partial sums into op->d_partial, their count into *dot_parts; one
-// checkerboard half only)
 static int col_field(Op* op, int opa, int opb, int dag, Field* x, Field* y, Field* out, double zc,
-                     const ColCoefsHost& h, Field* dot = nullptr, int* dot_parts = nullptr) {
+                     const ColCoefsHost& h) {
   const int halves = out->full() ? 2 : 1;
-  if (dot_parts) *dot_parts = 0;
   for (int k = 0; k < halves; k++) {
     const HalfView yv = y ? half_view(y, k) : HalfView{nullptr, nullptr, x->prec};
-    const bool fuse = dot && halves == 1 && dot->prec == x->prec;
-    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h,
-                      fuse ? half_view(dot, k).data : nullptr, fuse ? op->d_partial : nullptr,
-                      fuse ? dot_parts : nullptr));
+    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h));
   }
   return GB_OK;
 }
@@ -451,7 +449,8 @@ static int tm_diag(Op* op, Field* in, Field* out, int dag, int inverse, Field* z
   return GB_OK;
 }
 
-int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
+int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc, int* norm_parts) {
+  if (norm_parts) *norm_parts = 0;
   if (in->full() != out->full()) { set_error("Mooee: in and out must both be full or both half fields"); return GB_ERR_BAD_PARITY; }
   out->subset = in->subset;
   if (op->tm) return tm_diag(op, in, out, dag, 0, z, zc);
@@ -466,7 +465,7 @@ int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc) {
   }
   std::vector<double> l, d, u;
   coeffs_mooee(op, dag, l, d, u);
-  return m5d_field(op, in, in, out, l, d, u, dag, z, zc);
+  return m5d_field(op, in, in, out, l, d, u, dag, z, zc, norm_parts);
 }
 
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
@@ -486,10 +485,11 @@ int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
   return GB_OK;
 }
 
-// SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349).  With dot (MpcDag of
-// an FP32 Moebius operator) the last program also reduces Re<dot|out> (see col_field).
-int op_mpc(Op* op, Field* in, Field* out, int dag, Field* dot, int* dot_parts) {
-  if (dot_parts) *dot_parts = 0;
+// SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349).  With norm_parts (Mpc
+// of a FP32 / FP16 Moebius operator with one right-hand side) the last kernel also reduces
+// |out|^2 (see launch_m5d_pair).
+int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts) {
+  if (norm_parts) *norm_parts = 0;
   if (in->subset != GB_ODD) { set_error("Mpc: odd checkerboard expected"); return GB_ERR_BAD_PARITY; }
   Field *te1, *te2, *to;
   GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E1, &te1));
@@ -509,7 +509,7 @@ int op_mpc(Op* op, Field* in, Field* out, int dag, Field* dot, int* dot_parts) {
       GB_TRY(op_dhop_cb(op, to, te1, 0));
       GB_TRY(col_field(op, COL_INV_M5D, COLB_NONE, 0, te1, nullptr, te2, 0.0, meo));
       GB_TRY(op_dhop_cb(op, te2, to, 0));
-      return op_mooee(op, in, out, 0, to, -1.0);
+      return op_mooee(op, in, out, 0, to, -1.0, norm_parts);
     }
     GB_TRY(op_dhop_cb(op, in, te1, 1));
     GB_TRY(col_field(op, COL_M5D_INV, COLB_NONE, 1, te1, nullptr, te2, 0.0, meo));
@@ -517,19 +517,20 @@ int op_mpc(Op* op, Field* in, Field* out, int dag, Field* dot, int* dot_parts) {
     ColCoefsHost h;
     coeffs_mooee(op, 1, h.l1, h.d1, h.u1);
     h.l2 = meo.l1; h.d2 = meo.d1; h.u2 = meo.u1;
-    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h, dot, dot_parts);
+    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h);
   }
   GB_TRY(op_meooe(op, in, te1, dag));
   GB_TRY(op_mooee_inv(op, te1, te2, dag));
   GB_TRY(op_meooe(op, te2, to, dag));
-  return op_mooee(op, in, out, dag, to, -1.0);  // out = Mooee in - tmp
+  return op_mooee(op, in, out, dag, to, -1.0, dag ? nullptr : norm_parts);  // out = Mooee in - tmp
 }
 
-int op_mpcdagmpc(Op* op, Field* in, Field* out, int* dot_parts) {
+int op_mpcdagmpc(Op* op, Field* in, Field* out, int* d_parts, Field** mpc_in) {
   Field* t;
   GB_TRY(ws_get(op, GB_ODD, in->prec, WS_MPCDAGMPC, &t));
-  GB_TRY(op_mpc(op, in, t, 0));
-  return op_mpc(op, t, out, 1, dot_parts ? in : nullptr, dot_parts);
+  GB_TRY(op_mpc(op, in, t, 0, d_parts));
+  if (mpc_in) *mpc_in = t;
+  return op_mpc(op, t, out, 1);
 }
 
 // M / Mdag on full fields (WilsonFermionImplementation.h:113-127,
@@ -559,10 +560,11 @@ int op_m(Op* op, Field* in, Field* out, int dag) {
   return m5d_field(op, in, Din, out, l, d, u, 1, in, 1.0);  // out = M5Ddag(psi, Din) + psi
 }
 
-int op_mdagm(Op* op, Field* in, Field* out) {
+int op_mdagm(Op* op, Field* in, Field* out, Field** m_in) {
   Field* t;
   GB_TRY(ws_get(op, GB_FULL, in->prec, WS_MDAGM, &t));
   GB_TRY(op_m(op, in, t, 0));
+  if (m_in) *m_in = t;
   return op_m(op, t, out, 1);
 }
 

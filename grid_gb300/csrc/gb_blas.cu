@@ -117,20 +117,12 @@ struct RedShape {
   int L5, Ls, nrhs;
 };
 
-struct CGFields {
-  void* psi; float* psin;
-  const void* p; const float* pn;
-};
-
 // kind 0: |x|^2 ; kind 1: <x|y> ; kind 2: z = a x + y (a from host), |z|^2 ;
-// kind 3: r = r - a[rhs] mmp, psi += a[rhs] p (a from the device CG scalars), |r|^2;
-// TS is the storage of psi (FP32 when r, p, mmp are FP16: an FP16 solution accumulator
-// would round the small increments a*p away)
-template <class T, int KIND, class TS = T>
+// kind 3: r = r - a[rhs] mmp (a from the device CG scalars), |r|^2
+template <class T, int KIND>
 __global__ void __launch_bounds__(256) reduce_kernel(const RedShape sh, const void* x, const float* xn, const void* y,
                                                      const float* yn, void* z, float* zn, double a,
-                                                     const CGScalars* cg, const CGFields cf, size_t n5,
-                                                     double* partial) {
+                                                     const CGScalars* cg, size_t n5, double* partial) {
   using R = typename Arith<T>::type;
   constexpr int NV = KIND == 1 ? 2 : 1;
   double v[NV];
@@ -175,18 +167,6 @@ __global__ void __launch_bounds__(256) reduce_kernel(const RedShape sh, const vo
       }
       SpinorIO<T>::store(z, zn, n5, i, fy);
       v[0] += double(s);
-      if (KIND == 3) {
-        Spinor<R> fp;
-        Spinor<typename Arith<TS>::type> fs;
-        SpinorIO<T>::load(cf.p, cf.pn, n5, i, fp);
-        SpinorIO<TS>::load(cf.psi, cf.psin, n5, i, fs);
-#pragma unroll
-        for (int k = 0; k < 12; k++) {
-          fs.re[k] = fma(-ar, fp.re[k], fs.re[k]);
-          fs.im[k] = fma(-ar, fp.im[k], fs.im[k]);
-        }
-        SpinorIO<TS>::store(cf.psi, cf.psin, n5, i, fs);
-      }
     }
   }
   block_reduce_rhs<NV>(v, sh.L5, sh.Ls, sh.nrhs, partial);
@@ -209,62 +189,41 @@ int red_grid(Op* op, size_t n5, int* blocks, int* threads) {
   return GB_OK;
 }
 
-template <class T, int KIND, class TS = T>
-static int reduce_t(Op* op, HalfView x, HalfView y, HalfView z, double a, const CGFields& cf, size_t n5,
-                    double* partial) {
+template <class T, int KIND>
+static int reduce_t(Op* op, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial) {
   int g, B;
   GB_TRY(red_grid(op, n5, &g, &B));
   RedShape sh{op->L5, op->Ls, op->nrhs};
   const int NV = KIND == 1 ? 2 : 1;
   size_t smem = size_t(NV) * (op->nrhs == 1 ? 32 : B) * sizeof(double);
-  reduce_kernel<T, KIND, TS><<<g, B, smem, op->stream>>>(sh, x.data, x.norms, y.data, y.norms, z.data, z.norms, a, op->d_cg,
-                                                    cf, n5, partial);
+  reduce_kernel<T, KIND><<<g, B, smem, op->stream>>>(sh, x.data, x.norms, y.data, y.norms, z.data, z.norms, a, op->d_cg,
+                                                     n5, partial);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
-}
-
-template <int KIND>
-static int reduce_p(Op* op, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial,
-                    const CGFields& cf = CGFields{nullptr, nullptr, nullptr, nullptr}) {
-  switch (x.prec) {
-    case GB_F64: return reduce_t<double, KIND>(op, x, y, z, a, cf, n5, partial);
-    case GB_F32: return reduce_t<float, KIND>(op, x, y, z, a, cf, n5, partial);
-    case GB_F16: return reduce_t<__half, KIND>(op, x, y, z, a, cf, n5, partial);
-  }
-  return GB_ERR_BAD_ARG;
 }
 
 // FP32 / FP16 fields reduce through the pair kernels (gb_pair.cu), whose partial count
 // red_parts() reports; FP64 through reduce_kernel
 int launch_norm2_partial(Op* op, HalfView x, size_t n5, double* partial) {
-  if (x.prec != GB_F64) return launch_reduce_pair(op, 0, x, x, x, 0.0, n5, partial, nullptr, nullptr);
-  return reduce_p<0>(op, x, x, x, 0.0, n5, partial);
+  if (x.prec != GB_F64) return launch_reduce_pair(op, 0, x, x, x, 0.0, n5, partial);
+  return reduce_t<double, 0>(op, x, x, x, 0.0, n5, partial);
 }
 int launch_inner_partial(Op* op, HalfView a, HalfView b, size_t n5, double* partial) {
   if (a.prec != b.prec) { set_error("innerProduct: mixed precisions"); return GB_ERR_BAD_ARG; }
-  if (a.prec != GB_F64) return launch_reduce_pair(op, 1, a, b, a, 0.0, n5, partial, nullptr, nullptr);
-  return reduce_p<1>(op, a, b, a, 0.0, n5, partial);
+  if (a.prec != GB_F64) return launch_reduce_pair(op, 1, a, b, a, 0.0, n5, partial);
+  return reduce_t<double, 1>(op, a, b, a, 0.0, n5, partial);
 }
 // z = a x + y, |z|^2
 int launch_axpy_norm_partial(Op* op, HalfView z, double a, HalfView x, HalfView y, size_t n5, double* partial) {
   if (x.prec != y.prec || z.prec != x.prec) { set_error("axpy_norm: mixed precisions"); return GB_ERR_BAD_ARG; }
-  if (x.prec != GB_F64) return launch_reduce_pair(op, 2, x, y, z, a, n5, partial, nullptr, nullptr);
-  return reduce_p<2>(op, x, y, z, a, n5, partial);
+  if (x.prec != GB_F64) return launch_reduce_pair(op, 2, x, y, z, a, n5, partial);
+  return reduce_t<double, 2>(op, x, y, z, a, n5, partial);
 }
-int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, HalfView psi, HalfView p, size_t n5, double* partial) {
-  if (r.prec != mmp.prec || p.prec != r.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
-  if (r.prec != GB_F64) {
-    if (!(psi.prec == r.prec || (r.prec == GB_F16 && psi.prec == GB_F32))) {
-      set_error("CG update: solution precision %d with residual precision %d", psi.prec, r.prec);
-      return GB_ERR_BAD_ARG;
-    }
-    return launch_reduce_pair(op, 3, mmp, r, r, 0.0, n5, partial, &psi, &p);
-  }
-  CGFields cf{psi.data, psi.norms, p.data, p.norms};
-  if (psi.prec == r.prec) return reduce_p<3>(op, mmp, r, r, 0.0, n5, partial, cf);
-  if (r.prec == GB_F16 && psi.prec == GB_F32) return reduce_t<__half, 3, float>(op, mmp, r, r, 0.0, cf, n5, partial);
-  set_error("CG update: solution precision %d with residual precision %d", psi.prec, r.prec);
-  return GB_ERR_BAD_ARG;
+// r -= a[rhs] mmp, |r|^2: Grid's axpy_norm(r, -a, mmp, r) with the device CG scalars
+int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, size_t n5, double* partial) {
+  if (r.prec != mmp.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
+  if (r.prec != GB_F64) return launch_reduce_pair(op, 3, mmp, r, r, 0.0, n5, partial);
+  return reduce_t<double, 3>(op, mmp, r, r, 0.0, n5, partial);
 }
 
 // partial: [nparts][nrhs][nv] -> out[nrhs][nv]; one CTA per rhs, fixed summation order
@@ -346,9 +305,10 @@ __device__ double cta_sum_fixed(const double* partial, int nparts, int stride, i
 
 // launched with 256 threads: the partial sums of every right-hand side are reduced by the
 // whole CTA (a single thread walking thousands of partials would take ~100 us)
-__global__ void __launch_bounds__(256) cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs) {
+__global__ void __launch_bounds__(256) cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs,
+                                                       int nv) {
   for (int r = 0; r < nrhs; r++) {
-    const double d = cta_sum_fixed(partial, nparts, nrhs * 2, r * 2);
+    const double d = cta_sum_fixed(partial, nparts, nrhs * nv, r * nv);
     if (threadIdx.x == 0) {
       cg[r].d = d;
       cg[r].a = cg[r].done ? 0.0 : cg[r].c / d;
@@ -405,8 +365,8 @@ int launch_cg_init(Op* op, const double* d_ssq, const double* d_cp, double tol, 
   return GB_OK;
 }
 // the scalar kernels reduce the per-block partial sums themselves, in a fixed order
-int launch_cg_alpha(Op* op, const double* partial_inner, int nparts) {
-  cg_alpha_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial_inner, nparts, op->nrhs);
+int launch_cg_alpha(Op* op, const double* partial, int nparts, int nv) {
+  cg_alpha_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial, nparts, op->nrhs, nv);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -469,6 +429,43 @@ int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5) {
   if (p.prec != GB_F64) return launch_cg_p_pair(op, p, r, n5);
   RedShape sh{op->L5, op->Ls, op->nrhs};
   cg_p_kernel<double><<<nblk(n5), 256, 0, op->stream>>>(sh, p.data, p.norms, r.data, r.norms, op->d_cg, n5);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// psi += a p, then (PUPD) p = b p + r: the CG's linear combination after the residual
+// update (ConjugateGradient.h:174-183), FP64 fields
+template <bool PUPD>
+__global__ void __launch_bounds__(256) cg_xp_kernel(const RedShape sh, double2* psi, double2* p, const double2* r,
+                                                    const CGScalars* cg, size_t n5) {
+  const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n5) return;
+  const CGScalars& c = cg[int(i % sh.L5) / sh.Ls];
+  const double a = c.a, b = c.b;
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const double2 pk = p[size_t(k) * n5 + i];
+    double2 x = psi[size_t(k) * n5 + i];
+    x.x = fma(a, pk.x, x.x);
+    x.y = fma(a, pk.y, x.y);
+    psi[size_t(k) * n5 + i] = x;
+    if (PUPD) {
+      const double2 rk = r[size_t(k) * n5 + i];
+      p[size_t(k) * n5 + i] = make_double2(fma(b, pk.x, rk.x), fma(b, pk.y, rk.y));
+    }
+  }
+}
+
+int launch_cg_xp_update(Op* op, HalfView psi, HalfView p, HalfView r, size_t n5, int update_p) {
+  if (p.prec != r.prec) { set_error("CG update: mixed precisions"); return GB_ERR_BAD_ARG; }
+  if (p.prec != GB_F64) return launch_cg_xp_pair(op, psi, p, r, n5, update_p);
+  if (psi.prec != GB_F64) { set_error("CG update: FP64 fields expected"); return GB_ERR_BAD_ARG; }
+  RedShape sh{op->L5, op->Ls, op->nrhs};
+  auto* x = static_cast<double2*>(psi.data);
+  auto* pp = static_cast<double2*>(p.data);
+  auto* rr = static_cast<const double2*>(r.data);
+  if (update_p) cg_xp_kernel<true><<<nblk(n5), 256, 0, op->stream>>>(sh, x, pp, rr, op->d_cg, n5);
+  else cg_xp_kernel<false><<<nblk(n5), 256, 0, op->stream>>>(sh, x, pp, rr, op->d_cg, n5);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }

@@ -45,8 +45,6 @@ struct ColParams {
   size_t np;  // 16-byte vectors per plane (site pairs per half field)
   size_t nq;  // columns: 4D sites x right-hand sides
   float zc;
-  const float4* dotp;  // FP32: Re<dotp|out> per CTA into dotpart[CTA][2]
-  double* dotpart;
 };
 
 // stage one input into the [12][Q][ST] float4 tile: FP32 copies the vectors, FP16 decodes
@@ -290,7 +288,7 @@ __device__ __forceinline__ void col_issue(const float4* x, float4* tile, size_t 
   }
 }
 
-template <int LS, bool DAG, int OPA, int OPB, bool DOT>
+template <int LS, bool DAG, int OPA, int OPB>
 __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParams p, const ColCoef<LS> c) {
   constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>(), NIN = OPB != COLB_NONE ? 2 : 1;
   constexpr int TILE = 12 * Q * ST;   // float4 of one input tile
@@ -310,7 +308,6 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     cp_async_commit();
   };
   size_t tile = blockIdx.x;
-  double dot = 0.0;  // DOT: this thread's share of Re<dotp|out>, FP32 per tile, FP64 across tiles
   for (int k0 = 0; k0 < kColStages - 1; k0++) issue(tile + size_t(k0) * gridDim.x, k0);
   for (int st = 0; tile < ntiles; tile += gridDim.x, st = st + 1 == kColStages ? 0 : st + 1) {
     // refill the stage computed last (stored out before the last barrier), then wait for
@@ -322,38 +319,17 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     const int nv = vectors(tile);
     if (qq < nv / H) col_run<LS, DAG, OPA, OPB>(base + (k * Q + qq) * ST, base + TILE + (k * Q + qq) * ST, p.zc, c, k < 6);
     __syncthreads();
-    float dt = 0.f;
 #pragma unroll 4
     for (int e = t; e < 12 * Q * H; e += 12 * Q) {
       const int kk = e / (Q * H), r = e - kk * (Q * H);
       if (r < nv) {
         const int q2 = r / H, m = r - q2 * H;
-        const size_t gi = size_t(kk) * p.np + tile * Q * H + r;
-        const float4 v = base[(kk * Q + q2) * ST + m];
-        o[gi] = v;
-        if (DOT) {  // (re_s, re_s+1, im_s, im_s+1): Re(conj(d) v) = d.re v.re + d.im v.im
-          const float4 d = __ldg(p.dotp + gi);
-          dt = fmaf(d.x, v.x, fmaf(d.y, v.y, fmaf(d.z, v.z, fmaf(d.w, v.w, dt))));
-        }
+        o[size_t(kk) * p.np + tile * Q * H + r] = base[(kk * Q + q2) * ST + m];
       }
     }
-    if (DOT) dot += double(dt);
     __syncthreads();  // the stage is read out before it is refilled
   }
   cp_async_wait<0>();
-  if (DOT) {  // fixed-order CTA sum: warp shuffles, then the warps' sums in order
-    __shared__ double wsum[12 * kColPipeQ / 32];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, off);
-    if ((t & 31) == 0) wsum[t >> 5] = dot;
-    __syncthreads();
-    if (t == 0) {
-      double s = 0.0;
-      for (int w = 0; w < 12 * kColPipeQ / 32; w++) s += wsum[w];
-      p.dotpart[2 * size_t(blockIdx.x)] = s;
-      p.dotpart[2 * size_t(blockIdx.x) + 1] = 0.0;
-    }
-  }
 }
 
 // FP16 programs on the same ring: each stage holds a tile's raw vectors (6 planes of
@@ -460,17 +436,17 @@ template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost
 #define GB_COL_PIPE 1
 #endif
 
-template <int LS, bool DAG, int OPA, int OPB, bool DOT = false>
-static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* dot_parts = nullptr) {
+template <int LS, bool DAG, int OPA, int OPB>
+static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
   constexpr int NIN = OPB != COLB_NONE ? 2 : 1;
   const size_t smem = size_t(kColStages) * NIN * 12 * kColPipeQ * col_stride<LS>() * sizeof(float4);
   static std::atomic<int> per_sm{0};
   static std::atomic<int> sms{0};
   if (per_sm.load() == 0) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_kernel<LS, DAG, OPA, OPB, DOT>,
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_kernel<LS, DAG, OPA, OPB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int n = 0, dev = 0, count = 0;
-    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_kernel<LS, DAG, OPA, OPB, DOT>,
+    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_kernel<LS, DAG, OPA, OPB>,
                                                                 12 * kColPipeQ, smem));
     GB_CHECK_CUDA(cudaGetDevice(&dev));
     GB_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
@@ -478,12 +454,10 @@ static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* do
     per_sm.store(n > 0 ? n : 1);
   }
   const size_t ntiles = (p.nq + kColPipeQ - 1) / kColPipeQ;
-  size_t slots = size_t(per_sm.load()) * size_t(sms.load());
-  if (DOT && slots > size_t(2) * kRedBlocks) slots = size_t(2) * kRedBlocks;  // the partial buffer's CTAs
+  const size_t slots = size_t(per_sm.load()) * size_t(sms.load());
   const unsigned blocks = unsigned(ntiles < slots ? ntiles : slots);
-  col_pipe_kernel<LS, DAG, OPA, OPB, DOT><<<blocks, 12 * kColPipeQ, smem, op->stream>>>(p, c);
+  col_pipe_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * kColPipeQ, smem, op->stream>>>(p, c);
   GB_CHECK_CUDA(cudaGetLastError());
-  if (dot_parts) *dot_parts = DOT ? int(blocks) : 0;
   return GB_OK;
 }
 
@@ -535,11 +509,9 @@ static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
 
 // the programs the operators use; the others are not instantiated
 template <class T, int LS>
-static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h, int* dot_parts) {
+static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h) {
   ColCoef<LS> c;
   fill_col<LS>(op, dag, h, c);
-  if (GB_COL_PIPE && sizeof(T) == 4 && p.dotp && dag && opa == COL_M5D && opb == COLB_M5D)
-    return col_pipe_go<LS, true, COL_M5D, COLB_M5D, true>(op, p, c, dot_parts);
   const int key = (dag ? 100 : 0) + opa * 10 + opb;
   switch (key) {
     case 0 + COL_M5D * 10 + COLB_NONE: return col_go<T, LS, false, COL_M5D, COLB_NONE>(op, p, c);
@@ -565,8 +537,7 @@ bool col_available(const Op* op, int prec) {
 }
 
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
-               const ColCoefsHost& h, const void* dotp, double* dot_partial, int* dot_parts) {
-  if (dot_parts) *dot_parts = 0;
+               const ColCoefsHost& h) {
   if (!col_available(op, x.prec) || out.prec != x.prec || (opb != COLB_NONE && y.prec != x.prec)) {
     set_error("column kernel: FP32 or FP16 Moebius fields with an instantiated Ls expected");
     return GB_ERR_UNSUPPORTED;
@@ -577,14 +548,10 @@ int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfVi
   p.np = op->n5() >> 1;
   p.nq = size_t(op->half4) * op->nrhs;
   p.zc = float(zc);
-  const bool fuse = dotp && dot_partial && dot_parts && x.prec == GB_F32 && op->nrhs == 1;
-  p.dotp = fuse ? static_cast<const float4*>(dotp) : nullptr;
-  p.dotpart = fuse ? dot_partial : nullptr;
-  int* parts = fuse ? dot_parts : nullptr;
   const bool half = x.prec == GB_F16;
   switch (op->Ls) {
 #define GB_COL_LS(L) \
-  case L: return half ? col_ls<__half, L>(op, opa, opb, dag, p, h, parts) : col_ls<float, L>(op, opa, opb, dag, p, h, parts);
+  case L: return half ? col_ls<__half, L>(op, opa, opb, dag, p, h) : col_ls<float, L>(op, opa, opb, dag, p, h);
     GB_COL_LS(4) GB_COL_LS(6) GB_COL_LS(8) GB_COL_LS(10) GB_COL_LS(12) GB_COL_LS(16) GB_COL_LS(20) GB_COL_LS(24)
 #undef GB_COL_LS
   }

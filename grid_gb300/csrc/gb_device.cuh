@@ -192,6 +192,14 @@ template <> struct PairIO<float> {
 #pragma unroll
     for (int k = 0; k < 12; k++) p[size_t(k) * np] = make_float4(f.re[k].x, f.re[k].y, f.im[k].x, f.im[k].y);
   }
+  // store, and return |stored site|^2 per lane
+  static __device__ __forceinline__ float2 store_n2(void* base, float2* n, size_t np, size_t q, const Pair12& f) {
+    store(base, n, np, q, f);
+    float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 12; k++) s = __ffma2_rn(f.re[k], f.re[k], __ffma2_rn(f.im[k], f.im[k], s));
+    return s;
+  }
 };
 
 template <> struct PairIO<__half> {
@@ -274,6 +282,36 @@ template <> struct PairIO<__half> {
       p[size_t(g) * np] = v;
     }
     norms[q] = make_float2(m0, m1);
+  }
+  // store, and return |stored site|^2 per lane: the squares of the halves as a later load
+  // decodes them, times the site norm squared
+  static __device__ __forceinline__ float2 store_n2(void* base, float2* norms, size_t np, size_t q, const Pair12& f) {
+    float m0 = 0.f, m1 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      m0 = fmaxf(m0, fmaxf(fabsf(f.re[k].x), fabsf(f.im[k].x)));
+      m1 = fmaxf(m1, fmaxf(fabsf(f.re[k].y), fabsf(f.im[k].y)));
+    }
+    const float2 inv = make_float2(m0 > 0.f ? 1.0f / m0 : 0.f, m1 > 0.f ? 1.0f / m1 : 0.f);
+    uint4* p = static_cast<uint4*>(base) + q;
+    float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int g = 0; g < 6; g++) {
+      uint4 v;
+      __half2* h = reinterpret_cast<__half2*>(&v);
+      h[0] = __float22half2_rn(__fmul2_rn(f.re[2 * g], inv));
+      h[1] = __float22half2_rn(__fmul2_rn(f.im[2 * g], inv));
+      h[2] = __float22half2_rn(__fmul2_rn(f.re[2 * g + 1], inv));
+      h[3] = __float22half2_rn(__fmul2_rn(f.im[2 * g + 1], inv));
+      p[size_t(g) * np] = v;
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const float2 d = __half22float2(h[e]);
+        s = __ffma2_rn(d, d, s);
+      }
+    }
+    norms[q] = make_float2(m0, m1);
+    return make_float2(s.x * m0 * m0, s.y * m1 * m1);
   }
 };
 

@@ -189,11 +189,16 @@ int launch_reduce_final(Op* op, const double* partial, int nparts, int nv, doubl
 int red_grid(Op* op, size_t n5, int* blocks, int* threads);
 // pair-layout (FP32 / FP16) kernels, gb_pair.cu
 int red_grid_pair(Op* op, size_t np, int* blocks, int* threads);
+// norm_parts (non-null): with z, no dagger and one right-hand side the kernel also writes
+// per-CTA sums of |chi|^2 as stored into op->d_partial ([CTA][2], imaginary parts 0) and
+// their count into *norm_parts; otherwise *norm_parts = 0
 int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
-                    const double* upper, int dag, size_t n5, const HalfView* z, double zc);
-int launch_reduce_pair(Op* op, int kind, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial,
-                       HalfView* psi, HalfView* p);
+                    const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts = nullptr);
+// kind 0: |x|^2 ; 1: <x|y> ; 2: z = a x + y, |z|^2 ; 3: y -= a[rhs] x (the device CG
+// scalars), |y|^2
+int launch_reduce_pair(Op* op, int kind, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial);
 int launch_cg_p_pair(Op* op, HalfView p, HalfView r, size_t n5);
+int launch_cg_xp_pair(Op* op, HalfView psi, HalfView p, HalfView r, size_t n5, int update_p);
 int launch_axpby_pair(Op* op, HalfView z, double a, HalfView x, double b, HalfView y, size_t n5, int use_y);
 // partial sums per checkerboard half that a reduction over a field of precision prec writes
 inline int red_parts(Op* op, int prec) {
@@ -222,12 +227,8 @@ struct ZCoefsHost {
 enum { ZPROG_M5D = 0, ZPROG_INV = 2, ZPROG_DIAG = 3 };
 bool zmobius_ls_supported(int Ls);
 int launch_zcol(Op* op, int prog, int dag, HalfView x, const HalfView* y, HalfView out, double zc, const ZCoefsHost& h);
-// With dotp (FP32, the program MooeeDag - M5Ddag z of MpcDag only) the kernel also
-// writes Re<dotp|out> as per-CTA partial sums [CTA][2] into dot_partial and their count
-// into *dot_parts (0 when it could not fuse; the caller then reduces separately).
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
-               const ColCoefsHost& h, const void* dotp = nullptr, double* dot_partial = nullptr,
-               int* dot_parts = nullptr);
+               const ColCoefsHost& h);
 
 // layout conversion between canonical FP64 (device) and the device layout
 // canonical host layout (complex double or, with canon_prec = GB_F32, complex float) <->
@@ -254,9 +255,13 @@ int build_neighbours(Op* op);
 // CG kernels (gb_blas.cu)
 // init from device arrays ssq[nrhs] and cp[nrhs]
 int launch_cg_init(Op* op, const double* d_ssq, const double* d_cp, double tol, double delta);
-int launch_cg_alpha(Op* op, const double* partial_inner, int nparts);
-// r -= a mmp ; psi += a p ; partial |r|^2
-int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, HalfView psi, HalfView p, size_t n5, double* partial);
+// a = c / d per rhs, d from partial sums [nparts][nrhs][nv] (nv = 2: inner-product
+// partials, real part first; nv = 1: norm partials)
+int launch_cg_alpha(Op* op, const double* partial, int nparts, int nv);
+// r -= a mmp ; partial |r|^2
+int launch_cg_r_update(Op* op, HalfView r, HalfView mmp, size_t n5, double* partial);
+// psi += a p ; with update_p also p = b p + r
+int launch_cg_xp_update(Op* op, HalfView psi, HalfView p, HalfView r, size_t n5, int update_p);
 int launch_cg_beta(Op* op, const double* partial_norm, int nparts);
 // p = b p + r
 int launch_cg_p_update(Op* op, HalfView p, HalfView r, size_t n5);

@@ -40,21 +40,24 @@ int ensure_stage(Op* op, size_t bytes);
 int check_device_error(Op* op);
 
 int launch_m5d_z(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
-                 const double* upper, int dag, size_t n5, const HalfView* z, double zc);
+                 const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts = nullptr);
 
 int op_meooe5d(Op* op, Field* in, Field* out, int dag);
 int op_dhop_cb(Op* op, Field* in, Field* out, int dag);
 int op_dhop_full(Op* op, Field* in, Field* out, int dag);
 int op_meooe(Op* op, Field* in, Field* out, int dag);
-int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc);
+int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc, int* norm_parts = nullptr);
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag);
-int op_mpc(Op* op, Field* in, Field* out, int dag, Field* dot = nullptr, int* dot_parts = nullptr);
-// dot_parts: when non-null, the last kernel may also reduce Re<in|out> into op->d_partial
-// ([CTA][2], the layout of the inner-product partials) and sets *dot_parts to the number of
-// CTA sums written, or to 0 when it did not
-int op_mpcdagmpc(Op* op, Field* in, Field* out, int* dot_parts = nullptr);
+// norm_parts (Mpc only): when non-null, the last kernel may also reduce |out|^2 into
+// op->d_partial ([CTA][2], the layout of the inner-product partials, imaginary parts 0) and
+// sets *norm_parts to the number of CTA sums written, or to 0 when it did not
+int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts = nullptr);
+// d_parts: as norm_parts, for |Mpc in|^2 = <in|MpcDagMpc in>; mpc_in: the workspace field
+// that holds Mpc in afterwards
+int op_mpcdagmpc(Op* op, Field* in, Field* out, int* d_parts = nullptr, Field** mpc_in = nullptr);
 int op_m(Op* op, Field* in, Field* out, int dag);
-int op_mdagm(Op* op, Field* in, Field* out);
+// m_in: the workspace field that holds M in afterwards
+int op_mdagm(Op* op, Field* in, Field* out, Field** m_in = nullptr);
 int op_dminus(Op* op, Field* in, Field* out, int dag);
 // flops of one application of MdagM (kind 0) or MpcDagMpc (kind 1) in Grid's model
 double hermop_flops(const Op* op, int kind);
@@ -63,10 +66,12 @@ double hermop_flops(const Op* op, int kind);
 inline int op_hermop(Op* op, int kind, Field* in, Field* out) {
   return kind == 0 ? op_mdagm(op, in, out) : op_mpcdagmpc(op, in, out);
 }
-// the same, reducing Re<in|out> on the way where the operator's kernels allow it
-inline int op_hermop_dot(Op* op, int kind, Field* in, Field* out, int* dot_parts) {
-  *dot_parts = 0;
-  return kind == 0 ? op_mdagm(op, in, out) : op_mpcdagmpc(op, in, out, dot_parts);
+// the same for the CG, which also needs d = <in|out> = |A in|^2 (A = M, or Mpc): when the
+// last kernel of A reduced |A in|^2 on the way, *d_parts is the count of its per-CTA sums
+// in op->d_partial ([CTA][2]); otherwise *d_parts = 0 and *a_in is the field A in
+inline int op_hermop_d(Op* op, int kind, Field* in, Field* out, int* d_parts, Field** a_in) {
+  *d_parts = 0;
+  return kind == 0 ? op_mdagm(op, in, out, a_in) : op_mpcdagmpc(op, in, out, d_parts, a_in);
 }
 
 }  // namespace gb

@@ -3,9 +3,10 @@
 //
 //   m5d_pair_kernel     Grid's M5D / M5Ddag (CayleyFermion5Dcache.h:41-115), with the
 //                       optional fused "+ zc z" of SchurDiagMooeeOperator::Mpc
-//   reduce_pair_kernel  norm2 / innerProduct / axpy_norm / the fused CG update
-//                       (Lattice_reduction.h:202-372, ConjugateGradient.h:160-183)
+//   reduce_pair_kernel  norm2 / innerProduct / axpy_norm / the CG's r -= a Ap, |r|^2
+//                       (Lattice_reduction.h:202-372, ConjugateGradient.h:160-172)
 //   cg_p_pair_kernel    p = b p + r
+//   cg_xp_pair_kernel   psi += a p ; p = b p + r (ConjugateGradient.h:174-183)
 //   axpby_pair_kernel   z = a x + b y
 // Ls is even, so both lanes of a pair sit in the same right-hand side for Moebius; for
 // Wilson (Ls = 1) the two lanes are two right-hand sides, handled per lane.
@@ -36,73 +37,110 @@ struct M5PairParams {
   float zc;
   size_t np;  // pairs per half field
   int L5, Ls;
+  double* norm_part;  // NORM: per-CTA sums of |chi|^2 as stored, [CTA][2] (imaginary part 0)
 };
 
 template <class R> struct Coef5p {
   R d[kMaxLs], u[kMaxLs], l[kMaxLs];
 };
 
-template <class T, bool DAG, bool ZTERM, bool SAME>
+// NORM (one right-hand side): a grid-stride loop whose CTAs also sum |chi|^2 as stored, in
+// a fixed order (per thread in FP64, then warp shuffles, then the warps in order)
+template <class T, bool DAG, bool ZTERM, bool SAME, bool NORM>
 __global__ void __launch_bounds__(256) m5d_pair_kernel(const M5PairParams p, const Coef5p<float> c) {
-  const size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (q >= p.np) return;
-  const int hl = p.L5 >> 1, hs = p.Ls >> 1;
-  const int sp = int(q % hl);            // pair index within the 4D site
-  const int s = (2 * sp) % p.Ls;         // even
-  const int psb = sp % hs;               // pair index within the rhs block
-  const size_t qb = q - psb;             // first pair of the rhs block
-  const size_t qprev = psb == 0 ? qb + hs - 1 : q - 1;
-  const size_t qnext = psb == hs - 1 ? qb : q + 1;
-  Pair12 cur, prv, nxt, ph;
-  PairIO<T>::load(p.psi, p.psi_n, p.np, q, cur);
-  if (SAME) ph = cur; else PairIO<T>::load(p.phi, p.phi_n, p.np, q, ph);
-  // neighbour chirality halves: the upper (P+) half from s-1 (non-dag) / s+1 (dag), the
-  // lower (P-) half from the other side
-  PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qnext : qprev, 0, DAG ? nxt : prv);
-  PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qprev : qnext, 6, DAG ? prv : nxt);
-  const float2 d = make_float2(c.d[s], c.d[s + 1]);
-  const float2 cl = make_float2(c.l[s], c.l[s + 1]);  // coefficient of the s-1 neighbour
-  const float2 cu = make_float2(c.u[s], c.u[s + 1]);  // coefficient of the s+1 neighbour
-  Pair12 o;
-#pragma unroll
-  for (int k = 0; k < 12; k++) {
-    const bool upper = k < 6;
-    // s-1 neighbours: (prev lane 1, cur lane 0); s+1 neighbours: (cur lane 1, next lane 0)
-    const bool from_minus = DAG ? !upper : upper;
-    float2 nr, ni;
-    if (from_minus) {
-      nr = make_float2(prv.re[k].y, cur.re[k].x);
-      ni = make_float2(prv.im[k].y, cur.im[k].x);
-    } else {
-      nr = make_float2(cur.re[k].y, nxt.re[k].x);
-      ni = make_float2(cur.im[k].y, nxt.im[k].x);
-    }
-    const float2 cc = from_minus ? cl : cu;
-    o.re[k] = fma2s(cc, nr, __fmul2_rn(d, ph.re[k]));
-    o.im[k] = fma2s(cc, ni, __fmul2_rn(d, ph.im[k]));
-  }
-  if (ZTERM) {
-    Pair12 zz;
-    PairIO<T>::load(p.z, p.z_n, p.np, q, zz);
-    const float2 zc = make_float2(p.zc, p.zc);
+  double nacc = 0.0;
+  const size_t stride = NORM ? size_t(gridDim.x) * blockDim.x : p.np;
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < p.np; q += stride) {
+    const int hl = p.L5 >> 1, hs = p.Ls >> 1;
+    const int sp = int(q % hl);            // pair index within the 4D site
+    const int s = (2 * sp) % p.Ls;         // even
+    const int psb = sp % hs;               // pair index within the rhs block
+    const size_t qb = q - psb;             // first pair of the rhs block
+    const size_t qprev = psb == 0 ? qb + hs - 1 : q - 1;
+    const size_t qnext = psb == hs - 1 ? qb : q + 1;
+    Pair12 cur, prv, nxt, ph;
+    PairIO<T>::load(p.psi, p.psi_n, p.np, q, cur);
+    if (SAME) ph = cur; else PairIO<T>::load(p.phi, p.phi_n, p.np, q, ph);
+    // neighbour chirality halves: the upper (P+) half from s-1 (non-dag) / s+1 (dag), the
+    // lower (P-) half from the other side
+    PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qnext : qprev, 0, DAG ? nxt : prv);
+    PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qprev : qnext, 6, DAG ? prv : nxt);
+    const float2 d = make_float2(c.d[s], c.d[s + 1]);
+    const float2 cl = make_float2(c.l[s], c.l[s + 1]);  // coefficient of the s-1 neighbour
+    const float2 cu = make_float2(c.u[s], c.u[s + 1]);  // coefficient of the s+1 neighbour
+    Pair12 o;
 #pragma unroll
     for (int k = 0; k < 12; k++) {
-      o.re[k] = fma2s(zc, zz.re[k], o.re[k]);
-      o.im[k] = fma2s(zc, zz.im[k], o.im[k]);
+      const bool upper = k < 6;
+      // s-1 neighbours: (prev lane 1, cur lane 0); s+1 neighbours: (cur lane 1, next lane 0)
+      const bool from_minus = DAG ? !upper : upper;
+      float2 nr, ni;
+      if (from_minus) {
+        nr = make_float2(prv.re[k].y, cur.re[k].x);
+        ni = make_float2(prv.im[k].y, cur.im[k].x);
+      } else {
+        nr = make_float2(cur.re[k].y, nxt.re[k].x);
+        ni = make_float2(cur.im[k].y, nxt.im[k].x);
+      }
+      const float2 cc = from_minus ? cl : cu;
+      o.re[k] = fma2s(cc, nr, __fmul2_rn(d, ph.re[k]));
+      o.im[k] = fma2s(cc, ni, __fmul2_rn(d, ph.im[k]));
+    }
+    if (ZTERM) {
+      Pair12 zz;
+      PairIO<T>::load(p.z, p.z_n, p.np, q, zz);
+      const float2 zc = make_float2(p.zc, p.zc);
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        o.re[k] = fma2s(zc, zz.re[k], o.re[k]);
+        o.im[k] = fma2s(zc, zz.im[k], o.im[k]);
+      }
+    }
+    if (NORM) {
+      const float2 n2 = PairIO<T>::store_n2(p.chi, p.chi_n, p.np, q, o);
+      nacc += double(n2.x) + double(n2.y);
+    } else {
+      PairIO<T>::store(p.chi, p.chi_n, p.np, q, o);
     }
   }
-  PairIO<T>::store(p.chi, p.chi_n, p.np, q, o);
+  if (NORM) {
+    __shared__ double wsum[8];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) nacc += __shfl_down_sync(0xffffffffu, nacc, off);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = nacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < int(blockDim.x >> 5); w++) s += wsum[w];
+      p.norm_part[2 * size_t(blockIdx.x)] = s;
+      p.norm_part[2 * size_t(blockIdx.x) + 1] = 0.0;
+    }
+  }
+}
+
+// grid of the NORM variant: at most kRedBlocks CTAs (the partial buffer's size)
+static unsigned m5d_norm_blocks(size_t np) {
+  const size_t need = (np + 255) / 256;
+  return unsigned(need < size_t(kRedBlocks) ? need : size_t(kRedBlocks));
 }
 
 template <class T, bool DAG, bool Z>
-static void m5d_pair_go(Op* op, const M5PairParams& p, const Coef5p<float>& c, bool same) {
+static void m5d_pair_go(Op* op, const M5PairParams& p, const Coef5p<float>& c, bool same, bool norm) {
+  if constexpr (Z && !DAG) {  // the last kernel of Mpc: Mooee in - (the Dhop term)
+    if (norm) {
+      const unsigned blocks = m5d_norm_blocks(p.np);
+      if (same) m5d_pair_kernel<T, DAG, Z, true, true><<<blocks, 256, 0, op->stream>>>(p, c);
+      else m5d_pair_kernel<T, DAG, Z, false, true><<<blocks, 256, 0, op->stream>>>(p, c);
+      return;
+    }
+  }
   const unsigned blocks = unsigned((p.np + 255) / 256);
-  if (same) m5d_pair_kernel<T, DAG, Z, true><<<blocks, 256, 0, op->stream>>>(p, c);
-  else m5d_pair_kernel<T, DAG, Z, false><<<blocks, 256, 0, op->stream>>>(p, c);
+  if (same) m5d_pair_kernel<T, DAG, Z, true, false><<<blocks, 256, 0, op->stream>>>(p, c);
+  else m5d_pair_kernel<T, DAG, Z, false, false><<<blocks, 256, 0, op->stream>>>(p, c);
 }
 
 int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
-                    const double* upper, int dag, size_t n5, const HalfView* z, double zc) {
+                    const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts) {
   M5PairParams p;
   p.psi = psi.data; p.psi_n = reinterpret_cast<const float2*>(psi.norms);
   p.phi = phi.data; p.phi_n = reinterpret_cast<const float2*>(phi.norms);
@@ -112,16 +150,20 @@ int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const doub
   p.np = n5 >> 1;
   p.L5 = op->L5;
   p.Ls = op->Ls;
+  // |chi|^2 on the way for one right-hand side (every lane then belongs to it)
+  const bool norm = norm_parts && op->nrhs == 1 && z && !dag;
+  p.norm_part = norm ? op->d_partial : nullptr;
+  if (norm_parts) *norm_parts = norm ? int(m5d_norm_blocks(p.np)) : 0;
   Coef5p<float> c;
   for (int s = 0; s < op->Ls; s++) { c.d[s] = float(diag[s]); c.u[s] = float(upper[s]); c.l[s] = float(lower[s]); }
   const bool same = psi.data == phi.data;
   const bool zt = z != nullptr;
   if (psi.prec == GB_F32) {
-    if (dag) { if (zt) m5d_pair_go<float, true, true>(op, p, c, same); else m5d_pair_go<float, true, false>(op, p, c, same); }
-    else { if (zt) m5d_pair_go<float, false, true>(op, p, c, same); else m5d_pair_go<float, false, false>(op, p, c, same); }
+    if (dag) { if (zt) m5d_pair_go<float, true, true>(op, p, c, same, norm); else m5d_pair_go<float, true, false>(op, p, c, same, norm); }
+    else { if (zt) m5d_pair_go<float, false, true>(op, p, c, same, norm); else m5d_pair_go<float, false, false>(op, p, c, same, norm); }
   } else {
-    if (dag) { if (zt) m5d_pair_go<__half, true, true>(op, p, c, same); else m5d_pair_go<__half, true, false>(op, p, c, same); }
-    else { if (zt) m5d_pair_go<__half, false, true>(op, p, c, same); else m5d_pair_go<__half, false, false>(op, p, c, same); }
+    if (dag) { if (zt) m5d_pair_go<__half, true, true>(op, p, c, same, norm); else m5d_pair_go<__half, true, false>(op, p, c, same, norm); }
+    else { if (zt) m5d_pair_go<__half, false, true>(op, p, c, same, norm); else m5d_pair_go<__half, false, false>(op, p, c, same, norm); }
   }
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
@@ -133,11 +175,6 @@ int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const doub
 // sides.  The block sums go through shared memory as 2*blockDim "virtual threads"
 // (element order), then rows of L5 are folded and each rhs sums its Ls slots.
 // ---------------------------------------------------------------------------------------
-struct PairCG {
-  void* psi; float2* psin;
-  const void* p; const float2* pn;
-};
-
 template <int NV>
 __device__ __forceinline__ void block_reduce_pairs(const double (&v0)[NV], const double (&v1)[NV], int L5, int Ls,
                                                    int nrhs, double* out) {
@@ -187,13 +224,11 @@ __device__ __forceinline__ void block_reduce_pairs(const double (&v0)[NV], const
   }
 }
 
-// KIND 0: |x|^2 ; 1: <x|y> ; 2: z = a x + y, |z|^2 ; 3: r(=y) -= a[rhs] mmp(=x),
-// psi += a[rhs] p, |r|^2.  TS: storage of psi.
-template <class T, int KIND, class TS>
+// KIND 0: |x|^2 ; 1: <x|y> ; 2: z = a x + y, |z|^2 ; 3: r(=y) -= a[rhs] mmp(=x), |r|^2
+template <class T, int KIND>
 __global__ void __launch_bounds__(256) reduce_pair_kernel(const PairShape sh, const void* x, const float2* xn,
                                                           const void* y, const float2* yn, void* z, float2* zn,
-                                                          double a, const CGScalars* cg, const PairCG cf, size_t np,
-                                                          double* partial) {
+                                                          double a, const CGScalars* cg, size_t np, double* partial) {
   constexpr int NV = KIND == 1 ? 2 : 1;
   double v0[NV], v1[NV];
 #pragma unroll
@@ -238,18 +273,6 @@ __global__ void __launch_bounds__(256) reduce_pair_kernel(const PairShape sh, co
       PairIO<T>::store(z, zn, np, q, fy);
       v0[0] += double(s.x);
       v1[0] += double(s.y);
-      if (KIND == 3) {
-        Pair12 fp, fs;
-        PairIO<T>::load(cf.p, cf.pn, np, q, fp);
-        PairIO<TS>::load(cf.psi, cf.psin, np, q, fs);
-        const float2 na = make_float2(-ar.x, -ar.y);
-#pragma unroll
-        for (int k = 0; k < 12; k++) {
-          fs.re[k] = fma2s(na, fp.re[k], fs.re[k]);
-          fs.im[k] = fma2s(na, fp.im[k], fs.im[k]);
-        }
-        PairIO<TS>::store(cf.psi, cf.psin, np, q, fs);
-      }
     }
   }
   block_reduce_pairs<NV>(v0, v1, sh.L5, sh.Ls, sh.nrhs, partial);
@@ -273,35 +296,28 @@ int red_grid_pair(Op* op, size_t np, int* blocks, int* threads) {
   return GB_OK;
 }
 
-template <class T, int KIND, class TS = T>
-static int reduce_pair_t(Op* op, HalfView x, HalfView y, HalfView z, double a, const PairCG& cf, size_t n5,
-                         double* partial) {
+template <class T, int KIND>
+static int reduce_pair_t(Op* op, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial) {
   int g, B;
   const size_t np = n5 >> 1;
   GB_TRY(red_grid_pair(op, np, &g, &B));
   PairShape sh{op->L5, op->Ls, op->nrhs};
   const int NV = KIND == 1 ? 2 : 1;
   const size_t smem = size_t(NV) * (op->nrhs == 1 ? 32 : 2 * B) * sizeof(double);
-  reduce_pair_kernel<T, KIND, TS><<<g, B, smem, op->stream>>>(
+  reduce_pair_kernel<T, KIND><<<g, B, smem, op->stream>>>(
       sh, x.data, reinterpret_cast<const float2*>(x.norms), y.data, reinterpret_cast<const float2*>(y.norms), z.data,
-      reinterpret_cast<float2*>(z.norms), a, op->d_cg, cf, np, partial);
+      reinterpret_cast<float2*>(z.norms), a, op->d_cg, np, partial);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
 
-int launch_reduce_pair(Op* op, int kind, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial,
-                       HalfView* psi, HalfView* p) {
-  PairCG cf{psi ? psi->data : nullptr, psi ? reinterpret_cast<float2*>(psi->norms) : nullptr,
-            p ? p->data : nullptr, p ? reinterpret_cast<const float2*>(p->norms) : nullptr};
+int launch_reduce_pair(Op* op, int kind, HalfView x, HalfView y, HalfView z, double a, size_t n5, double* partial) {
   const bool h = x.prec == GB_F16;
   switch (kind) {
-    case 0: return h ? reduce_pair_t<__half, 0>(op, x, y, z, a, cf, n5, partial) : reduce_pair_t<float, 0>(op, x, y, z, a, cf, n5, partial);
-    case 1: return h ? reduce_pair_t<__half, 1>(op, x, y, z, a, cf, n5, partial) : reduce_pair_t<float, 1>(op, x, y, z, a, cf, n5, partial);
-    case 2: return h ? reduce_pair_t<__half, 2>(op, x, y, z, a, cf, n5, partial) : reduce_pair_t<float, 2>(op, x, y, z, a, cf, n5, partial);
-    case 3:
-      if (!h) return reduce_pair_t<float, 3>(op, x, y, z, a, cf, n5, partial);
-      if (psi && psi->prec == GB_F32) return reduce_pair_t<__half, 3, float>(op, x, y, z, a, cf, n5, partial);
-      return reduce_pair_t<__half, 3>(op, x, y, z, a, cf, n5, partial);
+    case 0: return h ? reduce_pair_t<__half, 0>(op, x, y, z, a, n5, partial) : reduce_pair_t<float, 0>(op, x, y, z, a, n5, partial);
+    case 1: return h ? reduce_pair_t<__half, 1>(op, x, y, z, a, n5, partial) : reduce_pair_t<float, 1>(op, x, y, z, a, n5, partial);
+    case 2: return h ? reduce_pair_t<__half, 2>(op, x, y, z, a, n5, partial) : reduce_pair_t<float, 2>(op, x, y, z, a, n5, partial);
+    case 3: return h ? reduce_pair_t<__half, 3>(op, x, y, z, a, n5, partial) : reduce_pair_t<float, 3>(op, x, y, z, a, n5, partial);
   }
   return GB_ERR_BAD_ARG;
 }
@@ -337,6 +353,66 @@ int launch_cg_p_pair(Op* op, HalfView p, HalfView r, size_t n5) {
   else
     cg_p_pair_kernel<__half><<<blocks, 256, 0, op->stream>>>(sh, p.data, reinterpret_cast<float2*>(p.norms), r.data,
                                                              reinterpret_cast<const float2*>(r.norms), op->d_cg, np);
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// psi += a[rhs] p, then (PUPD) p = b[rhs] p + r: the CG's linear combination after the
+// residual update, one pass over psi, p and r.  TS: storage of psi (FP32 for FP16 fields).
+template <class T, class TS, bool PUPD>
+__global__ void __launch_bounds__(256) cg_xp_pair_kernel(const PairShape sh, void* psi, float2* psin, void* p, float2* pn,
+                                                         const void* r, const float2* rn, const CGScalars* cg,
+                                                         size_t np) {
+  const size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= np) return;
+  const int s5 = int((2 * q) % sh.L5);
+  const CGScalars& c0 = cg[s5 / sh.Ls];
+  const CGScalars& c1 = cg[(s5 + 1) / sh.Ls];
+  const float2 a = make_float2(float(c0.a), float(c1.a));
+  Pair12 fp, fs;
+  PairIO<T>::load(p, pn, np, q, fp);
+  PairIO<TS>::load(psi, psin, np, q, fs);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    fs.re[k] = fma2s(a, fp.re[k], fs.re[k]);
+    fs.im[k] = fma2s(a, fp.im[k], fs.im[k]);
+  }
+  PairIO<TS>::store(psi, psin, np, q, fs);
+  if (PUPD) {
+    const float2 b = make_float2(float(c0.b), float(c1.b));
+    Pair12 fr;
+    PairIO<T>::load(r, rn, np, q, fr);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      fp.re[k] = fma2s(b, fp.re[k], fr.re[k]);
+      fp.im[k] = fma2s(b, fp.im[k], fr.im[k]);
+    }
+    PairIO<T>::store(p, pn, np, q, fp);
+  }
+}
+
+template <class T, class TS>
+static void cg_xp_pair_go(Op* op, HalfView psi, HalfView p, HalfView r, size_t np, bool pupd) {
+  PairShape sh{op->L5, op->Ls, op->nrhs};
+  const unsigned blocks = unsigned((np + 255) / 256);
+  auto* psin = reinterpret_cast<float2*>(psi.norms);
+  auto* pn = reinterpret_cast<float2*>(p.norms);
+  auto* rn = reinterpret_cast<const float2*>(r.norms);
+  if (pupd)
+    cg_xp_pair_kernel<T, TS, true><<<blocks, 256, 0, op->stream>>>(sh, psi.data, psin, p.data, pn, r.data, rn, op->d_cg, np);
+  else
+    cg_xp_pair_kernel<T, TS, false><<<blocks, 256, 0, op->stream>>>(sh, psi.data, psin, p.data, pn, r.data, rn, op->d_cg, np);
+}
+
+int launch_cg_xp_pair(Op* op, HalfView psi, HalfView p, HalfView r, size_t n5, int update_p) {
+  const size_t np = n5 >> 1;
+  if (p.prec == GB_F32 && psi.prec == GB_F32) cg_xp_pair_go<float, float>(op, psi, p, r, np, update_p != 0);
+  else if (p.prec == GB_F16 && psi.prec == GB_F32) cg_xp_pair_go<__half, float>(op, psi, p, r, np, update_p != 0);
+  else if (p.prec == GB_F16 && psi.prec == GB_F16) cg_xp_pair_go<__half, __half>(op, psi, p, r, np, update_p != 0);
+  else {
+    set_error("CG update: solution precision %d with search-direction precision %d", psi.prec, p.prec);
+    return GB_ERR_BAD_ARG;
+  }
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }

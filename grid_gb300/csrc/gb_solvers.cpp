@@ -4,6 +4,9 @@
 // Iteration (Grid/algorithms/iterative/ConjugateGradient.h:151-200), per right-hand side:
 //   c = cp ; mmp = A p ; d = <p|mmp> ; a = c/d ; r -= a mmp ; cp = |r|^2 ; b = cp/c ;
 //   psi += a p ; p = b p + r ; stop when cp <= tol^2 |src|^2
+// with A = Mdag M or MpcDag Mpc, d = <p|A p> is reduced as |M p|^2 (|Mpc p|^2): the same
+// number, from the intermediate field, by the kernel that writes it where it can.  As in
+// Grid, psi and p are updated in one pass after the residual.
 // All scalars live on the device (one set per right-hand side); the host only polls the
 // "all converged" flag every check_every iterations, so an iteration issues no host
 // synchronisation.  A right-hand side that converges freezes (a = b = 0) while the
@@ -37,21 +40,27 @@ Parts parts_of(Op* op, const Field* f) {
   return Parts{red_parts(op, f->prec), f->full() ? 2 : 1};
 }
 
-// d = <p|mmp> -> a
-int cg_alpha(Op* op, Field* p, Field* mmp) {
-  Parts P = parts_of(op, p);
+// d = |ap|^2 (ap = M p or Mpc p) -> a
+int cg_alpha_norm(Op* op, Field* ap) {
+  Parts P = parts_of(op, ap);
   for (int h = 0; h < P.halves; h++)
-    GB_TRY(launch_inner_partial(op, half_view(p, h), half_view(mmp, h), p->n5,
-                                op->d_partial + size_t(h) * P.g * op->nrhs * 2));
-  return launch_cg_alpha(op, op->d_partial, P.g * P.halves);
+    GB_TRY(launch_norm2_partial(op, half_view(ap, h), ap->n5, op->d_partial + size_t(h) * P.g * op->nrhs));
+  return launch_cg_alpha(op, op->d_partial, P.g * P.halves, 1);
 }
-// r -= a mmp ; psi += a p ; cp = |r|^2 -> b
-int cg_update(Op* op, Field* r, Field* mmp, Field* psi, Field* p) {
+// r -= a mmp ; cp = |r|^2 -> b
+int cg_r_update(Op* op, Field* r, Field* mmp) {
   Parts P = parts_of(op, r);
   for (int h = 0; h < P.halves; h++)
-    GB_TRY(launch_cg_r_update(op, half_view(r, h), half_view(mmp, h), half_view(psi, h), half_view(p, h), r->n5,
+    GB_TRY(launch_cg_r_update(op, half_view(r, h), half_view(mmp, h), r->n5,
                               op->d_partial + size_t(h) * P.g * op->nrhs));
   return launch_cg_beta(op, op->d_partial, P.g * P.halves);
+}
+// psi += a p ; with update_p also p = b p + r
+int cg_xp_update(Op* op, Field* psi, Field* p, Field* r, int update_p) {
+  const int halves = p->full() ? 2 : 1;
+  for (int h = 0; h < halves; h++)
+    GB_TRY(launch_cg_xp_update(op, half_view(psi, h), half_view(p, h), half_view(r, h), p->n5, update_p));
+  return GB_OK;
 }
 int cg_p_update(Op* op, Field* p, Field* r) {
   const int halves = p->full() ? 2 : 1;
@@ -100,8 +109,11 @@ int field_for(Op* op, int kind, int subset_half, int prec, int slot_half, int sl
   return ws_get(op, subset_half, prec, slot_half, out);
 }
 
-// m CG iterations on op's stream, every one identical (the p update of the first one is
-// p = 0*p + r = r), so a chunk of `chunk` iterations can be captured once as a CUDA graph
+// m CG iterations on op's stream.  A chunk starts with p = b p + r (p = r at the start of a
+// solve, where b = 0; after a reliable update with the new r and b, as Grid's
+// ConjugateGradientReliableUpdate does), its iterations update psi and p in one pass, and
+// its last one updates psi only, so the host can replace r between chunks.  Every chunk of
+// `chunk` iterations is the same launch sequence, so it is captured once as a CUDA graph
 // and replayed: the first chunk runs as direct launches (it allocates the workspace), the
 // following full chunks replay the graph.
 struct ChunkRunner {
@@ -156,14 +168,16 @@ struct ChunkRunner {
     return GB_OK;
   }
   int launch(int m) {
+    GB_TRY(cg_p_update(op, p, r));
     for (int j = 0; j < m; j++) {
-      GB_TRY(cg_p_update(op, p, r));
-      // d = <p|mmp>: reduced by the HermOp's last kernel where it can, else by a pass of its own
+      // d = |A p|^2: reduced by the kernel that writes A p where it can, else by a pass of its own
       int parts = 0;
-      GB_TRY(op_hermop_dot(op, kind, p, mmp, &parts));
-      if (parts > 0) GB_TRY(launch_cg_alpha(op, op->d_partial, parts));
-      else GB_TRY(cg_alpha(op, p, mmp));
-      GB_TRY(cg_update(op, r, mmp, psi, p));
+      Field* ap = nullptr;
+      GB_TRY(op_hermop_d(op, kind, p, mmp, &parts, &ap));
+      if (parts > 0) GB_TRY(launch_cg_alpha(op, op->d_partial, parts, 2));
+      else GB_TRY(cg_alpha_norm(op, ap));
+      GB_TRY(cg_r_update(op, r, mmp));
+      GB_TRY(cg_xp_update(op, psi, p, r, j + 1 < m));
     }
     return GB_OK;
   }
