@@ -308,12 +308,18 @@ static int m5d_field(Op* op, Field* psi, Field* phi, Field* chi, const std::vect
 }
 
 // a fused s-column program on every checkerboard half of the fields (FP32 Moebius)
+// (r_upd: the CG's residual update in place of storing out where the kernel can, one
+// checkerboard half only; see launch_col)
 static int col_field(Op* op, int opa, int opb, int dag, Field* x, Field* y, Field* out, double zc,
-                     const ColCoefsHost& h) {
+                     const ColCoefsHost& h, Field* r_upd = nullptr, int* r_parts = nullptr) {
   const int halves = out->full() ? 2 : 1;
+  if (r_parts) *r_parts = 0;
   for (int k = 0; k < halves; k++) {
     const HalfView yv = y ? half_view(y, k) : HalfView{nullptr, nullptr, x->prec};
-    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h));
+    HalfView rv = r_upd ? half_view(r_upd, k) : HalfView{};
+    const bool fuse = r_upd && halves == 1;
+    GB_TRY(launch_col(op, opa, opb, dag, half_view(x, k), yv, half_view(out, k), zc, h, fuse ? &rv : nullptr,
+                      fuse ? r_parts : nullptr));
   }
   return GB_OK;
 }
@@ -487,9 +493,12 @@ int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
 
 // SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349).  With norm_parts (Mpc
 // of a FP32 / FP16 Moebius operator with one right-hand side) the last kernel also reduces
-// |out|^2 (see launch_m5d_pair).
-int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts) {
+// |out|^2 (see launch_m5d_pair).  With r_upd (MpcDag of a FP32 Moebius operator with one
+// right-hand side) the last kernel applies r -= a out for the CG instead of storing out
+// (see launch_col).
+int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts, Field* r_upd, int* r_parts) {
   if (norm_parts) *norm_parts = 0;
+  if (r_parts) *r_parts = 0;
   if (in->subset != GB_ODD) { set_error("Mpc: odd checkerboard expected"); return GB_ERR_BAD_PARITY; }
   Field *te1, *te2, *to;
   GB_TRY(ws_get(op, GB_EVEN, in->prec, WS_MPC_E1, &te1));
@@ -517,7 +526,7 @@ int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts) {
     ColCoefsHost h;
     coeffs_mooee(op, 1, h.l1, h.d1, h.u1);
     h.l2 = meo.l1; h.d2 = meo.d1; h.u2 = meo.u1;
-    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h);
+    return col_field(op, COL_M5D, COLB_M5D, 1, in, to, out, -1.0, h, r_upd, r_parts);
   }
   GB_TRY(op_meooe(op, in, te1, dag));
   GB_TRY(op_mooee_inv(op, te1, te2, dag));
@@ -525,11 +534,10 @@ int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts) {
   return op_mooee(op, in, out, dag, to, -1.0, dag ? nullptr : norm_parts);  // out = Mooee in - tmp
 }
 
-int op_mpcdagmpc(Op* op, Field* in, Field* out, int* d_parts, Field** mpc_in) {
+int op_mpcdagmpc(Op* op, Field* in, Field* out) {
   Field* t;
   GB_TRY(ws_get(op, GB_ODD, in->prec, WS_MPCDAGMPC, &t));
-  GB_TRY(op_mpc(op, in, t, 0, d_parts));
-  if (mpc_in) *mpc_in = t;
+  GB_TRY(op_mpc(op, in, t, 0));
   return op_mpc(op, t, out, 1);
 }
 

@@ -45,6 +45,12 @@ struct ColParams {
   size_t np;  // 16-byte vectors per plane (site pairs per half field)
   size_t nq;  // columns: 4D sites x right-hand sides
   float zc;
+  // RUPD (the last program of MpcDag in the CG, one right-hand side): instead of storing
+  // out, r -= a out with the CG's a, and per-CTA sums of |r|^2 into rpart[CTA] (the layout
+  // of the norm partials)
+  float4* r;
+  double* rpart;
+  const CGScalars* cg;
 };
 
 // stage one input into the [12][Q][ST] float4 tile: FP32 copies the vectors, FP16 decodes
@@ -288,7 +294,7 @@ __device__ __forceinline__ void col_issue(const float4* x, float4* tile, size_t 
   }
 }
 
-template <int LS, bool DAG, int OPA, int OPB>
+template <int LS, bool DAG, int OPA, int OPB, bool RUPD>
 __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParams p, const ColCoef<LS> c) {
   constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>(), NIN = OPB != COLB_NONE ? 2 : 1;
   constexpr int TILE = 12 * Q * ST;   // float4 of one input tile
@@ -308,28 +314,71 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     cp_async_commit();
   };
   size_t tile = blockIdx.x;
+  double rn = 0.0;  // RUPD: this thread's share of |r|^2, FP32 per tile, FP64 across tiles
+  float ma = 0.f;   // RUPD: -a
+  if (RUPD) ma = -float(p.cg[0].a);
   for (int k0 = 0; k0 < kColStages - 1; k0++) issue(tile + size_t(k0) * gridDim.x, k0);
   for (int st = 0; tile < ntiles; tile += gridDim.x, st = st + 1 == kColStages ? 0 : st + 1) {
     // refill the stage computed last (stored out before the last barrier), then wait for
     // this stage's group: all but the newest kColStages - 1 groups have landed
     issue(tile + size_t(kColStages - 1) * gridDim.x, st == 0 ? kColStages - 1 : st - 1);
+    const int nv = vectors(tile);
+    // RUPD: this thread's H vectors of r (the ones its store loop updates) are loaded
+    // before the wait, so they arrive while the tile lands and its columns compute
+    float4 rv[RUPD ? H : 1];
+    if (RUPD) {
+#pragma unroll
+      for (int j = 0; j < H; j++) {
+        const int e = t + j * 12 * Q, kk = e / (Q * H), r = e - kk * (Q * H);
+        if (r < nv) rv[j] = p.r[size_t(kk) * p.np + tile * Q * H + r];
+      }
+    }
     cp_async_wait<kColStages - 1>();
     __syncthreads();
     float4* base = col_ring + size_t(st) * NIN * TILE;
-    const int nv = vectors(tile);
     if (qq < nv / H) col_run<LS, DAG, OPA, OPB>(base + (k * Q + qq) * ST, base + TILE + (k * Q + qq) * ST, p.zc, c, k < 6);
     __syncthreads();
+    if (RUPD) {
+      float tn = 0.f;
+#pragma unroll
+      for (int j = 0; j < H; j++) {
+        const int e = t + j * 12 * Q, kk = e / (Q * H), r = e - kk * (Q * H);
+        if (r < nv) {
+          const int q2 = r / H, m = r - q2 * H;
+          const float4 v = base[(kk * Q + q2) * ST + m];
+          float4 w = rv[j];
+          w.x = fmaf(ma, v.x, w.x); w.y = fmaf(ma, v.y, w.y);
+          w.z = fmaf(ma, v.z, w.z); w.w = fmaf(ma, v.w, w.w);
+          p.r[size_t(kk) * p.np + tile * Q * H + r] = w;
+          tn = fmaf(w.x, w.x, fmaf(w.y, w.y, fmaf(w.z, w.z, fmaf(w.w, w.w, tn))));
+        }
+      }
+      rn += double(tn);
+    } else {
 #pragma unroll 4
-    for (int e = t; e < 12 * Q * H; e += 12 * Q) {
-      const int kk = e / (Q * H), r = e - kk * (Q * H);
-      if (r < nv) {
-        const int q2 = r / H, m = r - q2 * H;
-        o[size_t(kk) * p.np + tile * Q * H + r] = base[(kk * Q + q2) * ST + m];
+      for (int e = t; e < 12 * Q * H; e += 12 * Q) {
+        const int kk = e / (Q * H), r = e - kk * (Q * H);
+        if (r < nv) {
+          const int q2 = r / H, m = r - q2 * H;
+          o[size_t(kk) * p.np + tile * Q * H + r] = base[(kk * Q + q2) * ST + m];
+        }
       }
     }
     __syncthreads();  // the stage is read out before it is refilled
   }
   cp_async_wait<0>();
+  if (RUPD) {  // fixed-order CTA sum: warp shuffles, then the warps' sums in order
+    __shared__ double wsum[12 * kColPipeQ / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) rn += __shfl_down_sync(0xffffffffu, rn, off);
+    if ((t & 31) == 0) wsum[t >> 5] = rn;
+    __syncthreads();
+    if (t == 0) {
+      double s = 0.0;
+      for (int w = 0; w < 12 * kColPipeQ / 32; w++) s += wsum[w];
+      p.rpart[blockIdx.x] = s;
+    }
+  }
 }
 
 // FP16 programs on the same ring: each stage holds a tile's raw vectors (6 planes of
@@ -436,17 +485,17 @@ template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost
 #define GB_COL_PIPE 1
 #endif
 
-template <int LS, bool DAG, int OPA, int OPB>
-static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
+template <int LS, bool DAG, int OPA, int OPB, bool RUPD = false>
+static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* r_parts = nullptr) {
   constexpr int NIN = OPB != COLB_NONE ? 2 : 1;
   const size_t smem = size_t(kColStages) * NIN * 12 * kColPipeQ * col_stride<LS>() * sizeof(float4);
   static std::atomic<int> per_sm{0};
   static std::atomic<int> sms{0};
   if (per_sm.load() == 0) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_kernel<LS, DAG, OPA, OPB>,
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_kernel<LS, DAG, OPA, OPB, RUPD>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int n = 0, dev = 0, count = 0;
-    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_kernel<LS, DAG, OPA, OPB>,
+    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_kernel<LS, DAG, OPA, OPB, RUPD>,
                                                                 12 * kColPipeQ, smem));
     GB_CHECK_CUDA(cudaGetDevice(&dev));
     GB_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
@@ -454,10 +503,12 @@ static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
     per_sm.store(n > 0 ? n : 1);
   }
   const size_t ntiles = (p.nq + kColPipeQ - 1) / kColPipeQ;
-  const size_t slots = size_t(per_sm.load()) * size_t(sms.load());
+  size_t slots = size_t(per_sm.load()) * size_t(sms.load());
+  if (RUPD && slots > size_t(2) * kRedBlocks) slots = size_t(2) * kRedBlocks;  // the partial buffer's CTAs
   const unsigned blocks = unsigned(ntiles < slots ? ntiles : slots);
-  col_pipe_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * kColPipeQ, smem, op->stream>>>(p, c);
+  col_pipe_kernel<LS, DAG, OPA, OPB, RUPD><<<blocks, 12 * kColPipeQ, smem, op->stream>>>(p, c);
   GB_CHECK_CUDA(cudaGetLastError());
+  if (r_parts) *r_parts = RUPD ? int(blocks) : 0;
   return GB_OK;
 }
 
@@ -509,9 +560,11 @@ static int col_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
 
 // the programs the operators use; the others are not instantiated
 template <class T, int LS>
-static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h) {
+static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h, int* r_parts) {
   ColCoef<LS> c;
   fill_col<LS>(op, dag, h, c);
+  if (GB_COL_PIPE && sizeof(T) == 4 && p.r && dag && opa == COL_M5D && opb == COLB_M5D)
+    return col_pipe_go<LS, true, COL_M5D, COLB_M5D, true>(op, p, c, r_parts);
   const int key = (dag ? 100 : 0) + opa * 10 + opb;
   switch (key) {
     case 0 + COL_M5D * 10 + COLB_NONE: return col_go<T, LS, false, COL_M5D, COLB_NONE>(op, p, c);
@@ -537,7 +590,8 @@ bool col_available(const Op* op, int prec) {
 }
 
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
-               const ColCoefsHost& h) {
+               const ColCoefsHost& h, HalfView* r_upd, int* r_parts) {
+  if (r_parts) *r_parts = 0;
   if (!col_available(op, x.prec) || out.prec != x.prec || (opb != COLB_NONE && y.prec != x.prec)) {
     set_error("column kernel: FP32 or FP16 Moebius fields with an instantiated Ls expected");
     return GB_ERR_UNSUPPORTED;
@@ -548,10 +602,16 @@ int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfVi
   p.np = op->n5() >> 1;
   p.nq = size_t(op->half4) * op->nrhs;
   p.zc = float(zc);
+  const bool rupd = r_upd && r_parts && x.prec == GB_F32 && r_upd->prec == GB_F32 && op->nrhs == 1 && dag &&
+                    opa == COL_M5D && opb == COLB_M5D;
+  p.r = rupd ? static_cast<float4*>(r_upd->data) : nullptr;
+  p.rpart = rupd ? op->d_partial : nullptr;
+  p.cg = op->d_cg;
+  int* parts = rupd ? r_parts : nullptr;
   const bool half = x.prec == GB_F16;
   switch (op->Ls) {
 #define GB_COL_LS(L) \
-  case L: return half ? col_ls<__half, L>(op, opa, opb, dag, p, h) : col_ls<float, L>(op, opa, opb, dag, p, h);
+  case L: return half ? col_ls<__half, L>(op, opa, opb, dag, p, h, parts) : col_ls<float, L>(op, opa, opb, dag, p, h, parts);
     GB_COL_LS(4) GB_COL_LS(6) GB_COL_LS(8) GB_COL_LS(10) GB_COL_LS(12) GB_COL_LS(16) GB_COL_LS(20) GB_COL_LS(24)
 #undef GB_COL_LS
   }

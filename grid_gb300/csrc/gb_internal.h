@@ -227,8 +227,12 @@ struct ZCoefsHost {
 enum { ZPROG_M5D = 0, ZPROG_INV = 2, ZPROG_DIAG = 3 };
 bool zmobius_ls_supported(int Ls);
 int launch_zcol(Op* op, int prog, int dag, HalfView x, const HalfView* y, HalfView out, double zc, const ZCoefsHost& h);
+// With r_upd (FP32, one right-hand side, the program MooeeDag - M5Ddag z that ends MpcDag)
+// the kernel does not store out: it applies the CG's residual update r -= a out (a from
+// op->d_cg) and writes per-CTA sums of |r|^2 [CTA] into op->d_partial, their count into
+// *r_parts (0 when it could not fuse; out is then stored and the caller updates r).
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
-               const ColCoefsHost& h);
+               const ColCoefsHost& h, HalfView* r_upd = nullptr, int* r_parts = nullptr);
 
 // layout conversion between canonical FP64 (device) and the device layout
 // canonical host layout (complex double or, with canon_prec = GB_F32, complex float) <->

@@ -50,11 +50,14 @@ int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc, int* n
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag);
 // norm_parts (Mpc only): when non-null, the last kernel may also reduce |out|^2 into
 // op->d_partial ([CTA][2], the layout of the inner-product partials, imaginary parts 0) and
-// sets *norm_parts to the number of CTA sums written, or to 0 when it did not
-int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts = nullptr);
-// d_parts: as norm_parts, for |Mpc in|^2 = <in|MpcDagMpc in>; mpc_in: the workspace field
-// that holds Mpc in afterwards
-int op_mpcdagmpc(Op* op, Field* in, Field* out, int* d_parts = nullptr, Field** mpc_in = nullptr);
+// sets *norm_parts to the number of CTA sums written, or to 0 when it did not.
+// r_upd, r_parts (MpcDag only, for the CG): when both are non-null, the last kernel may
+// instead of storing out apply r_upd -= a out (a: the CG scalars of op) and reduce
+// |r_upd|^2 into op->d_partial ([CTA]); *r_parts is the number of CTA sums written, or
+// 0 when it stored out and left r_upd alone
+int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts = nullptr, Field* r_upd = nullptr,
+           int* r_parts = nullptr);
+int op_mpcdagmpc(Op* op, Field* in, Field* out);
 int op_m(Op* op, Field* in, Field* out, int dag);
 // m_in: the workspace field that holds M in afterwards
 int op_mdagm(Op* op, Field* in, Field* out, Field** m_in = nullptr);
@@ -66,12 +69,6 @@ double hermop_flops(const Op* op, int kind);
 inline int op_hermop(Op* op, int kind, Field* in, Field* out) {
   return kind == 0 ? op_mdagm(op, in, out) : op_mpcdagmpc(op, in, out);
 }
-// the same for the CG, which also needs d = <in|out> = |A in|^2 (A = M, or Mpc): when the
-// last kernel of A reduced |A in|^2 on the way, *d_parts is the count of its per-CTA sums
-// in op->d_partial ([CTA][2]); otherwise *d_parts = 0 and *a_in is the field A in
-inline int op_hermop_d(Op* op, int kind, Field* in, Field* out, int* d_parts, Field** a_in) {
-  *d_parts = 0;
-  return kind == 0 ? op_mdagm(op, in, out, a_in) : op_mpcdagmpc(op, in, out, d_parts, a_in);
-}
+
 
 }  // namespace gb

@@ -55,6 +55,28 @@ int cg_r_update(Op* op, Field* r, Field* mmp) {
                               op->d_partial + size_t(h) * P.g * op->nrhs));
   return launch_cg_beta(op, op->d_partial, P.g * P.halves);
 }
+// One CG matrix step on p: A = MdagM (kind 0) or MpcDagMpc (kind 1) with d = |M p|^2
+// (|Mpc p|^2) -> a, then r -= a A p, cp = |r|^2 -> b.  For a one-right-hand-side FP32
+// Moebius Schur operator the norm comes from the kernel that stores Mpc p, and MpcDag's
+// last kernel updates r in place of storing A p (mmp is then not written).
+int cg_matrix_step(Op* op, int kind, Field* p, Field* mmp, Field* r) {
+  int rparts = 0;
+  if (kind == 0) {
+    Field* mp = nullptr;
+    GB_TRY(op_mdagm(op, p, mmp, &mp));
+    GB_TRY(cg_alpha_norm(op, mp));
+  } else {
+    Field* z;
+    GB_TRY(ws_get(op, GB_ODD, p->prec, WS_MPCDAGMPC, &z));
+    int dparts = 0;
+    GB_TRY(op_mpc(op, p, z, 0, &dparts));
+    if (dparts > 0) GB_TRY(launch_cg_alpha(op, op->d_partial, dparts, 2));
+    else GB_TRY(cg_alpha_norm(op, z));
+    GB_TRY(op_mpc(op, z, mmp, 1, nullptr, r, &rparts));
+  }
+  if (rparts > 0) return launch_cg_beta(op, op->d_partial, rparts);
+  return cg_r_update(op, r, mmp);
+}
 // psi += a p ; with update_p also p = b p + r
 int cg_xp_update(Op* op, Field* psi, Field* p, Field* r, int update_p) {
   const int halves = p->full() ? 2 : 1;
@@ -170,13 +192,7 @@ struct ChunkRunner {
   int launch(int m) {
     GB_TRY(cg_p_update(op, p, r));
     for (int j = 0; j < m; j++) {
-      // d = |A p|^2: reduced by the kernel that writes A p where it can, else by a pass of its own
-      int parts = 0;
-      Field* ap = nullptr;
-      GB_TRY(op_hermop_d(op, kind, p, mmp, &parts, &ap));
-      if (parts > 0) GB_TRY(launch_cg_alpha(op, op->d_partial, parts, 2));
-      else GB_TRY(cg_alpha_norm(op, ap));
-      GB_TRY(cg_r_update(op, r, mmp));
+      GB_TRY(cg_matrix_step(op, kind, p, mmp, r));
       GB_TRY(cg_xp_update(op, psi, p, r, j + 1 < m));
     }
     return GB_OK;
