@@ -682,6 +682,7 @@ DHOP_PROFILE_CASES = {
     "dwf_fp16": ("mobius", (32, 32, 32, 32), 12, 1, "F16"),
     "dwf_fp64": ("mobius", (16, 16, 16, 16), 16, 2, "F64"),
     "dwf_fp32": ("mobius", (16, 16, 16, 16), 16, 1, "F32"),
+    "dwf24_ls12_fp32": ("mobius", (24, 24, 24, 24), 12, 1, "F32"),
 }
 
 
