@@ -177,8 +177,8 @@ int red_grid(Op* op, size_t n5, int* blocks, int* threads) {
   int m = 1;
   while (L5 * m * 2 <= 256) m *= 2;
   int B = op->nrhs == 1 ? 256 : L5 * m;
-  if (B > 1024) {
-    set_error("reduction: L5 = %d too large", L5);
+  if (B > 256) {  // the kernel's launch bound: blockDim is a multiple of L5
+    set_error("reduction: FP64 fields with L5 = %d above 256 are not supported", L5);
     return GB_ERR_UNSUPPORTED;
   }
   size_t need = (n5 + B - 1) / B;

@@ -45,12 +45,13 @@ struct ColParams {
   size_t np;  // 16-byte vectors per plane (site pairs per half field)
   size_t nq;  // columns: 4D sites x right-hand sides
   float zc;
-  // RUPD (the last program of MpcDag in the CG, one right-hand side): instead of storing
-  // out, r -= a out with the CG's a, and per-CTA sums of |r|^2 into rpart[CTA] (the layout
-  // of the norm partials)
+  // RUPD (the last program of MpcDag in the CG): instead of storing out, r -= a out with
+  // each right-hand side's CG scalar a, and per-CTA sums of |r|^2 per right-hand side into
+  // rpart[CTA][nrhs] (the layout of the norm partials); nrhs divides the tile's columns
   float4* r;
   double* rpart;
   const CGScalars* cg;
+  int nrhs;
 };
 
 // stage one input into the [12][Q][ST] float4 tile: FP32 copies the vectors, FP16 decodes
@@ -314,9 +315,13 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     cp_async_commit();
   };
   size_t tile = blockIdx.x;
-  double rn = 0.0;  // RUPD: this thread's share of |r|^2, FP32 per tile, FP64 across tiles
-  float ma = 0.f;   // RUPD: -a
-  if (RUPD) ma = -float(p.cg[0].a);
+  // RUPD: -a per right-hand side; |r|^2 of each element of the tile, then per column (one
+  // (4D site, rhs) each; tiles start at a multiple of nrhs columns, so column q2 of every
+  // tile belongs to right-hand side q2 % nrhs), FP32 per tile and FP64 across tiles
+  __shared__ float sma[kColPipeQ];
+  __shared__ float cn[RUPD ? 12 * Q * H : 1];
+  double colacc = 0.0;  // thread t < Q: |r|^2 of column t of this CTA's tiles
+  if (RUPD && t < p.nrhs) sma[t] = -float(p.cg[t].a);  // read after the loop's first barrier
   for (int k0 = 0; k0 < kColStages - 1; k0++) issue(tile + size_t(k0) * gridDim.x, k0);
   for (int st = 0; tile < ntiles; tile += gridDim.x, st = st + 1 == kColStages ? 0 : st + 1) {
     // refill the stage computed last (stored out before the last barrier), then wait for
@@ -339,21 +344,28 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     if (qq < nv / H) col_run<LS, DAG, OPA, OPB>(base + (k * Q + qq) * ST, base + TILE + (k * Q + qq) * ST, p.zc, c, k < 6);
     __syncthreads();
     if (RUPD) {
-      float tn = 0.f;
 #pragma unroll
       for (int j = 0; j < H; j++) {
         const int e = t + j * 12 * Q, kk = e / (Q * H), r = e - kk * (Q * H);
         if (r < nv) {
           const int q2 = r / H, m = r - q2 * H;
           const float4 v = base[(kk * Q + q2) * ST + m];
+          const float ma = sma[q2 % p.nrhs];
           float4 w = rv[j];
           w.x = fmaf(ma, v.x, w.x); w.y = fmaf(ma, v.y, w.y);
           w.z = fmaf(ma, v.z, w.z); w.w = fmaf(ma, v.w, w.w);
           p.r[size_t(kk) * p.np + tile * Q * H + r] = w;
-          tn = fmaf(w.x, w.x, fmaf(w.y, w.y, fmaf(w.z, w.z, fmaf(w.w, w.w, tn))));
+          cn[(kk * Q + q2) * H + m] = fmaf(w.x, w.x, fmaf(w.y, w.y, fmaf(w.z, w.z, w.w * w.w)));
         }
       }
-      rn += double(tn);
+      __syncthreads();
+      if (t < nv / H) {
+        float s = 0.f;
+        for (int kk = 0; kk < 12; kk++)
+#pragma unroll
+          for (int m = 0; m < H; m++) s += cn[(kk * Q + t) * H + m];
+        colacc += double(s);
+      }
     } else {
 #pragma unroll 4
       for (int e = t; e < 12 * Q * H; e += 12 * Q) {
@@ -367,16 +379,14 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
     __syncthreads();  // the stage is read out before it is refilled
   }
   cp_async_wait<0>();
-  if (RUPD) {  // fixed-order CTA sum: warp shuffles, then the warps' sums in order
-    __shared__ double wsum[12 * kColPipeQ / 32];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) rn += __shfl_down_sync(0xffffffffu, rn, off);
-    if ((t & 31) == 0) wsum[t >> 5] = rn;
+  if (RUPD) {  // per right-hand side: its columns' sums in column order
+    __shared__ double csum[kColPipeQ];
+    if (t < Q) csum[t] = colacc;
     __syncthreads();
-    if (t == 0) {
+    if (t < p.nrhs) {
       double s = 0.0;
-      for (int w = 0; w < 12 * kColPipeQ / 32; w++) s += wsum[w];
-      p.rpart[blockIdx.x] = s;
+      for (int q2 = t; q2 < Q; q2 += p.nrhs) s += csum[q2];
+      p.rpart[size_t(blockIdx.x) * p.nrhs + t] = s;
     }
   }
 }
@@ -504,7 +514,7 @@ static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* r_
   }
   const size_t ntiles = (p.nq + kColPipeQ - 1) / kColPipeQ;
   size_t slots = size_t(per_sm.load()) * size_t(sms.load());
-  if (RUPD && slots > size_t(2) * kRedBlocks) slots = size_t(2) * kRedBlocks;  // the partial buffer's CTAs
+  if (RUPD && slots > size_t(2) * kRedBlocks) slots = size_t(2) * kRedBlocks;  // the partial buffer's [CTA][nrhs]
   const unsigned blocks = unsigned(ntiles < slots ? ntiles : slots);
   col_pipe_kernel<LS, DAG, OPA, OPB, RUPD><<<blocks, 12 * kColPipeQ, smem, op->stream>>>(p, c);
   GB_CHECK_CUDA(cudaGetLastError());
@@ -602,11 +612,12 @@ int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfVi
   p.np = op->n5() >> 1;
   p.nq = size_t(op->half4) * op->nrhs;
   p.zc = float(zc);
-  const bool rupd = r_upd && r_parts && x.prec == GB_F32 && r_upd->prec == GB_F32 && op->nrhs == 1 && dag &&
-                    opa == COL_M5D && opb == COLB_M5D;
+  const bool rupd = r_upd && r_parts && x.prec == GB_F32 && r_upd->prec == GB_F32 && kColPipeQ % op->nrhs == 0 &&
+                    dag && opa == COL_M5D && opb == COLB_M5D;
   p.r = rupd ? static_cast<float4*>(r_upd->data) : nullptr;
   p.rpart = rupd ? op->d_partial : nullptr;
   p.cg = op->d_cg;
+  p.nrhs = op->nrhs;
   int* parts = rupd ? r_parts : nullptr;
   const bool half = x.prec == GB_F16;
   switch (op->Ls) {

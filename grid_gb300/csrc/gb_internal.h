@@ -189,9 +189,9 @@ int launch_reduce_final(Op* op, const double* partial, int nparts, int nv, doubl
 int red_grid(Op* op, size_t n5, int* blocks, int* threads);
 // pair-layout (FP32 / FP16) kernels, gb_pair.cu
 int red_grid_pair(Op* op, size_t np, int* blocks, int* threads);
-// norm_parts (non-null): with z, no dagger and one right-hand side the kernel also writes
-// per-CTA sums of |chi|^2 as stored into op->d_partial ([CTA][2], imaginary parts 0) and
-// their count into *norm_parts; otherwise *norm_parts = 0
+// norm_parts (non-null): with z and no dagger the kernel also writes per-CTA sums of
+// |chi|^2 as stored into op->d_partial ([CTA][nrhs]) and their count into *norm_parts;
+// otherwise *norm_parts = 0
 int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
                     const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts = nullptr);
 // kind 0: |x|^2 ; 1: <x|y> ; 2: z = a x + y, |z|^2 ; 3: y -= a[rhs] x (the device CG
@@ -227,10 +227,11 @@ struct ZCoefsHost {
 enum { ZPROG_M5D = 0, ZPROG_INV = 2, ZPROG_DIAG = 3 };
 bool zmobius_ls_supported(int Ls);
 int launch_zcol(Op* op, int prog, int dag, HalfView x, const HalfView* y, HalfView out, double zc, const ZCoefsHost& h);
-// With r_upd (FP32, one right-hand side, the program MooeeDag - M5Ddag z that ends MpcDag)
-// the kernel does not store out: it applies the CG's residual update r -= a out (a from
-// op->d_cg) and writes per-CTA sums of |r|^2 [CTA] into op->d_partial, their count into
-// *r_parts (0 when it could not fuse; out is then stored and the caller updates r).
+// With r_upd (FP32, nrhs dividing 16, the program MooeeDag - M5Ddag z that ends MpcDag)
+// the kernel does not store out: it applies the CG's residual update r -= a out (a per
+// right-hand side from op->d_cg) and writes per-CTA sums of |r|^2 [CTA][nrhs] into
+// op->d_partial, their count into *r_parts (0 when it could not fuse; out is then stored
+// and the caller updates r).
 int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfView out, double zc,
                const ColCoefsHost& h, HalfView* r_upd = nullptr, int* r_parts = nullptr);
 

@@ -49,11 +49,11 @@ int op_meooe(Op* op, Field* in, Field* out, int dag);
 int op_mooee(Op* op, Field* in, Field* out, int dag, Field* z, double zc, int* norm_parts = nullptr);
 int op_mooee_inv(Op* op, Field* in, Field* out, int dag);
 // norm_parts (Mpc only): when non-null, the last kernel may also reduce |out|^2 into
-// op->d_partial ([CTA][2], the layout of the inner-product partials, imaginary parts 0) and
-// sets *norm_parts to the number of CTA sums written, or to 0 when it did not.
+// op->d_partial ([CTA][nrhs], the layout of the norm partials) and sets *norm_parts to the
+// number of CTA sums written, or to 0 when it did not.
 // r_upd, r_parts (MpcDag only, for the CG): when both are non-null, the last kernel may
 // instead of storing out apply r_upd -= a out (a: the CG scalars of op) and reduce
-// |r_upd|^2 into op->d_partial ([CTA]); *r_parts is the number of CTA sums written, or
+// |r_upd|^2 into op->d_partial ([CTA][nrhs]); *r_parts is the number of CTA sums written, or
 // 0 when it stored out and left r_upd alone
 int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts = nullptr, Field* r_upd = nullptr,
            int* r_parts = nullptr);

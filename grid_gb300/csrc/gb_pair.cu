@@ -23,158 +23,11 @@ struct PairShape {
 
 __device__ __forceinline__ float2 fma2s(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-// ---------------------------------------------------------------------------------------
-// M5D on pairs.  Lane 0 = s (even), lane 1 = s+1.  For the upper (P+) components the
-// s-1 neighbours are (previous pair lane 1, this pair lane 0); for the lower (P-) ones the
-// s+1 neighbours are (this pair lane 1, next pair lane 0), with the wrap inside the
-// right-hand side's block of Ls.  Dagger exchanges the roles of s-1 and s+1.
-// ---------------------------------------------------------------------------------------
-struct M5PairParams {
-  const void* psi; const float2* psi_n;
-  const void* phi; const float2* phi_n;
-  void* chi; float2* chi_n;
-  const void* z; const float2* z_n;
-  float zc;
-  size_t np;  // pairs per half field
-  int L5, Ls;
-  double* norm_part;  // NORM: per-CTA sums of |chi|^2 as stored, [CTA][2] (imaginary part 0)
-};
-
-template <class R> struct Coef5p {
-  R d[kMaxLs], u[kMaxLs], l[kMaxLs];
-};
-
-// NORM (one right-hand side): a grid-stride loop whose CTAs also sum |chi|^2 as stored, in
-// a fixed order (per thread in FP64, then warp shuffles, then the warps in order)
-template <class T, bool DAG, bool ZTERM, bool SAME, bool NORM>
-__global__ void __launch_bounds__(256) m5d_pair_kernel(const M5PairParams p, const Coef5p<float> c) {
-  double nacc = 0.0;
-  const size_t stride = NORM ? size_t(gridDim.x) * blockDim.x : p.np;
-  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < p.np; q += stride) {
-    const int hl = p.L5 >> 1, hs = p.Ls >> 1;
-    const int sp = int(q % hl);            // pair index within the 4D site
-    const int s = (2 * sp) % p.Ls;         // even
-    const int psb = sp % hs;               // pair index within the rhs block
-    const size_t qb = q - psb;             // first pair of the rhs block
-    const size_t qprev = psb == 0 ? qb + hs - 1 : q - 1;
-    const size_t qnext = psb == hs - 1 ? qb : q + 1;
-    Pair12 cur, prv, nxt, ph;
-    PairIO<T>::load(p.psi, p.psi_n, p.np, q, cur);
-    if (SAME) ph = cur; else PairIO<T>::load(p.phi, p.phi_n, p.np, q, ph);
-    // neighbour chirality halves: the upper (P+) half from s-1 (non-dag) / s+1 (dag), the
-    // lower (P-) half from the other side
-    PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qnext : qprev, 0, DAG ? nxt : prv);
-    PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qprev : qnext, 6, DAG ? prv : nxt);
-    const float2 d = make_float2(c.d[s], c.d[s + 1]);
-    const float2 cl = make_float2(c.l[s], c.l[s + 1]);  // coefficient of the s-1 neighbour
-    const float2 cu = make_float2(c.u[s], c.u[s + 1]);  // coefficient of the s+1 neighbour
-    Pair12 o;
-#pragma unroll
-    for (int k = 0; k < 12; k++) {
-      const bool upper = k < 6;
-      // s-1 neighbours: (prev lane 1, cur lane 0); s+1 neighbours: (cur lane 1, next lane 0)
-      const bool from_minus = DAG ? !upper : upper;
-      float2 nr, ni;
-      if (from_minus) {
-        nr = make_float2(prv.re[k].y, cur.re[k].x);
-        ni = make_float2(prv.im[k].y, cur.im[k].x);
-      } else {
-        nr = make_float2(cur.re[k].y, nxt.re[k].x);
-        ni = make_float2(cur.im[k].y, nxt.im[k].x);
-      }
-      const float2 cc = from_minus ? cl : cu;
-      o.re[k] = fma2s(cc, nr, __fmul2_rn(d, ph.re[k]));
-      o.im[k] = fma2s(cc, ni, __fmul2_rn(d, ph.im[k]));
-    }
-    if (ZTERM) {
-      Pair12 zz;
-      PairIO<T>::load(p.z, p.z_n, p.np, q, zz);
-      const float2 zc = make_float2(p.zc, p.zc);
-#pragma unroll
-      for (int k = 0; k < 12; k++) {
-        o.re[k] = fma2s(zc, zz.re[k], o.re[k]);
-        o.im[k] = fma2s(zc, zz.im[k], o.im[k]);
-      }
-    }
-    if (NORM) {
-      const float2 n2 = PairIO<T>::store_n2(p.chi, p.chi_n, p.np, q, o);
-      nacc += double(n2.x) + double(n2.y);
-    } else {
-      PairIO<T>::store(p.chi, p.chi_n, p.np, q, o);
-    }
-  }
-  if (NORM) {
-    __shared__ double wsum[8];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) nacc += __shfl_down_sync(0xffffffffu, nacc, off);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = nacc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int w = 0; w < int(blockDim.x >> 5); w++) s += wsum[w];
-      p.norm_part[2 * size_t(blockIdx.x)] = s;
-      p.norm_part[2 * size_t(blockIdx.x) + 1] = 0.0;
-    }
-  }
-}
-
-// grid of the NORM variant: at most kRedBlocks CTAs (the partial buffer's size)
-static unsigned m5d_norm_blocks(size_t np) {
-  const size_t need = (np + 255) / 256;
-  return unsigned(need < size_t(kRedBlocks) ? need : size_t(kRedBlocks));
-}
-
-template <class T, bool DAG, bool Z>
-static void m5d_pair_go(Op* op, const M5PairParams& p, const Coef5p<float>& c, bool same, bool norm) {
-  if constexpr (Z && !DAG) {  // the last kernel of Mpc: Mooee in - (the Dhop term)
-    if (norm) {
-      const unsigned blocks = m5d_norm_blocks(p.np);
-      if (same) m5d_pair_kernel<T, DAG, Z, true, true><<<blocks, 256, 0, op->stream>>>(p, c);
-      else m5d_pair_kernel<T, DAG, Z, false, true><<<blocks, 256, 0, op->stream>>>(p, c);
-      return;
-    }
-  }
-  const unsigned blocks = unsigned((p.np + 255) / 256);
-  if (same) m5d_pair_kernel<T, DAG, Z, true, false><<<blocks, 256, 0, op->stream>>>(p, c);
-  else m5d_pair_kernel<T, DAG, Z, false, false><<<blocks, 256, 0, op->stream>>>(p, c);
-}
-
-int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
-                    const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts) {
-  M5PairParams p;
-  p.psi = psi.data; p.psi_n = reinterpret_cast<const float2*>(psi.norms);
-  p.phi = phi.data; p.phi_n = reinterpret_cast<const float2*>(phi.norms);
-  p.chi = chi.data; p.chi_n = reinterpret_cast<float2*>(chi.norms);
-  p.z = z ? z->data : nullptr; p.z_n = z ? reinterpret_cast<const float2*>(z->norms) : nullptr;
-  p.zc = float(zc);
-  p.np = n5 >> 1;
-  p.L5 = op->L5;
-  p.Ls = op->Ls;
-  // |chi|^2 on the way for one right-hand side (every lane then belongs to it)
-  const bool norm = norm_parts && op->nrhs == 1 && z && !dag;
-  p.norm_part = norm ? op->d_partial : nullptr;
-  if (norm_parts) *norm_parts = norm ? int(m5d_norm_blocks(p.np)) : 0;
-  Coef5p<float> c;
-  for (int s = 0; s < op->Ls; s++) { c.d[s] = float(diag[s]); c.u[s] = float(upper[s]); c.l[s] = float(lower[s]); }
-  const bool same = psi.data == phi.data;
-  const bool zt = z != nullptr;
-  if (psi.prec == GB_F32) {
-    if (dag) { if (zt) m5d_pair_go<float, true, true>(op, p, c, same, norm); else m5d_pair_go<float, true, false>(op, p, c, same, norm); }
-    else { if (zt) m5d_pair_go<float, false, true>(op, p, c, same, norm); else m5d_pair_go<float, false, false>(op, p, c, same, norm); }
-  } else {
-    if (dag) { if (zt) m5d_pair_go<__half, true, true>(op, p, c, same, norm); else m5d_pair_go<__half, true, false>(op, p, c, same, norm); }
-    else { if (zt) m5d_pair_go<__half, false, true>(op, p, c, same, norm); else m5d_pair_go<__half, false, false>(op, p, c, same, norm); }
-  }
-  GB_CHECK_CUDA(cudaGetLastError());
-  return GB_OK;
-}
-
-// ---------------------------------------------------------------------------------------
-// Reductions on pairs.  A thread keeps one FP64 accumulator per lane; the grid-stride
-// (in pairs) is a multiple of L5/2, so every thread's lanes stay on fixed right-hand
-// sides.  The block sums go through shared memory as 2*blockDim "virtual threads"
-// (element order), then rows of L5 are folded and each rhs sums its Ls slots.
-// ---------------------------------------------------------------------------------------
+// Per-rhs block sums of per-lane FP64 values.  A thread keeps one accumulator per lane; the
+// grid-stride (in pairs) is a multiple of L5/2, so every thread's lanes stay on fixed right-
+// hand sides.  The block sums go through shared memory as 2*blockDim "virtual threads"
+// (element order), then rows of L5 are folded and each rhs sums its Ls slots.  out:
+// [block][nrhs][NV].
 template <int NV>
 __device__ __forceinline__ void block_reduce_pairs(const double (&v0)[NV], const double (&v1)[NV], int L5, int Ls,
                                                    int nrhs, double* out) {
@@ -224,9 +77,146 @@ __device__ __forceinline__ void block_reduce_pairs(const double (&v0)[NV], const
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// M5D on pairs.  Lane 0 = s (even), lane 1 = s+1.  For the upper (P+) components the
+// s-1 neighbours are (previous pair lane 1, this pair lane 0); for the lower (P-) ones the
+// s+1 neighbours are (this pair lane 1, next pair lane 0), with the wrap inside the
+// right-hand side's block of Ls.  Dagger exchanges the roles of s-1 and s+1.
+// ---------------------------------------------------------------------------------------
+struct M5PairParams {
+  const void* psi; const float2* psi_n;
+  const void* phi; const float2* phi_n;
+  void* chi; float2* chi_n;
+  const void* z; const float2* z_n;
+  float zc;
+  size_t np;  // pairs per half field
+  int L5, Ls, nrhs;
+  double* norm_part;  // NORM: per-CTA sums of |chi|^2 as stored, [CTA][nrhs]
+};
+
+template <class R> struct Coef5p {
+  R d[kMaxLs], u[kMaxLs], l[kMaxLs];
+};
+
+// NORM: a grid-stride loop (blockDim a multiple of L5/2) whose CTAs also sum |chi|^2 as
+// stored per right-hand side, in a fixed order (block_reduce_pairs)
+template <class T, bool DAG, bool ZTERM, bool SAME, bool NORM>
+__global__ void __launch_bounds__(512) m5d_pair_kernel(const M5PairParams p, const Coef5p<float> c) {
+  double nv0[1] = {0.0}, nv1[1] = {0.0};
+  const size_t stride = NORM ? size_t(gridDim.x) * blockDim.x : p.np;
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < p.np; q += stride) {
+    const int hl = p.L5 >> 1, hs = p.Ls >> 1;
+    const int sp = int(q % hl);            // pair index within the 4D site
+    const int s = (2 * sp) % p.Ls;         // even
+    const int psb = sp % hs;               // pair index within the rhs block
+    const size_t qb = q - psb;             // first pair of the rhs block
+    const size_t qprev = psb == 0 ? qb + hs - 1 : q - 1;
+    const size_t qnext = psb == hs - 1 ? qb : q + 1;
+    Pair12 cur, prv, nxt, ph;
+    PairIO<T>::load(p.psi, p.psi_n, p.np, q, cur);
+    if (SAME) ph = cur; else PairIO<T>::load(p.phi, p.phi_n, p.np, q, ph);
+    // neighbour chirality halves: the upper (P+) half from s-1 (non-dag) / s+1 (dag), the
+    // lower (P-) half from the other side
+    PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qnext : qprev, 0, DAG ? nxt : prv);
+    PairIO<T>::load6(p.psi, p.psi_n, p.np, DAG ? qprev : qnext, 6, DAG ? prv : nxt);
+    const float2 d = make_float2(c.d[s], c.d[s + 1]);
+    const float2 cl = make_float2(c.l[s], c.l[s + 1]);  // coefficient of the s-1 neighbour
+    const float2 cu = make_float2(c.u[s], c.u[s + 1]);  // coefficient of the s+1 neighbour
+    Pair12 o;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const bool upper = k < 6;
+      // s-1 neighbours: (prev lane 1, cur lane 0); s+1 neighbours: (cur lane 1, next lane 0)
+      const bool from_minus = DAG ? !upper : upper;
+      float2 nr, ni;
+      if (from_minus) {
+        nr = make_float2(prv.re[k].y, cur.re[k].x);
+        ni = make_float2(prv.im[k].y, cur.im[k].x);
+      } else {
+        nr = make_float2(cur.re[k].y, nxt.re[k].x);
+        ni = make_float2(cur.im[k].y, nxt.im[k].x);
+      }
+      const float2 cc = from_minus ? cl : cu;
+      o.re[k] = fma2s(cc, nr, __fmul2_rn(d, ph.re[k]));
+      o.im[k] = fma2s(cc, ni, __fmul2_rn(d, ph.im[k]));
+    }
+    if (ZTERM) {
+      Pair12 zz;
+      PairIO<T>::load(p.z, p.z_n, p.np, q, zz);
+      const float2 zc = make_float2(p.zc, p.zc);
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        o.re[k] = fma2s(zc, zz.re[k], o.re[k]);
+        o.im[k] = fma2s(zc, zz.im[k], o.im[k]);
+      }
+    }
+    if (NORM) {
+      const float2 n2 = PairIO<T>::store_n2(p.chi, p.chi_n, p.np, q, o);
+      nv0[0] += double(n2.x);
+      nv1[0] += double(n2.y);
+    } else {
+      PairIO<T>::store(p.chi, p.chi_n, p.np, q, o);
+    }
+  }
+  if (NORM) block_reduce_pairs<1>(nv0, nv1, p.L5, p.Ls, p.nrhs, p.norm_part);
+}
+
+template <class T, bool DAG, bool Z>
+static void m5d_pair_go(Op* op, const M5PairParams& p, const Coef5p<float>& c, bool same, bool norm) {
+  if constexpr (Z && !DAG) {  // the last kernel of Mpc: Mooee in - (the Dhop term)
+    if (norm) {  // the reductions' grid: blockDim a multiple of L5/2, at most kRedBlocks CTAs
+      int g = 1, B = 256;
+      red_grid_pair(op, p.np, &g, &B);
+      const size_t smem = size_t(op->nrhs == 1 ? 32 : 2 * B) * sizeof(double);
+      if (same) m5d_pair_kernel<T, DAG, Z, true, true><<<g, B, smem, op->stream>>>(p, c);
+      else m5d_pair_kernel<T, DAG, Z, false, true><<<g, B, smem, op->stream>>>(p, c);
+      return;
+    }
+  }
+  const unsigned blocks = unsigned((p.np + 255) / 256);
+  if (same) m5d_pair_kernel<T, DAG, Z, true, false><<<blocks, 256, 0, op->stream>>>(p, c);
+  else m5d_pair_kernel<T, DAG, Z, false, false><<<blocks, 256, 0, op->stream>>>(p, c);
+}
+
+int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const double* lower, const double* diag,
+                    const double* upper, int dag, size_t n5, const HalfView* z, double zc, int* norm_parts) {
+  M5PairParams p;
+  p.psi = psi.data; p.psi_n = reinterpret_cast<const float2*>(psi.norms);
+  p.phi = phi.data; p.phi_n = reinterpret_cast<const float2*>(phi.norms);
+  p.chi = chi.data; p.chi_n = reinterpret_cast<float2*>(chi.norms);
+  p.z = z ? z->data : nullptr; p.z_n = z ? reinterpret_cast<const float2*>(z->norms) : nullptr;
+  p.zc = float(zc);
+  p.np = n5 >> 1;
+  p.L5 = op->L5;
+  p.Ls = op->Ls;
+  p.nrhs = op->nrhs;
+  // |chi|^2 per right-hand side on the way (Ls even: both lanes of a pair are one rhs)
+  int g = 0, B = 0;
+  const bool norm = norm_parts && z && !dag && red_grid_pair(op, p.np, &g, &B) == GB_OK;
+  p.norm_part = norm ? op->d_partial : nullptr;
+  if (norm_parts) *norm_parts = norm ? g : 0;
+  Coef5p<float> c;
+  for (int s = 0; s < op->Ls; s++) { c.d[s] = float(diag[s]); c.u[s] = float(upper[s]); c.l[s] = float(lower[s]); }
+  const bool same = psi.data == phi.data;
+  const bool zt = z != nullptr;
+  if (psi.prec == GB_F32) {
+    if (dag) { if (zt) m5d_pair_go<float, true, true>(op, p, c, same, norm); else m5d_pair_go<float, true, false>(op, p, c, same, norm); }
+    else { if (zt) m5d_pair_go<float, false, true>(op, p, c, same, norm); else m5d_pair_go<float, false, false>(op, p, c, same, norm); }
+  } else {
+    if (dag) { if (zt) m5d_pair_go<__half, true, true>(op, p, c, same, norm); else m5d_pair_go<__half, true, false>(op, p, c, same, norm); }
+    else { if (zt) m5d_pair_go<__half, false, true>(op, p, c, same, norm); else m5d_pair_go<__half, false, false>(op, p, c, same, norm); }
+  }
+  GB_CHECK_CUDA(cudaGetLastError());
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Reductions on pairs (block sums: block_reduce_pairs above)
+// ---------------------------------------------------------------------------------------
+
 // KIND 0: |x|^2 ; 1: <x|y> ; 2: z = a x + y, |z|^2 ; 3: r(=y) -= a[rhs] mmp(=x), |r|^2
 template <class T, int KIND>
-__global__ void __launch_bounds__(256) reduce_pair_kernel(const PairShape sh, const void* x, const float2* xn,
+__global__ void __launch_bounds__(512) reduce_pair_kernel(const PairShape sh, const void* x, const float2* xn,
                                                           const void* y, const float2* yn, void* z, float2* zn,
                                                           double a, const CGScalars* cg, size_t np, double* partial) {
   constexpr int NV = KIND == 1 ? 2 : 1;
@@ -278,7 +268,8 @@ __global__ void __launch_bounds__(256) reduce_pair_kernel(const PairShape sh, co
   block_reduce_pairs<NV>(v0, v1, sh.L5, sh.Ls, sh.nrhs, partial);
 }
 
-// grid of the pair reductions: blockDim a multiple of L5/2 (about 256), grid <= kRedBlocks
+// grid of the pair reductions: blockDim a multiple of L5/2 (about 256, at most 512 for
+// L5 = kMaxL5), grid <= kRedBlocks
 int red_grid_pair(Op* op, size_t np, int* blocks, int* threads) {
   const int h = op->L5 >> 1;
   int B = 256;
@@ -286,7 +277,7 @@ int red_grid_pair(Op* op, size_t np, int* blocks, int* threads) {
     int m = 1;
     while (h * m * 2 <= 256) m *= 2;
     B = h * m;
-    if (B > 1024) { set_error("reduction: L5 = %d too large", op->L5); return GB_ERR_UNSUPPORTED; }
+    if (B > 512) { set_error("reduction: L5 = %d too large", op->L5); return GB_ERR_UNSUPPORTED; }
   }
   const size_t need = (np + B - 1) / B;
   int g = int(need < size_t(kRedBlocks) ? need : size_t(kRedBlocks));
