@@ -161,12 +161,19 @@ __global__ void __launch_bounds__(512) m5d_pair_kernel(const M5PairParams p, con
   if (NORM) block_reduce_pairs<1>(nv0, nv1, p.L5, p.Ls, p.nrhs, p.norm_part);
 }
 
+// grid of the NORM variant: the reductions' grid (blockDim a multiple of L5/2, at most
+// kRedBlocks CTAs).  Covering the field in one pass (3888 CTAs at 24^4 x 12) measured
+// slower than the grid-stride loop over kRedBlocks CTAs: 102.7 against 95.4 us.
+static int m5d_norm_grid(Op* op, size_t np, int* blocks, int* threads) {
+  return red_grid_pair(op, np, blocks, threads);
+}
+
 template <class T, bool DAG, bool Z>
 static void m5d_pair_go(Op* op, const M5PairParams& p, const Coef5p<float>& c, bool same, bool norm) {
   if constexpr (Z && !DAG) {  // the last kernel of Mpc: Mooee in - (the Dhop term)
-    if (norm) {  // the reductions' grid: blockDim a multiple of L5/2, at most kRedBlocks CTAs
+    if (norm) {
       int g = 1, B = 256;
-      red_grid_pair(op, p.np, &g, &B);
+      m5d_norm_grid(op, p.np, &g, &B);
       const size_t smem = size_t(op->nrhs == 1 ? 32 : 2 * B) * sizeof(double);
       if (same) m5d_pair_kernel<T, DAG, Z, true, true><<<g, B, smem, op->stream>>>(p, c);
       else m5d_pair_kernel<T, DAG, Z, false, true><<<g, B, smem, op->stream>>>(p, c);
@@ -192,7 +199,7 @@ int launch_m5d_pair(Op* op, HalfView psi, HalfView phi, HalfView chi, const doub
   p.nrhs = op->nrhs;
   // |chi|^2 per right-hand side on the way (Ls even: both lanes of a pair are one rhs)
   int g = 0, B = 0;
-  const bool norm = norm_parts && z && !dag && red_grid_pair(op, p.np, &g, &B) == GB_OK;
+  const bool norm = norm_parts && z && !dag && m5d_norm_grid(op, p.np, &g, &B) == GB_OK;
   p.norm_part = norm ? op->d_partial : nullptr;
   if (norm_parts) *norm_parts = norm ? g : 0;
   Coef5p<float> c;
