@@ -305,6 +305,37 @@ def test_mixed_precision_schur_reaches_1e10(gpu_available, lo):
     assert o.rel_l2(x, xr) < 1e-7
 
 
+@pytest.mark.parametrize("lo", [g.F32, g.F16])
+def test_multi_rhs_mobius_mixed_cg_each_equals_single(gpu_available, lo):
+    """A 4-RHS Moebius operator pair through the mixed-precision Schur CG: the per-rhs
+    reductions fused into the operator (|Mpc p|^2 in Mpc's last kernel; in FP32 also
+    MpcDag's residual update) keep every right-hand side on its own solve.  Each solution
+    meets the tolerance against the oracle's FP64 M and agrees with its single-RHS solve."""
+    dims, Ls, nrhs = (4, 4, 4, 8), 8, 4
+    U = g.random_gauge(dims, 0.6, 5)
+    srcs = [fermion(512, Ls, 130 + r) for r in range(nrhs)]
+    ref = o.OracleOp(1, 0, dims, Ls, [0.01, 1.8, 1.5, 0.5], U, g.antiperiodic_t())
+
+    def solve(n, src):
+        od = g.MobiusFermion(U, dims, Ls, 0.01, 1.8, 1.5, 0.5, precision=g.F64, nrhs=n)
+        of = g.MobiusFermion(U, dims, Ls, 0.01, 1.8, 1.5, 0.5, precision=lo, nrhs=n)
+        fs = od.FermionField().import_(src)
+        fx = od.FermionField().zero()
+        cg = g.ConjugateGradientReliableUpdate(1e-10, 20000, 1e-6, g.SchurDiagMooeeOperator(of),
+                                               g.SchurDiagMooeeOperator(od), relup_every=100, use_graphs=1)
+        g.SchurRedBlackDiagMooeeSolve(cg)(od, fs, fx)
+        return fx.export(), cg
+
+    xb, cb = solve(nrhs, np.concatenate(srcs))
+    got = xb.reshape(nrhs, -1)
+    for r in range(nrhs):
+        x1, c1 = solve(1, srcs[r])
+        assert cb.per_rhs_true_residual[r] < 1e-10 and c1.TrueResidual < 1e-10
+        assert abs(cb.per_rhs_iterations[r] - c1.IterationsToComplete) <= 0.1 * c1.IterationsToComplete
+        assert o.rel_l2(ref.apply(o.OP_M, got[r]), srcs[r]) < 1e-9
+        assert o.rel_l2(got[r], x1) < 1e-7
+
+
 def test_multi_rhs_cg_each_equals_single(gpu_available):
     """Batched CG keeps independent alpha/beta per right-hand side (CGmultiRHS semantics,
     BlockConjugateGradient.h:412-540): each result equals its own single solve."""
