@@ -492,10 +492,10 @@ int op_mooee_inv(Op* op, Field* in, Field* out, int dag) {
 }
 
 // SchurDiagMooeeOperator::Mpc / MpcDag (LinearOperator.h:330-349).  With norm_parts (Mpc
-// of a FP32 / FP16 Moebius operator with one right-hand side) the last kernel also reduces
-// |out|^2 (see launch_m5d_pair).  With r_upd (MpcDag of a FP32 Moebius operator with one
-// right-hand side) the last kernel applies r -= a out for the CG instead of storing out
-// (see launch_col).
+// of a FP32 / FP16 Moebius operator) the last kernel also reduces |out|^2 per right-hand
+// side (see launch_m5d_pair).  With r_upd (MpcDag of a FP32 / FP16 Moebius operator whose
+// right-hand-side count divides 16) the last kernel applies r -= a out for the CG instead
+// of storing out (see launch_col).
 int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts, Field* r_upd, int* r_parts) {
   if (norm_parts) *norm_parts = 0;
   if (r_parts) *r_parts = 0;

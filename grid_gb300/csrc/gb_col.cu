@@ -48,7 +48,8 @@ struct ColParams {
   // RUPD (the last program of MpcDag in the CG): instead of storing out, r -= a out with
   // each right-hand side's CG scalar a, and per-CTA sums of |r|^2 per right-hand side into
   // rpart[CTA][nrhs] (the layout of the norm partials); nrhs divides the tile's columns
-  float4* r;
+  void* r;
+  float* rn;  // FP16: the per-5D-site norms of r
   double* rpart;
   const CGScalars* cg;
   int nrhs;
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
 #pragma unroll
       for (int j = 0; j < H; j++) {
         const int e = t + j * 12 * Q, kk = e / (Q * H), r = e - kk * (Q * H);
-        if (r < nv) rv[j] = p.r[size_t(kk) * p.np + tile * Q * H + r];
+        if (r < nv) rv[j] = static_cast<const float4*>(p.r)[size_t(kk) * p.np + tile * Q * H + r];
       }
     }
     cp_async_wait<kColStages - 1>();
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_kernel(const ColParam
           float4 w = rv[j];
           w.x = fmaf(ma, v.x, w.x); w.y = fmaf(ma, v.y, w.y);
           w.z = fmaf(ma, v.z, w.z); w.w = fmaf(ma, v.w, w.w);
-          p.r[size_t(kk) * p.np + tile * Q * H + r] = w;
+          static_cast<float4*>(p.r)[size_t(kk) * p.np + tile * Q * H + r] = w;
           cn[(kk * Q + q2) * H + m] = fmaf(w.x, w.x, fmaf(w.y, w.y, fmaf(w.z, w.z, w.w * w.w)));
         }
       }
@@ -428,23 +429,29 @@ __device__ __forceinline__ void col_decode_half(const uint4* raw, const float* r
   }
 }
 
-template <int LS, bool DAG, int OPA, int OPB>
+// RUPD (the last program of MpcDag in the CG, two inputs): r is a third raw input of the
+// ring; after the program it is decoded into the y tile (free by then), r -= a[rhs] out is
+// formed there and stored through the FP16 encoder, and |r|^2 (before encoding, as the
+// separate update pass sums it) is summed per column and right-hand side as in
+// col_pipe_kernel.
+template <int LS, bool DAG, int OPA, int OPB, bool RUPD>
 __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_half_kernel(const ColParams p, const ColCoef<LS> c) {
   constexpr int Q = kColPipeQ, H = LS / 2, ST = col_stride<LS>(), NIN = OPB != COLB_NONE ? 2 : 1;
+  constexpr int NRING = NIN + (RUPD ? 1 : 0);  // raw inputs staged per tile
   constexpr int RAW = 6 * Q * H;      // uint4 of one input's raw tile
   constexpr int TILE = 12 * Q * ST;   // float4 of one input's decoded tile
-  // [NIN float tiles][kColStages][NIN][raw tile][Q * LS norms], then Q * LS floats of scratch
+  // [NIN float tiles][kColStages][NRING][raw tile][Q * LS norms], then Q * LS floats of scratch
   extern __shared__ float4 col_half_smem[];
   float4* ftile = col_half_smem;
   uint4* ring = reinterpret_cast<uint4*>(col_half_smem + NIN * TILE);
   constexpr int SLOT = RAW + Q * LS / 4;  // uint4 per input per stage (norms packed 4 per uint4)
-  float* snorm = reinterpret_cast<float*>(ring + size_t(kColStages) * NIN * SLOT);
+  float* snorm = reinterpret_cast<float*>(ring + size_t(kColStages) * NRING * SLOT);
   const size_t ntiles = (p.nq + Q - 1) / Q;
   const uint4* xs = static_cast<const uint4*>(p.x);
   const uint4* ys = static_cast<const uint4*>(p.y);
   const int t = threadIdx.x, k = t / Q, qq = t - k * Q;
   auto vectors = [&](size_t tile) { return int(min(p.nq - tile * Q, size_t(Q))) * H; };
-  auto slot = [&](int st, int j) { return ring + (size_t(st) * NIN + j) * SLOT; };
+  auto slot = [&](int st, int j) { return ring + (size_t(st) * NRING + j) * SLOT; };
   auto issue = [&](size_t tile, int st) {
     if (tile < ntiles) {
       col_issue_half<LS>(xs, p.xn, slot(st, 0), reinterpret_cast<float*>(slot(st, 0) + RAW), p.np, tile * Q,
@@ -452,9 +459,16 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_half_kernel(const Col
       if (NIN == 2)
         col_issue_half<LS>(ys, p.yn, slot(st, 1), reinterpret_cast<float*>(slot(st, 1) + RAW), p.np, tile * Q,
                            vectors(tile));
+      if (RUPD)
+        col_issue_half<LS>(static_cast<const uint4*>(p.r), p.rn, slot(st, NIN),
+                           reinterpret_cast<float*>(slot(st, NIN) + RAW), p.np, tile * Q, vectors(tile));
     }
     cp_async_commit();
   };
+  __shared__ float sma[kColPipeQ];
+  __shared__ float cn[RUPD ? 12 * Q * H : 1];
+  double colacc = 0.0;  // thread t < Q: |r|^2 of column t of this CTA's tiles
+  if (RUPD && t < p.nrhs) sma[t] = -float(p.cg[t].a);  // read after the loop's first barrier
   size_t tile = blockIdx.x;
   for (int k0 = 0; k0 < kColStages - 1; k0++) issue(tile + size_t(k0) * gridDim.x, k0);
   for (int st = 0; tile < ntiles; tile += gridDim.x, st = st + 1 == kColStages ? 0 : st + 1) {
@@ -467,10 +481,48 @@ __global__ void __launch_bounds__(12 * kColPipeQ) col_pipe_half_kernel(const Col
     __syncthreads();
     if (qq < nv / H) col_run<LS, DAG, OPA, OPB>(ftile + (k * Q + qq) * ST, ftile + TILE + (k * Q + qq) * ST, p.zc, c, k < 6);
     __syncthreads();
-    ColIO<__half, LS, Q>::store(p.out, p.outn, snorm, ftile, p.np, tile * Q, nv);
+    if (RUPD) {
+      float4* rt = ftile + TILE;  // the y tile, read by the program only
+      col_decode_half<LS>(slot(st, NIN), reinterpret_cast<const float*>(slot(st, NIN) + RAW), rt, nv);
+      __syncthreads();
+      for (int e = t; e < 12 * Q * H; e += 12 * Q) {
+        const int kk = e / (Q * H), r = e - kk * (Q * H);
+        if (r < nv) {
+          const int q2 = r / H, m = r - q2 * H, i = (kk * Q + q2) * ST + m;
+          const float ma = sma[q2 % p.nrhs];
+          const float4 v = ftile[i];
+          float4 w = rt[i];
+          w.x = fmaf(ma, v.x, w.x); w.y = fmaf(ma, v.y, w.y);
+          w.z = fmaf(ma, v.z, w.z); w.w = fmaf(ma, v.w, w.w);
+          rt[i] = w;
+          cn[(kk * Q + q2) * H + m] = fmaf(w.x, w.x, fmaf(w.y, w.y, fmaf(w.z, w.z, w.w * w.w)));
+        }
+      }
+      __syncthreads();
+      if (t < nv / H) {
+        float s = 0.f;
+        for (int kk = 0; kk < 12; kk++)
+#pragma unroll
+          for (int m = 0; m < H; m++) s += cn[(kk * Q + t) * H + m];
+        colacc += double(s);
+      }
+      ColIO<__half, LS, Q>::store(p.r, p.rn, snorm, rt, p.np, tile * Q, nv);
+    } else {
+      ColIO<__half, LS, Q>::store(p.out, p.outn, snorm, ftile, p.np, tile * Q, nv);
+    }
     __syncthreads();  // the float tile and this stage are read out before they are reused
   }
   cp_async_wait<0>();
+  if (RUPD) {  // per right-hand side: its columns' sums in column order
+    __shared__ double csum[kColPipeQ];
+    if (t < Q) csum[t] = colacc;
+    __syncthreads();
+    if (t < p.nrhs) {
+      double s = 0.0;
+      for (int q2 = t; q2 < Q; q2 += p.nrhs) s += csum[q2];
+      p.rpart[size_t(blockIdx.x) * p.nrhs + t] = s;
+    }
+  }
 }
 
 template <int LS> static void fill_col(const Op* op, int dag, const ColCoefsHost& h, ColCoef<LS>& c) {
@@ -522,30 +574,32 @@ static int col_pipe_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* r_
   return GB_OK;
 }
 
-template <int LS, bool DAG, int OPA, int OPB>
-static int col_pipe_half_go(Op* op, const ColParams& p, const ColCoef<LS>& c) {
-  constexpr int Q = kColPipeQ, NIN = OPB != COLB_NONE ? 2 : 1;
+template <int LS, bool DAG, int OPA, int OPB, bool RUPD = false>
+static int col_pipe_half_go(Op* op, const ColParams& p, const ColCoef<LS>& c, int* r_parts = nullptr) {
+  constexpr int Q = kColPipeQ, NIN = OPB != COLB_NONE ? 2 : 1, NRING = NIN + (RUPD ? 1 : 0);
   constexpr size_t RAW = size_t(6) * Q * (LS / 2), SLOT = RAW + Q * LS / 4;
   const size_t smem = size_t(NIN) * 12 * Q * col_stride<LS>() * sizeof(float4) +
-                      size_t(kColStages) * NIN * SLOT * sizeof(uint4) + size_t(Q) * LS * sizeof(float);
+                      size_t(kColStages) * NRING * SLOT * sizeof(uint4) + size_t(Q) * LS * sizeof(float);
   static std::atomic<int> per_sm{0};
   static std::atomic<int> sms{0};
   if (per_sm.load() == 0) {
-    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_half_kernel<LS, DAG, OPA, OPB>,
+    GB_CHECK_CUDA(cudaFuncSetAttribute(col_pipe_half_kernel<LS, DAG, OPA, OPB, RUPD>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int n = 0, dev = 0, count = 0;
-    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_half_kernel<LS, DAG, OPA, OPB>, 12 * Q,
-                                                                smem));
+    GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, col_pipe_half_kernel<LS, DAG, OPA, OPB, RUPD>,
+                                                                12 * Q, smem));
     GB_CHECK_CUDA(cudaGetDevice(&dev));
     GB_CHECK_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
     sms.store(count);
     per_sm.store(n > 0 ? n : 1);
   }
   const size_t ntiles = (p.nq + Q - 1) / Q;
-  const size_t slots = size_t(per_sm.load()) * size_t(sms.load());
+  size_t slots = size_t(per_sm.load()) * size_t(sms.load());
+  if (RUPD && slots > size_t(2) * kRedBlocks) slots = size_t(2) * kRedBlocks;  // the partial buffer's [CTA][nrhs]
   const unsigned blocks = unsigned(ntiles < slots ? ntiles : slots);
-  col_pipe_half_kernel<LS, DAG, OPA, OPB><<<blocks, 12 * Q, smem, op->stream>>>(p, c);
+  col_pipe_half_kernel<LS, DAG, OPA, OPB, RUPD><<<blocks, 12 * Q, smem, op->stream>>>(p, c);
   GB_CHECK_CUDA(cudaGetLastError());
+  if (r_parts) *r_parts = RUPD ? int(blocks) : 0;
   return GB_OK;
 }
 
@@ -573,8 +627,10 @@ template <class T, int LS>
 static int col_ls(Op* op, int opa, int opb, int dag, const ColParams& p, const ColCoefsHost& h, int* r_parts) {
   ColCoef<LS> c;
   fill_col<LS>(op, dag, h, c);
-  if (GB_COL_PIPE && sizeof(T) == 4 && p.r && dag && opa == COL_M5D && opb == COLB_M5D)
-    return col_pipe_go<LS, true, COL_M5D, COLB_M5D, true>(op, p, c, r_parts);
+  if (GB_COL_PIPE && p.r && dag && opa == COL_M5D && opb == COLB_M5D) {
+    if (sizeof(T) == 4) return col_pipe_go<LS, true, COL_M5D, COLB_M5D, true>(op, p, c, r_parts);
+    return col_pipe_half_go<LS, true, COL_M5D, COLB_M5D, true>(op, p, c, r_parts);
+  }
   const int key = (dag ? 100 : 0) + opa * 10 + opb;
   switch (key) {
     case 0 + COL_M5D * 10 + COLB_NONE: return col_go<T, LS, false, COL_M5D, COLB_NONE>(op, p, c);
@@ -612,9 +668,10 @@ int launch_col(Op* op, int opa, int opb, int dag, HalfView x, HalfView y, HalfVi
   p.np = op->n5() >> 1;
   p.nq = size_t(op->half4) * op->nrhs;
   p.zc = float(zc);
-  const bool rupd = r_upd && r_parts && x.prec == GB_F32 && r_upd->prec == GB_F32 && kColPipeQ % op->nrhs == 0 &&
-                    dag && opa == COL_M5D && opb == COLB_M5D;
-  p.r = rupd ? static_cast<float4*>(r_upd->data) : nullptr;
+  const bool rupd = r_upd && r_parts && r_upd->prec == x.prec && kColPipeQ % op->nrhs == 0 && dag &&
+                    opa == COL_M5D && opb == COLB_M5D;
+  p.r = rupd ? r_upd->data : nullptr;
+  p.rn = rupd ? r_upd->norms : nullptr;
   p.rpart = rupd ? op->d_partial : nullptr;
   p.cg = op->d_cg;
   p.nrhs = op->nrhs;

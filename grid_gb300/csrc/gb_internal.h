@@ -227,7 +227,7 @@ struct ZCoefsHost {
 enum { ZPROG_M5D = 0, ZPROG_INV = 2, ZPROG_DIAG = 3 };
 bool zmobius_ls_supported(int Ls);
 int launch_zcol(Op* op, int prog, int dag, HalfView x, const HalfView* y, HalfView out, double zc, const ZCoefsHost& h);
-// With r_upd (FP32, nrhs dividing 16, the program MooeeDag - M5Ddag z that ends MpcDag)
+// With r_upd (FP32 or FP16, nrhs dividing 16, the program MooeeDag - M5Ddag z that ends MpcDag)
 // the kernel does not store out: it applies the CG's residual update r -= a out (a per
 // right-hand side from op->d_cg) and writes per-CTA sums of |r|^2 [CTA][nrhs] into
 // op->d_partial, their count into *r_parts (0 when it could not fuse; out is then stored

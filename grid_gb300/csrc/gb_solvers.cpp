@@ -56,9 +56,9 @@ int cg_r_update(Op* op, Field* r, Field* mmp) {
   return launch_cg_beta(op, op->d_partial, P.g * P.halves);
 }
 // One CG matrix step on p: A = MdagM (kind 0) or MpcDagMpc (kind 1) with d = |M p|^2
-// (|Mpc p|^2) -> a, then r -= a A p, cp = |r|^2 -> b.  For a Moebius Schur operator the
-// norm comes from the kernel that stores Mpc p (FP32, FP16), and in FP32 MpcDag's last
-// kernel updates r in place of storing A p (mmp is then not written).
+// (|Mpc p|^2) -> a, then r -= a A p, cp = |r|^2 -> b.  For a FP32 / FP16 Moebius Schur
+// operator the norm comes from the kernel that stores Mpc p, and MpcDag's last kernel
+// updates r in place of storing A p (mmp is then not written).
 int cg_matrix_step(Op* op, int kind, Field* p, Field* mmp, Field* r) {
   int rparts = 0;
   if (kind == 0) {
