@@ -106,7 +106,10 @@ extern "C" int gb_field_norm2_noalloc(gb_field_t f, double* out) {
   int m = 1;
   while (op->L5 * m * 2 <= 256) m *= 2;
   const int B = op->nrhs == 1 ? 256 : op->L5 * m;
-  if (B > 1024) { set_error("norm2 (no allocation): L5 = %d too large", op->L5); return GB_ERR_UNSUPPORTED; }
+  if (B > 256) {  // the kernel's launch bound: blockDim is a multiple of L5
+    set_error("norm2 (no allocation): L5 = %d above 256 is not supported", op->L5);
+    return GB_ERR_UNSUPPORTED;
+  }
   size_t need = (f->n5 + B - 1) / B;
   const int g = int(need < size_t(kNaMaxBlocks) ? (need < 1 ? 1 : need) : size_t(kNaMaxBlocks));
   const size_t smem = size_t(op->nrhs == 1 ? 32 : B) * sizeof(double);

@@ -172,7 +172,8 @@ int gb_field_set_checkerboard(gb_field_t full, gb_field_t half);
  * in a context where allocator calls are forbidden or would stall the device.  The
  * reduction's partial sums go to one static device array of 64.1 KB that every GPU which
  * loads the library keeps until the process exits.  Limit: at most 16 right-hand sides
- * per field (larger fields are rejected with GB_ERR_UNSUPPORTED); any lattice size.
+ * per field, and Ls x right-hand sides at most 256 when there are several (larger fields
+ * are rejected with GB_ERR_UNSUPPORTED); any lattice size.
  * The first call on a device looks up that array's device address (a one-time set-up
  * per device); make that first call before any stream capture.  All calls share the
  * array: calls whose work overlaps on the GPU (other streams or threads) race and must
