@@ -336,7 +336,8 @@ def run_gpu(args, ws, rank, local, dist):
     }
     if ws == 1 and not args.no_extras:
         extras = {}
-        for name, fn in (("wilson_8^4_cg", lambda: extra_wilson_cg(g)),
+        for name, fn in (("cpu_kernels_16^4xLs16", extra_cpu_kernels),
+                         ("wilson_8^4_cg", lambda: extra_wilson_cg(g)),
                          ("cg_schur_24^4xLs12", lambda: extra_cg_schur(g)),
                          ("multi_rhs_wilson_32^3x64", lambda: extra_multi_rhs(g)),
                          ("serving", lambda: extra_serving(g, max_requests=args.serve_requests,
@@ -354,6 +355,28 @@ def run_gpu(args, ws, rank, local, dist):
 # ---------------------------------------------------------------------------------------
 # the other workloads of the path, reported beside the headline (N = 1 only)
 # ---------------------------------------------------------------------------------------
+def extra_cpu_kernels(budget_s=3.0):
+    """The CPU side of the kernel table: the oracle's FP32 Mooee and MooeeInv (one
+    checkerboard of the 16^4 x 16 workload, OpenMP over the host cores) beside the GPU
+    kernels_ms, each repeated for about budget_s; GB/s on the 192 B/site algorithmic bytes."""
+    from oracle import oracle as o
+    threads = o.max_threads()
+    o.set_threads(threads)
+    ref = o.OracleOp(1, 1, DIMS, LS, [MF, M5, B, C], o.random_gauge(DIMS, EPS, 1234), ANTIPERIODIC_T)
+    nh = int(np.prod(DIMS)) // 2 * LS
+    x = o.random_gaussian(nh * 12, 3)
+    out = {"cores": threads, "sample": "oracle/oracle.hpp FP32 (complex128 in and out), one checkerboard"}
+    for name, code in (("Mooee", o.OP_MOOEE), ("MooeeInv", o.OP_MOOEE_INV)):
+        ref.apply(code, x, 1)
+        n, t0 = 0, time.perf_counter()
+        while n < 1 or time.perf_counter() - t0 < budget_s:
+            ref.apply(code, x, 1)
+            n += 1
+        dt = (time.perf_counter() - t0) / n
+        out[name] = {"ms": dt * 1e3, "gbs": nh * 192 / dt / 1e9, "reps": n}
+    return out
+
+
 def extra_cg_schur(g, fp64_maxit=20000):
     """Mixed-precision SchurRedBlack CG on Moebius DWF 24^4 x Ls=12, mf=0.005, gauge eps=0.6,
     to a true residual of 1e-10: FP32 inner, FP16-stored inner (FP32 norms/arithmetic), a
