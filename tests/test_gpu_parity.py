@@ -280,6 +280,28 @@ def test_schur_solve_mobius_fp64(gpu_available):
     assert o.rel_l2(x, xr) < 1e-7
 
 
+def test_cg_converged_guess_reports_the_same_true_residual(gpu_available):
+    """A CG whose guess already meets the tolerance runs no iteration and reports the true
+    residual of the r = b - A x it starts from; it equals, bit for bit, the true residual
+    the converged solve reported after applying A to the same x."""
+    dims, Ls = (4, 4, 4, 8), 8
+    op, ref, U = mobius_pair(dims, Ls, 0.01, g.F64)
+    nh = 256
+    b = op.FermionRedBlackField(1).import_(fermion(nh, Ls, 101))
+    x = op.FermionRedBlackField(1).zero()
+    lin = g.SchurDiagMooeeOperator(op)
+    c1 = g.ConjugateGradient(1e-10, 5000)
+    c1(lin, b, x)
+    assert c1.IterationsToComplete > 0
+    c2 = g.ConjugateGradient(1e-10, 5000)
+    c2(lin, b, x)
+    assert c2.IterationsToComplete == 0
+    assert c2.TrueResidual == c1.TrueResidual
+    got = x.export()
+    bh = fermion(nh, Ls, 101)
+    assert abs(o.rel_l2(ref.apply(o.OP_MPCDAGMPC, got, 1), bh) - c2.TrueResidual) < 1e-3 * c2.TrueResidual
+
+
 @pytest.mark.parametrize("lo", [g.F32, g.F16])
 def test_mixed_precision_schur_reaches_1e10(gpu_available, lo):
     """FP32 (or FP16-stored) inner CG with FP64 reliable updates reaches a true residual
