@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <new>
@@ -517,6 +518,18 @@ int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts, Field* r_upd
       GB_TRY(op_meooe5d(op, in, to, 0));
       GB_TRY(op_dhop_cb(op, to, te1, 0));
       GB_TRY(col_field(op, COL_INV_M5D, COLB_NONE, 0, te1, nullptr, te2, 0.0, meo));
+      // FP32, one right-hand side: the second Dhop ends with Mooee in - (its result) and the
+      // norm, in one launch; otherwise the Dhop and the Mooee kernel run separately
+      std::vector<double> ml, md, mu;
+      coeffs_mooee(op, 0, ml, md, mu);
+      int fused = 0;
+      GB_TRY(launch_dhop_mooee(op, half_view(te2, 0), half_view(in, 0), half_view(out, 0), GB_ODD, ml.data(),
+                               md.data(), mu.data(), &fused));
+      if (fused) {
+        out->subset = GB_ODD;
+        if (norm_parts) *norm_parts = fused;
+        return GB_OK;
+      }
       GB_TRY(op_dhop_cb(op, te2, to, 0));
       return op_mooee(op, in, out, 0, to, -1.0, norm_parts);
     }
@@ -761,7 +774,11 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
     alloc(reinterpret_cast<void**>(&op->nbr[p]), size_t(op->half4) * 8 * sizeof(int));
   }
   alloc(reinterpret_cast<void**>(&op->d_err), sizeof(int));
-  alloc(reinterpret_cast<void**>(&op->d_partial), size_t(2) * kRedBlocks * nrhs * 2 * sizeof(double));
+  // the reductions' [2 halves][kRedBlocks][nrhs][2]; an FP32 Dhop with the Mooee epilogue
+  // (one right-hand side) writes one sum per CTA
+  op->partial_doubles = size_t(2) * kRedBlocks * nrhs * 2;
+  if (op->prec == GB_F32 && nrhs == 1) op->partial_doubles = std::max(op->partial_doubles, dhop_pair_ctas(op));
+  alloc(reinterpret_cast<void**>(&op->d_partial), op->partial_doubles * sizeof(double));
   alloc(reinterpret_cast<void**>(&op->d_result), size_t(nrhs) * 8 * sizeof(double));
   alloc(reinterpret_cast<void**>(&op->d_cg), size_t(nrhs) * sizeof(CGScalars));
   alloc(reinterpret_cast<void**>(&op->d_all_done), 4 * sizeof(int));

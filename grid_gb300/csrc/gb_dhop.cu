@@ -50,6 +50,12 @@ struct DhopParams {
   int sgn[4];     // the (real) boundary phase of each direction
   int parity;     // output checkerboard (parity2 for blockIdx.z == 1)
   int parity2;
+  // MOOEE epilogue (FP32, one right-hand side: the last two steps of Mpc in one launch):
+  // out = M5D x5 - (the Dhop) with the Mooee coefficients, |out|^2 per CTA into dpart
+  const void* x5;
+  double* dpart;
+  int Ls;
+  float md[kMaxLs], ml[kMaxLs], mu[kMaxLs];
 };
 
 // the parameters of this CTA's checkerboard (both parities of a full Dhop run in one grid)
@@ -436,10 +442,50 @@ __device__ __forceinline__ void dhop_pair_step(const DhopParams& p, const int (&
 #define GB_DHOP_THREADS 128
 #endif
 
+// MOOEE epilogue of one thread: out(q) = M5D(x5)(q) - acc with the Mooee coefficients
+// (the same fused multiply-adds as m5d_pair_kernel with its z term, so the result equals the
+// separate Dhop and Mooee launches bit for bit); returns |out(q)|^2 per lane
+// (p: the kernel's __grid_constant__ parameter, so the coefficient arrays are indexed in
+// the parameter bank, not copied to local memory)
+__device__ __forceinline__ float2 dhop_mooee_epilogue(const DhopParams& p, size_t np, size_t q, int sp,
+                                                      const Pair12& acc) {
+  const int hs = p.Ls >> 1;
+  const int s = 2 * sp;                 // one right-hand side: the pair's slots are s, s + 1
+  const size_t qb = q - sp;             // the site's first pair
+  const size_t qprev = sp == 0 ? qb + hs - 1 : q - 1;
+  const size_t qnext = sp == hs - 1 ? qb : q + 1;
+  const float4* x = static_cast<const float4*>(p.x5);
+  float4* o = static_cast<float4*>(p.out);
+  const float2 d = make_float2(p.md[s], p.md[s + 1]);
+  const float2 cl = make_float2(p.ml[s], p.ml[s + 1]);
+  const float2 cu = make_float2(p.mu[s], p.mu[s + 1]);
+  const float2 zc = make_float2(-1.f, -1.f);
+  float2 n2 = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const float4 cur = __ldg(x + size_t(k) * np + q);
+    const float4 nb = __ldg(x + size_t(k) * np + (k < 6 ? qprev : qnext));
+    float2 nr, ni, cc;
+    if (k < 6) {  // P+ components from s - 1: (previous pair's lane 1, this pair's lane 0)
+      nr = make_float2(nb.y, cur.x); ni = make_float2(nb.w, cur.z); cc = cl;
+    } else {      // P- components from s + 1: (this pair's lane 1, next pair's lane 0)
+      nr = make_float2(cur.y, nb.x); ni = make_float2(cur.w, nb.z); cc = cu;
+    }
+    float2 ore = __ffma2_rn(cc, nr, __fmul2_rn(d, make_float2(cur.x, cur.y)));
+    float2 oim = __ffma2_rn(cc, ni, __fmul2_rn(d, make_float2(cur.z, cur.w)));
+    ore = __ffma2_rn(zc, acc.re[k], ore);
+    oim = __ffma2_rn(zc, acc.im[k], oim);
+    o[size_t(k) * np + q] = make_float4(ore.x, ore.y, oim.x, oim.y);
+    n2 = __ffma2_rn(ore, ore, __ffma2_rn(oim, oim, n2));
+  }
+  return n2;
+}
+
 // CTA = k4 4D sites x hc pair threads.  Thread (j, sp) computes the 5D sites
-// (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.
-template <class T, bool DAG, bool RECON>
-__global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kernel(const DhopParams p0) {
+// (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.  MOOEE: the
+// result goes through dhop_mooee_epilogue, and the CTA writes the sum of |out|^2.
+template <class T, bool DAG, bool RECON, bool MOOEE = false>
+__global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kernel(const __grid_constant__ DhopParams p0) {
   const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
   float* slink = reinterpret_cast<float*>(dyn_smem);  // k4 * kLinkStride floats
@@ -485,17 +531,38 @@ __global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kerne
                              slink + (e >> 3) * kLinkStride + (e & 7) * 18);
     __syncthreads();
   }
-  if (!ok || !active) return;
+  if (!ok) return;  // every thread of the CTA sees the same wait result
+  if (!MOOEE && !active) return;
   const size_t np = p.n5 >> 1;
-  const float2* U = reinterpret_cast<const float2*>(slink + j * kLinkStride);
-  Pair12 acc;
-  typename PairIO<T>::Raw buf[GB_DHOP_PF + 1];
+  double nsum = 0.0;  // MOOEE: this thread's |out|^2
+  if (active) {
+    const float2* U = reinterpret_cast<const float2*>(slink + j * kLinkStride);
+    Pair12 acc;
+    typename PairIO<T>::Raw buf[GB_DHOP_PF + 1];
 #pragma unroll
-  for (int i = 0; i < GB_DHOP_PF; i++)
-    PairIO<T>::load_raw(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[kLegOrder[i]]) * hl + sp,
-                        buf[i]);
-  dhop_pair_step<T, DAG, GB_DHOP_PF, 0>(p, nb, sp, np, hl, U, buf, acc);
-  PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
+    for (int i = 0; i < GB_DHOP_PF; i++)
+      PairIO<T>::load_raw(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[kLegOrder[i]]) * hl + sp,
+                          buf[i]);
+    dhop_pair_step<T, DAG, GB_DHOP_PF, 0>(p, nb, sp, np, hl, U, buf, acc);
+    if constexpr (MOOEE) {
+      const float2 n2 = dhop_mooee_epilogue(p0, np, size_t(x0 + j) * hl + sp, sp, acc);
+      nsum = double(n2.x) + double(n2.y);
+    } else {
+      PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
+    }
+  }
+  if constexpr (MOOEE) {  // fixed-order CTA sum: warp shuffles, then the warps in order
+    __shared__ double wsum[GB_DHOP_THREADS / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) nsum += __shfl_down_sync(0xffffffffu, nsum, off);
+    if ((t & 31) == 0) wsum[t >> 5] = nsum;
+    __syncthreads();
+    if (t == 0) {
+      double s = 0.0;
+      for (int w = 0; w < int((blockDim.x + 31) >> 5); w++) s += wsum[w];
+      p.dpart[size_t(blockIdx.y) * gridDim.x + blockIdx.x] = s;
+    }
+  }
 }
 
 // CTA = k4 4D sites x (L5c/2) pair threads, about 128 threads
@@ -508,27 +575,51 @@ static int pick_k4_pair(int hc) {
   return k4 < 1 ? 1 : k4;
 }
 
-template <class T, bool DAG, bool RECON> static int launch_dhop_pair_t(Op* op, DhopParams p) {
-  p.L5c = p.L5 > 256 ? 256 : p.L5;  // even
+// the site-pair kernel's launch shape for a fifth dimension of L5 slots: pairs per CTA
+// chunk (L5c / 2), 4D sites per CTA, CTAs along the sites and the L5 chunks
+struct PairShapeDhop {
+  int L5c, k4, threads;
+  int64_t blocks;
+  unsigned ychunks;
+};
+static PairShapeDhop dhop_pair_shape(int L5, int64_t n4h) {
+  PairShapeDhop s;
+  s.L5c = L5 > 256 ? 256 : L5;  // even
   // A fifth dimension of several 8-pair groups (multi-RHS operators) is split into CTAs of
   // 8 pairs: a warp then covers 4 sites x 8 pairs, whole 128-byte lines of every plane,
   // where 48 slots (3 x 128 B per site) in one CTA would straddle lines
-  if (p.L5 > 16 && p.L5 % 16 == 0) p.L5c = 16;
-  p.k4 = pick_k4_pair(p.L5c / 2);
-  const int threads = (p.L5c / 2) * p.k4;
-  const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
-  const unsigned ychunks = unsigned((p.L5 + p.L5c - 1) / p.L5c);
+  if (L5 > 16 && L5 % 16 == 0) s.L5c = 16;
+  s.k4 = pick_k4_pair(s.L5c / 2);
+  s.threads = (s.L5c / 2) * s.k4;
+  s.blocks = (n4h + s.k4 - 1) / s.k4;
+  s.ychunks = unsigned((L5 + s.L5c - 1) / s.L5c);
+  return s;
+}
+
+size_t dhop_pair_ctas(const Op* op) {
+  const PairShapeDhop s = dhop_pair_shape(op->L5, op->half4);
+  return size_t(s.blocks) * s.ychunks;
+}
+
+template <class T, bool DAG, bool RECON, bool MOOEE = false> static int launch_dhop_pair_t(Op* op, DhopParams p) {
+  const PairShapeDhop s = dhop_pair_shape(p.L5, p.n4h);
+  p.L5c = s.L5c;
+  p.k4 = s.k4;
   const size_t smem = size_t(p.k4) * (kLinkStride + (RECON ? 96 : 0)) * sizeof(float);
   static std::atomic<bool> configured{false};
   if (!configured.load()) {  // up to 64 sites x 976 B with 12-real staging
-    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_pair_kernel<T, DAG, RECON>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       64 * 1024));
+    GB_CHECK_CUDA(cudaFuncSetAttribute(dhop_pair_kernel<T, DAG, RECON, MOOEE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
     configured.store(true);
   }
-  dhop_pair_kernel<T, DAG, RECON><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
+  dhop_pair_kernel<T, DAG, RECON, MOOEE>
+      <<<dim3(unsigned(s.blocks), s.ychunks, p.in2 ? 2u : 1u), dim3(s.threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
+
+static void fill_dhop_params(Op* op, HalfView in, HalfView out, int out_parity, const HalfView* in2,
+                             const HalfView* out2, DhopParams& p);
 
 static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, const HalfView* in2,
                              const HalfView* out2, int dag) {
@@ -545,6 +636,24 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
     return GB_ERR_TIMEOUT;
   }
   DhopParams p;
+  fill_dhop_params(op, in, out, out_parity, in2, out2, p);
+  const int key = (op->prec << 2) | (dag ? 2 : 0) | (op->recon12 ? 1 : 0);
+  switch (key) {
+#define GB_DHOP_CASE(PREC, LAUNCH, T)                                        \
+  case (PREC << 2) | 0: return LAUNCH<T, false, false>(op, p);              \
+  case (PREC << 2) | 1: return LAUNCH<T, false, true>(op, p);               \
+  case (PREC << 2) | 2: return LAUNCH<T, true, false>(op, p);               \
+  case (PREC << 2) | 3: return LAUNCH<T, true, true>(op, p);
+    GB_DHOP_CASE(GB_F64, launch_dhop_t, double)
+    GB_DHOP_CASE(GB_F32, launch_dhop_pair_t, float)
+    GB_DHOP_CASE(GB_F16, launch_dhop_pair_t, __half)
+#undef GB_DHOP_CASE
+  }
+  return GB_ERR_BAD_ARG;
+}
+
+static void fill_dhop_params(Op* op, HalfView in, HalfView out, int out_parity, const HalfView* in2,
+                             const HalfView* out2, DhopParams& p) {
   p.in = in.data;
   p.in_norms = in.norms;
   p.out = out.data;
@@ -571,19 +680,35 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
   }
   p.parity = out_parity;
   p.parity2 = 1 - out_parity;
-  const int key = (op->prec << 2) | (dag ? 2 : 0) | (op->recon12 ? 1 : 0);
-  switch (key) {
-#define GB_DHOP_CASE(PREC, LAUNCH, T)                                        \
-  case (PREC << 2) | 0: return LAUNCH<T, false, false>(op, p);              \
-  case (PREC << 2) | 1: return LAUNCH<T, false, true>(op, p);               \
-  case (PREC << 2) | 2: return LAUNCH<T, true, false>(op, p);               \
-  case (PREC << 2) | 3: return LAUNCH<T, true, true>(op, p);
-    GB_DHOP_CASE(GB_F64, launch_dhop_t, double)
-    GB_DHOP_CASE(GB_F32, launch_dhop_pair_t, float)
-    GB_DHOP_CASE(GB_F16, launch_dhop_pair_t, __half)
-#undef GB_DHOP_CASE
+  p.x5 = nullptr;
+  p.dpart = nullptr;
+  p.Ls = op->Ls;
+}
+
+int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_parity, const double* lower,
+                      const double* diag, const double* upper, int* parts) {
+  *parts = 0;
+  // a 4-RHS variant (per-rhs CTA sums) measured slower than the separate Dhop and Mooee
+  // launches, so several right-hand sides take the separate launches
+  if (op->prec != GB_F32 || in.prec != GB_F32 || x5.prec != GB_F32 || out.prec != GB_F32 || op->nrhs != 1 ||
+      op->L5 != op->Ls || op->Ls > kMaxLs || op->poisoned)
+    return GB_OK;  // not this launch's case: the caller runs the Dhop and Mooee separately
+  const PairShapeDhop s = dhop_pair_shape(op->L5, op->half4);
+  if (s.threads % 32 != 0 || size_t(s.blocks) * s.ychunks > op->partial_doubles) return GB_OK;
+  DhopParams p;
+  fill_dhop_params(op, in, out, out_parity, nullptr, nullptr, p);
+  p.x5 = x5.data;
+  p.dpart = op->d_partial;
+  for (int k = 0; k < op->Ls; k++) {
+    p.md[k] = float(diag[k]);
+    p.ml[k] = float(lower[k]);
+    p.mu[k] = float(upper[k]);
   }
-  return GB_ERR_BAD_ARG;
+  const int rc = op->recon12 ? launch_dhop_pair_t<float, false, true, true>(op, p)
+                             : launch_dhop_pair_t<float, false, false, true>(op, p);
+  if (rc != GB_OK) return rc;
+  *parts = int(size_t(s.blocks) * s.ychunks);
+  return GB_OK;
 }
 
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag) {
