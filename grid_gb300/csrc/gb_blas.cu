@@ -286,11 +286,14 @@ __global__ void cg_init_kernel(CGScalars* cg, const double* ssq, const double* c
   if (r == 0) { flags[0] = (nd == nrhs); flags[1] = 0; }
 }
 
-// sum over b of partial[b * stride + offset] by one CTA of 256 threads in a fixed order
-// (strided per-thread sums, then a tree); every thread gets the result
+// sum over b of partial[b * stride + offset] by one CTA (a power of two, at most 1024
+// threads) in a fixed order (strided per-thread sums, then a tree); every thread gets the
+// result
 __device__ double cta_sum_fixed(const double* partial, int nparts, int stride, int offset) {
-  __shared__ double sm[256];
+  __shared__ double sm[1024];
   double s = 0;
+  // unrolled so that several loads are in flight before the (ordered) adds
+#pragma unroll 8
   for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += partial[size_t(b) * stride + offset];
   sm[threadIdx.x] = s;
   __syncthreads();
@@ -303,9 +306,10 @@ __device__ double cta_sum_fixed(const double* partial, int nparts, int stride, i
   return r;
 }
 
-// launched with 256 threads: the partial sums of every right-hand side are reduced by the
-// whole CTA (a single thread walking thousands of partials would take ~100 us)
-__global__ void __launch_bounds__(256) cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs,
+// launched with 256 threads, 1024 above 2048 partial sums (one per CTA of an FP32 Dhop):
+// the partial sums of every right-hand side are reduced by the whole CTA (a single thread
+// walking thousands of partials would take ~100 us)
+__global__ void __launch_bounds__(1024) cg_alpha_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs,
                                                        int nv) {
   for (int r = 0; r < nrhs; r++) {
     const double d = cta_sum_fixed(partial, nparts, nrhs * nv, r * nv);
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(256) cg_alpha_kernel(CGScalars* cg, const doub
   }
 }
 
-__global__ void __launch_bounds__(256) cg_beta_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs,
+__global__ void __launch_bounds__(1024) cg_beta_kernel(CGScalars* cg, const double* partial, int nparts, int nrhs,
                                                       int* flags) {
   int nd = 0, nr = 0;
   for (int r = 0; r < nrhs; r++) {
@@ -365,8 +369,9 @@ int launch_cg_init(Op* op, const double* d_ssq, const double* d_cp, double tol, 
   return GB_OK;
 }
 // the scalar kernels reduce the per-block partial sums themselves, in a fixed order
+static inline int sum_threads(int nparts) { return nparts > 2048 ? 1024 : 256; }
 int launch_cg_alpha(Op* op, const double* partial, int nparts, int nv) {
-  cg_alpha_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial, nparts, op->nrhs, nv);
+  cg_alpha_kernel<<<1, sum_threads(nparts), 0, op->stream>>>(op->d_cg, partial, nparts, op->nrhs, nv);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -395,7 +400,7 @@ int launch_cg_loop_check(Op* op, cudaGraphConditionalHandle h) {
 }
 
 int launch_cg_beta(Op* op, const double* partial_norm, int nparts) {
-  cg_beta_kernel<<<1, 256, 0, op->stream>>>(op->d_cg, partial_norm, nparts, op->nrhs, op->d_all_done);
+  cg_beta_kernel<<<1, sum_threads(nparts), 0, op->stream>>>(op->d_cg, partial_norm, nparts, op->nrhs, op->d_all_done);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
