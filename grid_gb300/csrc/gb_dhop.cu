@@ -50,11 +50,12 @@ struct DhopParams {
   int sgn[4];     // the (real) boundary phase of each direction
   int parity;     // output checkerboard (parity2 for blockIdx.z == 1)
   int parity2;
-  // MOOEE epilogue (FP32, one right-hand side: the last two steps of Mpc in one launch):
-  // out = M5D x5 - (the Dhop) with the Mooee coefficients, |out|^2 per CTA into dpart
+  // MOOEE epilogue (FP32: the last two steps of Mpc in one launch): out = M5D x5 - (the
+  // Dhop) with the Mooee coefficients, |out|^2 per CTA (and per right-hand side when there
+  // are several: dpart[CTA][nrhs])
   const void* x5;
   double* dpart;
-  int Ls;
+  int Ls, nrhs;
   float md[kMaxLs], ml[kMaxLs], mu[kMaxLs];
 };
 
@@ -444,16 +445,19 @@ __device__ __forceinline__ void dhop_pair_step(const DhopParams& p, const int (&
 
 // MOOEE epilogue of one thread: out(q) = M5D(x5)(q) - acc with the Mooee coefficients
 // (the same fused multiply-adds as m5d_pair_kernel with its z term, so the result equals the
-// separate Dhop and Mooee launches bit for bit); returns |out(q)|^2 per lane
+// separate Dhop and Mooee launches bit for bit); returns |out(q)|^2 per lane.  MODE 1: one
+// right-hand side; 2: several, the s -+ 1 neighbours wrapping inside each rhs block.
 // (p: the kernel's __grid_constant__ parameter, so the coefficient arrays are indexed in
 // the parameter bank, not copied to local memory)
+template <int MODE>
 __device__ __forceinline__ float2 dhop_mooee_epilogue(const DhopParams& p, size_t np, size_t q, int sp,
                                                       const Pair12& acc) {
   const int hs = p.Ls >> 1;
-  const int s = 2 * sp;                 // one right-hand side: the pair's slots are s, s + 1
-  const size_t qb = q - sp;             // the site's first pair
-  const size_t qprev = sp == 0 ? qb + hs - 1 : q - 1;
-  const size_t qnext = sp == hs - 1 ? qb : q + 1;
+  const int psb = MODE == 1 ? sp : sp % hs;  // pair index within the rhs block
+  const int s = 2 * psb;                     // the pair's slots s, s + 1 in its rhs
+  const size_t qb = q - psb;                 // the block's first pair
+  const size_t qprev = psb == 0 ? qb + hs - 1 : q - 1;
+  const size_t qnext = psb == hs - 1 ? qb : q + 1;
   const float4* x = static_cast<const float4*>(p.x5);
   float4* o = static_cast<float4*>(p.out);
   const float2 d = make_float2(p.md[s], p.md[s + 1]);
@@ -482,9 +486,11 @@ __device__ __forceinline__ float2 dhop_mooee_epilogue(const DhopParams& p, size_
 }
 
 // CTA = k4 4D sites x hc pair threads.  Thread (j, sp) computes the 5D sites
-// (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.  MOOEE: the
-// result goes through dhop_mooee_epilogue, and the CTA writes the sum of |out|^2.
-template <class T, bool DAG, bool RECON, bool MOOEE = false>
+// (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.  MOOEE (1: one
+// right-hand side, 2: several, with CTAs over 8-pair chunks that each touch at most two
+// right-hand sides): the result goes through dhop_mooee_epilogue, and the CTA writes the
+// sums of |out|^2, nrhs of them for MOOEE 2 (zero for the right-hand sides it does not touch).
+template <class T, bool DAG, bool RECON, int MOOEE = 0>
 __global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kernel(const __grid_constant__ DhopParams p0) {
   const DhopParams p = dhop_side(p0);
   extern __shared__ __align__(128) unsigned char dyn_smem[];
@@ -544,14 +550,14 @@ __global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kerne
       PairIO<T>::load_raw(p.in, reinterpret_cast<const float2*>(p.in_norms), np, size_t(nb[kLegOrder[i]]) * hl + sp,
                           buf[i]);
     dhop_pair_step<T, DAG, GB_DHOP_PF, 0>(p, nb, sp, np, hl, U, buf, acc);
-    if constexpr (MOOEE) {
-      const float2 n2 = dhop_mooee_epilogue(p0, np, size_t(x0 + j) * hl + sp, sp, acc);
+    if constexpr (MOOEE != 0) {
+      const float2 n2 = dhop_mooee_epilogue<MOOEE>(p0, np, size_t(x0 + j) * hl + sp, sp, acc);
       nsum = double(n2.x) + double(n2.y);
     } else {
       PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
     }
   }
-  if constexpr (MOOEE) {  // fixed-order CTA sum: warp shuffles, then the warps in order
+  if constexpr (MOOEE == 1) {  // fixed-order CTA sum: warp shuffles, then the warps in order
     __shared__ double wsum[GB_DHOP_THREADS / 32];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) nsum += __shfl_down_sync(0xffffffffu, nsum, off);
@@ -561,6 +567,27 @@ __global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kerne
       double s = 0.0;
       for (int w = 0; w < int((blockDim.x + 31) >> 5); w++) s += wsum[w];
       p.dpart[size_t(blockIdx.y) * gridDim.x + blockIdx.x] = s;
+    }
+  }
+  if constexpr (MOOEE == 2) {  // the chunk's first rhs and the next: two fixed-order sums
+    const int rlo = (2 * int(blockIdx.y) * hc) / p.Ls;
+    double lo = 0.0, hi = 0.0;
+    if (active) {
+      if ((2 * sp) / p.Ls == rlo) lo = nsum; else hi = nsum;
+    }
+    __shared__ double wlo[GB_DHOP_THREADS / 32], whi[GB_DHOP_THREADS / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      lo += __shfl_down_sync(0xffffffffu, lo, off);
+      hi += __shfl_down_sync(0xffffffffu, hi, off);
+    }
+    if ((t & 31) == 0) { wlo[t >> 5] = lo; whi[t >> 5] = hi; }
+    __syncthreads();
+    if (t < p.nrhs) {
+      double s = 0.0;
+      if (t == rlo || t == rlo + 1)
+        for (int w = 0; w < int((blockDim.x + 31) >> 5); w++) s += t == rlo ? wlo[w] : whi[w];
+      p.dpart[(size_t(blockIdx.y) * gridDim.x + blockIdx.x) * p.nrhs + t] = s;
     }
   }
 }
@@ -601,7 +628,7 @@ size_t dhop_pair_ctas(const Op* op) {
   return size_t(s.blocks) * s.ychunks;
 }
 
-template <class T, bool DAG, bool RECON, bool MOOEE = false> static int launch_dhop_pair_t(Op* op, DhopParams p) {
+template <class T, bool DAG, bool RECON, int MOOEE = 0> static int launch_dhop_pair_t(Op* op, DhopParams p) {
   const PairShapeDhop s = dhop_pair_shape(p.L5, p.n4h);
   p.L5c = s.L5c;
   p.k4 = s.k4;
@@ -683,18 +710,25 @@ static void fill_dhop_params(Op* op, HalfView in, HalfView out, int out_parity, 
   p.x5 = nullptr;
   p.dpart = nullptr;
   p.Ls = op->Ls;
+  p.nrhs = op->nrhs;
 }
 
 int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_parity, const double* lower,
                       const double* diag, const double* upper, int* parts) {
   *parts = 0;
-  // a 4-RHS variant (per-rhs CTA sums) measured slower than the separate Dhop and Mooee
-  // launches, so several right-hand sides take the separate launches
-  if (op->prec != GB_F32 || in.prec != GB_F32 || x5.prec != GB_F32 || out.prec != GB_F32 || op->nrhs != 1 ||
-      op->L5 != op->Ls || op->Ls > kMaxLs || op->poisoned)
+  if (op->prec != GB_F32 || in.prec != GB_F32 || x5.prec != GB_F32 || out.prec != GB_F32 || op->Ls > kMaxLs ||
+      op->poisoned)
     return GB_OK;  // not this launch's case: the caller runs the Dhop and Mooee separately
   const PairShapeDhop s = dhop_pair_shape(op->L5, op->half4);
-  if (s.threads % 32 != 0 || size_t(s.blocks) * s.ychunks > op->partial_doubles) return GB_OK;
+  int mode = 0;
+  if (op->nrhs == 1 && op->L5 == op->Ls) {
+    mode = 1;
+  } else if (op->nrhs > 1 && s.L5c == 16 && s.ychunks > 1) {  // CTAs over 8-pair chunks
+    mode = 2;
+    for (unsigned c = 0; c < s.ychunks; c++)  // each chunk's 16 slots in at most two rhs blocks
+      if ((16 * int(c) + 15) / op->Ls - (16 * int(c)) / op->Ls > 1) mode = 0;
+  }
+  if (mode == 0 || s.threads % 32 != 0 || size_t(s.blocks) * s.ychunks * op->nrhs > op->partial_doubles) return GB_OK;
   DhopParams p;
   fill_dhop_params(op, in, out, out_parity, nullptr, nullptr, p);
   p.x5 = x5.data;
@@ -704,8 +738,11 @@ int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_pa
     p.ml[k] = float(lower[k]);
     p.mu[k] = float(upper[k]);
   }
-  const int rc = op->recon12 ? launch_dhop_pair_t<float, false, true, true>(op, p)
-                             : launch_dhop_pair_t<float, false, false, true>(op, p);
+  int rc;
+  if (mode == 1)
+    rc = op->recon12 ? launch_dhop_pair_t<float, false, true, 1>(op, p) : launch_dhop_pair_t<float, false, false, 1>(op, p);
+  else
+    rc = op->recon12 ? launch_dhop_pair_t<float, false, true, 2>(op, p) : launch_dhop_pair_t<float, false, false, 2>(op, p);
   if (rc != GB_OK) return rc;
   *parts = int(size_t(s.blocks) * s.ychunks);
   return GB_OK;

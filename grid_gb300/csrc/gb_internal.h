@@ -98,7 +98,7 @@ struct Op {
 
   // reduction scratch
   double* d_partial = nullptr;  // per-CTA partial sums, partial_doubles of them
-  size_t partial_doubles = 0;    // 4 kRedBlocks nrhs, or a single-checkerboard Dhop's CTAs if more
+  size_t partial_doubles = 0;    // 4 kRedBlocks nrhs, or a single-checkerboard Dhop's CTAs x nrhs if more
   double* d_result = nullptr;   // nrhs * 4
   double* h_result = nullptr;   // pinned, nrhs * 4
   // canonical FP64 staging buffer for import/export (device)
@@ -169,10 +169,11 @@ struct HalfView {
 inline HalfView half_view(const Field* f, int parity) { return HalfView{f->half_ptr(parity), f->half_norms(parity), f->prec}; }
 
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag);
-// FP32, one right-hand side (L5 = Ls): out = M5D(x5) - DhopEO/OE(in) in one launch (M5D
-// with the given coefficients: Mooee for the end of Mpc), |out|^2 per CTA into
-// op->d_partial ([CTA], the norm partials' layout) and the CTA count into *parts.  When the
-// operator is not such a case it launches nothing and sets *parts = 0.
+// FP32: out = M5D(x5) - DhopEO/OE(in) in one launch (M5D with the given coefficients:
+// Mooee for the end of Mpc), |out|^2 per CTA and right-hand side into op->d_partial
+// ([CTA][nrhs], the norm partials' layout) and the CTA count into *parts.  Cases: one
+// right-hand side, or several whose Dhop CTAs run 8-pair chunks of at most two right-hand
+// sides each.  Otherwise it launches nothing and sets *parts = 0.
 int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_parity, const double* lower,
                       const double* diag, const double* upper, int* parts);
 // CTAs of one single-checkerboard launch of the FP32 / FP16 Dhop kernel
