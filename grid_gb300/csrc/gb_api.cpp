@@ -774,10 +774,11 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
     alloc(reinterpret_cast<void**>(&op->nbr[p]), size_t(op->half4) * 8 * sizeof(int));
   }
   alloc(reinterpret_cast<void**>(&op->d_err), sizeof(int));
-  // the reductions' [2 halves][kRedBlocks][nrhs][2]; an FP32 Dhop with the Mooee epilogue
-  // writes nrhs sums per CTA
+  // the reductions' [2 halves][kRedBlocks][nrhs][2]; an FP32 Moebius Dhop with the Mooee
+  // epilogue writes nrhs sums per CTA
   op->partial_doubles = size_t(2) * kRedBlocks * nrhs * 2;
-  if (op->prec == GB_F32) op->partial_doubles = std::max(op->partial_doubles, dhop_pair_ctas(op) * nrhs);
+  if (op->prec == GB_F32 && op->kind == 1)
+    op->partial_doubles = std::max(op->partial_doubles, dhop_pair_ctas(op) * nrhs);
   alloc(reinterpret_cast<void**>(&op->d_partial), op->partial_doubles * sizeof(double));
   alloc(reinterpret_cast<void**>(&op->d_result), size_t(nrhs) * 8 * sizeof(double));
   alloc(reinterpret_cast<void**>(&op->d_cg), size_t(nrhs) * sizeof(CGScalars));
