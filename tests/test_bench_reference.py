@@ -44,3 +44,15 @@ def test_reference_arm_loads_no_product_library():
     run = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert run.returncode == 0, run.stderr[-2000:]
     assert "clean" in run.stdout
+
+
+def test_cpu_kernel_table_times_the_oracle_only():
+    """The bench's CPU kernel table (Mooee, MooeeInv of the 16^4 x 16 workload on the host
+    cores) runs the oracle's FP32 loops and reports positive times and GB/s."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    out = bench.extra_cpu_kernels(budget_s=0.05)
+    assert out["cores"] >= 1
+    for name in ("Mooee", "MooeeInv"):
+        assert out[name]["reps"] >= 1 and out[name]["ms"] > 0 and out[name]["gbs"] > 0
