@@ -518,8 +518,9 @@ int op_mpc(Op* op, Field* in, Field* out, int dag, int* norm_parts, Field* r_upd
       GB_TRY(op_meooe5d(op, in, to, 0));
       GB_TRY(op_dhop_cb(op, to, te1, 0));
       GB_TRY(col_field(op, COL_INV_M5D, COLB_NONE, 0, te1, nullptr, te2, 0.0, meo));
-      // FP32, one right-hand side: the second Dhop ends with Mooee in - (its result) and the
-      // norm, in one launch; otherwise the Dhop and the Mooee kernel run separately
+      // FP32 / FP16 (one right-hand side, or 16-slot column blocks of two rhs at most): the
+      // second Dhop ends with Mooee in - (its result) and the norm, in one launch; otherwise
+      // the Dhop and the Mooee kernel run separately
       std::vector<double> ml, md, mu;
       coeffs_mooee(op, 0, ml, md, mu);
       int fused = 0;
@@ -777,7 +778,7 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
   // the reductions' [2 halves][kRedBlocks][nrhs][2]; an FP32 Moebius Dhop with the Mooee
   // epilogue writes nrhs sums per CTA
   op->partial_doubles = size_t(2) * kRedBlocks * nrhs * 2;
-  if (op->prec == GB_F32 && op->kind == 1)
+  if (op->prec != GB_F64 && op->kind == 1)
     op->partial_doubles = std::max(op->partial_doubles, dhop_pair_ctas(op) * nrhs);
   alloc(reinterpret_cast<void**>(&op->d_partial), op->partial_doubles * sizeof(double));
   alloc(reinterpret_cast<void**>(&op->d_result), size_t(nrhs) * 8 * sizeof(double));

@@ -54,6 +54,7 @@ struct DhopParams {
   // Dhop) with the Mooee coefficients, |out|^2 per CTA (and per right-hand side when there
   // are several: dpart[CTA][nrhs])
   const void* x5;
+  const float* x5_norms;  // FP16: the per-5D-site norms of x5
   double* dpart;
   int Ls, nrhs;
   float md[kMaxLs], ml[kMaxLs], mu[kMaxLs];
@@ -485,6 +486,53 @@ __device__ __forceinline__ float2 dhop_mooee_epilogue(const DhopParams& p, size_
   return n2;
 }
 
+// The same for FP16 storage: x5 is decoded with its site norms (as the Mooee kernel decodes
+// it), out = M5D(x5) - acc is formed in place of acc two components at a time and stored
+// through the FP16 encoder; returns |out|^2 as stored.  Unlike the separate launches, the
+// Dhop result is not rounded to FP16 before the subtraction.
+template <int MODE>
+__device__ __forceinline__ float2 dhop_mooee_epilogue_half(const DhopParams& p, size_t np, size_t q, int sp,
+                                                           Pair12& acc) {
+  const int hs = p.Ls >> 1;
+  const int psb = MODE == 1 ? sp : sp % hs;
+  const int s = 2 * psb;
+  const size_t qb = q - psb;
+  const size_t qprev = psb == 0 ? qb + hs - 1 : q - 1;
+  const size_t qnext = psb == hs - 1 ? qb : q + 1;
+  const uint4* x = static_cast<const uint4*>(p.x5);
+  const float2* xn = reinterpret_cast<const float2*>(p.x5_norms);
+  const float2 ncur = __ldg(xn + q), nprv = __ldg(xn + qprev), nnxt = __ldg(xn + qnext);
+  const float2 d = make_float2(p.md[s], p.md[s + 1]);
+  const float2 cl = make_float2(p.ml[s], p.ml[s + 1]);
+  const float2 cu = make_float2(p.mu[s], p.mu[s + 1]);
+  const float2 zc = make_float2(-1.f, -1.f);
+#pragma unroll
+  for (int g = 0; g < 6; g++) {
+    const uint4 vc = __ldg(x + size_t(g) * np + q);
+    const uint4 vb = __ldg(x + size_t(g) * np + (g < 3 ? qprev : qnext));
+    const __half2* hc = reinterpret_cast<const __half2*>(&vc);
+    const __half2* hb = reinterpret_cast<const __half2*>(&vb);
+    const float2 nb = g < 3 ? nprv : nnxt;
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int k = 2 * g + e;
+      const float2 cre = __fmul2_rn(__half22float2(hc[2 * e]), ncur), cim = __fmul2_rn(__half22float2(hc[2 * e + 1]), ncur);
+      const float2 bre = __fmul2_rn(__half22float2(hb[2 * e]), nb), bim = __fmul2_rn(__half22float2(hb[2 * e + 1]), nb);
+      float2 nr, ni, cc;
+      if (k < 6) {  // P+ from s - 1: (previous pair's lane 1, this pair's lane 0)
+        nr = make_float2(bre.y, cre.x); ni = make_float2(bim.y, cim.x); cc = cl;
+      } else {      // P- from s + 1: (this pair's lane 1, next pair's lane 0)
+        nr = make_float2(cre.y, bre.x); ni = make_float2(cim.y, bim.x); cc = cu;
+      }
+      const float2 ore = __ffma2_rn(cc, nr, __fmul2_rn(d, cre));
+      const float2 oim = __ffma2_rn(cc, ni, __fmul2_rn(d, cim));
+      acc.re[k] = __ffma2_rn(zc, acc.re[k], ore);
+      acc.im[k] = __ffma2_rn(zc, acc.im[k], oim);
+    }
+  }
+  return PairIO<__half>::store_n2(p.out, reinterpret_cast<float2*>(p.out_norms), np, q, acc);
+}
+
 // CTA = k4 4D sites x hc pair threads.  Thread (j, sp) computes the 5D sites
 // (2 sp, 2 sp + 1) of 4D site x0 + j: eight legs, +mu and -mu back to back.  MOOEE (1: one
 // right-hand side, 2: several, with CTAs over 8-pair chunks that each touch at most two
@@ -551,7 +599,9 @@ __global__ void __launch_bounds__(GB_DHOP_THREADS, GB_DHOP_MINB) dhop_pair_kerne
                           buf[i]);
     dhop_pair_step<T, DAG, GB_DHOP_PF, 0>(p, nb, sp, np, hl, U, buf, acc);
     if constexpr (MOOEE != 0) {
-      const float2 n2 = dhop_mooee_epilogue<MOOEE>(p0, np, size_t(x0 + j) * hl + sp, sp, acc);
+      float2 n2;
+      if constexpr (sizeof(T) == 4) n2 = dhop_mooee_epilogue<MOOEE>(p0, np, size_t(x0 + j) * hl + sp, sp, acc);
+      else n2 = dhop_mooee_epilogue_half<MOOEE>(p0, np, size_t(x0 + j) * hl + sp, sp, acc);
       nsum = double(n2.x) + double(n2.y);
     } else {
       PairIO<T>::store(p.out, reinterpret_cast<float2*>(p.out_norms), np, size_t(x0 + j) * hl + sp, acc);
@@ -708,6 +758,7 @@ static void fill_dhop_params(Op* op, HalfView in, HalfView out, int out_parity, 
   p.parity = out_parity;
   p.parity2 = 1 - out_parity;
   p.x5 = nullptr;
+  p.x5_norms = nullptr;
   p.dpart = nullptr;
   p.Ls = op->Ls;
   p.nrhs = op->nrhs;
@@ -716,8 +767,8 @@ static void fill_dhop_params(Op* op, HalfView in, HalfView out, int out_parity, 
 int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_parity, const double* lower,
                       const double* diag, const double* upper, int* parts) {
   *parts = 0;
-  if (op->prec != GB_F32 || in.prec != GB_F32 || x5.prec != GB_F32 || out.prec != GB_F32 || op->Ls > kMaxLs ||
-      op->poisoned)
+  if ((op->prec != GB_F32 && op->prec != GB_F16) || in.prec != op->prec || x5.prec != op->prec ||
+      out.prec != op->prec || op->Ls > kMaxLs || op->poisoned)
     return GB_OK;  // not this launch's case: the caller runs the Dhop and Mooee separately
   const PairShapeDhop s = dhop_pair_shape(op->L5, op->half4);
   int mode = 0;
@@ -732,6 +783,7 @@ int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_pa
   DhopParams p;
   fill_dhop_params(op, in, out, out_parity, nullptr, nullptr, p);
   p.x5 = x5.data;
+  p.x5_norms = x5.norms;
   p.dpart = op->d_partial;
   for (int k = 0; k < op->Ls; k++) {
     p.md[k] = float(diag[k]);
@@ -739,10 +791,17 @@ int launch_dhop_mooee(Op* op, HalfView in, HalfView x5, HalfView out, int out_pa
     p.mu[k] = float(upper[k]);
   }
   int rc;
-  if (mode == 1)
-    rc = op->recon12 ? launch_dhop_pair_t<float, false, true, 1>(op, p) : launch_dhop_pair_t<float, false, false, 1>(op, p);
-  else
-    rc = op->recon12 ? launch_dhop_pair_t<float, false, true, 2>(op, p) : launch_dhop_pair_t<float, false, false, 2>(op, p);
+  if (op->prec == GB_F32) {
+    if (mode == 1)
+      rc = op->recon12 ? launch_dhop_pair_t<float, false, true, 1>(op, p) : launch_dhop_pair_t<float, false, false, 1>(op, p);
+    else
+      rc = op->recon12 ? launch_dhop_pair_t<float, false, true, 2>(op, p) : launch_dhop_pair_t<float, false, false, 2>(op, p);
+  } else {
+    if (mode == 1)
+      rc = op->recon12 ? launch_dhop_pair_t<__half, false, true, 1>(op, p) : launch_dhop_pair_t<__half, false, false, 1>(op, p);
+    else
+      rc = op->recon12 ? launch_dhop_pair_t<__half, false, true, 2>(op, p) : launch_dhop_pair_t<__half, false, false, 2>(op, p);
+  }
   if (rc != GB_OK) return rc;
   *parts = int(size_t(s.blocks) * s.ychunks);
   return GB_OK;

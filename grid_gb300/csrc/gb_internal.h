@@ -169,7 +169,7 @@ struct HalfView {
 inline HalfView half_view(const Field* f, int parity) { return HalfView{f->half_ptr(parity), f->half_norms(parity), f->prec}; }
 
 int launch_dhop(Op* op, HalfView in, HalfView out, int out_parity, int dag);
-// FP32: out = M5D(x5) - DhopEO/OE(in) in one launch (M5D with the given coefficients:
+// FP32 / FP16: out = M5D(x5) - DhopEO/OE(in) in one launch (M5D with the given coefficients:
 // Mooee for the end of Mpc), |out|^2 per CTA and right-hand side into op->d_partial
 // ([CTA][nrhs], the norm partials' layout) and the CTA count into *parts.  Cases: one
 // right-hand side, or several whose Dhop CTAs run 8-pair chunks of at most two right-hand
