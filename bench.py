@@ -380,7 +380,8 @@ def extra_cpu_kernels(budget_s=3.0):
 def extra_cg_schur(g, fp64_maxit=20000):
     """Mixed-precision SchurRedBlack CG on Moebius DWF 24^4 x Ls=12, mf=0.005, gauge eps=0.6,
     to a true residual of 1e-10: FP32 inner, FP16-stored inner (FP32 norms/arithmetic), a
-    4-RHS batched mixed solve, and the plain FP64 CG.  Reliable updates every 100
+    4-RHS batched mixed solve, and the plain FP64 CG; the FP32 mixed solve and the FP64 CG
+    again with the FP64 hopping term in double-float arithmetic (GB_FLAG_DF64).  Reliable updates every 100
     iterations or when |r|^2 drops by 1e-6 (|r| by 1e-3).  Every solve captures its
     iteration chunks as CUDA graphs (use_graphs=1)."""
     dims, Ls, mf = (24, 24, 24, 24), 12, 0.005
@@ -388,8 +389,8 @@ def extra_cg_schur(g, fp64_maxit=20000):
     vol = int(np.prod(dims))
     out = {"workload": "mobius_dwf_24^4xLs12_mf0.005_schur_cg_1e-10"}
 
-    def solve(inner, nrhs, seed, graphs=1):
-        od = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=g.F64, nrhs=nrhs)
+    def solve(inner, nrhs, seed, graphs=1, outer_flags=0):
+        od = g.MobiusFermion(U, dims, Ls, mf, M5, B, C, precision=g.F64, nrhs=nrhs, flags=outer_flags)
         src = g.random_gaussian(vol * Ls * 12 * nrhs, seed)
         fs = od.FermionField().import_(src)
         fx = od.FermionField().zero()
@@ -447,12 +448,23 @@ def extra_cg_schur(g, fp64_maxit=20000):
 
     m32, x32 = solve(g.F32, 1, 77)
     m32_loop, _ = solve(g.F32, 1, 77, graphs=2)  # the CG loop on the device (conditional graph node)
+    # the FP64 operator with its hopping term in double-float arithmetic (GB_FLAG_DF64):
+    # as the outer operator of the mixed solve, and for the whole FP64 CG
+    try:
+        m32_df, x32_df = solve(g.F32, 1, 77, outer_flags=g.DF64)
+        f64_df, x64_df = solve(None, 1, 77, outer_flags=g.DF64)
+    except Exception as e:  # reported, the other solves still run
+        m32_df = f64_df = {"error": f"{type(e).__name__}: {e}"}
+        x32_df = x64_df = None
     m16, x16 = solve(g.F16, 1, 77)
     mb, _ = solve(g.F32, 4, 78)
     f64, x64 = solve(None, 1, 77)
     from oracle import oracle as o
     m32["solution_rel_err_vs_fp64"] = o.rel_l2(x32, x64)
     m16["solution_rel_err_vs_fp64"] = o.rel_l2(x16, x64)
+    if x32_df is not None:
+        m32_df["solution_rel_err_vs_fp64"] = o.rel_l2(x32_df, x64)
+        f64_df["solution_rel_err_vs_fp64"] = o.rel_l2(x64_df, x64)
     # bounded CPU baseline: one FP64 MpcDagMpc of the oracle on the host cores, times the
     # FP64 iteration count
     ref = o.OracleOp(1, 0, dims, Ls, [mf, M5, B, C], U, g.antiperiodic_t())
@@ -466,6 +478,7 @@ def extra_cg_schur(g, fp64_maxit=20000):
                          "sample": "one FP64 MpcDagMpc of the 24^4 x 12 operator, scaled by the FP64 CG iterations"}
     out["mixed_fp32_restarted"] = solve_restart(77)
     out.update({"mixed_fp32": m32, "mixed_fp32_device_loop": m32_loop, "mixed_fp16": m16, "mixed_fp32_batched4": mb, "fp64": f64,
+                "mixed_fp32_df64_outer": m32_df, "fp64_df64": f64_df,
                 "speedup_mixed_vs_fp64": m32["solves_per_s"] / f64["solves_per_s"],
                 "speedup_mixed_batched_vs_fp64": mb["solves_per_s"] / f64["solves_per_s"]})
     return out

@@ -6,7 +6,7 @@ operator and solver classes over that ABI.  Importing the package loads the libr
 raises if it has not been built: there is no CPU fallback.
 """
 from .api import (  # noqa: F401
-    GridError, lib, LIB_PATH, F64, F32, F16, RECON12, EVEN, ODD, FULL, DaggerNo, DaggerYes,
+    GridError, lib, LIB_PATH, F64, F32, F16, RECON12, DF64, EVEN, ODD, FULL, DaggerNo, DaggerYes,
     FermionField, WilsonFermion, MobiusFermion, ZMobiusFermion, MobiusZolotarevFermion, ShamirZolotarevFermion,
     ScaledShamirFermion, zolotarev, higham, computeZmobiusGamma, WilsonTMFermion5D, FourierAcceleratedPV,
     PauliVillarsSolverFourierAccel, dft_s, copy_slice5, chiral_scale, MdagMLinearOperator, SchurDiagMooeeOperator,

@@ -27,6 +27,7 @@ LIB_PATH = Path(__file__).resolve().with_name("libgbdwf.so")
 
 F64, F32, F16 = 0, 1, 2
 RECON12 = 1  # gb_*_create flag GB_FLAG_RECON12: 12-real links
+DF64 = 2  # gb_*_create flag GB_FLAG_DF64: FP64 hopping term in double-float arithmetic
 EVEN, ODD, FULL = 0, 1, 2
 DaggerNo, DaggerYes = 0, 1
 

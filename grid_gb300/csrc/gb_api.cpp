@@ -763,6 +763,12 @@ static int op_create(int kind, const int dims[4], int Ls, double mass, double M5
     set_error("12-real links need real boundary phases (+1 or -1)");
     return GB_ERR_UNSUPPORTED;
   }
+  if ((flags & GB_FLAG_DF64) && (precision != GB_F64 || op->recon12)) {
+    delete op;
+    set_error("double-float arithmetic is for FP64 operators with 18-real links");
+    return GB_ERR_UNSUPPORTED;
+  }
+  op->df64 = (flags & GB_FLAG_DF64) != 0;
   if (kind == 1) cayley_setup(op);
   keep_pool_memory(op->device);
   int rc = GB_OK;

@@ -5,6 +5,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "gb_df64.cuh"
 #include "gb_internal.h"
 
 namespace gb {
@@ -45,6 +46,27 @@ template <> struct SpinorIO<double> {
     double2* p = static_cast<double2*>(base);
 #pragma unroll
     for (int k = 0; k < 12; k++) p[size_t(k) * n5 + i] = make_double2(f.re[k], f.im[k]);
+  }
+};
+
+// FP64 storage with double-float arithmetic (the hopping term of operators created with
+// GB_FLAG_DF64): the FP64 planes, each double split into (hi, lo) floats on load and
+// hi + lo rounded back to a double on store.
+struct DF64 {};
+template <> struct SpinorIO<DF64> {
+  static __device__ __forceinline__ void load(const void* base, const float*, size_t n5, size_t i, Spinor<dfloat>& f) {
+    const double2* p = static_cast<const double2*>(base);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const double2 v = __ldg(p + size_t(k) * n5 + i);
+      f.re[k] = df::split(v.x);
+      f.im[k] = df::split(v.y);
+    }
+  }
+  static __device__ __forceinline__ void store(void* base, float*, size_t n5, size_t i, const Spinor<dfloat>& f) {
+    double2* p = static_cast<double2*>(base);
+#pragma unroll
+    for (int k = 0; k < 12; k++) p[size_t(k) * n5 + i] = make_double2(df::to_double(f.re[k]), df::to_double(f.im[k]));
   }
 };
 
@@ -318,6 +340,7 @@ template <> struct PairIO<__half> {
 // arithmetic type for a storage type
 template <class T> struct Arith { using type = T; };
 template <> struct Arith<__half> { using type = float; };
+template <> struct Arith<DF64> { using type = dfloat; };
 
 // ---------------------------------------------------------------------------------------
 // TMA bulk copy global -> shared with an mbarrier and a bounded wait.

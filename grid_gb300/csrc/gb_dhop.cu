@@ -19,6 +19,7 @@
 #include <cuda_fp16.h>
 
 #include <atomic>
+#include <type_traits>
 
 #include "gb_device.cuh"
 
@@ -184,6 +185,36 @@ __device__ __forceinline__ void su3_mul(const R* __restrict__ U, const R (&hr)[6
   }
 }
 
+// The same product in double-float arithmetic: each real output is one Dot2 of six
+// products (the link's real and imaginary parts against the two-spinor's).
+template <>
+__device__ __forceinline__ void su3_mul<dfloat>(const dfloat* __restrict__ U, const dfloat (&hr)[6],
+                                                const dfloat (&hi)[6], dfloat (&ur)[6], dfloat (&ui)[6]) {
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int sp = 0; sp < 2; sp++) {
+      const int o = sp * 3;
+      DfDot xr, xi;
+#pragma unroll
+      for (int b = 0; b < 3; b++) {
+        const dfloat vr = U[(a * 3 + b) * 2], vi = U[(a * 3 + b) * 2 + 1];
+        if (b == 0) {
+          xr.first(vr, hr[o]);
+          xi.first(vr, hi[o]);
+        } else {
+          xr.mac(vr, hr[o + b]);
+          xi.mac(vr, hi[o + b]);
+        }
+        xr.mac(-vi, hi[o + b]);
+        xi.mac(vi, hr[o + b]);
+      }
+      ur[o + a] = xr.result();
+      ui[o + a] = xi.result();
+    }
+  }
+}
+
 template <class T, bool DAG, int LEG>
 __device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8], int s, const typename Arith<T>::type* U,
                                          Spinor<typename Arith<T>::type>& acc) {
@@ -199,7 +230,7 @@ __device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8]
 }
 
 template <class T, bool DAG, bool RECON>
-__global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
+__device__ __forceinline__ void dhop_body(const DhopParams& p0) {
   const DhopParams p = dhop_side(p0);
   using R = typename Arith<T>::type;
   extern __shared__ __align__(128) unsigned char dyn_smem[];
@@ -232,7 +263,14 @@ __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
   }
   const bool ok = mbar_wait_bounded(&bar, 0);
   if (!ok) atomicExch(p.err, 1);
-  if (RECON) {
+  if constexpr (std::is_same<T, DF64>::value) {
+    // the staged doubles become (hi, lo) pairs in place (the same 8 bytes)
+    static_assert(!RECON && sizeof(R) == sizeof(double), "double-float links: 18 reals, 8 bytes each");
+    if (ok)
+      for (int e = t; e < nsite * 144; e += blockDim.x) sU[e] = df::split(reinterpret_cast<const double*>(sU)[e]);
+    __syncthreads();
+  }
+  if constexpr (RECON) {
     if (ok)
       for (int e = t; e < nsite * 8; e += blockDim.x)
         expand_link12<R>(p, x0 + (e >> 3), e & 7, sraw + (e >> 3) * 96 + (e & 7) * 12, sU + (e >> 3) * 144 + (e & 7) * 18);
@@ -258,6 +296,18 @@ __global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
   }
 }
 
+template <class T, bool DAG, bool RECON>
+__global__ void __launch_bounds__(256) dhop_kernel(const DhopParams p0) {
+  dhop_body<T, DAG, RECON>(p0);
+}
+
+// double-float arithmetic: two CTAs of 256 threads per SM (128 registers at most) keep
+// enough warps to cover the dependent float chains
+template <bool DAG>
+__global__ void __launch_bounds__(256, 2) dhop_df64_kernel(const DhopParams p0) {
+  dhop_body<DF64, DAG, false>(p0);
+}
+
 // 4D sites per CTA: L5 * k4 threads, about 256, at most 40 KB of staged links, and a
 // multiple of 32 threads where possible
 static int pick_k4(int L5, size_t link_bytes_per_site) {
@@ -277,13 +327,15 @@ template <class T, bool DAG, bool RECON> static int launch_dhop_t(Op* op, const 
   const int64_t blocks = (p.n4h + p.k4 - 1) / p.k4;
   const unsigned ychunks = unsigned((p.L5a + p.L5c - 1) / p.L5c);
   const size_t smem = size_t(p.k4) * (RECON ? 240 : 144) * sizeof(R);
+  void (*kernel)(const DhopParams);
+  if constexpr (std::is_same<T, DF64>::value) kernel = dhop_df64_kernel<DAG>;
+  else kernel = dhop_kernel<T, DAG, RECON>;
   static std::atomic<bool> configured{false};
   if (!configured.load()) {
-    GB_CHECK_CUDA(
-        cudaFuncSetAttribute(dhop_kernel<T, DAG, RECON>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    GB_CHECK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     configured.store(true);
   }
-  dhop_kernel<T, DAG, RECON><<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
+  kernel<<<dim3(unsigned(blocks), ychunks, p.in2 ? 2u : 1u), dim3(threads), smem, op->stream>>>(p);
   GB_CHECK_CUDA(cudaGetLastError());
   return GB_OK;
 }
@@ -714,6 +766,8 @@ static int launch_dhop_sides(Op* op, HalfView in, HalfView out, int out_parity, 
   }
   DhopParams p;
   fill_dhop_params(op, in, out, out_parity, in2, out2, p);
+  if (op->df64)  // FP64 fields, double-float arithmetic (18-real links only)
+    return dag ? launch_dhop_t<DF64, true, false>(op, p) : launch_dhop_t<DF64, false, false>(op, p);
   const int key = (op->prec << 2) | (dag ? 2 : 0) | (op->recon12 ? 1 : 0);
   switch (key) {
 #define GB_DHOP_CASE(PREC, LAUNCH, T)                                        \

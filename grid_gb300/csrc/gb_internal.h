@@ -72,6 +72,7 @@ struct Op {
   bool phases_pm1 = true;  // every phase is +1 or -1 (12-real reconstruction allowed)
   unsigned flags = 0;
   bool recon12 = false;
+  bool df64 = false;     // FP64: the hopping term in double-float arithmetic (GB_FLAG_DF64)
   cudaStream_t stream = nullptr;
   int device = 0;
   bool gauge_loaded = false;

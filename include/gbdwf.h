@@ -72,8 +72,14 @@ int gb_device_count(int* n);
  * flags: GB_FLAG_RECON12 = store the doubled links as 12 reals (rows 0, 1) and rebuild
  * row 2 in the Dhop kernel (the optional 12-real reconstruction); needs real boundary
  * phases (+1 / -1), else GB_ERR_UNSUPPORTED.
+ * GB_FLAG_DF64 (GB_F64 operators with 18-real links, else GB_ERR_UNSUPPORTED): the hopping
+ * term computes in double-float arithmetic (pairs of floats, about 48 significant bits:
+ * relative L2 error near 5e-15 per application) on the FP32 pipes instead of the FP64
+ * pipe, which on GB300 runs at 1/64 of the FP32 rate; fields stay FP64.  Every other
+ * FP64 kernel is unchanged.
  */
 #define GB_FLAG_RECON12 1u
+#define GB_FLAG_DF64 2u
 int gb_wilson_create(const int dims[4], double mass, const double* phases, int precision, int nrhs, void* stream,
                      unsigned flags, gb_op_t* out);
 int gb_mobius_create(const int dims[4], int Ls, double mf, double M5, double b, double c, const double* phases,

@@ -9,8 +9,9 @@ answer y holds |y|^2, four inner products <w_k, y> and sixteen entries; a result
 rel_l2(y', y) <= tol satisfies
   | |y'|^2 - |y|^2 | <= (2 tol + tol^2) |y|^2,  |<w, y'> - <w, y>| <= tol |w| |y|,
   |y'_i - y_i| <= tol |y|,
-and those are the checks.  Tolerances (relative L2): FP64 1e-13, FP32 1e-6 for Wilson and
-Moebius, ten times that for ZMobius; the Schur solution 1e-8 (solved to 1e-12)."""
+and those are the checks.  Tolerances (relative L2): FP64 1e-13 (native, and with the
+double-float hopping term of GB_FLAG_DF64), FP32 1e-6 for Wilson and Moebius, ten times
+that for ZMobius; the Schur solution 1e-8 (solved to 1e-12)."""
 import json
 from pathlib import Path
 
@@ -71,18 +72,18 @@ def test_oracle_reproduces_known_answers():
         check_functionals(s_got, s_ans, 1e-8, (case["name"], "schur_solve"), mk.o.random_gaussian)
 
 
-def make_op(case, prec):
+def make_op(case, prec, flags=0):
     dims = case["dims"]
     U = g.random_gauge(dims, case["gauge"]["eps"], case["gauge"]["seed"])
     ph = np.asarray(GOLDEN["phases"], dtype=np.float64)
     if case["kind"] == "wilson":
-        return g.WilsonFermion(U, dims, case["mass"], phases=ph, precision=prec)
+        return g.WilsonFermion(U, dims, case["mass"], phases=ph, precision=prec, flags=flags)
     if case["kind"] == "mobius":
         return g.MobiusFermion(U, dims, case["L5"], case["mass"], case["M5"], case["b"], case["c"], phases=ph,
-                               precision=prec)
+                               precision=prec, flags=flags)
     gamma = [complex(re, im) for re, im in case["gamma"]]
     return g.ZMobiusFermion(U, dims, gamma, case["mass"], case["M5"], case["b"], case["c"], phases=ph,
-                            precision=prec)
+                            precision=prec, flags=flags)
 
 
 def apply(op, name, x, domain):
@@ -100,12 +101,12 @@ def apply(op, name, x, domain):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", [g.F64, g.F32])
+@pytest.mark.parametrize("prec,flags", [(g.F64, 0), (g.F64, g.DF64), (g.F32, 0)])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_cuda_path_matches_known_answers(gpu_available, name, prec):
+def test_cuda_path_matches_known_answers(gpu_available, name, prec, flags):
     case = CASES[name]
     tol = {g.F64: 1e-13, g.F32: 1e-6}[prec] * (10 if case["kind"] == "zmobius" else 1)
-    op = make_op(case, prec)
+    op = make_op(case, prec, flags)
     vol = int(np.prod(case["dims"]))
     seeds = GOLDEN["field_seeds"]
     full = g.random_gaussian(vol * case["L5"] * 12, seeds["full"])
