@@ -221,10 +221,24 @@ __device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8]
   using R = typename Arith<T>::type;
   constexpr int MU = LEG & 3;
   constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
-  Spinor<R> f;
-  SpinorIO<T>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
   R hr[6], hi[6], ur[6], ui[6];
-  project<MU, S>(f, hr, hi);
+  if constexpr (std::is_same<T, DF64>::value) {
+    // double-float: the projection's 24 adds run on the FP64 pipe (otherwise idle here)
+    // and only the twelve projected values are split
+    Spinor<double> f;
+    SpinorIO<double>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
+    double dr[6], di[6];
+    project<MU, S>(f, dr, di);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      hr[k] = df::split(dr[k]);
+      hi[k] = df::split(di[k]);
+    }
+  } else {
+    Spinor<R> f;
+    SpinorIO<T>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
+    project<MU, S>(f, hr, hi);
+  }
   su3_mul<R>(U + LEG * 18, hr, hi, ur, ui);
   reconstruct<MU, S, LEG == 0>(acc, ur, ui);
 }
