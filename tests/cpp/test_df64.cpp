@@ -90,8 +90,9 @@ int main() {
     expect(err <= 8 * u48, "dot", err, 8 * u48);
   }
 
-  // a hopping-term site: eight legs of (two-spinor = f_a - f_b) x (3x3 complex link),
-  // accumulated; relative L2 error over many sites against long double
+  // a hopping-term site as the kernel forms it: eight legs of (two-spinor = f_a -+ f_b,
+  // projected in double, then split) x (3x3 complex link in double-float), accumulated in
+  // double-float; relative L2 error over many sites against long double
   long double e2 = 0, n2 = 0;
   for (int site = 0; site < 20000; site++) {
     long double xr[6] = {}, xi[6] = {};
@@ -103,8 +104,8 @@ int main() {
       dfloat hr[6], hi[6];
       long double lr[6], li[6];
       for (int k = 0; k < 6; k++) {
-        hr[k] = gb::df::split(f[4 * k]) - gb::df::split(f[4 * k + 1]);
-        hi[k] = gb::df::split(f[4 * k + 2]) + gb::df::split(f[4 * k + 3]);
+        hr[k] = gb::df::split(f[4 * k] - f[4 * k + 1]);
+        hi[k] = gb::df::split(f[4 * k + 2] + f[4 * k + 3]);
         lr[k] = (long double)f[4 * k] - f[4 * k + 1];
         li[k] = (long double)f[4 * k + 2] + f[4 * k + 3];
       }
