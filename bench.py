@@ -717,6 +717,7 @@ DHOP_PROFILE_CASES = {
     "wilson16rhs_fp32": ("wilson", (24, 24, 24, 32), 1, 16, "F32"),
     "dwf_fp16": ("mobius", (32, 32, 32, 32), 12, 1, "F16"),
     "dwf_fp64": ("mobius", (16, 16, 16, 16), 16, 2, "F64"),
+    "dwf_df64": ("mobius", (16, 16, 16, 16), 16, 2, "DF64"),  # FP64 fields, double-float arithmetic
     "dwf_fp32": ("mobius", (16, 16, 16, 16), 16, 1, "F32"),
     "dwf24_ls12_fp32": ("mobius", (24, 24, 24, 24), 12, 1, "F32"),
 }
@@ -726,12 +727,13 @@ def dhop_profile(g, case, launches=3):
     """For a profiler's capture, not a measurement: `launches` DhopEO launches of a small
     case of each Dhop kernel (DHOP_PROFILE_CASES)."""
     kind, dims, Ls, nrhs, prec = DHOP_PROFILE_CASES[case]
-    prec = getattr(g, prec)
+    flags = g.DF64 if prec == "DF64" else 0
+    prec = g.F64 if prec == "DF64" else getattr(g, prec)
     U = g.random_gauge(dims, EPS, 1234)
     if kind == "wilson":
-        op = g.WilsonFermion(U, dims, 0.02, precision=prec, nrhs=nrhs)
+        op = g.WilsonFermion(U, dims, 0.02, precision=prec, nrhs=nrhs, flags=flags)
     else:
-        op = g.MobiusFermion(U, dims, Ls, MF, M5, B, C, precision=prec, nrhs=nrhs)
+        op = g.MobiusFermion(U, dims, Ls, MF, M5, B, C, precision=prec, nrhs=nrhs, flags=flags)
     n = op.half_sites4 * Ls * nrhs * 12
     fin = op.FermionRedBlackField(g.ODD).import_(g.random_gaussian(n, 7))
     fout = op.FermionRedBlackField(g.EVEN)
