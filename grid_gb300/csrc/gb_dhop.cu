@@ -221,26 +221,73 @@ __device__ __forceinline__ void dhop_leg(const DhopParams& p, const int (&nb)[8]
   using R = typename Arith<T>::type;
   constexpr int MU = LEG & 3;
   constexpr int S = (LEG < 4 ? -1 : 1) * (DAG ? -1 : 1);
+  Spinor<R> f;
+  SpinorIO<T>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
   R hr[6], hi[6], ur[6], ui[6];
-  if constexpr (std::is_same<T, DF64>::value) {
-    // double-float: the projection's 24 adds run on the FP64 pipe (otherwise idle here)
-    // and only the twelve projected values are split
+  project<MU, S>(f, hr, hi);
+  su3_mul<R>(U + LEG * 18, hr, hi, ur, ui);
+  reconstruct<MU, S, LEG == 0>(acc, ur, ui);
+}
+
+// The double-float legs as one loop: unrolled over the eight legs, the double-float
+// arithmetic (about 1 200 instructions per leg) no longer fits the instruction cache.  The
+// projection (in double, a switch on the leg), the split, the SU(3) product and the
+// reconstruction are one body; the reconstruction adds u to spins 0, 1 and a phase
+// (+-1 or +-i) times u0 or u1 to spins 2, 3, as Grid's accumRecon{X,Y,Z,T}{p,m} do.
+template <bool DAG>
+__device__ __forceinline__ void dhop_df64_legs(const DhopParams& p, const int* __restrict__ nbrow, int s,
+                                               const dfloat* U, Spinor<dfloat>& acc) {
+  constexpr int SF = DAG ? 1 : -1;  // the sign S of the forward legs 0..3 (backward: -SF)
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    acc.re[k] = dfloat(0);
+    acc.im[k] = dfloat(0);
+  }
+#pragma unroll 1
+  for (int leg = 0; leg < 8; leg++) {
     Spinor<double> f;
-    SpinorIO<double>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
+    SpinorIO<double>::load(p.in, nullptr, p.n5, size_t(__ldg(nbrow + leg)) * p.L5 + s, f);
     double dr[6], di[6];
-    project<MU, S>(f, dr, di);
+    switch (leg) {
+      case 0: project<0, SF>(f, dr, di); break;
+      case 1: project<1, SF>(f, dr, di); break;
+      case 2: project<2, SF>(f, dr, di); break;
+      case 3: project<3, SF>(f, dr, di); break;
+      case 4: project<0, -SF>(f, dr, di); break;
+      case 5: project<1, -SF>(f, dr, di); break;
+      case 6: project<2, -SF>(f, dr, di); break;
+      default: project<3, -SF>(f, dr, di); break;
+    }
+    dfloat hr[6], hi[6], ur[6], ui[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       hr[k] = df::split(dr[k]);
       hi[k] = df::split(di[k]);
     }
-  } else {
-    Spinor<R> f;
-    SpinorIO<T>::load(p.in, p.in_norms, p.n5, size_t(nb[LEG]) * p.L5 + s, f);
-    project<MU, S>(f, hr, hi);
+    su3_mul<dfloat>(U + leg * 18, hr, hi, ur, ui);
+    const int mu = leg & 3;
+    const int S = leg < 4 ? SF : -SF;
+    const bool imag = (mu & 1) == 0;               // MU = 0, 2: the phases are +-i
+    const bool neg2 = imag ? S > 0 : S < 0;        // spin 2: -S i (MU 0, 2) or S (MU 1, 3)
+    const bool neg3 = mu < 2 ? S > 0 : S < 0;      // spin 3: -S i, -S, S i, S for MU 0..3
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      acc.re[c] += ur[c];
+      acc.im[c] += ui[c];
+      acc.re[3 + c] += ur[3 + c];
+      acc.im[3 + c] += ui[3 + c];
+      // spin 2 takes u1 for MU 0, 1 and u0 for MU 2, 3; spin 3 the other one
+      const dfloat v2r = mu < 2 ? ur[3 + c] : ur[c], v2i = mu < 2 ? ui[3 + c] : ui[c];
+      const dfloat v3r = mu < 2 ? ur[c] : ur[3 + c], v3i = mu < 2 ? ui[c] : ui[3 + c];
+      // (sign) x v, or (sign) x i v = (sign) x (-v_im, v_re)
+      const dfloat a2 = imag ? -v2i : v2r, b2 = imag ? v2r : v2i;
+      const dfloat a3 = imag ? -v3i : v3r, b3 = imag ? v3r : v3i;
+      acc.re[6 + c] += neg2 ? -a2 : a2;
+      acc.im[6 + c] += neg2 ? -b2 : b2;
+      acc.re[9 + c] += neg3 ? -a3 : a3;
+      acc.im[9 + c] += neg3 ? -b3 : b3;
+    }
   }
-  su3_mul<R>(U + LEG * 18, hr, hi, ur, ui);
-  reconstruct<MU, S, LEG == 0>(acc, ur, ui);
 }
 
 template <class T, bool DAG, bool RECON>
@@ -293,14 +340,18 @@ __device__ __forceinline__ void dhop_body(const DhopParams& p0) {
   if (!ok || !active) return;
   const R* U = sU + j * 144;
   Spinor<R> acc;
-  dhop_leg<T, DAG, 0>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 1>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 2>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 3>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 4>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 5>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 6>(p, nb, s, U, acc);
-  dhop_leg<T, DAG, 7>(p, nb, s, U, acc);
+  if constexpr (std::is_same<T, DF64>::value) {
+    dhop_df64_legs<DAG>(p, p.nbr + (x0 + j) * 8, s, U, acc);
+  } else {
+    dhop_leg<T, DAG, 0>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 1>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 2>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 3>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 4>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 5>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 6>(p, nb, s, U, acc);
+    dhop_leg<T, DAG, 7>(p, nb, s, U, acc);
+  }
   SpinorIO<T>::store(p.out, p.out_norms, p.n5, size_t(x0 + j) * p.L5 + s, acc);
   if (s == 0 && p.L5a < p.L5) {
     Spinor<R> zero;
