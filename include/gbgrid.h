@@ -417,6 +417,9 @@ typedef SU<3> SU3;
 // ---- fermion operators (FermionOperator.h:40-192) ------------------------------------
 struct WilsonImplParams {
   std::vector<ComplexD> boundary_phases = std::vector<ComplexD>(Nd, ComplexD(1, 0));
+  // this library's operator options (not in Grid): GB_FLAG_RECON12 (12-real links),
+  // GB_FLAG_DF64 (FP64 operators: the hopping term in double-float arithmetic)
+  unsigned flags = 0;
   WilsonImplParams() {}
   explicit WilsonImplParams(const std::vector<ComplexD>& phi) : boundary_phases(phi) {}
 };
@@ -514,8 +517,8 @@ template <class Impl> class WilsonFermion : public FermionOperator<Impl> {
                 const ImplParams& p = ImplParams())
       : Base(&Fgrid, &Hgrid, &Fgrid, &Hgrid, mass) {
     const std::vector<double> ph = Base::phases(p);
-    gbdetail::check(gb_wilson_create(Fgrid.dims4.data(), mass, ph.data(), Impl::precision, 1, gbdetail::stream(), 0,
-                                     &this->op_),
+    gbdetail::check(gb_wilson_create(Fgrid.dims4.data(), mass, ph.data(), Impl::precision, 1, gbdetail::stream(),
+                                     p.flags, &this->op_),
                     "WilsonFermion");
     this->ImportGauge(U);
   }
@@ -540,7 +543,7 @@ template <class Impl> class MobiusFermion : public FermionOperator<Impl> {
         Ls(FiveDimGrid.Ls), M5(M5_), b(b_), c(c_), params(p) {
     const std::vector<double> ph = Base::phases(p);
     gbdetail::check(gb_mobius_create(FourDimGrid.dims4.data(), Ls, mass, M5_, b_, c_, ph.data(), Impl::precision, 1,
-                                     gbdetail::stream(), 0, &this->op_),
+                                     gbdetail::stream(), p.flags, &this->op_),
                     "MobiusFermion");
     this->ImportGauge(U);
   }
@@ -616,7 +619,7 @@ template <class Impl> class ZMobiusFermion : public MobiusFermion<Impl> {
     const std::vector<double> ph = FermionOperator<Impl>::phases(p);
     gbdetail::check(gb_zmobius_create(FourDimGrid.dims4.data(), this->Ls, mass, M5_,
                                       reinterpret_cast<const double*>(gamma.data()), b_, c_, ph.data(),
-                                      Impl::precision, 1, gbdetail::stream(), 0, &this->op_),
+                                      Impl::precision, 1, gbdetail::stream(), p.flags, &this->op_),
                     "ZMobiusFermion");
     this->ImportGauge(U);
   }

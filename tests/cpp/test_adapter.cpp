@@ -2,7 +2,8 @@
 // tests/core/Test_mobius_even_odd.cc, the Schur red-black solve, the mixed-precision
 // reliable-update CG of tests/Test_dwf_mixedcg_prec.cc, the multishift CG, the unpreconditioned Wilson CG of
 // tests/solver/Test_wilson_cg_unprec.cc, a user-defined linear operator through the
-// host-driven CG, the 4D <-> 5D surface fields, MADWF and the ZMobius even-odd identities.  Exit status 0 when every check holds.
+// host-driven CG, the 4D <-> 5D surface fields, MADWF, the ZMobius even-odd identities and
+// the double-float FP64 option.  Exit status 0 when every check holds.
 #include <cstdio>
 #include <cstdlib>
 
@@ -71,6 +72,16 @@ int main() {
   Ddwf.M(src, ref);
   tmp = ref - r_eo;
   expect(std::sqrt(norm2(tmp) / norm2(ref)) < 1e-13, "Meooe + Mooee == M", std::sqrt(norm2(tmp) / norm2(ref)));
+  {
+    // the library option through ImplParams: the double-float hopping term keeps M to 1e-13
+    WilsonImplParams pdf = params;
+    pdf.flags = GB_FLAG_DF64;
+    MobiusFermionD Ddf(Umu, *FGrid, *FrbGrid, *UGrid, *UrbGrid, mass, M5, b, c, pdf);
+    LatticeFermion mdf(FGrid);
+    Ddf.M(src, mdf);
+    tmp = ref - mdf;
+    expect(std::sqrt(norm2(tmp) / norm2(ref)) < 1e-13, "M with GB_FLAG_DF64 == M", std::sqrt(norm2(tmp) / norm2(ref)));
+  }
 
   Ddwf.Mooee(src_o, t_o);
   Ddwf.MooeeInv(t_o, r_o);
