@@ -51,7 +51,7 @@ struct DhopParams {
   int sgn[4];     // the (real) boundary phase of each direction
   int parity;     // output checkerboard (parity2 for blockIdx.z == 1)
   int parity2;
-  // MOOEE epilogue (FP32: the last two steps of Mpc in one launch): out = M5D x5 - (the
+  // MOOEE epilogue (FP32 / FP16: the last two steps of Mpc in one launch): out = M5D x5 - (the
   // Dhop) with the Mooee coefficients, |out|^2 per CTA (and per right-hand side when there
   // are several: dpart[CTA][nrhs])
   const void* x5;
