@@ -165,7 +165,8 @@ GB_HD dfloat& operator+=(dfloat& a, dfloat b) {
   a = a + b;
   return a;
 }
-// +-1 times a value (the projector and reconstruction signs)
+// s times a value for s = +1 or -1 only (the projector and reconstruction signs); any
+// other s is treated as its sign
 GB_HD dfloat operator*(int s, dfloat a) { return s < 0 ? -a : a; }
 
 // Dot2: sum of a_k b_k with TwoProduct on the high parts, the cross terms and the
